@@ -1,0 +1,463 @@
+// C ABI of libdymgpu (declared in include/dymgpu.h): group and chain handles,
+// sweeps, observables and configuration transfer.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "chain.h"
+#include "dym_core.h"
+
+namespace dym {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+static int cuda_fail(cudaError_t e, const char* what) {
+  return fail(DYM_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define DYM_CUDA(call, what)                      \
+  do {                                            \
+    cudaError_t _e = (call);                      \
+    if (_e != cudaSuccess) return cuda_fail(_e, what); \
+  } while (0)
+
+template <class T>
+static cudaError_t dmalloc(T** p, size_t n) {
+  return cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T));
+}
+
+int group_to_device(Group* g) {
+  int dev = 0;
+  DYM_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+  if (g->device == dev) return DYM_OK;
+  if (g->device >= 0) return fail(DYM_ENOTSUP, "a group handle is bound to one device; load it again for another");
+  const size_t P = g->P;
+  DYM_CUDA(dmalloc((uint16_t**)&g->d_mult, P * P), "cudaMalloc(mult)");
+  DYM_CUDA(dmalloc((uint16_t**)&g->d_inv, P), "cudaMalloc(inv)");
+  DYM_CUDA(dmalloc((double**)&g->d_retr, P), "cudaMalloc(retr)");
+  DYM_CUDA(dmalloc((double**)&g->d_imtr, P), "cudaMalloc(imtr)");
+  DYM_CUDA(dmalloc((uint8_t**)&g->d_cls, P), "cudaMalloc(cls)");
+  DYM_CUDA(dmalloc((double**)&g->d_clsval, std::max(g->ncls, 1)), "cudaMalloc(clsval)");
+  DYM_CUDA(cudaMemcpy(g->d_mult, g->mult.data(), P * P * 2, cudaMemcpyHostToDevice), "upload mult");
+  DYM_CUDA(cudaMemcpy(g->d_inv, g->inv.data(), P * 2, cudaMemcpyHostToDevice), "upload inv");
+  DYM_CUDA(cudaMemcpy(g->d_retr, g->retr.data(), P * 8, cudaMemcpyHostToDevice), "upload retr");
+  DYM_CUDA(cudaMemcpy(g->d_imtr, g->imtr.data(), P * 8, cudaMemcpyHostToDevice), "upload imtr");
+  DYM_CUDA(cudaMemcpy(g->d_cls, g->cls.data(), P, cudaMemcpyHostToDevice), "upload cls");
+  DYM_CUDA(cudaMemcpy(g->d_clsval, g->cls_val.data(), g->ncls * 8, cudaMemcpyHostToDevice), "upload clsval");
+  g->device = dev;
+  return DYM_OK;
+}
+
+void group_free(Group* g) {
+  if (!g) return;
+  if (g->device >= 0) {
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(g->device);
+    cudaFree(g->d_mult);
+    cudaFree(g->d_inv);
+    cudaFree(g->d_retr);
+    cudaFree(g->d_imtr);
+    cudaFree(g->d_cls);
+    cudaFree(g->d_clsval);
+    cudaSetDevice(cur);
+  }
+  delete g;
+}
+
+static int bits_for(uint32_t n) {  // bits to hold values 0..n-1
+  int b = 0;
+  while ((1u << b) < n) ++b;
+  return std::max(b, 1);
+}
+
+// Whether the shared sub-table kernel applies to this group and pool size.
+static bool fast_eligible(const Group& g, uint32_t npool, int device) {
+  if (!g.assoc_ok || !g.cls_conj_invariant || g.ncls > 255) return false;
+  if (bits_for(g.P) + bits_for((uint32_t)g.ncls) > 16) return false;
+  int optin = 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) return false;
+  return fast_smem_bytes(g.P, npool, g.ncls) <= (size_t)optin;
+}
+
+// Bound on |dS_fp32 - dS_fp64| for the fast kernel (see k_sweep_fast).
+static double fast_eps(const Group& g, int D, double b0, double b1, double b2) {
+  const double R = g.max_abs_retr, sig = g.cls_spread;
+  const double u32 = std::ldexp(1.0, -24), u64 = std::ldexp(1.0, -53);
+  const double n1 = 2.0 * (D - 1), n2 = 6.0 * (D - 1);
+  auto part = [&](double n) { return 2 * n * (R * u32 + sig) + 2 * n * n * R * u32 + 6 * n * R * u32; };
+  const double A = std::fabs(b0) + std::fabs(b1) * n1 * R + std::fabs(b2) * n2 * R;
+  return 4.0 * (std::fabs(b1) * part(n1) + std::fabs(b2) * part(n2)) + 16.0 * A * n2 * u64 + 1e-30;
+}
+
+static int build_fast_tables(dym_chain* c) {
+  const Group& g = *c->grp->g;
+  const uint32_t P = g.P, np = c->dev.npool;
+  const int shift = bits_for(P);
+  std::vector<uint16_t> sub((size_t)np * P);
+  std::vector<uint16_t> pool(np);
+  DYM_CUDA(cudaMemcpy(pool.data(), c->dev.pool, np * 2, cudaMemcpyDeviceToHost), "download pool");
+  for (uint32_t k = 0; k < np; ++k)
+    for (uint32_t u = 0; u < P; ++u) {
+      const uint32_t p = g.mult[(size_t)u * P + pool[k]];
+      sub[(size_t)k * P + u] = (uint16_t)(p | ((uint32_t)g.cls[p] << shift));
+    }
+  std::vector<float> v32(g.ncls);
+  for (int i = 0; i < g.ncls; ++i) v32[i] = (float)g.cls_val[i];
+  FastTables& ft = c->dev.fast;
+  DYM_CUDA(dmalloc(&ft.sub, sub.size()), "cudaMalloc(sub)");
+  DYM_CUDA(dmalloc(&ft.cls_val32, g.ncls), "cudaMalloc(cv32)");
+  DYM_CUDA(cudaMemcpy(ft.sub, sub.data(), sub.size() * 2, cudaMemcpyHostToDevice), "upload sub");
+  DYM_CUDA(cudaMemcpy(ft.cls_val32, v32.data(), g.ncls * 4, cudaMemcpyHostToDevice), "upload cv32");
+  ft.cls = (uint8_t*)g.d_cls;
+  ft.cls_val64 = (double*)g.d_clsval;
+  ft.ncls = g.ncls;
+  ft.shift = shift;
+  ft.exact = g.cls_exact ? 1 : 0;
+  c->dev.fast_ok = true;
+  return DYM_OK;
+}
+
+static SweepArgs sweep_args(dym_chain* c) {
+  const Group& g = *c->grp->g;
+  SweepArgs a{};
+  a.links = c->dev.links;
+  a.V = c->dev.V;
+  a.Nt = c->p.Nt;
+  a.Nx = c->p.Nx;
+  a.mult = (const uint16_t*)g.d_mult;
+  a.inv = (const uint16_t*)g.d_inv;
+  a.retr = (const double*)g.d_retr;
+  a.pool = c->dev.pool;
+  a.P = g.P;
+  a.npool = c->dev.npool;
+  a.id = g.id;
+  a.beta0 = c->p.beta0;
+  a.beta1 = c->p.beta1;
+  a.beta2 = c->p.beta2;
+  a.seed = c->p.seed;
+  a.counters = c->dev.counters;
+  return a;
+}
+
+static void chain_release(dym_chain* c) {
+  if (!c) return;
+  cudaSetDevice(c->p.device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  cudaFree(c->dev.links);
+  cudaFree(c->dev.sites);
+  cudaFree(c->dev.pool);
+  cudaFree(c->dev.counters);
+  cudaFree(c->dev.fast.sub);
+  cudaFree(c->dev.fast.cls_val32);
+  cudaFree(c->d_hist);
+  cudaFree(c->d_meas_scratch);
+  if (c->h_counters) cudaFreeHost(c->h_counters);
+  if (c->h_hist) cudaFreeHost(c->h_hist);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+}  // namespace dym
+
+using namespace dym;
+
+extern "C" {
+
+const char* dym_last_error(void) { return g_last_error.c_str(); }
+const char* dym_version(void) { return "dymgpu 0.1 (sm_103a)"; }
+
+int dym_group_load(const char* path, dym_group** out) {
+  if (!out) return fail(DYM_EINVAL, "dym_group_load: out is NULL");
+  *out = nullptr;
+  Group* g = nullptr;
+  int rc = group_load(path, &g);
+  if (rc) return rc;
+  *out = new dym_group{g};
+  return DYM_OK;
+}
+
+int dym_group_free(dym_group* g) {
+  if (!g) return DYM_OK;
+  group_free(g->g);
+  delete g;
+  return DYM_OK;
+}
+
+int dym_group_get_info(const dym_group* gh, dym_group_info* out) {
+  if (!gh || !out) return fail(DYM_EINVAL, "dym_group_get_info: null argument");
+  const Group& g = *gh->g;
+  out->order = g.P;
+  out->identity = g.id;
+  out->pool_nearest = (uint32_t)g.pool_nearest.size();
+  out->min_retr = g.min_retr;
+  out->nn_retr = g.nn_retr;
+  out->n_classes = g.ncls;
+  out->classes_exact = g.cls_exact ? 1 : 0;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  out->fast_path = 0;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0)
+    out->fast_path = fast_eligible(g, (uint32_t)g.pool_nearest.size(), dev) ? 1 : 0;
+  else
+    cudaGetLastError();
+  out->class_spread = g.cls_spread;
+  return DYM_OK;
+}
+
+int dym_group_get_tables(const dym_group* gh, int32_t* mult, int32_t* inv, double* retr, double* imtr,
+                         int32_t* pool) {
+  if (!gh) return fail(DYM_EINVAL, "dym_group_get_tables: null group");
+  const Group& g = *gh->g;
+  if (mult) for (size_t k = 0; k < g.mult.size(); ++k) mult[k] = g.mult[k];
+  if (inv) for (uint32_t k = 0; k < g.P; ++k) inv[k] = g.inv[k];
+  if (retr) std::memcpy(retr, g.retr.data(), g.P * 8);
+  if (imtr) std::memcpy(imtr, g.imtr.data(), g.P * 8);
+  if (pool) for (size_t k = 0; k < g.pool_nearest.size(); ++k) pool[k] = g.pool_nearest[k];
+  return DYM_OK;
+}
+
+int dym_schedule_check(int32_t D, int32_t Nt, int32_t Nx, int32_t* nphase, uint64_t* conflicts) {
+  Schedule s;
+  int rc = schedule_build(D, Nt, Nx, &s);
+  if (rc) return rc;
+  if (nphase) *nphase = (int32_t)s.phase_dir.size();
+  if (conflicts) *conflicts = schedule_conflicts(s);
+  return DYM_OK;
+}
+
+int dym_schedule_get(int32_t D, int32_t Nt, int32_t Nx, uint32_t* V, int32_t* nphase, int32_t* phase_dir,
+                     uint32_t* phase_len, uint32_t* sites) {
+  Schedule s;
+  int rc = schedule_build(D, Nt, Nx, &s);
+  if (rc) return rc;
+  if (V) *V = s.V;
+  if (nphase) *nphase = (int32_t)s.phase_dir.size();
+  if (phase_dir) for (size_t p = 0; p < s.phase_dir.size(); ++p) phase_dir[p] = s.phase_dir[p];
+  if (phase_len) for (size_t p = 0; p < s.phase_len.size(); ++p) phase_len[p] = s.phase_len[p];
+  if (sites) std::memcpy(sites, s.sites.data(), s.sites.size() * 4);
+  return DYM_OK;
+}
+
+int dym_chain_create(const dym_group* gh, const dym_chain_params* p, dym_chain** out) {
+  if (!gh || !p || !out) return fail(DYM_EINVAL, "dym_chain_create: null argument");
+  *out = nullptr;
+  if (p->start != DYM_START_HOT && p->start != DYM_START_COLD) return fail(DYM_EINVAL, "start must be hot or cold");
+  if (p->pool != DYM_POOL_NEAREST && p->pool != DYM_POOL_ALL) return fail(DYM_EINVAL, "unknown proposal pool");
+  if (p->precision != DYM_PREC_FP64 && p->precision != DYM_PREC_MIXED) return fail(DYM_EINVAL, "unknown precision");
+  std::unique_ptr<dym_chain, void (*)(dym_chain*)> c(new dym_chain, chain_release);
+  c->grp = const_cast<dym_group*>(gh);
+  c->p = *p;
+  int rc = schedule_build(p->D, p->Nt, p->Nx, &c->sched);
+  if (rc) return rc;
+  int ndev = 0;
+  DYM_CUDA(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
+  if (p->device < 0 || p->device >= ndev) return fail(DYM_EINVAL, "bad device ordinal");
+  DYM_CUDA(cudaSetDevice(p->device), "cudaSetDevice");
+  Group& g = *gh->g;
+  rc = group_to_device(&g);
+  if (rc) return rc;
+  if (g.pool_nearest.empty() && p->pool == DYM_POOL_NEAREST)
+    return fail(DYM_EINVAL, "group has an empty nearest-to-identity proposal pool");
+  const uint32_t V = c->sched.V;
+  ChainDev& d = c->dev;
+  d.D = p->D; d.Nt = p->Nt; d.Nx = p->Nx; d.V = V;
+  DYM_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  DYM_CUDA(dmalloc(&d.links, (size_t)V * p->D), "cudaMalloc(links)");
+  DYM_CUDA(dmalloc(&d.sites, c->sched.sites.size()), "cudaMalloc(sites)");
+  DYM_CUDA(cudaMemcpy(d.sites, c->sched.sites.data(), c->sched.sites.size() * 4, cudaMemcpyHostToDevice),
+           "upload sites");
+  std::vector<uint16_t> pool;
+  if (p->pool == DYM_POOL_NEAREST) pool = g.pool_nearest;
+  else for (uint32_t k = 0; k < g.P; ++k) pool.push_back((uint16_t)k);
+  d.npool = (uint32_t)pool.size();
+  DYM_CUDA(dmalloc(&d.pool, pool.size()), "cudaMalloc(pool)");
+  DYM_CUDA(cudaMemcpy(d.pool, pool.data(), pool.size() * 2, cudaMemcpyHostToDevice), "upload pool");
+  DYM_CUDA(dmalloc(&d.counters, 4), "cudaMalloc(counters)");
+  DYM_CUDA(cudaHostAlloc((void**)&c->h_counters, 4 * sizeof(unsigned long long), cudaHostAllocDefault),
+           "cudaHostAlloc");
+  if (p->precision == DYM_PREC_MIXED && fast_eligible(g, d.npool, p->device)) {
+    rc = build_fast_tables(c.get());
+    if (rc) return rc;
+  }
+  if (p->start == DYM_START_HOT)
+    DYM_CUDA(launch_hot_start(d.links, V, p->D, g.P, p->seed, c->stream), "hot start");
+  else
+    DYM_CUDA(launch_fill(d.links, (size_t)V * p->D, (uint16_t)g.id, c->stream), "cold start");
+  DYM_CUDA(cudaStreamSynchronize(c->stream), "start configuration");
+  *out = c.release();
+  return DYM_OK;
+}
+
+int dym_chain_free(dym_chain* c) {
+  chain_release(c);
+  return DYM_OK;
+}
+
+int dym_chain_set_beta(dym_chain* c, double beta0, double beta1, double beta2) {
+  if (!c) return fail(DYM_EINVAL, "dym_chain_set_beta: null chain");
+  c->p.beta0 = beta0;
+  c->p.beta1 = beta1;
+  c->p.beta2 = beta2;
+  return DYM_OK;
+}
+
+int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
+  if (!c) return fail(DYM_EINVAL, "dym_sweep: null chain");
+  if (nsweeps < 0 || nhit < 0 || nhit > (1 << 20)) return fail(DYM_EINVAL, "dym_sweep: bad nsweeps or nhit");
+  DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+  DYM_CUDA(cudaMemsetAsync(c->dev.counters, 0, 4 * sizeof(unsigned long long), c->stream), "reset counters");
+  SweepArgs a = sweep_args(c);
+  a.nhit = nhit;
+  FastTables ft = c->dev.fast;
+  ft.eps = fast_eps(*c->grp->g, c->p.D, c->p.beta0, c->p.beta1, c->p.beta2);
+  const Schedule& s = c->sched;
+  for (int k = 0; k < nsweeps; ++k) {
+    a.sweep = c->sweep;
+    for (size_t p = 0; p < s.phase_dir.size(); ++p) {
+      a.sites = c->dev.sites + s.phase_off[p];
+      a.n = s.phase_len[p];
+      cudaError_t e = c->dev.fast_ok
+                          ? launch_sweep_fast(c->p.D, s.phase_dir[p], a, ft, (double*)(c->dev.counters + 3),
+                                              c->stream)
+                          : launch_sweep_direct(c->p.D, s.phase_dir[p], a, c->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
+    }
+    ++c->sweep;
+  }
+  DYM_CUDA(cudaMemcpyAsync(c->h_counters, c->dev.counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                           c->stream),
+           "read counters");
+  DYM_CUDA(cudaStreamSynchronize(c->stream), "sweep");
+  if (out) {
+    out->hits = c->h_counters[0];
+    out->accepts = c->h_counters[1];
+    out->rechecks = c->h_counters[2];
+    double me;
+    std::memcpy(&me, &c->h_counters[3], 8);
+    out->max_ds_err = me;
+    out->sweep = c->sweep;
+  }
+  return DYM_OK;
+}
+
+int dym_measure(dym_chain* c, const dym_meas_opts* opts, dym_obs* out, double* wloop) {
+  if (!c || !out) return fail(DYM_EINVAL, "dym_measure: null argument");
+  DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+  const Group& g = *c->grp->g;
+  int nk = opts && opts->wl_nx > 0 ? opts->wl_nx : c->p.Nx;
+  int nl = opts && opts->wl_nt > 0 ? opts->wl_nt : c->p.Nt;
+  if (opts && (opts->wl_nx < 0 || opts->wl_nt < 0)) nk = nl = 0;
+  MeasArgs m{c->dev.links, c->dev.V, c->p.D, c->p.Nt, c->p.Nx, (const uint16_t*)g.d_mult,
+             (const uint16_t*)g.d_inv, g.P, g.id};
+  const size_t slots = 3 + (size_t)nk * nl;
+  const size_t hist_elems = slots * g.P;
+  if (hist_elems > c->hist_elems) {
+    cudaFree(c->d_hist);
+    c->d_hist = nullptr;
+    if (c->h_hist) cudaFreeHost(c->h_hist);
+    c->h_hist = nullptr;
+    DYM_CUDA(dmalloc(&c->d_hist, hist_elems), "cudaMalloc(hist)");
+    DYM_CUDA(cudaHostAlloc((void**)&c->h_hist, hist_elems * 8, cudaHostAllocDefault), "cudaHostAlloc(hist)");
+    c->hist_elems = hist_elems;
+  }
+  const size_t scr = measure_scratch_elems(m, nk, nl, g.assoc_ok);
+  if (scr > c->meas_scratch_elems) {
+    cudaFree(c->d_meas_scratch);
+    c->d_meas_scratch = nullptr;
+    DYM_CUDA(dmalloc(&c->d_meas_scratch, scr), "cudaMalloc(measure scratch)");
+    c->meas_scratch_elems = scr;
+  }
+  DYM_CUDA(cudaMemsetAsync(c->d_hist, 0, hist_elems * 8, c->stream), "clear hist");
+  DYM_CUDA(launch_measure(m, nk, nl, g.assoc_ok, c->d_hist, c->d_meas_scratch, c->stream), "measure launch");
+  DYM_CUDA(cudaMemcpyAsync(c->h_hist, c->d_hist, hist_elems * 8, cudaMemcpyDeviceToHost, c->stream), "read hist");
+  DYM_CUDA(cudaStreamSynchronize(c->stream), "measure");
+  const unsigned long long* h = c->h_hist;
+  const uint32_t P = g.P, V = c->dev.V;
+  const int D = c->p.D;
+  auto dot = [&](const unsigned long long* hh, const std::vector<double>& w) {
+    double s = 0;
+    for (uint32_t n = 0; n < P; ++n) s += (double)hh[n] * w[n];
+    return s;
+  };
+  out->plaq = dot(h, g.retr) / (double)(V * D * (D - 1) / 2);
+  out->rect = dot(h + P, g.retr) / (double)(V * D * (D - 1));
+  out->poly_re = dot(h + 2 * P, g.retr) / (double)(V / c->p.Nt);
+  out->poly_im = dot(h + 2 * P, g.imtr) / (double)(V / c->p.Nt);
+  out->wl_nx = nk;
+  out->wl_nt = nl;
+  if (wloop)
+    for (int k = 0; k < nk; ++k)
+      for (int l = 0; l < nl; ++l)
+        wloop[k * nl + l] = dot(h + (3 + (size_t)k * nl + l) * P, g.retr) / (double)(V * (D - 1));
+  return DYM_OK;
+}
+
+int dym_links_get(dym_chain* c, uint16_t* host_out) {
+  if (!c || !host_out) return fail(DYM_EINVAL, "dym_links_get: null argument");
+  DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+  DYM_CUDA(cudaMemcpyAsync(host_out, c->dev.links, (size_t)c->dev.V * c->p.D * 2, cudaMemcpyDeviceToHost, c->stream),
+           "download links");
+  DYM_CUDA(cudaStreamSynchronize(c->stream), "download links");
+  return DYM_OK;
+}
+
+int dym_links_set(dym_chain* c, const uint16_t* host_in) {
+  if (!c || !host_in) return fail(DYM_EINVAL, "dym_links_set: null argument");
+  const uint32_t P = c->grp->g->P;
+  const size_t n = (size_t)c->dev.V * c->p.D;
+  for (size_t k = 0; k < n; ++k)
+    if (host_in[k] >= P) return fail(DYM_EINVAL, "dym_links_set: element id out of range at " + std::to_string(k));
+  DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+  DYM_CUDA(cudaMemcpyAsync(c->dev.links, host_in, n * 2, cudaMemcpyHostToDevice, c->stream), "upload links");
+  DYM_CUDA(cudaStreamSynchronize(c->stream), "upload links");
+  return DYM_OK;
+}
+
+int dym_chain_get_schedule(const dym_chain* c, uint32_t* V, int32_t* nphase, int32_t* phase_dir,
+                           uint32_t* phase_len, uint32_t* sites) {
+  if (!c) return fail(DYM_EINVAL, "dym_chain_get_schedule: null chain");
+  const Schedule& s = c->sched;
+  if (V) *V = s.V;
+  if (nphase) *nphase = (int32_t)s.phase_dir.size();
+  if (phase_dir) for (size_t p = 0; p < s.phase_dir.size(); ++p) phase_dir[p] = s.phase_dir[p];
+  if (phase_len) for (size_t p = 0; p < s.phase_len.size(); ++p) phase_len[p] = s.phase_len[p];
+  if (sites) std::memcpy(sites, s.sites.data(), s.sites.size() * 4);
+  return DYM_OK;
+}
+
+int dym_chain_staples(dym_chain* c, int32_t dir, const uint32_t* sites, int32_t n, uint16_t* out) {
+  if (!c || (!sites && n) || (!out && n) || n < 0) return fail(DYM_EINVAL, "dym_chain_staples: bad argument");
+  if (dir < 0 || dir >= c->p.D) return fail(DYM_EINVAL, "dym_chain_staples: bad direction");
+  for (int32_t k = 0; k < n; ++k)
+    if (sites[k] >= c->dev.V) return fail(DYM_EINVAL, "dym_chain_staples: site out of range");
+  if (n == 0) return DYM_OK;
+  DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+  const int ns = 8 * (c->p.D - 1);
+  uint32_t* d_sites = nullptr;
+  uint16_t* d_out = nullptr;
+  DYM_CUDA(dmalloc(&d_sites, n), "cudaMalloc");
+  cudaError_t e = dmalloc(&d_out, (size_t)n * ns);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_sites, sites, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = launch_staples(c->p.D, dir, sweep_args(c), d_sites, (uint32_t)n, d_out, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out, d_out, (size_t)n * ns * 2, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d_sites);
+  cudaFree(d_out);
+  if (e != cudaSuccess) return cuda_fail(e, "staples");
+  return DYM_OK;
+}
+
+}  // extern "C"

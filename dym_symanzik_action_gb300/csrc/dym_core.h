@@ -1,0 +1,154 @@
+// Shared host/device arithmetic of the Metropolis engine: the random stream
+// and the exponential used by the accept test.  Everything here must give the
+// same bits on the CPU (x86-64 or aarch64, compiled with -ffp-contract=off)
+// and on the GPU (explicit __dmul_rn/__dadd_rn/__fma_rn), because the link
+// configuration after every sweep is compared bit for bit between the two.
+#pragma once
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define DYM_HD __host__ __device__ __forceinline__
+#else
+#define DYM_HD static inline
+#endif
+
+#if defined(__CUDA_ARCH__)
+#define DYM_MUL(a, b) __dmul_rn((a), (b))
+#define DYM_ADD(a, b) __dadd_rn((a), (b))
+#define DYM_SUB(a, b) __dsub_rn((a), (b))
+#define DYM_FMA(a, b, c) __fma_rn((a), (b), (c))
+#else
+#include <math.h>
+#define DYM_MUL(a, b) ((a) * (b))
+#define DYM_ADD(a, b) ((a) + (b))
+#define DYM_SUB(a, b) ((a) - (b))
+#define DYM_FMA(a, b, c) fma((a), (b), (c))
+#endif
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw, "Parallel
+// random numbers: as easy as 1, 2, 3", SC'11).  Multipliers and Weyl key
+// increments are the ones published with the algorithm.
+// ---------------------------------------------------------------------------
+typedef struct { uint32_t v[4]; } dym_u32x4;
+
+#define DYM_PHILOX_M0 0xD2511F53u
+#define DYM_PHILOX_M1 0xCD9E8D57u
+#define DYM_PHILOX_W0 0x9E3779B9u
+#define DYM_PHILOX_W1 0xBB67AE85u
+
+DYM_HD dym_u32x4 dym_philox4x32_10(dym_u32x4 c, uint32_t k0, uint32_t k1) {
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int r = 0; r < 10; ++r) {
+    uint64_t p0 = (uint64_t)DYM_PHILOX_M0 * c.v[0];
+    uint64_t p1 = (uint64_t)DYM_PHILOX_M1 * c.v[2];
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    dym_u32x4 o;
+    o.v[0] = hi1 ^ c.v[1] ^ k0;
+    o.v[1] = lo1;
+    o.v[2] = hi0 ^ c.v[3] ^ k1;
+    o.v[3] = lo0;
+    c = o;
+    k0 += DYM_PHILOX_W0;
+    k1 += DYM_PHILOX_W1;
+  }
+  return c;
+}
+
+// Stream tags: word 3 of the counter, so that different uses of one seed never
+// share a counter.
+#define DYM_TAG_METRO 0x4D455452u  // Metropolis hits
+#define DYM_TAG_HOT   0x484F5453u  // hot-start link draws
+#define DYM_TAG_LLR   0x4C4C5231u  // interval-restricted (LLR) hits
+
+// Counter layout of one Metropolis hit.  The key is the 64-bit chain seed.
+// The colour of a link is a function of (site, dir), so the tuple
+// (seed, sweep, link, hit) identifies the hit uniquely.
+DYM_HD dym_u32x4 dym_hit_random(uint64_t seed, uint32_t sweep, uint32_t site,
+                                uint32_t dir, uint32_t hit, uint32_t tag) {
+  dym_u32x4 c;
+  c.v[0] = site;
+  c.v[1] = sweep;
+  c.v[2] = (dir << 20) | (hit & 0xFFFFFu);
+  c.v[3] = tag;
+  return dym_philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+}
+
+// u1 = r0 * 2^-32 in [0,1); the proposal index floor(n * u1) equals
+// (r0 * n) >> 32 exactly for n < 2^21 (both products are exact in double).
+DYM_HD uint32_t dym_pick(uint32_t r0, uint32_t n) {
+  return (uint32_t)(((uint64_t)r0 * n) >> 32);
+}
+
+// u2 in [0,1) with 53 random bits: (r1 * 2^21 + (r2 >> 11)) * 2^-53.
+DYM_HD double dym_u53(uint32_t r1, uint32_t r2) {
+  uint64_t m = ((uint64_t)r1 << 21) | (r2 >> 11);
+  return (double)m * 0x1.0p-53;
+}
+
+// ---------------------------------------------------------------------------
+// exp(x) for the Metropolis ratio.  Cody-Waite argument reduction
+// x = k ln2 + r with ln2 split into a 24-bit head (k*LN2_HI exact for |k| <
+// 2^28) and a tail, then the Taylor series of e^r to degree 13 by Horner's rule
+// with fused multiply-adds (|r| <= ln2/2, truncation < 0.05 ulp), then scaling
+// by 2^k built from its bit pattern.  Accuracy is about 1 ulp; what matters is
+// that host and device produce identical bits.
+// ---------------------------------------------------------------------------
+DYM_HD double dym_bits_to_double(uint64_t b) {
+  union { uint64_t u; double d; } x; x.u = b; return x.d;
+}
+
+DYM_HD double dym_exp(double x) {
+  if (!(x == x)) return x;                 // NaN
+  if (x > 709.0) return dym_bits_to_double(0x7FF0000000000000ull);  // +inf
+  if (x < -745.5) return 0.0;
+  const double LOG2E = 0x1.71547652b82fep+0;
+  const double LN2_HI = 0x1.62e42f0000000p-1;
+  const double LN2_LO = 0x1.df473de6af279p-26;
+  double kd = DYM_MUL(x, LOG2E);
+#if defined(__CUDA_ARCH__)
+  kd = rint(kd);
+#else
+  kd = nearbyint(kd);
+#endif
+  int k = (int)kd;
+  double r = DYM_FMA(-kd, LN2_HI, x);
+  r = DYM_FMA(-kd, LN2_LO, r);
+  // 1/n!, n = 13 .. 0, each the double nearest the exact rational.
+  double p = 0x1.6124613a86d09p-33;
+  p = DYM_FMA(p, r, 0x1.1eed8eff8d898p-29);
+  p = DYM_FMA(p, r, 0x1.ae64567f544e4p-26);
+  p = DYM_FMA(p, r, 0x1.27e4fb7789f5cp-22);
+  p = DYM_FMA(p, r, 0x1.71de3a556c734p-19);
+  p = DYM_FMA(p, r, 0x1.a01a01a01a01ap-16);
+  p = DYM_FMA(p, r, 0x1.a01a01a01a01ap-13);
+  p = DYM_FMA(p, r, 0x1.6c16c16c16c17p-10);
+  p = DYM_FMA(p, r, 0x1.1111111111111p-7);
+  p = DYM_FMA(p, r, 0x1.5555555555555p-5);
+  p = DYM_FMA(p, r, 0x1.5555555555555p-3);
+  p = DYM_FMA(p, r, 0.5);
+  p = DYM_FMA(p, r, 1.0);
+  p = DYM_FMA(p, r, 1.0);
+  if (k >= -1020) {
+    return DYM_MUL(p, dym_bits_to_double((uint64_t)(k + 1023) << 52));
+  }
+  // Result near or below the normal range: scale in two exact-or-rounded steps.
+  double s1 = dym_bits_to_double((uint64_t)(k + 54 + 1023) << 52);
+  return DYM_MUL(DYM_MUL(p, s1), 0x1.0p-54);
+}
+
+// Reference accept rule (dym-mod-metro.cpp:180-187): with
+//   oldact = beta0 + beta1*r1    + beta2*m1
+//   newact = beta0 + beta1*r1new + beta2*m1new
+// accept iff (newact <= oldact ? 1 : exp(-(newact-oldact))) > u2.
+DYM_HD double dym_action(double b0, double b1, double b2, double r1, double m1) {
+  return DYM_ADD(DYM_ADD(b0, DYM_MUL(b1, r1)), DYM_MUL(b2, m1));
+}
+
+DYM_HD int dym_accept(double oldact, double newact, double u2) {
+  double probrat = (newact <= oldact) ? 1.0 : dym_exp(-DYM_SUB(newact, oldact));
+  return probrat > u2;
+}

@@ -1,0 +1,129 @@
+// Device-side lattice geometry and staple construction.
+//
+// Site index i = t + Nt*(x1 + Nx*(x2 + ...)) with periodic wrap (lattice.c
+// getidx/getpos, lattice.c:119-132 of the reference).  Links are stored
+// direction-major: links[dir*V + site], uint16 element ids.
+#pragma once
+#include <stdint.h>
+
+namespace dym {
+
+// Relative index offsets for a move of -2..+2 along each axis from the site's
+// own coordinates: off[b][k] = (wrap(x_b + k - 2) - x_b) * stride_b.
+template <int D>
+struct SiteGeo {
+  int off[D][5];
+};
+
+template <int D>
+__device__ __forceinline__ void site_geo(uint32_t i, int Nt, int Nx, SiteGeo<D>& g) {
+  int stride = 1;
+#pragma unroll
+  for (int b = 0; b < D; ++b) {
+    const int N = (b == 0) ? Nt : Nx;
+    const int xb = (int)(i % (uint32_t)N);
+    i /= (uint32_t)N;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      int c = xb + k - 2;
+      c = ((c % N) + N) % N;
+      g.off[b][k] = (c - xb) * stride;
+    }
+    stride *= N;
+  }
+}
+
+// Table access policies.  `Tab` provides mul(g, h), inv(g) for uint32 ids.
+struct GlobalTab {
+  const uint16_t* __restrict__ mult;  // P*P, L2-resident
+  const uint16_t* inv;                // shared memory copy
+  uint32_t P;
+  __device__ __forceinline__ uint32_t mul(uint32_t g, uint32_t h) const { return __ldg(mult + g * P + h); }
+  __device__ __forceinline__ uint32_t iv(uint32_t g) const { return inv[g]; }
+};
+
+struct SharedTab {  // whole Cayley table staged in shared memory (small groups)
+  const uint16_t* mult;
+  const uint16_t* inv;
+  uint32_t P;
+  __device__ __forceinline__ uint32_t mul(uint32_t g, uint32_t h) const { return mult[g * P + h]; }
+  __device__ __forceinline__ uint32_t iv(uint32_t g) const { return inv[g]; }
+};
+
+// Build the 2(D-1) plaquette staples then the 6(D-1) rectangle staples of link
+// (i, DIR), element for element as get_staples (dym-mod-metro.cpp:63-78) and
+// get_rect_loops (dym-mod-metro.cpp:83-142).  The reference's leading
+// mult[id][x] in each rectangle is the identity map and is skipped.
+// e = e_DIR, f = e_d1.  LD(site, dir) loads a link.
+template <int D, int DIR, class Tab, class LD>
+__device__ __forceinline__ void build_staples(uint32_t i, const SiteGeo<D>& geo, const Tab& T, LD ld,
+                                              uint32_t* st /* 2(D-1) */, uint32_t* re /* 6(D-1) */) {
+#define DYM_S(de, df) ((uint32_t)((int)i + geo.off[DIR][(de) + 2] + geo.off[d1][(df) + 2]))
+  int k = 0, kr = 0;
+#pragma unroll
+  for (int d1 = 0; d1 < D; ++d1) {
+    if (d1 == DIR) continue;
+    // Loads shared by the staples of this (DIR, d1) plane.
+    const uint32_t a_e_f1 = ld(DYM_S(1, 0), d1);      // a[i+e, d1]
+    const uint32_t a_0_d1 = ld(DYM_S(0, 0), d1);      // a[i, d1]
+    const uint32_t a_f_d = ld(DYM_S(0, 1), DIR);      // a[i+f, d]
+    const uint32_t a_emf_f = ld(DYM_S(1, -1), d1);    // a[i+e-f, d1]
+    const uint32_t a_mf_d = ld(DYM_S(0, -1), DIR);    // a[i-f, d]
+    const uint32_t a_mf_f = ld(DYM_S(0, -1), d1);     // a[i-f, d1]
+    const uint32_t a_e_d = ld(DYM_S(1, 0), DIR);      // a[i+e, d]
+    const uint32_t a_me_d = ld(DYM_S(-1, 0), DIR);    // a[i-e, d]
+    const uint32_t a_me_f = ld(DYM_S(-1, 0), d1);     // a[i-e, d1]
+    // Plaquette staples (dym-mod-metro.cpp:68-76).
+    {
+      uint32_t g = T.mul(a_e_f1, T.iv(a_f_d));
+      st[k++] = T.mul(g, T.iv(a_0_d1));
+      g = T.mul(T.iv(a_emf_f), T.iv(a_mf_d));
+      st[k++] = T.mul(g, a_mf_f);
+    }
+    // Rectangle 1 (:88-95): a[i+e,f] a[i+e+f,f] a[i+2f,d]^-1 a[i+f,f]^-1 a[i,f]^-1
+    {
+      uint32_t g = T.mul(a_e_f1, ld(DYM_S(1, 1), d1));
+      g = T.mul(g, T.iv(ld(DYM_S(0, 2), DIR)));
+      g = T.mul(g, T.iv(ld(DYM_S(0, 1), d1)));
+      re[kr++] = T.mul(g, T.iv(a_0_d1));
+    }
+    // Rectangle 2 (:97-104): a[i+e,d] a[i+2e,f] a[i+e+f,d]^-1 a[i+f,d]^-1 a[i,f]^-1
+    {
+      uint32_t g = T.mul(a_e_d, ld(DYM_S(2, 0), d1));
+      g = T.mul(g, T.iv(ld(DYM_S(1, 1), DIR)));
+      g = T.mul(g, T.iv(a_f_d));
+      re[kr++] = T.mul(g, T.iv(a_0_d1));
+    }
+    // Rectangle 3 (:106-113): a[i+e,f] a[i+f,d]^-1 a[i+f-e,d]^-1 a[i-e,f]^-1 a[i-e,d]
+    {
+      uint32_t g = T.mul(a_e_f1, T.iv(a_f_d));
+      g = T.mul(g, T.iv(ld(DYM_S(-1, 1), DIR)));
+      g = T.mul(g, T.iv(a_me_f));
+      re[kr++] = T.mul(g, a_me_d);
+    }
+    // Rectangle 4 (:115-122): a[i+e-f,f]^-1 a[i+e-2f,f]^-1 a[i-2f,d]^-1 a[i-2f,f] a[i-f,f]
+    {
+      uint32_t g = T.mul(T.iv(a_emf_f), T.iv(ld(DYM_S(1, -2), d1)));
+      g = T.mul(g, T.iv(ld(DYM_S(0, -2), DIR)));
+      g = T.mul(g, ld(DYM_S(0, -2), d1));
+      re[kr++] = T.mul(g, a_mf_f);
+    }
+    // Rectangle 5 (:124-131): a[i+e,d] a[i+2e-f,f]^-1 a[i+e-f,d]^-1 a[i-f,d]^-1 a[i-f,f]
+    {
+      uint32_t g = T.mul(a_e_d, T.iv(ld(DYM_S(2, -1), d1)));
+      g = T.mul(g, T.iv(ld(DYM_S(1, -1), DIR)));
+      g = T.mul(g, T.iv(a_mf_d));
+      re[kr++] = T.mul(g, a_mf_f);
+    }
+    // Rectangle 6 (:133-140): a[i+e-f,f]^-1 a[i-f,d]^-1 a[i-f-e,d]^-1 a[i-e-f,f] a[i-e,d]
+    {
+      uint32_t g = T.mul(T.iv(a_emf_f), T.iv(a_mf_d));
+      g = T.mul(g, T.iv(ld(DYM_S(-1, -1), DIR)));
+      g = T.mul(g, ld(DYM_S(-1, -1), d1));
+      re[kr++] = T.mul(g, a_me_d);
+    }
+  }
+#undef DYM_S
+}
+
+}  // namespace dym

@@ -1,0 +1,166 @@
+/*
+ * libdymgpu -- C ABI of the GB300 discrete-group Symanzik Metropolis engine.
+ *
+ * The reference (hlammiv/dym_symanzik_action) has no library API: its hot path
+ * is the `dym-mod-metro` process, whose C-linkage internals are the globals
+ * and functions of group.h:8-16 and lattice.h:7-16, driven by update() and the
+ * measurement block of dym-mod-metro.cpp:146-337.  Each entry point below
+ * names the reference piece it replaces.
+ *
+ * Conventions
+ *   - Every function returns an int status: DYM_OK (0) or a negative DYM_E*.
+ *     The library never aborts or exits; dym_last_error() gives the message.
+ *   - Opaque handles are created and freed by the library.  Host buffers
+ *     belong to the caller.  No torch or CUDA types cross this boundary.
+ *   - A chain owns one CUDA stream; calls on one chain are serialised by the
+ *     caller.  Entry points that return results synchronise that stream.
+ *   - Link layout of host buffers: uint16 element ids, direction-major,
+ *     links[d*V + site], site = t + Nt*(x1 + Nx*(x2 + ...)) (lattice.c
+ *     getidx, lattice.c:119-125 of the reference).
+ */
+#ifndef DYMGPU_H
+#define DYMGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DYM_OK 0
+#define DYM_EINVAL -1     /* bad argument */
+#define DYM_EIO -2        /* file cannot be opened or read */
+#define DYM_EFORMAT -3    /* group file malformed: truncated, out of range, no identity/inverse */
+#define DYM_ENOMEM -4     /* host or device allocation failed */
+#define DYM_ECUDA -5      /* CUDA runtime error (no device, launch failure) */
+#define DYM_ENOTSUP -6    /* combination not supported (e.g. D out of range) */
+#define DYM_ETIMEDOUT -7  /* bounded device wait expired */
+#define DYM_ERANGE -8     /* size limit exceeded (group order > DYM_PMAX, ...) */
+
+/* Largest group order accepted; same limit as the reference's PMAX (group.h:4). */
+#define DYM_PMAX 5040
+
+#define DYM_START_HOT 0   /* every link a uniform random element (dym-mod-metro.cpp:255) */
+#define DYM_START_COLD 1  /* every link the identity */
+
+#define DYM_POOL_NEAREST 0 /* elements of the 2nd-smallest ReTr (dym-mod-metro.cpp:239-245) */
+#define DYM_POOL_ALL 1     /* uniform over the whole group */
+
+#define DYM_PREC_FP64 0    /* every accept test in FP64, as the reference */
+#define DYM_PREC_MIXED 1   /* FP32 dS with FP64 re-evaluation near the threshold;
+                              accept decisions identical to DYM_PREC_FP64 */
+
+typedef struct dym_group dym_group;
+typedef struct dym_chain dym_chain;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* dym_last_error(void);
+/* Library version string. */
+const char* dym_version(void);
+
+/* ---------------------------------------------------------------- group --- */
+
+/* Parse a group file (format of groups/README.md:7-21; replaces load_group,
+ * group.c:13-81).  Finds the identity and inverses as the reference does;
+ * returns DYM_EFORMAT where the reference would abort, DYM_ERANGE for P >
+ * DYM_PMAX, DYM_EIO if the file cannot be read.  Trailing tokens are ignored. */
+int dym_group_load(const char* path, dym_group** out);
+int dym_group_free(dym_group* g);
+
+typedef struct {
+  uint32_t order;          /* P */
+  uint32_t identity;       /* id */
+  uint32_t pool_nearest;   /* size of the nearest-to-identity proposal pool */
+  double min_retr;         /* reference min_retr (dym-mod-metro.cpp:239-241) */
+  double nn_retr;          /* reference nn_retr (dym-mod-metro.cpp:242) */
+  int32_t n_classes;       /* distinct ReTr values (tolerance 1e-9) */
+  int32_t classes_exact;   /* 1 if each ReTr value class is one bit pattern */
+  int32_t fast_path;       /* 1 if the shared-memory sub-table path applies */
+  double class_spread;     /* largest ReTr deviation inside a class */
+} dym_group_info;
+
+int dym_group_get_info(const dym_group* g, dym_group_info* out);
+/* Copy the tables out (any pointer may be NULL): mult[P*P] row-major,
+ * inv[P], retr[P], imtr[P], pool[pool_nearest]. */
+int dym_group_get_tables(const dym_group* g, int32_t* mult, int32_t* inv,
+                         double* retr, double* imtr, int32_t* pool);
+
+/* ---------------------------------------------------------------- chain --- */
+
+typedef struct {
+  int32_t D, Nt, Nx;             /* lattice.h:7 (D, Nt, Nx); V = Nt*Nx^(D-1) */
+  double beta0, beta1, beta2;    /* lattice.h:8 */
+  uint64_t seed;                 /* Philox key (reference: per-site minstd seeds) */
+  int32_t start;                 /* DYM_START_HOT / DYM_START_COLD */
+  int32_t pool;                  /* DYM_POOL_NEAREST / DYM_POOL_ALL */
+  int32_t precision;             /* DYM_PREC_FP64 / DYM_PREC_MIXED */
+  int32_t device;                /* CUDA device ordinal */
+} dym_chain_params;
+
+/* Create a chain on the device with its start configuration (replaces
+ * dym-mod-metro.cpp:221-268: V, rnd[], hot/cold start, parity table). */
+int dym_chain_create(const dym_group* g, const dym_chain_params* p, dym_chain** out);
+int dym_chain_free(dym_chain* c);
+/* Change the couplings of an existing chain (beta scans). */
+int dym_chain_set_beta(dym_chain* c, double beta0, double beta1, double beta2);
+
+typedef struct {
+  uint64_t hits;        /* Metropolis hits (reference `hit`) */
+  uint64_t accepts;     /* accepted hits (reference `acc`) */
+  uint64_t rechecks;    /* mixed precision: hits re-evaluated in FP64 */
+  double max_ds_err;    /* mixed precision: max |dS_fp32 - dS_fp64| seen on rechecks */
+  uint32_t sweep;       /* sweeps done by the chain so far */
+} dym_stats;
+
+/* nsweeps full sweeps with nhit hits per link (replaces update(),
+ * dym-mod-metro.cpp:146-197, called nsweeps times).  Counters in `out`
+ * (may be NULL) are for this call only. */
+int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out);
+
+typedef struct {
+  int32_t wl_nx;   /* Wilson grid spatial extent 1..wl_nx (0: Nx, as the reference) */
+  int32_t wl_nt;   /* temporal extent 1..wl_nt (0: Nt) */
+} dym_meas_opts;
+
+typedef struct {
+  double poly_re, poly_im;   /* getpoly (lattice.c:179-194) */
+  double plaq;               /* mean plaquette ReTr (dym-mod-metro.cpp:285-291) */
+  double rect;               /* mean rectangle ReTr (dym-mod-metro.cpp:297-303) */
+  int32_t wl_nx, wl_nt;      /* grid actually measured */
+} dym_obs;
+
+/* Observables of the current configuration (dym-mod-metro.cpp:282-318).
+ * wloop (may be NULL) receives wl_nx*wl_nt doubles, spatial extent outer:
+ * wloop[k*wl_nt + l] for a (k+1) x (l+1) loop.  Sums are exact integer
+ * histograms over group elements followed by one FP64 dot product. */
+int dym_measure(dym_chain* c, const dym_meas_opts* opts, dym_obs* out, double* wloop);
+
+/* Host <-> device copies of the configuration (layout in the header comment). */
+int dym_links_get(dym_chain* c, uint16_t* host_out);
+int dym_links_set(dym_chain* c, const uint16_t* host_in);
+
+/* Lattice and schedule facts: V, number of colour phases per sweep, and the
+ * phase layout (arrays may be NULL; sizes nphase, nphase, V*D). */
+int dym_chain_get_schedule(const dym_chain* c, uint32_t* V, int32_t* nphase,
+                           int32_t* phase_dir, uint32_t* phase_len, uint32_t* sites);
+
+/* Staple elements of links (site[k], dir) built on the device: out[k*ns + j],
+ * ns = 8*(D-1): the 2(D-1) plaquette staples (get_staples,
+ * dym-mod-metro.cpp:63-78) then the 6(D-1) rectangle staples (get_rect_loops,
+ * dym-mod-metro.cpp:83-142), in the reference's order. */
+int dym_chain_staples(dym_chain* c, int32_t dir, const uint32_t* sites, int32_t n, uint16_t* out);
+
+/* Same-phase read conflicts of a lattice shape's schedule (0 = race-free);
+ * host-only, no device needed. */
+int dym_schedule_check(int32_t D, int32_t Nt, int32_t Nx, int32_t* nphase, uint64_t* conflicts);
+/* The colour schedule of a lattice shape without a device: call once with
+ * NULL arrays to get V and nphase, then with arrays of nphase, nphase and V*D
+ * entries.  Phases are ordered by direction (as the reference's d-major loop,
+ * dym-mod-metro.cpp:152-153), sites ascending inside a phase. */
+int dym_schedule_get(int32_t D, int32_t Nt, int32_t Nx, uint32_t* V, int32_t* nphase, int32_t* phase_dir,
+                     uint32_t* phase_len, uint32_t* sites);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DYMGPU_H */

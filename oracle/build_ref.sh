@@ -1,0 +1,44 @@
+#!/bin/sh
+# Builds the reference-derived checkers into oracle/_ref/ (git-ignored), from
+# the reference's sources where they lie (REF_DIR, default /root/reference);
+# nothing is copied.  Test infrastructure only.
+#
+#   _ref/libdymref.so   the reference's group.c, lattice.c and dym-mod-metro.cpp
+#                       (main renamed) + oracle/ref_harness.cpp, no OpenMP so
+#                       every sum runs in the reference's serial order
+#   _ref/dym-mod-metro  the unmodified reference executable, built with the
+#                       flags of the reference Makefile (-O3 -g -pg -fopenmp)
+#   _ref/dym-mod-metro-nhit10   the same with NHIT 10 instead of 20: the source
+#                       is streamed through sed into the compiler (no copy)
+set -e
+REF_DIR=${REF_DIR:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+CORE="$HERE/../dym_symanzik_action_gb300/csrc"
+CC=${CC:-gcc}
+CXX=${CXX:-g++}
+if [ ! -f "$REF_DIR/dym-mod-metro.cpp" ]; then
+  echo "reference sources not found in $REF_DIR" >&2
+  exit 2
+fi
+mkdir -p "$OUT"
+# harness library (serial)
+$CC -O2 -fPIC -std=gnu99 -w -c "$REF_DIR/group.c" -o "$OUT/h_group.o"
+$CC -O2 -fPIC -std=gnu99 -w -c "$REF_DIR/lattice.c" -o "$OUT/h_lattice.o"
+$CXX -O2 -fPIC -std=c++11 -w -ffp-contract=off -Dmain=dym_reference_main -I"$REF_DIR" \
+  -c "$REF_DIR/dym-mod-metro.cpp" -o "$OUT/h_metro.o"
+$CXX -O2 -fPIC -std=c++11 -w -c "$REF_DIR/timer.cpp" -o "$OUT/h_timer.o"
+$CXX -O2 -fPIC -std=c++17 -ffp-contract=off -I"$REF_DIR" -I"$CORE" -c "$HERE/ref_harness.cpp" -o "$OUT/h_harness.o"
+# -Bsymbolic: the reference's step() must not resolve to glibc's legacy
+# regexp step() when the library is loaded into a running process.
+$CXX -shared -Wl,-Bsymbolic -o "$OUT/libdymref.so" "$OUT/h_harness.o" "$OUT/h_metro.o" "$OUT/h_lattice.o" "$OUT/h_group.o" "$OUT/h_timer.o"
+# unmodified executable, reference Makefile flags
+$CC -O3 -std=gnu99 -Wall -fopenmp -w -c "$REF_DIR/group.c" -o "$OUT/group.o"
+$CC -O3 -std=gnu99 -Wall -fopenmp -w -c "$REF_DIR/lattice.c" -o "$OUT/lattice.o"
+$CXX -O3 -g -pg -fopenmp -std=c++11 -w -c "$REF_DIR/timer.cpp" -o "$OUT/timer.o"
+$CXX -O3 -g -pg -fopenmp -std=c++11 -w -I"$REF_DIR" "$REF_DIR/dym-mod-metro.cpp" \
+  "$OUT/lattice.o" "$OUT/group.o" "$OUT/timer.o" -lm -o "$OUT/dym-mod-metro"
+sed 's/^#define NHIT[ \t]*20/#define NHIT 10/' "$REF_DIR/dym-mod-metro.cpp" | \
+  $CXX -O3 -g -pg -fopenmp -std=c++11 -w -I"$REF_DIR" -x c++ - -x none \
+  "$OUT/lattice.o" "$OUT/group.o" "$OUT/timer.o" -lm -o "$OUT/dym-mod-metro-nhit10"
+echo "built $OUT"

@@ -1,0 +1,442 @@
+/*
+ * ORACLE -- test infrastructure only.  A CPU restatement of the reference's
+ * discrete-group Symanzik Metropolis path (hlammiv/dym_symanzik_action), used
+ * by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the
+ * checker.  Nothing in the product links or calls this file.
+ *
+ * Parity is pinned: tests/golden/ holds fixtures produced by the reference's
+ * own get_staples/get_rect_loops/plaquette/wilson/getpoly/load_group compiled
+ * from its sources (oracle/build_ref.sh), and tests check this file against
+ * them bit for bit.
+ *
+ * What is restated, with the reference lines it follows:
+ *   - group file parse, identity and inverse search     group.c:13-98
+ *   - site index and neighbour table                     lattice.c:119-153
+ *   - plaquette / polyakov / getpoly / wilson            lattice.c:157-205
+ *   - plaquette and rectangle staples                    dym-mod-metro.cpp:63-142
+ *   - proposal pool of nearest elements                  dym-mod-metro.cpp:239-245
+ *   - the multi-hit Metropolis update of one link        dym-mod-metro.cpp:161-192
+ *   - observables of one measurement                     dym-mod-metro.cpp:282-318
+ * What differs from the reference, by design of the engine under test:
+ *   - links are visited in the race-free colour phases passed in by the
+ *     caller instead of the racy two-parity checkerboard (dym-mod-metro.cpp:152-159);
+ *   - the per-site minstd engines are replaced by Philox4x32-10 keyed by
+ *     (seed, sweep, link, hit), and glibc exp by dym_exp (dym_core.h);
+ *   - observables sum integer histograms over group elements, then take one
+ *     FP64 dot product in ascending element order.
+ * Data layout follows the reference (AoS int links a[i*D+mu], int Cayley rows,
+ * a neighbour table), so that its timing is representative of the reference's
+ * OpenMP CPU code.
+ */
+#include <errno.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../dym_symanzik_action_gb300/csrc/dym_core.h"
+
+#define OR_PMAX 5040
+
+typedef struct {
+  unsigned P;
+  double* ReTr;
+  double* ImTr;
+  int* block;
+  int** mult;
+  int* inv;
+  int id;
+  int* pool;  /* nearest-to-identity proposal pool */
+  int npool;
+} or_group;
+
+typedef struct {
+  const or_group* g;
+  unsigned D, Nt, Nx, V;
+  int* a;          /* a[i*D + mu] */
+  unsigned* nn;    /* nn[i*2D + 2d + (s>0)] */
+} or_lattice;
+
+/* ------------------------------------------------------------------ group */
+
+void or_group_free(or_group* g) {
+  if (!g) return;
+  free(g->ReTr); free(g->ImTr); free(g->block); free(g->mult); free(g->inv); free(g->pool);
+  free(g);
+}
+
+/* 0 ok; -2 cannot open; -3 malformed (truncated, out of range, no identity or
+ * inverse); -8 order above OR_PMAX. */
+int or_group_load(const char* fn, or_group** out) {
+  *out = NULL;
+  FILE* f = fopen(fn, "r");
+  if (!f) return -2;
+  int P = 0;
+  if (fscanf(f, "%d", &P) != 1 || P <= 0) { fclose(f); return -3; }
+  if (P > OR_PMAX) { fclose(f); return -8; }
+  or_group* g = (or_group*)calloc(1, sizeof *g);
+  g->P = (unsigned)P;
+  g->ReTr = (double*)malloc(sizeof(double) * P);
+  g->ImTr = (double*)malloc(sizeof(double) * P);
+  g->block = (int*)malloc(sizeof(int) * (size_t)P * P);
+  g->mult = (int**)malloc(sizeof(int*) * P);
+  g->inv = (int*)malloc(sizeof(int) * P);
+  for (int n = 0; n < P; ++n) g->mult[n] = g->block + (size_t)n * P;
+  int bad = 0;
+  for (int n = 0; n < P && !bad; ++n) bad = fscanf(f, "%lf", &g->ReTr[n]) != 1;
+  for (int n = 0; n < P && !bad; ++n) bad = fscanf(f, "%lf", &g->ImTr[n]) != 1;
+  for (size_t k = 0; k < (size_t)P * P && !bad; ++k) {
+    bad = fscanf(f, "%d", &g->block[k]) != 1;
+    if (!bad && (g->block[k] < 0 || g->block[k] >= P)) bad = 1;
+  }
+  fclose(f);
+  if (bad) { or_group_free(g); return -3; }
+  /* identity: first n whose row and column are the identity map */
+  g->id = -1;
+  for (int n = 0; n < P && g->id < 0; ++n) {
+    int ok = 1;
+    for (int m = 0; m < P && ok; ++m) ok = g->mult[n][m] == m && g->mult[m][n] == m;
+    if (ok) g->id = n;
+  }
+  if (g->id < 0) { or_group_free(g); return -3; }
+  for (int n = 0; n < P; ++n) {
+    int found = -1;
+    for (int m = 0; m < P && found < 0; ++m)
+      if (g->mult[n][m] == g->id && g->mult[m][n] == g->id) found = m;
+    if (found < 0) { or_group_free(g); return -3; }
+    g->inv[n] = found;
+  }
+  /* proposal pool: elements at the second-smallest ReTr; min starts at 0
+   * and the runner-up at 10, as in the reference */
+  double lo = 0, next = 10;
+  for (int n = 0; n < P; ++n) if (g->ReTr[n] < lo) lo = g->ReTr[n];
+  for (int n = 0; n < P; ++n) if (g->ReTr[n] > lo && g->ReTr[n] < next) next = g->ReTr[n];
+  g->pool = (int*)malloc(sizeof(int) * P);
+  g->npool = 0;
+  for (int n = 0; n < P; ++n)
+    if (g->ReTr[n] < next + 1e-6 && g->ReTr[n] > lo) g->pool[g->npool++] = n;
+  *out = g;
+  return 0;
+}
+
+int or_group_order(const or_group* g) { return (int)g->P; }
+int or_group_identity(const or_group* g) { return g->id; }
+int or_group_pool(const or_group* g, int* pool) {
+  if (pool) memcpy(pool, g->pool, sizeof(int) * g->npool);
+  return g->npool;
+}
+void or_group_tables(const or_group* g, int* mult, int* inv, double* retr, double* imtr) {
+  if (mult) memcpy(mult, g->block, sizeof(int) * (size_t)g->P * g->P);
+  if (inv) memcpy(inv, g->inv, sizeof(int) * g->P);
+  if (retr) memcpy(retr, g->ReTr, sizeof(double) * g->P);
+  if (imtr) memcpy(imtr, g->ImTr, sizeof(double) * g->P);
+}
+
+/* ---------------------------------------------------------------- lattice */
+
+static void coords_of(const or_lattice* L, unsigned idx, int* pos) {
+  pos[0] = (int)(idx % L->Nt);
+  idx /= L->Nt;
+  for (unsigned d = 1; d < L->D; ++d) { pos[d] = (int)(idx % L->Nx); idx /= L->Nx; }
+}
+
+static unsigned index_of(const or_lattice* L, const int* pos) {
+  long idx = 0;
+  for (int d = (int)L->D - 1; d > 0; --d) idx = ((pos[d] + (long)L->Nx) % L->Nx) + (long)L->Nx * idx;
+  return (unsigned)(((pos[0] + (long)L->Nt) % L->Nt) + (long)L->Nt * idx);
+}
+
+void or_lattice_free(or_lattice* L) {
+  if (!L) return;
+  free(L->a); free(L->nn); free(L);
+}
+
+int or_lattice_create(const or_group* g, int D, int Nt, int Nx, or_lattice** out) {
+  *out = NULL;
+  if (D < 2 || D > 8 || Nt < 1 || Nx < 1) return -1;
+  or_lattice* L = (or_lattice*)calloc(1, sizeof *L);
+  L->g = g; L->D = (unsigned)D; L->Nt = (unsigned)Nt; L->Nx = (unsigned)Nx;
+  L->V = (unsigned)Nt;
+  for (int d = 1; d < D; ++d) L->V *= (unsigned)Nx;
+  L->a = (int*)malloc(sizeof(int) * (size_t)L->V * D);
+  L->nn = (unsigned*)malloc(sizeof(unsigned) * (size_t)L->V * 2 * D);
+  int pos[8];
+  for (unsigned i = 0; i < L->V; ++i) {
+    coords_of(L, i, pos);
+    for (int d = 0; d < D; ++d) {
+      pos[d] -= 1; L->nn[2 * D * i + 2 * d + 0] = index_of(L, pos);
+      pos[d] += 2; L->nn[2 * D * i + 2 * d + 1] = index_of(L, pos);
+      pos[d] -= 1;
+    }
+  }
+  for (size_t k = 0; k < (size_t)L->V * D; ++k) L->a[k] = g->id;
+  *out = L;
+  return 0;
+}
+
+unsigned or_lattice_volume(const or_lattice* L) { return L->V; }
+
+static inline unsigned stp(const or_lattice* L, unsigned i, unsigned d, int s) {
+  return L->nn[i * 2 * L->D + d * 2 + (s > 0)];
+}
+
+/* Links in the engine's host layout: dm[d*V + site]. */
+void or_set_links(or_lattice* L, const uint16_t* dm) {
+  for (unsigned d = 0; d < L->D; ++d)
+    for (unsigned i = 0; i < L->V; ++i) L->a[i * L->D + d] = dm[(size_t)d * L->V + i];
+}
+void or_get_links(const or_lattice* L, uint16_t* dm) {
+  for (unsigned d = 0; d < L->D; ++d)
+    for (unsigned i = 0; i < L->V; ++i) dm[(size_t)d * L->V + i] = (uint16_t)L->a[i * L->D + d];
+}
+
+/* Hot start: link (i, d) = floor(P * u), u from Philox counter (i, 0, d, HOT). */
+void or_hot_start(or_lattice* L, uint64_t seed) {
+  for (unsigned d = 0; d < L->D; ++d)
+    for (unsigned i = 0; i < L->V; ++i) {
+      dym_u32x4 c = {{i, 0u, d, DYM_TAG_HOT}};
+      dym_u32x4 r = dym_philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+      L->a[i * L->D + d] = (int)dym_pick(r.v[0], L->g->P);
+    }
+}
+
+/* ---------------------------------------------------------------- staples */
+
+/* A link term of a staple: the link at x + de*e_d + df*e_d1 in direction d
+ * (DIR_D) or d1 (DIR_F), used inverted or not.  The eight staples of one
+ * (d, d1) plane, in the reference's order: the two plaquette staples of
+ * get_staples (dym-mod-metro.cpp:68-76), then the six rectangle staples of
+ * get_rect_loops (dym-mod-metro.cpp:88-140). */
+enum { DIR_D = 0, DIR_F = 1 };
+typedef struct { int de, df, dir, inv; } term;
+static const term PLAQ[2][3] = {
+  {{1, 0, DIR_F, 0}, {0, 1, DIR_D, 1}, {0, 0, DIR_F, 1}},
+  {{1, -1, DIR_F, 1}, {0, -1, DIR_D, 1}, {0, -1, DIR_F, 0}},
+};
+static const term RECT[6][5] = {
+  {{1, 0, DIR_F, 0}, {1, 1, DIR_F, 0}, {0, 2, DIR_D, 1}, {0, 1, DIR_F, 1}, {0, 0, DIR_F, 1}},
+  {{1, 0, DIR_D, 0}, {2, 0, DIR_F, 0}, {1, 1, DIR_D, 1}, {0, 1, DIR_D, 1}, {0, 0, DIR_F, 1}},
+  {{1, 0, DIR_F, 0}, {0, 1, DIR_D, 1}, {-1, 1, DIR_D, 1}, {-1, 0, DIR_F, 1}, {-1, 0, DIR_D, 0}},
+  {{1, -1, DIR_F, 1}, {1, -2, DIR_F, 1}, {0, -2, DIR_D, 1}, {0, -2, DIR_F, 0}, {0, -1, DIR_F, 0}},
+  {{1, 0, DIR_D, 0}, {2, -1, DIR_F, 1}, {1, -1, DIR_D, 1}, {0, -1, DIR_D, 1}, {0, -1, DIR_F, 0}},
+  {{1, -1, DIR_F, 1}, {0, -1, DIR_D, 1}, {-1, -1, DIR_D, 1}, {-1, -1, DIR_F, 0}, {-1, 0, DIR_D, 0}},
+};
+
+static unsigned walk(const or_lattice* L, unsigned i, unsigned d, unsigned d1, int de, int df) {
+  for (; de > 0; --de) i = stp(L, i, d, 1);
+  for (; de < 0; ++de) i = stp(L, i, d, -1);
+  for (; df > 0; --df) i = stp(L, i, d1, 1);
+  for (; df < 0; ++df) i = stp(L, i, d1, -1);
+  return i;
+}
+
+static int fold(const or_lattice* L, unsigned i, unsigned d, unsigned d1, const term* t, int n) {
+  const or_group* g = L->g;
+  int acc = g->id;
+  for (int k = 0; k < n; ++k) {
+    unsigned s = walk(L, i, d, d1, t[k].de, t[k].df);
+    int x = L->a[s * L->D + (t[k].dir == DIR_D ? d : d1)];
+    if (t[k].inv) x = g->inv[x];
+    acc = g->mult[acc][x];
+  }
+  return acc;
+}
+
+/* st: 2(D-1) plaquette staples; re: 6(D-1) rectangle staples. */
+void or_staples(const or_lattice* L, unsigned i, unsigned d, int* st, int* re) {
+  int k = 0, kr = 0;
+  for (unsigned d1 = 0; d1 < L->D; ++d1) {
+    if (d1 == d) continue;
+    for (int p = 0; p < 2; ++p) st[k++] = fold(L, i, d, d1, PLAQ[p], 3);
+    for (int r = 0; r < 6; ++r) re[kr++] = fold(L, i, d, d1, RECT[r], 5);
+  }
+}
+
+/* Links (site, dir) read by the staples of link (i, d): out[2*k], out[2*k+1];
+ * returns the count, 16*(D-1)*... terms with repeats. */
+static int read_set(const or_lattice* L, unsigned i, unsigned d, unsigned* out) {
+  int n = 0;
+  for (unsigned d1 = 0; d1 < L->D; ++d1) {
+    if (d1 == d) continue;
+    for (int p = 0; p < 2; ++p)
+      for (int k = 0; k < 3; ++k) {
+        out[n++] = walk(L, i, d, d1, PLAQ[p][k].de, PLAQ[p][k].df);
+        out[n++] = PLAQ[p][k].dir == DIR_D ? d : d1;
+      }
+    for (int r = 0; r < 6; ++r)
+      for (int k = 0; k < 5; ++k) {
+        out[n++] = walk(L, i, d, d1, RECT[r][k].de, RECT[r][k].df);
+        out[n++] = RECT[r][k].dir == DIR_D ? d : d1;
+      }
+  }
+  return n / 2;
+}
+
+/* Pairs (x, y) in one phase where updating x reads the link updated at y
+ * (y != x), from the staple read sets above; 0 proves the schedule race-free.
+ * Also counts links not visited exactly once per sweep. */
+uint64_t or_schedule_conflicts(const or_lattice* L, const int* phase_dir, const uint32_t* phase_len,
+                               const uint32_t* sites, int nphase) {
+  const unsigned D = L->D, V = L->V;
+  int* ph = (int*)malloc(sizeof(int) * V * D);
+  int* seen = (int*)calloc((size_t)V * D, sizeof(int));
+  for (size_t k = 0; k < (size_t)V * D; ++k) ph[k] = -1;
+  size_t off = 0;
+  for (int p = 0; p < nphase; ++p) {
+    for (uint32_t k = 0; k < phase_len[p]; ++k) {
+      ph[sites[off + k] * D + phase_dir[p]] = p;
+      seen[sites[off + k] * D + phase_dir[p]]++;
+    }
+    off += phase_len[p];
+  }
+  uint64_t bad = 0;
+  unsigned rs[2 * 8 * 40];
+  off = 0;
+  for (int p = 0; p < nphase; ++p) {
+    const unsigned d = (unsigned)phase_dir[p];
+    for (uint32_t k = 0; k < phase_len[p]; ++k) {
+      const unsigned i = sites[off + k];
+      int n = read_set(L, i, d, rs);
+      for (int t = 0; t < n; ++t) {
+        unsigned s = rs[2 * t], dd = rs[2 * t + 1];
+        if (!(s == i && dd == d) && ph[s * D + dd] == p) ++bad;
+      }
+    }
+    off += phase_len[p];
+  }
+  for (size_t k = 0; k < (size_t)V * D; ++k) if (seen[k] != 1) ++bad;
+  free(ph); free(seen);
+  return bad;
+}
+
+/* ------------------------------------------------------------------ sweep */
+
+/* One multi-hit Metropolis visit of link (i, d) (dym-mod-metro.cpp:161-192).
+ * pool == NULL: proposals uniform over the group. */
+static void visit(or_lattice* L, unsigned i, unsigned d, double b0, double b1, double b2, uint64_t seed,
+                  uint32_t sweep, int nhit, const int* pool, int npool, long* hit, long* acc) {
+  const or_group* g = L->g;
+  const int ns = 2 * ((int)L->D - 1), nr = 6 * ((int)L->D - 1);
+  int st[2 * 7], re[6 * 7];
+  or_staples(L, i, d, st, re);
+  int b = L->a[i * L->D + d];
+  double r1 = 0, m1 = 0;
+  for (int j = 0; j < ns; ++j) r1 += g->ReTr[g->mult[b][st[j]]];
+  for (int k = 0; k < nr; ++k) m1 += g->ReTr[g->mult[b][re[k]]];
+  for (int h = 0; h < nhit; ++h) {
+    dym_u32x4 r = dym_hit_random(seed, sweep, i, d, (uint32_t)h, DYM_TAG_METRO);
+    /* reference: smallgroup[ smallgroup.size() * rand01 ] with truncation */
+    const double u1 = (double)r.v[0] * 0x1p-32;
+    const int gi = pool ? pool[(size_t)(npool * u1)] : (int)(size_t)(g->P * u1);
+    const int bnew = g->mult[b][gi];
+    double r1new = 0, m1new = 0;
+    for (int j = 0; j < ns; ++j) r1new += g->ReTr[g->mult[bnew][st[j]]];
+    for (int k = 0; k < nr; ++k) m1new += g->ReTr[g->mult[bnew][re[k]]];
+    double oldact = b0 + b1 * r1 + b2 * m1;
+    double newact = b0 + b1 * r1new + b2 * m1new;
+    double probrat = (newact <= oldact) ? 1.0 : dym_exp(-(newact - oldact));
+    ++*hit;
+    if (probrat > dym_u53(r.v[1], r.v[2])) {
+      L->a[i * L->D + d] = bnew;
+      b = bnew; r1 = r1new; m1 = m1new;
+      ++*acc;
+    }
+  }
+}
+
+/* nsweeps sweeps over the colour phases, sweep counters first_sweep, +1, ...
+ * pool_all != 0: proposals uniform over the group.  nthreads <= 0: OpenMP
+ * default.  counters[0] += hits, counters[1] += accepts. */
+void or_sweep(or_lattice* L, const int* phase_dir, const uint32_t* phase_len, const uint32_t* sites, int nphase,
+              double b0, double b1, double b2, uint64_t seed, uint32_t first_sweep, int nsweeps, int nhit,
+              int pool_all, uint64_t* counters, int nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+  const int* pool = pool_all ? NULL : L->g->pool;
+  const int npool = L->g->npool;
+  for (int s = 0; s < nsweeps; ++s) {
+    size_t off = 0;
+    for (int p = 0; p < nphase; ++p) {
+      const unsigned d = (unsigned)phase_dir[p];
+      const uint32_t* ps = sites + off;
+      const long n = (long)phase_len[p];
+      long lhit = 0, lacc = 0;
+#pragma omp parallel for schedule(static) reduction(+ : lhit, lacc)
+      for (long k = 0; k < n; ++k)
+        visit(L, ps[k], d, b0, b1, b2, seed, first_sweep + (uint32_t)s, nhit, pool, npool, &lhit, &lacc);
+      counters[0] += (uint64_t)lhit;
+      counters[1] += (uint64_t)lacc;
+      off += phase_len[p];
+    }
+  }
+}
+
+/* ------------------------------------------------------------ observables */
+
+static int plaq_elem(const or_lattice* L, unsigned i, unsigned d1, unsigned d2) {
+  const or_group* g = L->g;
+  int x = g->mult[g->id][L->a[i * L->D + d1]];
+  x = g->mult[x][L->a[stp(L, i, d1, 1) * L->D + d2]];
+  x = g->mult[x][g->inv[L->a[stp(L, i, d2, 1) * L->D + d1]]];
+  return g->mult[x][g->inv[L->a[i * L->D + d2]]];
+}
+
+static int wilson_elem(const or_lattice* L, unsigned i, unsigned d1, unsigned d2, int n1, int n2) {
+  const or_group* g = L->g;
+  int x = g->id;
+  for (int j = 0; j < n1; ++j) { x = g->mult[x][L->a[i * L->D + d1]]; i = stp(L, i, d1, 1); }
+  for (int j = 0; j < n2; ++j) { x = g->mult[x][L->a[i * L->D + d2]]; i = stp(L, i, d2, 1); }
+  for (int j = 0; j < n1; ++j) { i = stp(L, i, d1, -1); x = g->mult[x][g->inv[L->a[i * L->D + d1]]]; }
+  for (int j = 0; j < n2; ++j) { i = stp(L, i, d2, -1); x = g->mult[x][g->inv[L->a[i * L->D + d2]]]; }
+  return x;
+}
+
+static double dot(const uint64_t* h, const double* w, unsigned P) {
+  double s = 0;
+  for (unsigned n = 0; n < P; ++n) s += (double)h[n] * w[n];
+  return s;
+}
+
+/* out[0..3] = poly_re, poly_im, plaq, rect; out[4 + k*wl_nt + l] = Wilson
+ * loop (k+1) x (l+1) for k < wl_nx, l < wl_nt.  hist (may be NULL) receives
+ * the (3 + wl_nx*wl_nt) x P element histograms. */
+void or_measure(const or_lattice* L, int wl_nx, int wl_nt, double* out, uint64_t* hist) {
+  const or_group* g = L->g;
+  const unsigned P = g->P, D = L->D, V = L->V;
+  const size_t slots = 3 + (size_t)(wl_nx > 0 ? wl_nx : 0) * (wl_nt > 0 ? wl_nt : 0);
+  uint64_t* h = (uint64_t*)calloc(slots * P, sizeof(uint64_t));
+  int pos[8];
+  for (unsigned i = 0; i < V; ++i) {
+    for (unsigned d1 = 0; d1 < D; ++d1)
+      for (unsigned d2 = d1 + 1; d2 < D; ++d2) h[plaq_elem(L, i, d1, d2)]++;
+    for (unsigned d1 = 0; d1 < D; ++d1)
+      for (unsigned d2 = 0; d2 < D; ++d2)
+        if (d1 != d2) h[P + wilson_elem(L, i, d1, d2, 2, 1)]++;
+    coords_of(L, i, pos);
+    if (pos[0] == 0) {
+      int r = g->id;
+      unsigned s = i;
+      do { r = g->mult[r][L->a[s * D + 0]]; s = stp(L, s, 0, 1); } while (s != i);
+      h[2 * P + r]++;
+    }
+    for (int k = 0; k < wl_nx; ++k)
+      for (int l = 0; l < wl_nt; ++l)
+        for (unsigned d1 = 1; d1 < D; ++d1)
+          h[(3 + (size_t)k * wl_nt + l) * P + wilson_elem(L, i, d1, 0, k + 1, l + 1)]++;
+  }
+  out[2] = dot(h, g->ReTr, P) / (double)(V * D * (D - 1) / 2);
+  out[3] = dot(h + P, g->ReTr, P) / (double)(V * D * (D - 1));
+  out[0] = dot(h + 2 * P, g->ReTr, P) / (double)(V / L->Nt);
+  out[1] = dot(h + 2 * P, g->ImTr, P) / (double)(V / L->Nt);
+  for (int k = 0; k < wl_nx; ++k)
+    for (int l = 0; l < wl_nt; ++l)
+      out[4 + k * wl_nt + l] = dot(h + (3 + (size_t)k * wl_nt + l) * P, g->ReTr, P) / (double)(V * (D - 1));
+  if (hist) memcpy(hist, h, slots * P * sizeof(uint64_t));
+  free(h);
+}

@@ -1,0 +1,210 @@
+"""ctypes loader of the oracle (oracle/dym_oracle.c) -- test infrastructure.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module, as the checker or the timed CPU baseline; the engine never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "dym_oracle.c")
+OUT = os.path.join(HERE, "_build", "liboracle.so")
+CORE = os.path.join(os.path.dirname(HERE), "dym_symanzik_action_gb300", "csrc", "dym_core.h")
+REF_LIB = os.path.join(HERE, "_ref", "libdymref.so")
+
+
+def build() -> str:
+    os.makedirs(os.path.dirname(OUT), exist_ok=True)
+    if (not os.path.exists(OUT) or os.path.getmtime(OUT) < max(os.path.getmtime(SRC), os.path.getmtime(CORE))):
+        cmd = ["gcc", "-O2", "-std=gnu99", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-Wall",
+               SRC, "-o", OUT + ".tmp"]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if r.returncode:
+            raise RuntimeError("oracle build failed:\n" + r.stdout)
+        os.replace(OUT + ".tmp", OUT)
+    return OUT
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        l = C.CDLL(build())
+        vp, i, u32, u64, d = C.c_void_p, C.c_int, C.c_uint32, C.c_uint64, C.c_double
+        P = C.POINTER
+        sig = {
+            "or_group_load": (i, [C.c_char_p, P(vp)]),
+            "or_group_free": (None, [vp]),
+            "or_group_order": (i, [vp]),
+            "or_group_identity": (i, [vp]),
+            "or_group_pool": (i, [vp, P(C.c_int)]),
+            "or_group_tables": (None, [vp, P(C.c_int), P(C.c_int), P(d), P(d)]),
+            "or_lattice_create": (i, [vp, i, i, i, P(vp)]),
+            "or_lattice_free": (None, [vp]),
+            "or_lattice_volume": (C.c_uint, [vp]),
+            "or_set_links": (None, [vp, P(C.c_uint16)]),
+            "or_get_links": (None, [vp, P(C.c_uint16)]),
+            "or_hot_start": (None, [vp, u64]),
+            "or_staples": (None, [vp, C.c_uint, C.c_uint, P(C.c_int), P(C.c_int)]),
+            "or_schedule_conflicts": (u64, [vp, P(C.c_int), P(u32), P(u32), i]),
+            "or_sweep": (None, [vp, P(C.c_int), P(u32), P(u32), i, d, d, d, u64, u32, i, i, i, P(u64), i]),
+            "or_measure": (None, [vp, i, i, P(d), P(u64)]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(l, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = l
+    return _lib
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(C.POINTER(t))
+
+
+class OracleGroup:
+    def __init__(self, path: str):
+        h = C.c_void_p()
+        rc = lib().or_group_load(path.encode(), C.byref(h))
+        if rc:
+            raise ValueError(f"oracle: cannot load group {path} (code {rc})")
+        self.h = h
+        self.P = lib().or_group_order(h)
+        self.id = lib().or_group_identity(h)
+        pool = np.zeros(self.P, np.int32)
+        n = lib().or_group_pool(h, _p(pool, C.c_int))
+        self.pool = pool[:n].copy()
+
+    def tables(self):
+        P = self.P
+        mult = np.zeros((P, P), np.int32)
+        inv = np.zeros(P, np.int32)
+        re = np.zeros(P)
+        im = np.zeros(P)
+        lib().or_group_tables(self.h, _p(mult, C.c_int), _p(inv, C.c_int), _p(re, C.c_double), _p(im, C.c_double))
+        return mult, inv, re, im
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.or_group_free(self.h)
+            self.h = None
+
+
+class OracleLattice:
+    """Reference-layout lattice driven in the engine's colour phases."""
+
+    def __init__(self, group: OracleGroup, D: int, Nt: int, Nx: int):
+        h = C.c_void_p()
+        if lib().or_lattice_create(group.h, D, Nt, Nx, C.byref(h)):
+            raise ValueError("oracle: bad lattice shape")
+        self.h, self.group, self.D, self.Nt, self.Nx = h, group, D, Nt, Nx
+        self.V = lib().or_lattice_volume(h)
+        self.hits = 0
+        self.accepts = 0
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.or_lattice_free(self.h)
+            self.h = None
+
+    @property
+    def links(self) -> np.ndarray:
+        out = np.zeros(self.V * self.D, np.uint16)
+        lib().or_get_links(self.h, _p(out, C.c_uint16))
+        return out
+
+    @links.setter
+    def links(self, dm: np.ndarray) -> None:
+        dm = np.ascontiguousarray(dm, np.uint16)
+        assert dm.size == self.V * self.D
+        lib().or_set_links(self.h, _p(dm, C.c_uint16))
+
+    def hot_start(self, seed: int) -> None:
+        lib().or_hot_start(self.h, seed)
+
+    def staples(self, i: int, d: int):
+        st = np.zeros(2 * (self.D - 1), np.int32)
+        re = np.zeros(6 * (self.D - 1), np.int32)
+        lib().or_staples(self.h, i, d, _p(st, C.c_int), _p(re, C.c_int))
+        return st, re
+
+    def conflicts(self, sched) -> int:
+        pd, pl, sites = sched
+        return int(lib().or_schedule_conflicts(self.h, _p(pd, C.c_int), _p(pl, C.c_uint32), _p(sites, C.c_uint32),
+                                               len(pd)))
+
+    def sweep(self, sched, beta, seed, first_sweep, nsweeps, nhit, pool_all=False, nthreads=0):
+        pd, pl, sites = sched
+        ctr = np.zeros(2, np.uint64)
+        lib().or_sweep(self.h, _p(pd, C.c_int), _p(pl, C.c_uint32), _p(sites, C.c_uint32), len(pd),
+                       float(beta[0]), float(beta[1]), float(beta[2]), seed, first_sweep, nsweeps, nhit,
+                       1 if pool_all else 0, _p(ctr, C.c_uint64), nthreads)
+        self.hits += int(ctr[0])
+        self.accepts += int(ctr[1])
+        return int(ctr[0]), int(ctr[1])
+
+    def measure(self, wl_nx: int, wl_nt: int, want_hist: bool = False):
+        out = np.zeros(4 + max(wl_nx, 0) * max(wl_nt, 0))
+        hist = np.zeros((3 + max(wl_nx, 0) * max(wl_nt, 0)) * self.group.P, np.uint64) if want_hist else None
+        lib().or_measure(self.h, wl_nx, wl_nt, _p(out, C.c_double), _p(hist, C.c_uint64))
+        return (out, hist) if want_hist else out
+
+
+class RefHarness:
+    """The reference's own functions (oracle/_ref/libdymref.so, built here from
+    the reference sources by oracle/build_ref.sh); one lattice per process."""
+
+    def __init__(self):
+        if not os.path.exists(REF_LIB):
+            raise FileNotFoundError(REF_LIB)
+        l = C.CDLL(REF_LIB)
+        P = C.POINTER
+        l.refh_init.restype = C.c_int
+        l.refh_init.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int]
+        l.refh_set_links.argtypes = [P(C.c_uint16)]
+        l.refh_get_links.argtypes = [P(C.c_uint16)]
+        l.refh_staples.argtypes = [C.c_uint, C.c_uint, P(C.c_int), P(C.c_int)]
+        l.refh_sweep.argtypes = [P(C.c_int), P(C.c_uint32), P(C.c_uint32), C.c_int, C.c_double, C.c_double,
+                                 C.c_double, C.c_uint64, C.c_uint32, C.c_int, C.c_int, C.c_int, P(C.c_uint64)]
+        l.refh_measure.argtypes = [C.c_int, C.c_int, P(C.c_double)]
+        self.l = l
+
+    def init(self, path, D, Nt, Nx):
+        self.D, self.Nt, self.Nx = D, Nt, Nx
+        self.V = Nt * Nx ** (D - 1)
+        return self.l.refh_init(path.encode(), D, Nt, Nx)
+
+    def set_links(self, dm):
+        dm = np.ascontiguousarray(dm, np.uint16)
+        self.l.refh_set_links(_p(dm, C.c_uint16))
+
+    def get_links(self):
+        out = np.zeros(self.V * self.D, np.uint16)
+        self.l.refh_get_links(_p(out, C.c_uint16))
+        return out
+
+    def staples(self, i, d):
+        st = np.zeros(2 * (self.D - 1), np.int32)
+        re = np.zeros(6 * (self.D - 1), np.int32)
+        self.l.refh_staples(i, d, _p(st, C.c_int), _p(re, C.c_int))
+        return st, re
+
+    def sweep(self, sched, beta, seed, first_sweep, nsweeps, nhit, pool_all=False):
+        pd, pl, sites = sched
+        ctr = np.zeros(2, np.uint64)
+        self.l.refh_sweep(_p(pd, C.c_int), _p(pl, C.c_uint32), _p(sites, C.c_uint32), len(pd), float(beta[0]),
+                          float(beta[1]), float(beta[2]), seed, first_sweep, nsweeps, nhit, 1 if pool_all else 0,
+                          _p(ctr, C.c_uint64))
+        return int(ctr[0]), int(ctr[1])
+
+    def measure(self, wl_nx, wl_nt):
+        out = np.zeros(4 + wl_nx * wl_nt)
+        self.l.refh_measure(wl_nx, wl_nt, _p(out, C.c_double))
+        return out
