@@ -1,0 +1,307 @@
+#!/usr/bin/env python
+"""Benchmark of the discrete-group Symanzik Metropolis engine.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one GPU): a single S(1080) chain on a 32^3 x 8 lattice
+(262,144 sites, 1,048,576 uint16 links), cold start, couplings
+(beta0, beta1, beta2) = (0, 3.0, -0.15), 10 hits per link.  One step is one
+full sweep (every link visited once in the race-free colour phases).  The
+metric is link-hits/s = links * hits * sweeps / time.  Synthetic: the group
+table is generated (trace-isomorphic to the reference's mys1080-v4).
+
+Timing: W untimed sweeps, then K sweeps each timed with CUDA events on the
+chain's stream; a 256 MB buffer (> 129 MB L2) is written between sweeps so
+every step starts with the lattice and table out of L2.  `e2e` times the same
+sweep through the C ABI with the configuration copied in from and out to
+pinned host memory every step.
+
+--impl reference times the reference algorithm on the host cores (the oracle
+port, all threads) on the same workload; one step is one sweep.
+Under torchrun (N > 1) every rank runs its own replica of the chain
+(replicas only: a single chain is not sharded); value = total link-hits / the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(group="S1080", D=4, Nt=8, Nx=32, beta=(0.0, 3.0, -0.15), start="cold", nhit=10, seed=20261203)
+WORKLOAD_NAME = "single chain S(1080) 32^3x8 cold, beta=(0,3.0,-0.15), 10 hits/link, pool=nearest"
+
+
+def gathers_per_link_hit(nhit: int) -> float:
+    """Algorithmic mult-table gathers per link-hit of the reference algorithm:
+    108 per link visit (84 staple products + 24 initial traces) + 25 per hit."""
+    return 25.0 + 108.0 / nhit
+
+
+class Clocks:
+    """nvidia-smi clock/throttle samples every 200 ms while running."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_oracle_run(nsweeps: int, nthreads: int):
+    """Reference algorithm on the host (oracle port): returns (link-hits, seconds)."""
+    from dym_symanzik_action_gb300 import tables
+    from dym_symanzik_action_gb300.schedule import schedule
+    from oracle.oracle import OracleGroup, OracleLattice
+    w = WORKLOAD
+    og = OracleGroup(tables.ensure_table(w["group"]))
+    L = OracleLattice(og, w["D"], w["Nt"], w["Nx"])
+    sched = schedule(w["D"], w["Nt"], w["Nx"])
+    L.sweep(sched, w["beta"], w["seed"], 0, 1, w["nhit"], nthreads=nthreads)  # warm-up sweep
+    t0 = time.perf_counter()
+    L.sweep(sched, w["beta"], w["seed"], 1, nsweeps, w["nhit"], nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return L.V * w["D"] * w["nhit"] * nsweeps, dt
+
+
+def cpu_baseline(budget_s: float = 15.0):
+    from oracle import oracle
+    oracle.build()
+    n = os.cpu_count() or 1
+    hits1, dt1 = cpu_oracle_run(1, n)
+    ns = max(1, min(200, int(budget_s / max(dt1, 1e-3))))
+    hits, dt = cpu_oracle_run(ns, n)
+    return {"value": hits / dt, "unit": "link-hits/s", "cores": n, "kind": "port",
+            "sample": f"{ns} sweeps of the 32^3x8 cold chain ({hits:.3e} link-hits, {dt:.1f} s) with the oracle "
+                      f"port of the reference algorithm (reference data layout, OpenMP, {n} threads)"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle
+    oracle.build()
+    n = os.cpu_count() or 1
+    cpu_oracle_run(max(args.warmup, 0), n) if args.warmup else None
+    hits, dt = cpu_oracle_run(args.steps, n)
+    v = hits / dt
+    line = {"impl": "reference", "metric": "link-hits/s", "value": v, "unit": "link-hits/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD_NAME, "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": v, "unit": "link-hits/s", "cores": n, "kind": "port",
+                             "sample": f"{args.steps} sweeps of the full workload, oracle port of the reference "
+                                       f"algorithm, OpenMP {n} threads"},
+            "e2e": {"value": v, "unit": "link-hits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from dym_symanzik_action_gb300 import build as b
+    b.build()
+    import dym_symanzik_action_gb300 as dym
+    from dym_symanzik_action_gb300 import _lib, tables
+    from dym_symanzik_action_gb300._lib import check, lib, ptr
+
+    w = WORKLOAD
+    g = dym.load_group(tables.ensure_table(w["group"]))
+    lat = dym.Lattice(g, w["D"], w["Nt"], w["Nx"], *w["beta"], w["seed"] + rank, start=w["start"],
+                      precision="mixed", device=local)
+    links_per_sweep = lat.V * w["D"]
+    hits_per_step = links_per_sweep * w["nhit"]
+    nphase = len(lat.schedule()[0])
+
+    # L2 random-gather peak (roofline denominator), measured live.
+    sps = C.c_double()
+    check(lib().dym_probe_l2_gather(local, 1080 * 1080 * 2, C.byref(sps)))
+    l2_peak_gbs = sps.value * 32 / 1e9
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        lat.update(1, w["nhit"])
+    barrier()
+    dev_ms = 0.0
+    launches = 0
+    acc = 0
+    rechecks = 0
+    with Clocks(local) as clk:
+        t_wall0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)
+            torch.cuda.synchronize()
+            st = lat.update(1, w["nhit"])
+            dev_ms += st.device_ms
+            launches += st.launches
+            acc += st.accepts
+            rechecks += st.rechecks
+        barrier()
+        t_wall = time.perf_counter() - t_wall0
+    clocks = clk.summary()
+
+    # e2e: configuration in from / out to pinned host memory every step, through the C ABI.
+    n = links_per_sweep
+    host_in = torch.empty(n, dtype=torch.uint16, pin_memory=True).numpy()
+    host_out = torch.empty(n, dtype=torch.uint16, pin_memory=True).numpy()
+    host_in[:] = lat.links.ravel()
+    stt = _lib.Stats()
+    for _ in range(2):
+        check(lib().dym_links_set(lat._h, ptr(host_in, C.c_uint16)))
+        check(lib().dym_sweep(lat._h, 1, w["nhit"], C.byref(stt)))
+        check(lib().dym_links_get(lat._h, ptr(host_out, C.c_uint16)))
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        check(lib().dym_links_set(lat._h, ptr(host_in, C.c_uint16)))
+        check(lib().dym_sweep(lat._h, 1, w["nhit"], C.byref(stt)))
+        check(lib().dym_links_get(lat._h, ptr(host_out, C.c_uint16)))
+        host_in, host_out = host_out, host_in
+    barrier()
+    e2e_s = time.perf_counter() - t0
+
+    times = torch.tensor([dev_ms, e2e_s], dtype=torch.float64, device=f"cuda:{local}")
+    if world > 1:
+        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
+    dev_ms_max, e2e_max = times.tolist()
+    total_hits = hits_per_step * args.steps * world
+    value = total_hits / (dev_ms_max * 1e-3)
+    e2e_value = total_hits / e2e_max
+
+    G = gathers_per_link_hit(w["nhit"])
+    avg_launch_s = dev_ms * 1e-3 / max(launches, 1)
+    alg_bytes_per_launch = hits_per_step / nphase * G * 32
+    achieved = alg_bytes_per_launch / avg_launch_s / 1e9
+    hbm_bytes = links_per_sweep * 2 * 2  # every link read and written once per sweep
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    traffic = None
+    try:
+        traffic = json.load(open(os.path.join(ROOT, "profiles", "sweep_traffic.json"))).get("dram_bytes_per_launch")
+    except Exception:
+        pass
+
+    if rank == 0:
+        line = {
+            "metric": "link-hits/s", "value": value, "unit": "link-hits/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16/f32+f64",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD_NAME, "links": links_per_sweep, "nhit": w["nhit"],
+                       "colour_phases": nphase, "precision": "mixed (fp32 dS, fp64 recheck)",
+                       "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "l2", "achieved": achieved, "peak": l2_peak_gbs, "unit": "GB/s",
+                         "frac": achieved / l2_peak_gbs, "traffic": traffic,
+                         "peak_source": "measured live: random 2-byte L2 gathers (dym_probe_l2_gather), 32 B/sector",
+                         "algorithmic": f"{G:.1f} table gathers x 32 B per link-hit (reference algorithm)",
+                         "hbm": {"achieved": hbm_bytes / (dev_ms * 1e-3 / args.steps) / 1e9, "peak": hbm_peak,
+                                 "unit": "GB/s", "note": "compulsory link streaming, 4 B/link/sweep, of measured"}},
+            "e2e": {"value": e2e_value, "unit": "link-hits/s", "h2d_bytes_per_step": n * 2,
+                    "d2h_bytes_per_step": n * 2 + 4 * 8},
+            "gpu_launches": launches,
+            "acceptance": acc / (hits_per_step * args.steps), "recheck_fraction": rechecks / (hits_per_step * args.steps),
+            "clocks": clocks,
+            "wall_s_timed_region": t_wall,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline()
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -40,7 +40,8 @@ class ChainParams(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [("hits", C.c_uint64), ("accepts", C.c_uint64), ("rechecks", C.c_uint64),
-                ("max_ds_err", C.c_double), ("sweep", C.c_uint32)]
+                ("max_ds_err", C.c_double), ("sweep", C.c_uint32), ("launches", C.c_uint32),
+                ("device_ms", C.c_float)]
 
 
 class MeasOpts(C.Structure):
@@ -78,6 +79,7 @@ PROTOTYPES = {
     "dym_chain_staples": (C.c_int, [_P, C.c_int32, _u32p, C.c_int32, _u16p]),
     "dym_schedule_check": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _i32p, _u64p]),
     "dym_schedule_get": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _u32p, _i32p, _i32p, _u32p, _u32p]),
+    "dym_probe_l2_gather": (C.c_int, [C.c_int32, C.c_uint32, _f64p]),
 }
 
 _lib = None

@@ -26,7 +26,7 @@ LIB = os.path.join(LIBDIR, "libdymgpu.so")
 CLI = os.path.join(BINDIR, "dym-mod-metro")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["sweep.cu", "measure.cu", "capi.cu"]
+CU_SOURCES = ["sweep.cu", "measure.cu", "capi.cu", "probe.cu"]
 CXX_SOURCES = ["group.cpp", "schedule.cpp"]
 
 

@@ -164,6 +164,8 @@ static void chain_release(dym_chain* c) {
   cudaFree(c->d_meas_scratch);
   if (c->h_counters) cudaFreeHost(c->h_counters);
   if (c->h_hist) cudaFreeHost(c->h_hist);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -274,6 +276,8 @@ int dym_chain_create(const dym_group* gh, const dym_chain_params* p, dym_chain**
   ChainDev& d = c->dev;
   d.D = p->D; d.Nt = p->Nt; d.Nx = p->Nx; d.V = V;
   DYM_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  DYM_CUDA(cudaEventCreate(&c->ev0), "cudaEventCreate");
+  DYM_CUDA(cudaEventCreate(&c->ev1), "cudaEventCreate");
   DYM_CUDA(dmalloc(&d.links, (size_t)V * p->D), "cudaMalloc(links)");
   DYM_CUDA(dmalloc(&d.sites, c->sched.sites.size()), "cudaMalloc(sites)");
   DYM_CUDA(cudaMemcpy(d.sites, c->sched.sites.data(), c->sched.sites.size() * 4, cudaMemcpyHostToDevice),
@@ -323,6 +327,7 @@ int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
   FastTables ft = c->dev.fast;
   ft.eps = fast_eps(*c->grp->g, c->p.D, c->p.beta0, c->p.beta1, c->p.beta2);
   const Schedule& s = c->sched;
+  DYM_CUDA(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
   for (int k = 0; k < nsweeps; ++k) {
     a.sweep = c->sweep;
     for (size_t p = 0; p < s.phase_dir.size(); ++p) {
@@ -336,6 +341,7 @@ int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
     }
     ++c->sweep;
   }
+  DYM_CUDA(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");
   DYM_CUDA(cudaMemcpyAsync(c->h_counters, c->dev.counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                            c->stream),
            "read counters");
@@ -348,6 +354,10 @@ int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
     std::memcpy(&me, &c->h_counters[3], 8);
     out->max_ds_err = me;
     out->sweep = c->sweep;
+    out->launches = (uint32_t)(nsweeps * s.phase_dir.size());
+    float ms = 0;
+    DYM_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1), "cudaEventElapsedTime");
+    out->device_ms = ms;
   }
   return DYM_OK;
 }
@@ -457,6 +467,13 @@ int dym_chain_staples(dym_chain* c, int32_t dir, const uint32_t* sites, int32_t 
   cudaFree(d_sites);
   cudaFree(d_out);
   if (e != cudaSuccess) return cuda_fail(e, "staples");
+  return DYM_OK;
+}
+
+int dym_probe_l2_gather(int32_t device, uint32_t table_bytes, double* sectors_per_s) {
+  if (!sectors_per_s || table_bytes < 1024) return fail(DYM_EINVAL, "dym_probe_l2_gather: bad argument");
+  DYM_CUDA(cudaSetDevice(device), "cudaSetDevice");
+  DYM_CUDA(probe_l2_gather(table_bytes, sectors_per_s), "L2 gather probe");
   return DYM_OK;
 }
 

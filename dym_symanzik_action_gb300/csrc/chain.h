@@ -78,6 +78,7 @@ struct MeasArgs {
 cudaError_t launch_measure(const MeasArgs& m, int wl_nx, int wl_nt, bool assoc, unsigned long long* hist,
                            uint16_t* scratch, cudaStream_t s);
 size_t measure_scratch_elems(const MeasArgs& m, int wl_nx, int wl_nt, bool assoc);
+cudaError_t probe_l2_gather(uint32_t table_bytes, double* sectors_per_s);
 
 }  // namespace dym
 
@@ -87,6 +88,7 @@ struct dym_chain {
   dym::Schedule sched;
   dym::ChainDev dev;
   cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // device timing of sweeps
   uint32_t sweep = 0;
   unsigned long long* h_counters = nullptr;  // pinned
   // Measurement buffers (allocated on first use, sized for the largest grid).

@@ -110,6 +110,8 @@ typedef struct {
   uint64_t rechecks;    /* mixed precision: hits re-evaluated in FP64 */
   double max_ds_err;    /* mixed precision: max |dS_fp32 - dS_fp64| seen on rechecks */
   uint32_t sweep;       /* sweeps done by the chain so far */
+  uint32_t launches;    /* sweep kernels launched by this call */
+  float device_ms;      /* device time of those launches (CUDA events on the chain's stream) */
 } dym_stats;
 
 /* nsweeps full sweeps with nhit hits per link (replaces update(),
@@ -159,6 +161,12 @@ int dym_schedule_check(int32_t D, int32_t Nt, int32_t Nx, int32_t* nphase, uint6
  * dym-mod-metro.cpp:152-153), sites ascending inside a phase. */
 int dym_schedule_get(int32_t D, int32_t Nt, int32_t Nx, uint32_t* V, int32_t* nphase, int32_t* phase_dir,
                      uint32_t* phase_len, uint32_t* sites);
+
+/* Roofline probe (no reference counterpart): random 2-byte gathers from an
+ * L2-resident table of table_bytes bytes on `device`, as the sweep kernels
+ * issue them; returns the sustained gather rate in 32-byte sectors per second
+ * (one gather touches one sector). */
+int dym_probe_l2_gather(int32_t device, uint32_t table_bytes, double* sectors_per_s);
 
 #ifdef __cplusplus
 }

@@ -60,6 +60,16 @@ typedef struct {
   unsigned* nn;    /* nn[i*2D + 2d + (s>0)] */
 } or_lattice;
 
+/* ------------------------------------------- shared arithmetic (dym_core.h) */
+
+void or_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
+  dym_u32x4 c = {{ctr[0], ctr[1], ctr[2], ctr[3]}};
+  dym_u32x4 r = dym_philox4x32_10(c, key[0], key[1]);
+  memcpy(out, r.v, sizeof r.v);
+}
+double or_exp(double x) { return dym_exp(x); }
+uint32_t or_pick(uint32_t r0, uint32_t n) { return dym_pick(r0, n); }
+
 /* ------------------------------------------------------------------ group */
 
 void or_group_free(or_group* g) {

@@ -56,6 +56,9 @@ def lib() -> C.CDLL:
             "or_schedule_conflicts": (u64, [vp, P(C.c_int), P(u32), P(u32), i]),
             "or_sweep": (None, [vp, P(C.c_int), P(u32), P(u32), i, d, d, d, u64, u32, i, i, i, P(u64), i]),
             "or_measure": (None, [vp, i, i, P(d), P(u64)]),
+            "or_philox": (None, [P(u32), P(u32), P(u32)]),
+            "or_exp": (d, [d]),
+            "or_pick": (u32, [u32, u32]),
         }
         for name, (res, args) in sig.items():
             f = getattr(l, name)

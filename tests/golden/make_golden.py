@@ -1,0 +1,257 @@
+"""Generate the golden fixtures under tests/golden/ from the reference itself.
+
+Run in a container where the reference sources exist (REF_DIR, default
+/root/reference):
+
+    python tests/golden/make_golden.py
+
+It builds oracle/_ref/ (oracle/build_ref.sh) and writes:
+
+* tables_iso.npz -- for each generated table (S1080, BI, BT): an explicit
+  trace-preserving isomorphism pi onto the reference's own file
+  (mys1080-v4, myBI, myBT), the SHA-256 of the reference's Cayley table and of
+  ours, and the largest trace difference.  Tests rebuild the reference table
+  from ours through pi and compare hashes, so the reference file itself is
+  not needed at test time.
+* sweeps.npz -- configurations after every sweep, hit/accept counts and
+  observables, from the reference's get_staples/get_rect_loops/plaquette/
+  wilson/getpoly (compiled from its sources) driven by the Philox colour-phase
+  hit loop, for several groups, shapes, couplings and proposal pools.
+* staples.npz -- every staple of every link of a random S(1080) 4^4 field, by
+  the reference's get_staples and get_rect_loops.
+* chains_1sigma.npz -- GMES/RMES series of the unmodified reference
+  executable (its own table, NHIT 20, one thread) at the 4^4 couplings
+  (0, 1.5, 0.1) for several seeds: the oracle for the 1-sigma comparison.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from dym_symanzik_action_gb300 import tables  # noqa: E402
+from dym_symanzik_action_gb300.schedule import schedule  # noqa: E402
+from oracle.oracle import OracleGroup, OracleLattice, RefHarness  # noqa: E402
+
+REF_DIR = os.environ.get("REF_DIR", "/root/reference")
+REF_TABLES = {"S1080": "mys1080-v4", "BI": "myBI", "BT": "myBT"}
+
+# name: (group, D, Nt, Nx, (beta0, beta1, beta2), start, seed, nhit, pool_all, nsweeps, wl_nx, wl_nt)
+SWEEP_CASES = {
+    "s1080_4444_hot": ("S1080", 4, 4, 4, (0.0, 1.5, 0.1), "hot", 20261203, 10, False, 4, 4, 4),
+    "s1080_4444_hot_poolall": ("S1080", 4, 4, 4, (0.0, 1.5, 0.1), "hot", 7, 10, True, 3, 2, 2),
+    "s1080_4444_cold_b3": ("S1080", 4, 4, 4, (0.0, 3.0, -0.15), "cold", 11, 10, False, 3, 4, 4),
+    "s1080_2444_hot": ("S1080", 4, 2, 4, (0.0, 2.0, -0.1), "hot", 99, 10, False, 3, 4, 2),
+    "bi_4444_hot": ("BI", 4, 4, 4, (0.0, 2.0, 0.0), "hot", 5, 20, False, 3, 4, 4),
+    "bt_6666_hot": ("BT", 4, 6, 6, (0.3, 1.0, 0.2), "hot", 3, 5, False, 3, 3, 3),
+    "s1080_d3_844_hot": ("S1080", 3, 8, 4, (0.0, 2.5, -0.2), "hot", 13, 10, False, 3, 4, 8),
+    "bi_d2_88_hot": ("BI", 2, 8, 8, (0.0, 1.0, 0.5), "hot", 17, 20, False, 3, 8, 8),
+}
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a, np.int32).tobytes()).hexdigest()
+
+
+def load_text_table(path):
+    toks = open(path).read().split()
+    P = int(toks[0])
+    re_ = np.array(toks[1:1 + P], float)
+    im_ = np.array(toks[1 + P:1 + 2 * P], float)
+    m = np.array(toks[1 + 2 * P:1 + 2 * P + P * P], np.int64).reshape(P, P)
+    return P, re_, im_, m
+
+
+def find_isomorphism(mm, rm, rem, imm, rer, imr, seed=1):
+    """pi with rm[pi[x], pi[y]] == pi[mm[x, y]] and matching traces, or None."""
+    P = mm.shape[0]
+    ar = np.arange(P)
+
+    def ident(m):
+        return next(n for n in range(P) if (m[n] == ar).all() and (m[:, n] == ar).all())
+
+    def orders(m, e):
+        o = np.ones(P, int)
+        cur = ar.copy()
+        while True:
+            done = cur == e
+            if done.all():
+                return o
+            cur = np.where(done, cur, m[cur, ar])
+            o = np.where(done, o, o + 1)
+
+    em, er = ident(mm), ident(rm)
+    om, orr = orders(mm, em), orders(rm, er)
+    invr = np.argmax(rm == er, axis=1)
+    rng = np.random.default_rng(seed)
+
+    def gen_size(gs):
+        seen = {em}
+        q = [em]
+        for y in q:
+            for g in gs:
+                x = int(mm[g, y])
+                if x not in seen:
+                    seen.add(x)
+                    q.append(x)
+        return len(seen)
+
+    while True:
+        g0, g1 = (int(v) for v in rng.integers(0, P, 2))
+        if gen_size([g0, g1]) == P:
+            break
+
+    def key(re_, im_, o):
+        return (round(float(re_), 8), round(float(im_), 8), int(o))
+
+    kr = [key(rer[i], imr[i], orr[i]) for i in range(P)]
+    cand0 = [i for i in range(P) if kr[i] == key(rem[g0], imm[g0], om[g0])]
+    cand1 = [i for i in range(P) if kr[i] == key(rem[g1], imm[g1], om[g1])]
+    reps, covered = [], set()
+    for c in cand0:  # images of g0 up to conjugation in the reference group
+        if c in covered:
+            continue
+        reps.append(c)
+        covered.update(rm[rm[:, c], invr].tolist())
+    for c0 in reps:
+        for c1 in cand1:
+            pi = -np.ones(P, int)
+            pi[em] = er
+            used = np.zeros(P, bool)
+            used[er] = True
+            q = [em]
+            ok = True
+            for y in q:
+                for g, gi in ((g0, c0), (g1, c1)):
+                    x = int(mm[g, y])
+                    px = int(rm[gi, pi[y]])
+                    if pi[x] < 0:
+                        if used[px] or abs(rem[x] - rer[px]) > 1e-9 or abs(imm[x] - imr[px]) > 1e-9:
+                            ok = False
+                            break
+                        pi[x] = px
+                        used[px] = True
+                        q.append(x)
+                    elif pi[x] != px:
+                        ok = False
+                        break
+                if not ok:
+                    break
+            if ok and (pi >= 0).all() and (rm[pi[:, None], pi[None, :]] == pi[mm]).all():
+                return pi
+    return None
+
+
+def make_iso(tabdir):
+    out = {}
+    for mine, ref in REF_TABLES.items():
+        g = tables.generate(mine)
+        P, rer, imr, rm = load_text_table(os.path.join(REF_DIR, "groups", ref))
+        pi = find_isomorphism(g.mult.astype(np.int64), rm, g.retr, g.imtr, rer, imr)
+        assert pi is not None, mine
+        out[f"{mine}_pi"] = pi.astype(np.uint16)
+        out[f"{mine}_ref_sha"] = np.array(sha(rm))
+        out[f"{mine}_our_sha"] = np.array(sha(g.mult))
+        out[f"{mine}_max_dtrace"] = np.array(max(np.abs(g.retr - rer[pi]).max(), np.abs(g.imtr - imr[pi]).max()))
+        print(f"{mine}: isomorphic to {ref}, max trace difference {float(out[f'{mine}_max_dtrace']):.2e}")
+    np.savez_compressed(os.path.join(HERE, "tables_iso.npz"), **out)
+
+
+def make_sweeps(tabdir):
+    ref = RefHarness()
+    out = {}
+    for name, (gname, D, Nt, Nx, beta, start, seed, nhit, pool_all, nsw, wx, wt) in SWEEP_CASES.items():
+        path = tables.ensure_table(gname, tabdir)
+        og = OracleGroup(path)
+        ol = OracleLattice(og, D, Nt, Nx)
+        if start == "hot":
+            ol.hot_start(seed)
+        sched = schedule(D, Nt, Nx)
+        ref.init(path, D, Nt, Nx)
+        ref.set_links(ol.links)
+        links = [ref.get_links()]
+        counts = []
+        obs = []
+        for s in range(nsw):
+            counts.append(ref.sweep(sched, beta, seed, s, 1, nhit, pool_all))
+            links.append(ref.get_links())
+            obs.append(ref.measure(wx, wt))
+        out[name + "_links"] = np.stack(links)
+        out[name + "_counts"] = np.array(counts, np.uint64)
+        out[name + "_obs"] = np.stack(obs)
+        out[name + "_sched_dir"] = sched[0]
+        out[name + "_sched_len"] = sched[1]
+        out[name + "_sched_sites"] = sched[2]
+        acc = np.array(counts)[:, 1].sum() / max(np.array(counts)[:, 0].sum(), 1)
+        print(f"{name}: {nsw} sweeps, acceptance {acc:.3f}")
+    out["cases"] = np.array(repr(SWEEP_CASES))
+    np.savez_compressed(os.path.join(HERE, "sweeps.npz"), **out)
+
+
+def make_staples(tabdir):
+    ref = RefHarness()
+    path = tables.ensure_table("S1080", tabdir)
+    og = OracleGroup(path)
+    ol = OracleLattice(og, 4, 4, 4)
+    ol.hot_start(424242)
+    ref.init(path, 4, 4, 4)
+    ref.set_links(ol.links)
+    st = np.zeros((4, ol.V, 24), np.uint16)
+    for d in range(4):
+        for i in range(ol.V):
+            a, b = ref.staples(i, d)
+            st[d, i] = np.concatenate([a, b])
+    np.savez_compressed(os.path.join(HERE, "staples.npz"), links=ol.links, staples=st, seed=np.array(424242))
+    print("staples: 4^4 S1080, 1024 links x 24 staples")
+
+
+def parse_log(text):
+    gmes = [list(map(float, l.split()[1:])) for l in text.splitlines() if l.startswith("GMES:")]
+    rmes = [list(map(float, l.split()[1:])) for l in text.splitlines() if l.startswith("RMES:")]
+    acc = [float(l.split()[1]) for l in text.splitlines() if l.startswith("ACC:")]
+    return np.array(gmes), np.array(rmes), np.array(acc)
+
+
+def make_chains():
+    exe = os.path.join(ROOT, "oracle", "_ref", "dym-mod-metro")
+    table = os.path.join(REF_DIR, "groups", "mys1080-v4")
+    seeds = [101, 202, 303, 404, 505, 606]
+    out = {}
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    with tempfile.TemporaryDirectory() as td:  # the -pg build writes gmon.out into its cwd
+        for s in seeds:
+            r = subprocess.run([exe, table, "4", "4", "4", "0", "1.5", "0.1", str(s), "10", "100", "100"],
+                               cwd=td, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
+                               check=True)
+            g, rm, acc = parse_log(r.stdout)
+            out[f"gmes_{s}"] = g
+            out[f"rmes_{s}"] = rm
+            out[f"acc_{s}"] = acc
+            print(f"reference chain seed {s}: {len(g)} measurements, <plaq> {g[:, 3].mean():.4f}, "
+                  f"acceptance {acc[-1]:.3f}")
+    out["params"] = np.array("mys1080-v4 D=4 Nt=4 Nx=4 beta=(0,1.5,0.1) K=10 N=100 Ntherm=100 NHIT=20 hot")
+    out["seeds"] = np.array(seeds)
+    np.savez_compressed(os.path.join(HERE, "chains_1sigma.npz"), **out)
+
+
+def main():
+    subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True,
+                   env=dict(os.environ, REF_DIR=REF_DIR), stdout=subprocess.DEVNULL)
+    with tempfile.TemporaryDirectory() as tabdir:
+        make_iso(tabdir)
+        make_staples(tabdir)
+        make_sweeps(tabdir)
+    make_chains()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,131 @@
+"""GPU parity: the CUDA sweep and observables against the reference fixtures
+and the oracle.
+
+Bar: link configurations and hit/accept counts bit-exact after every sweep;
+observables bit-exact against the oracle's histogram sums and within 1e-12
+of the reference's site-order sums.  Both accept paths are covered: FP64
+(every decision as the reference) and mixed (FP32 dS with FP64 re-evaluation
+near the threshold), which must give identical configurations."""
+import numpy as np
+import pytest
+
+from conftest import golden, sweep_cases
+from dym_symanzik_action_gb300 import tables
+from dym_symanzik_action_gb300.schedule import schedule
+from oracle.oracle import OracleGroup, OracleLattice
+
+pytestmark = pytest.mark.gpu
+
+_groups = {}
+
+
+def group(engine, name):
+    if name not in _groups:
+        _groups[name] = engine.load_group(tables.ensure_table(name))
+    return _groups[name]
+
+
+def test_staples_match_reference(engine):
+    g = golden("staples.npz")
+    lat = engine.Lattice(group(engine, "S1080"), 4, 4, 4, 0, 1.5, 0.1, 1)
+    lat.links = g["links"].reshape(4, -1)
+    for d in range(4):
+        st = lat.staples(d, np.arange(lat.V))
+        assert (st == g["staples"][d]).all(), d
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", list(sweep_cases().keys()))
+def test_sweeps_match_reference(engine, sweeps_golden, name, precision):
+    gname, D, Nt, Nx, beta, start, seed, nhit, pool_all, nsw, wx, wt = sweep_cases()[name]
+    gold = sweeps_golden
+    lat = engine.Lattice(group(engine, gname), D, Nt, Nx, *beta, seed, start=start,
+                         pool="all" if pool_all else "nearest", precision=precision)
+    pd, pl, sites = lat.schedule()
+    assert (pd == gold[name + "_sched_dir"]).all() and (pl == gold[name + "_sched_len"]).all()
+    assert (sites == gold[name + "_sched_sites"]).all()
+    assert (lat.links.ravel() == gold[name + "_links"][0]).all()
+    og = OracleGroup(tables.ensure_table(gname))
+    ol = OracleLattice(og, D, Nt, Nx)
+    for s in range(nsw):
+        st = lat.update(1, nhit)
+        assert (st.hits, st.accepts) == tuple(int(x) for x in gold[name + "_counts"][s])
+        assert (lat.links.ravel() == gold[name + "_links"][s + 1]).all(), f"sweep {s}"
+        m = lat.measure(wx, wt)
+        got = np.concatenate([[m.poly_re, m.poly_im, m.plaq, m.rect], m.wloop.ravel()])
+        np.testing.assert_allclose(got, gold[name + "_obs"][s], rtol=0, atol=1e-12)
+        ol.links = lat.links.ravel()
+        assert (got == ol.measure(wx, wt)).all()
+
+
+CASES = [
+    # group, D, Nt, Nx, beta, start, pool, nhit, sweeps
+    ("S1080", 4, 8, 8, (0.0, 1.5, 0.1), "hot", "nearest", 10, 2),
+    ("S1080", 4, 8, 8, (0.0, 3.0, -0.15), "cold", "nearest", 10, 3),
+    ("S1080", 4, 12, 8, (0.2, 2.0, -0.1), "hot", "all", 7, 2),
+    ("BI", 4, 6, 6, (0.0, 3.0, 0.2), "hot", "nearest", 20, 2),
+    ("BI", 4, 2, 12, (0.0, 1.0, -0.3), "hot", "nearest", 10, 2),
+    ("BT", 3, 5, 5, (0.0, 2.0, 0.5), "hot", "nearest", 10, 2),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}-D{c[1]}-{c[2]}x{c[3]}-{c[5]}-{c[6]}" for c in CASES])
+def test_random_configs_match_oracle(engine, case):
+    gname, D, Nt, Nx, beta, start, pool, nhit, nsw = case
+    seed = 1000 + Nt * 7 + Nx
+    og = OracleGroup(tables.ensure_table(gname))
+    sched = schedule(D, Nt, Nx)
+    for precision in ("fp64", "mixed"):
+        lat = engine.Lattice(group(engine, gname), D, Nt, Nx, *beta, seed, start=start, pool=pool,
+                             precision=precision)
+        ol = OracleLattice(og, D, Nt, Nx)
+        ol.links = lat.links.ravel()
+        for s in range(nsw):
+            st = lat.update(1, nhit)
+            h, a = ol.sweep(sched, beta, seed, s, 1, nhit, pool == "all")
+            assert (st.hits, st.accepts) == (h, a)
+            assert (lat.links.ravel() == ol.links).all(), (precision, s)
+
+
+def test_full_size_cold_chain_matches_oracle(engine):
+    """32^3 x 8 (1,048,576 links), cold start at beta = (0, 3, -0.15), NHIT 10:
+    two sweeps bit-exact against the oracle, both accept paths."""
+    D, Nt, Nx, beta, nhit = 4, 8, 32, (0.0, 3.0, -0.15), 10
+    og = OracleGroup(tables.ensure_table("S1080"))
+    sched = schedule(D, Nt, Nx)
+    ol = OracleLattice(og, D, Nt, Nx)
+    res = {}
+    for precision in ("mixed", "fp64"):
+        lat = engine.Lattice(group(engine, "S1080"), D, Nt, Nx, *beta, 20261203, start="cold", precision=precision)
+        st = lat.update(2, nhit)
+        assert st.hits == lat.V * D * nhit * 2
+        res[precision] = (lat.links.ravel(), st.accepts)
+    assert (res["mixed"][0] == res["fp64"][0]).all() and res["mixed"][1] == res["fp64"][1]
+    h, a = ol.sweep(sched, beta, 20261203, 0, 2, nhit)
+    assert a == res["fp64"][1]
+    assert (ol.links == res["fp64"][0]).all()
+
+
+def test_full_size_hot_chain_matches_oracle(engine):
+    D, Nt, Nx, beta, nhit = 4, 8, 32, (0.0, 3.0, -0.15), 10
+    og = OracleGroup(tables.ensure_table("S1080"))
+    lat = engine.Lattice(group(engine, "S1080"), D, Nt, Nx, *beta, 77, start="hot", precision="mixed")
+    ol = OracleLattice(og, D, Nt, Nx)
+    ol.hot_start(77)
+    assert (ol.links == lat.links.ravel()).all()
+    st = lat.update(1, nhit)
+    h, a = ol.sweep(schedule(D, Nt, Nx), beta, 77, 0, 1, nhit)
+    assert (st.hits, st.accepts) == (h, a)
+    assert (ol.links == lat.links.ravel()).all()
+    m = lat.measure(4, 4)
+    ol_obs = ol.measure(4, 4)
+    got = np.concatenate([[m.poly_re, m.poly_im, m.plaq, m.rect], m.wloop.ravel()])
+    assert (got == ol_obs).all()
+
+
+def test_mixed_precision_reports_rechecks(engine):
+    lat = engine.Lattice(group(engine, "S1080"), 4, 8, 8, 0.0, 1.5, 0.1, 3, precision="mixed")
+    st = lat.update(3, 10)
+    assert st.hits == lat.V * 4 * 10 * 3
+    assert 0 < st.rechecks < st.hits
+    assert 0 <= st.max_ds_err < 1e-3
