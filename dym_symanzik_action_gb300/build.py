@@ -26,7 +26,12 @@ LIB = os.path.join(LIBDIR, "libdymgpu.so")
 CLI = os.path.join(BINDIR, "dym-mod-metro")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["sweep.cu", "measure.cu", "capi.cu", "probe.cu"]
+# DYM_BOUNDS_CHECK=1 builds the self-checking kernels (every index checked,
+# first bad one reported by dym_sweep) into a separate object directory.
+BOUNDS = os.environ.get("DYM_BOUNDS_CHECK") == "1"
+if BOUNDS:
+    OBJDIR = os.path.join(PKG, "_build_bounds")
+CU_SOURCES = ["sweep.cu", "measure.cu", "capi.cu", "probe.cu", "llr.cu"]
 CXX_SOURCES = ["group.cpp", "schedule.cpp"]
 
 
@@ -72,6 +77,7 @@ def build(verbose: bool = False) -> str:
         if _stale(o, [s] + hdrs):
             jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                          "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr", *inc,
+                         *(["-DDYM_BOUNDS_CHECK"] if BOUNDS else []),
                          "-c", s, "-o", o])
     for src in CXX_SOURCES:
         s = os.path.join(CSRC, src)
@@ -85,8 +91,13 @@ def build(verbose: bool = False) -> str:
             if verbose:
                 print(" ".join(cmd), flush=True)
         list(ex.map(_run, jobs))
-    if jobs or not os.path.exists(LIB):
+    flavor_file = LIB + ".flavor"
+    flavor = "bounds" if BOUNDS else "release"
+    old_flavor = open(flavor_file).read() if os.path.exists(flavor_file) else ""
+    if jobs or not os.path.exists(LIB) or old_flavor != flavor:
         _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs])
+        with open(flavor_file, "w") as f:
+            f.write(flavor)
     cli_src = os.path.join(CSRC, "dym_mod_metro.cpp")
     if os.path.exists(cli_src) and (_stale(CLI, [cli_src, LIB] + hdrs)):
         _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", *inc, cli_src, "-o", CLI,

@@ -47,12 +47,17 @@ int group_to_device(Group* g) {
   DYM_CUDA(dmalloc((double**)&g->d_retr, P), "cudaMalloc(retr)");
   DYM_CUDA(dmalloc((double**)&g->d_imtr, P), "cudaMalloc(imtr)");
   DYM_CUDA(dmalloc((uint8_t**)&g->d_cls, P), "cudaMalloc(cls)");
+  DYM_CUDA(dmalloc((uint16_t**)&g->d_cls16, P), "cudaMalloc(cls16)");
   DYM_CUDA(dmalloc((double**)&g->d_clsval, std::max(g->ncls, 1)), "cudaMalloc(clsval)");
   DYM_CUDA(cudaMemcpy(g->d_mult, g->mult.data(), P * P * 2, cudaMemcpyHostToDevice), "upload mult");
   DYM_CUDA(cudaMemcpy(g->d_inv, g->inv.data(), P * 2, cudaMemcpyHostToDevice), "upload inv");
   DYM_CUDA(cudaMemcpy(g->d_retr, g->retr.data(), P * 8, cudaMemcpyHostToDevice), "upload retr");
   DYM_CUDA(cudaMemcpy(g->d_imtr, g->imtr.data(), P * 8, cudaMemcpyHostToDevice), "upload imtr");
   DYM_CUDA(cudaMemcpy(g->d_cls, g->cls.data(), P, cudaMemcpyHostToDevice), "upload cls");
+  {
+    std::vector<uint16_t> c16(g->cls.begin(), g->cls.end());
+    DYM_CUDA(cudaMemcpy(g->d_cls16, c16.data(), P * 2, cudaMemcpyHostToDevice), "upload cls16");
+  }
   DYM_CUDA(cudaMemcpy(g->d_clsval, g->cls_val.data(), g->ncls * 8, cudaMemcpyHostToDevice), "upload clsval");
   g->device = dev;
   return DYM_OK;
@@ -69,62 +74,32 @@ void group_free(Group* g) {
     cudaFree(g->d_retr);
     cudaFree(g->d_imtr);
     cudaFree(g->d_cls);
+    cudaFree(g->d_cls16);
     cudaFree(g->d_clsval);
     cudaSetDevice(cur);
   }
   delete g;
 }
 
-static int bits_for(uint32_t n) {  // bits to hold values 0..n-1
-  int b = 0;
-  while ((1u << b) < n) ++b;
-  return std::max(b, 1);
-}
-
-// Whether the shared sub-table kernel applies to this group and pool size.
-static bool fast_eligible(const Group& g, uint32_t npool, int device) {
-  if (!g.assoc_ok || !g.cls_conj_invariant || g.ncls > 255) return false;
-  if (bits_for(g.P) + bits_for((uint32_t)g.ncls) > 16) return false;
+// Whether the shared sub-table kernel applies: the table is associative,
+// ReTr is one double per conjugacy class (so ReTr[u_j g] == ReTr[bnew s_j]
+// bit for bit), and the sub-table fits the shared-memory opt-in.
+static bool sub_eligible(const Group& g, uint32_t npool, int device) {
+  if (!g.assoc_ok || !g.cls_conj_invariant || !g.cls_exact) return false;
   int optin = 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) return false;
-  return fast_smem_bytes(g.P, npool, g.ncls) <= (size_t)optin;
+  return sub_smem_bytes(g.P, npool) <= (size_t)optin;
 }
 
-// Bound on |dS_fp32 - dS_fp64| for the fast kernel (see k_sweep_fast).
-static double fast_eps(const Group& g, int D, double b0, double b1, double b2) {
-  const double R = g.max_abs_retr, sig = g.cls_spread;
-  const double u32 = std::ldexp(1.0, -24), u64 = std::ldexp(1.0, -53);
-  const double n1 = 2.0 * (D - 1), n2 = 6.0 * (D - 1);
-  auto part = [&](double n) { return 2 * n * (R * u32 + sig) + 2 * n * n * R * u32 + 6 * n * R * u32; };
-  const double A = std::fabs(b0) + std::fabs(b1) * n1 * R + std::fabs(b2) * n2 * R;
-  return 4.0 * (std::fabs(b1) * part(n1) + std::fabs(b2) * part(n2)) + 16.0 * A * n2 * u64 + 1e-30;
-}
-
-static int build_fast_tables(dym_chain* c) {
+static int build_sub_table(dym_chain* c, const std::vector<uint16_t>& pool) {
   const Group& g = *c->grp->g;
-  const uint32_t P = g.P, np = c->dev.npool;
-  const int shift = bits_for(P);
+  const uint32_t P = g.P, np = (uint32_t)pool.size();
   std::vector<uint16_t> sub((size_t)np * P);
-  std::vector<uint16_t> pool(np);
-  DYM_CUDA(cudaMemcpy(pool.data(), c->dev.pool, np * 2, cudaMemcpyDeviceToHost), "download pool");
   for (uint32_t k = 0; k < np; ++k)
-    for (uint32_t u = 0; u < P; ++u) {
-      const uint32_t p = g.mult[(size_t)u * P + pool[k]];
-      sub[(size_t)k * P + u] = (uint16_t)(p | ((uint32_t)g.cls[p] << shift));
-    }
-  std::vector<float> v32(g.ncls);
-  for (int i = 0; i < g.ncls; ++i) v32[i] = (float)g.cls_val[i];
-  FastTables& ft = c->dev.fast;
-  DYM_CUDA(dmalloc(&ft.sub, sub.size()), "cudaMalloc(sub)");
-  DYM_CUDA(dmalloc(&ft.cls_val32, g.ncls), "cudaMalloc(cv32)");
-  DYM_CUDA(cudaMemcpy(ft.sub, sub.data(), sub.size() * 2, cudaMemcpyHostToDevice), "upload sub");
-  DYM_CUDA(cudaMemcpy(ft.cls_val32, v32.data(), g.ncls * 4, cudaMemcpyHostToDevice), "upload cv32");
-  ft.cls = (uint8_t*)g.d_cls;
-  ft.cls_val64 = (double*)g.d_clsval;
-  ft.ncls = g.ncls;
-  ft.shift = shift;
-  ft.exact = g.cls_exact ? 1 : 0;
-  c->dev.fast_ok = true;
+    for (uint32_t u = 0; u < P; ++u) sub[(size_t)k * P + u] = g.mult[(size_t)u * P + pool[k]];
+  DYM_CUDA(dmalloc(&c->dev.sub, sub.size()), "cudaMalloc(sub)");
+  DYM_CUDA(cudaMemcpy(c->dev.sub, sub.data(), sub.size() * 2, cudaMemcpyHostToDevice), "upload sub");
+  c->dev.sub_ok = true;
   return DYM_OK;
 }
 
@@ -147,6 +122,9 @@ static SweepArgs sweep_args(dym_chain* c) {
   a.beta2 = c->p.beta2;
   a.seed = c->p.seed;
   a.counters = c->dev.counters;
+#ifdef DYM_BOUNDS_CHECK
+  a.status = c->dev.counters + 4;
+#endif
   return a;
 }
 
@@ -158,10 +136,11 @@ static void chain_release(dym_chain* c) {
   cudaFree(c->dev.sites);
   cudaFree(c->dev.pool);
   cudaFree(c->dev.counters);
-  cudaFree(c->dev.fast.sub);
-  cudaFree(c->dev.fast.cls_val32);
+  cudaFree(c->dev.sub);
   cudaFree(c->d_hist);
   cudaFree(c->d_meas_scratch);
+  cudaFree(c->d_llr);
+  cudaFree(c->d_oldv);
   if (c->h_counters) cudaFreeHost(c->h_counters);
   if (c->h_hist) cudaFreeHost(c->h_hist);
   if (c->ev0) cudaEventDestroy(c->ev0);
@@ -211,7 +190,7 @@ int dym_group_get_info(const dym_group* gh, dym_group_info* out) {
   out->fast_path = 0;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0)
-    out->fast_path = fast_eligible(g, (uint32_t)g.pool_nearest.size(), dev) ? 1 : 0;
+    out->fast_path = sub_eligible(g, (uint32_t)g.pool_nearest.size(), dev) ? 1 : 0;
   else
     cudaGetLastError();
   out->class_spread = g.cls_spread;
@@ -288,11 +267,11 @@ int dym_chain_create(const dym_group* gh, const dym_chain_params* p, dym_chain**
   d.npool = (uint32_t)pool.size();
   DYM_CUDA(dmalloc(&d.pool, pool.size()), "cudaMalloc(pool)");
   DYM_CUDA(cudaMemcpy(d.pool, pool.data(), pool.size() * 2, cudaMemcpyHostToDevice), "upload pool");
-  DYM_CUDA(dmalloc(&d.counters, 4), "cudaMalloc(counters)");
-  DYM_CUDA(cudaHostAlloc((void**)&c->h_counters, 4 * sizeof(unsigned long long), cudaHostAllocDefault),
+  DYM_CUDA(dmalloc(&d.counters, 5), "cudaMalloc(counters)");
+  DYM_CUDA(cudaHostAlloc((void**)&c->h_counters, 5 * sizeof(unsigned long long), cudaHostAllocDefault),
            "cudaHostAlloc");
-  if (p->precision == DYM_PREC_MIXED && fast_eligible(g, d.npool, p->device)) {
-    rc = build_fast_tables(c.get());
+  if (p->precision == DYM_PREC_MIXED && sub_eligible(g, d.npool, p->device)) {
+    rc = build_sub_table(c.get(), pool);
     if (rc) return rc;
   }
   if (p->start == DYM_START_HOT)
@@ -321,11 +300,9 @@ int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
   if (!c) return fail(DYM_EINVAL, "dym_sweep: null chain");
   if (nsweeps < 0 || nhit < 0 || nhit > (1 << 20)) return fail(DYM_EINVAL, "dym_sweep: bad nsweeps or nhit");
   DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
-  DYM_CUDA(cudaMemsetAsync(c->dev.counters, 0, 4 * sizeof(unsigned long long), c->stream), "reset counters");
+  DYM_CUDA(cudaMemsetAsync(c->dev.counters, 0, 5 * sizeof(unsigned long long), c->stream), "reset counters");
   SweepArgs a = sweep_args(c);
   a.nhit = nhit;
-  FastTables ft = c->dev.fast;
-  ft.eps = fast_eps(*c->grp->g, c->p.D, c->p.beta0, c->p.beta1, c->p.beta2);
   const Schedule& s = c->sched;
   DYM_CUDA(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
   for (int k = 0; k < nsweeps; ++k) {
@@ -333,25 +310,27 @@ int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
     for (size_t p = 0; p < s.phase_dir.size(); ++p) {
       a.sites = c->dev.sites + s.phase_off[p];
       a.n = s.phase_len[p];
-      cudaError_t e = c->dev.fast_ok
-                          ? launch_sweep_fast(c->p.D, s.phase_dir[p], a, ft, (double*)(c->dev.counters + 3),
-                                              c->stream)
-                          : launch_sweep_direct(c->p.D, s.phase_dir[p], a, c->stream);
+      cudaError_t e = c->dev.sub_ok ? launch_sweep_sub(c->p.D, s.phase_dir[p], a, c->dev.sub, c->stream)
+                                    : launch_sweep_direct(c->p.D, s.phase_dir[p], a, c->stream);
       if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
     }
     ++c->sweep;
   }
   DYM_CUDA(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");
-  DYM_CUDA(cudaMemcpyAsync(c->h_counters, c->dev.counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+  DYM_CUDA(cudaMemcpyAsync(c->h_counters, c->dev.counters, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                            c->stream),
            "read counters");
   DYM_CUDA(cudaStreamSynchronize(c->stream), "sweep");
+  if (c->h_counters[4])
+    return fail(DYM_ECUDA, "bounds check: code " + std::to_string(c->h_counters[4] >> 32) + " value " +
+                               std::to_string(c->h_counters[4] & 0xFFFFFFFFull));
   if (out) {
     out->hits = c->h_counters[0];
     out->accepts = c->h_counters[1];
     out->rechecks = c->h_counters[2];
-    double me;
-    std::memcpy(&me, &c->h_counters[3], 8);
+    float me;  // FP32 bits in the low word of counter 3
+    const uint32_t bits = (uint32_t)(c->h_counters[3] & 0xFFFFFFFFull);
+    std::memcpy(&me, &bits, 4);
     out->max_ds_err = me;
     out->sweep = c->sweep;
     out->launches = (uint32_t)(nsweeps * s.phase_dir.size());
@@ -467,6 +446,136 @@ int dym_chain_staples(dym_chain* c, int32_t dir, const uint32_t* sites, int32_t 
   cudaFree(d_sites);
   cudaFree(d_out);
   if (e != cudaSuccess) return cuda_fail(e, "staples");
+  return DYM_OK;
+}
+
+// Element histograms of all plaquettes (slot 0) and oriented 1x2 rectangles
+// (slot 1) of the current configuration, folded into ReTr classes.
+static int class_histograms(dym_chain* c, long long h[2][kLlrMaxCls]) {
+  const Group& g = *c->grp->g;
+  dym_meas_opts mo{-1, -1};
+  dym_obs o;
+  int rc = dym_measure(c, &mo, &o, nullptr);
+  if (rc) return rc;
+  for (int k = 0; k < 2; ++k)
+    for (int q = 0; q < kLlrMaxCls; ++q) h[k][q] = 0;
+  for (uint32_t n = 0; n < g.P; ++n) {
+    h[0][g.cls[n]] += (long long)c->h_hist[n];
+    h[1][g.cls[n]] += (long long)c->h_hist[g.P + n];
+  }
+  return DYM_OK;
+}
+
+static double class_sum_host(const long long* h, const std::vector<double>& v, int ncls) {
+  double s = 0;
+  for (int q = 0; q < ncls; ++q) s = s + (double)h[q] * v[q];
+  return s;
+}
+
+int dym_llr_energy(dym_chain* c, double* S1, double* S2) {
+  if (!c) return fail(DYM_EINVAL, "dym_llr_energy: null chain");
+  const Group& g = *c->grp->g;
+  if (g.ncls > kLlrMaxCls || !g.cls_conj_invariant)
+    return fail(DYM_ENOTSUP, "LLR needs a table whose ReTr takes at most 32 class values");
+  long long h[2][kLlrMaxCls];
+  int rc = class_histograms(c, h);
+  if (rc) return rc;
+  if (S1) *S1 = class_sum_host(h[0], g.cls_val, g.ncls);
+  if (S2) *S2 = class_sum_host(h[1], g.cls_val, g.ncls);
+  return DYM_OK;
+}
+
+int dym_llr_run(dym_chain* c, const dym_llr_req* req, dym_llr_result* out, double* a_hist) {
+  if (!c || !req || !out) return fail(DYM_EINVAL, "dym_llr_run: null argument");
+  const Group& g = *c->grp->g;
+  if (req->axis != 1 && req->axis != 2) return fail(DYM_EINVAL, "axis must be 1 (S1 window) or 2 (S2 window)");
+  if (req->K < 1 || req->NRM < 0 || req->NRM > DYM_LLR_MAX_NRM || req->nhit < 0 || !(req->hw > 0) ||
+      req->drive_cap < 0)
+    return fail(DYM_EINVAL, "dym_llr_run: bad K, NRM, nhit, hw or drive_cap");
+  if (g.ncls > kLlrMaxCls || !g.cls_conj_invariant)
+    return fail(DYM_ENOTSUP, "LLR needs a table whose ReTr takes at most 32 class values");
+  if (req->axis == 2 && (c->p.Nt < 3 || c->p.Nx < 3))
+    return fail(DYM_ENOTSUP, "an S2 window needs every extent >= 3 (1x2 rectangles wrap otherwise)");
+  if (c->p.pool != DYM_POOL_NEAREST) return fail(DYM_ENOTSUP, "LLR proposals use the nearest-element pool");
+  DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+  if (!c->d_llr) {
+    DYM_CUDA(dmalloc(&c->d_llr, 1), "cudaMalloc(llr)");
+    uint32_t maxlen = 1;
+    for (auto l : c->sched.phase_len) maxlen = std::max(maxlen, l);
+    DYM_CUDA(dmalloc(&c->d_oldv, maxlen), "cudaMalloc(llr oldv)");
+  }
+  std::unique_ptr<LlrState> st(new LlrState());
+  std::memset(st.get(), 0, sizeof(LlrState));
+  int rc = class_histograms(c, st->h);
+  if (rc) return rc;
+  const double W = 2 * req->hw;
+  st->a = req->a0;
+  st->bg = req->bg;
+  st->ewin = req->ewin;
+  st->elo = req->ewin - req->hw;
+  st->ehi = req->ewin + req->hw;
+  st->emid = 0.5 * (st->elo + st->ehi);
+  st->w2 = W * W;
+  st->q = 1.0;
+  st->ncls = g.ncls;
+  for (int q = 0; q < g.ncls; ++q) st->v[q] = g.cls_val[q];
+  st->E[0] = class_sum_host(st->h[0], g.cls_val, g.ncls);
+  st->E[1] = class_sum_host(st->h[1], g.cls_val, g.ncls);
+  st->axis = req->axis;
+  st->K = req->K;
+  st->NRM = req->NRM;
+  st->drive_cap = req->drive_cap;
+  const double Ew = st->E[req->axis - 1];
+  st->mode = (Ew >= st->elo && Ew <= st->ehi) ? DYM_LLR_RM : DYM_LLR_DRIVE;
+  if (req->NRM == 0 && st->mode == DYM_LLR_RM) st->mode = DYM_LLR_DONE;
+  if (st->mode == DYM_LLR_DRIVE && req->drive_cap == 0) st->mode = DYM_LLR_UNREACHED;
+  DYM_CUDA(cudaMemcpyAsync(c->d_llr, st.get(), sizeof(LlrState), cudaMemcpyHostToDevice, c->stream), "upload llr");
+  DYM_CUDA(cudaMemsetAsync(c->dev.counters, 0, 5 * sizeof(unsigned long long), c->stream), "reset counters");
+  LlrArgs A{};
+  A.s = sweep_args(c);
+  A.s.nhit = req->nhit;
+  A.cls16 = (const uint16_t*)g.d_cls16;
+  A.st = c->d_llr;
+  A.oldv = c->d_oldv;
+  const Schedule& s = c->sched;
+  const long max_sweeps = (long)req->drive_cap + (long)req->K * req->NRM + 2;
+  int mode = st->mode;
+  long sweeps = 0;
+  while (mode < DYM_LLR_DONE && sweeps < max_sweeps) {
+    for (int chunk = 0; chunk < 8 && sweeps < max_sweeps; ++chunk, ++sweeps) {
+      A.s.sweep = c->sweep;
+      for (size_t p = 0; p < s.phase_dir.size(); ++p) {
+        A.s.sites = c->dev.sites + s.phase_off[p];
+        A.s.n = s.phase_len[p];
+        A.dir = s.phase_dir[p];
+        A.buf = (int)(c->llr_phase++ & 1);
+        cudaError_t e = launch_llr_phase(c->p.D, A, p + 1 == s.phase_dir.size(), c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "llr launch");
+      }
+      ++c->sweep;
+    }
+    DYM_CUDA(cudaMemcpyAsync(&st->mode, &c->d_llr->mode, sizeof(int), cudaMemcpyDeviceToHost, c->stream),
+             "read llr mode");
+    DYM_CUDA(cudaStreamSynchronize(c->stream), "llr sweeps");
+    mode = st->mode;
+  }
+  DYM_CUDA(cudaMemcpyAsync(st.get(), c->d_llr, sizeof(LlrState), cudaMemcpyDeviceToHost, c->stream), "read llr");
+  DYM_CUDA(cudaMemcpyAsync(c->h_counters, c->dev.counters, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                           c->stream),
+           "read counters");
+  DYM_CUDA(cudaStreamSynchronize(c->stream), "llr");
+  out->a = st->a;
+  out->S1 = st->E[0];
+  out->S2 = st->E[1];
+  out->status = st->mode;
+  out->drive_sweeps = st->drive_sweeps;
+  out->sweeps = (int32_t)sweeps;
+  out->hits = c->h_counters[0];
+  out->accepts = c->h_counters[1];
+  out->phase_accepts = st->phase_acc;
+  out->phase_rejects = st->phase_rej;
+  if (a_hist)
+    for (int m = 0; m < req->NRM; ++m) a_hist[m] = st->a_hist[m];
   return DYM_OK;
 }
 

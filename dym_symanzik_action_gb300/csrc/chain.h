@@ -28,18 +28,7 @@ struct SweepArgs {
   uint32_t sweep;
   int nhit;
   unsigned long long* counters;  // [0] hits, [1] accepts, [2] rechecks
-};
-
-// Shared-memory sub-table path (pool of nearest elements).
-struct FastTables {
-  uint16_t* sub;            // npool*P entries: (u*g_k) | (cls(u*g_k) << shift)
-  uint8_t* cls;             // P: ReTr class of each element
-  float* cls_val32;         // ncls
-  double* cls_val64;        // ncls
-  int ncls;
-  int shift;                // bits of the product field
-  int exact;                // 1: ReTr constant on classes (bitwise)
-  double eps;               // bound on |dS_fp32 - dS_fp64|, set per launch
+  unsigned long long* status;    // self-checking build only: first bad index
 };
 
 struct ChainDev {
@@ -50,21 +39,47 @@ struct ChainDev {
   uint16_t* pool = nullptr;    // proposal pool actually used
   uint32_t npool = 0;
   unsigned long long* counters = nullptr;
-  double* maxerr = nullptr;    // mixed precision: max |dS err| (bits as u64 atomics)
-  FastTables fast{};
-  bool fast_ok = false;
+  uint16_t* sub = nullptr;     // sub[k*P + u] = u * pool[k] (shared sub-table kernel)
+  bool sub_ok = false;
 };
 
 // Launch one colour phase of the FP64 direct sweep.
 cudaError_t launch_sweep_direct(int D, int dir, const SweepArgs& a, cudaStream_t s);
-// Launch one colour phase of the mixed-precision shared sub-table sweep.
-cudaError_t launch_sweep_fast(int D, int dir, const SweepArgs& a, const FastTables& ft, double* maxerr,
-                              cudaStream_t s);
-size_t fast_smem_bytes(uint32_t P, uint32_t npool, int ncls);
+// Launch one colour phase of the shared sub-table sweep.
+cudaError_t launch_sweep_sub(int D, int dir, const SweepArgs& a, const uint16_t* sub, cudaStream_t s);
+size_t sub_smem_bytes(uint32_t P, uint32_t npool);
 cudaError_t launch_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uint64_t seed, cudaStream_t s);
 cudaError_t launch_fill(uint16_t* links, size_t n, uint16_t v, cudaStream_t s);
 cudaError_t launch_staples(int D, int dir, const SweepArgs& a, const uint32_t* sites, uint32_t n, uint16_t* out,
                            cudaStream_t s);
+
+// LLR (interval-restricted sweeps with Robbins-Monro updates): per-chain
+// state in device memory, updated by the commit kernel after every colour
+// phase.  Energies are exact: integer class histograms of all plaquettes (h[0])
+// and rectangles (h[1]), one FP64 dot product with the class values.
+constexpr int kLlrMaxCls = 32;
+struct LlrState {
+  double a, bg, elo, ehi, emid, ewin, w2, q;
+  double E[2];
+  double sumE;
+  double v[kLlrMaxCls];
+  long long h[2][kLlrMaxCls];
+  long long d[2][2][kLlrMaxCls];  // [phase parity][plaquette|rectangle][class]
+  double a_hist[DYM_LLR_MAX_NRM];
+  int axis, mode, k, m, K, NRM, drive_sweeps, drive_cap, ncls, pad;
+  unsigned long long phase_acc, phase_rej;
+};
+
+struct LlrArgs {
+  SweepArgs s;
+  const uint16_t* cls16;  // ReTr class of each element
+  LlrState* st;
+  uint16_t* oldv;         // value of each phase link before the proposal
+  int buf;                // phase parity
+  int dir;
+};
+
+cudaError_t launch_llr_phase(int D, const LlrArgs& a, bool last_in_sweep, cudaStream_t s);
 
 // Observables.
 struct MeasArgs {
@@ -98,4 +113,8 @@ struct dym_chain {
   size_t meas_scratch_elems = 0;
   unsigned long long* h_hist = nullptr;
   size_t h_hist_elems = 0;
+  // LLR state (allocated on first use).
+  dym::LlrState* d_llr = nullptr;
+  uint16_t* d_oldv = nullptr;
+  uint64_t llr_phase = 0;  // colour phases run by LLR sweeps (delta-buffer parity)
 };

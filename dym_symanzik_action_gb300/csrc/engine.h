@@ -44,6 +44,7 @@ struct Group {
   void* d_retr = nullptr;
   void* d_imtr = nullptr;
   void* d_cls = nullptr;
+  void* d_cls16 = nullptr;     // the same classes as uint16
   void* d_clsval = nullptr;
   int device = -1;
 };

@@ -34,12 +34,36 @@ __device__ __forceinline__ void site_geo(uint32_t i, int Nt, int Nx, SiteGeo<D>&
 }
 
 // Table access policies.  `Tab` provides mul(g, h), inv(g) for uint32 ids.
+// Opt-in self-checking build (-DDYM_BOUNDS_CHECK): every table and lattice
+// index is checked; the first bad one is recorded in *status as
+// (code << 32 | value) and the access is skipped.
+#ifdef DYM_BOUNDS_CHECK
+__device__ __forceinline__ bool dym_bc(bool ok, unsigned long long* status, uint32_t code, uint32_t val) {
+  if (!ok) {
+    printf("bounds check failed: code %u value %u thread %u block %u status %p\n", code, val, threadIdx.x,
+           blockIdx.x, (void*)status);
+    if (status) atomicCAS(status, 0ull, ((unsigned long long)code << 32) | val);
+  }
+  return ok;
+}
+#define DYM_BC(ok, st, code, val) dym_bc((ok), (st), (code), (val))
+#else
+#define DYM_BC(ok, st, code, val) true
+#endif
+
 struct GlobalTab {
   const uint16_t* __restrict__ mult;  // P*P, L2-resident
   const uint16_t* inv;                // shared memory copy
   uint32_t P;
-  __device__ __forceinline__ uint32_t mul(uint32_t g, uint32_t h) const { return __ldg(mult + g * P + h); }
-  __device__ __forceinline__ uint32_t iv(uint32_t g) const { return inv[g]; }
+  unsigned long long* status = nullptr;  // only read by the self-checking build
+  __device__ __forceinline__ uint32_t mul(uint32_t g, uint32_t h) const {
+    if (!DYM_BC(g < P && h < P, status, 3, g < P ? h : g)) return 0;
+    return __ldg(mult + g * P + h);
+  }
+  __device__ __forceinline__ uint32_t iv(uint32_t g) const {
+    if (!DYM_BC(g < P, status, 4, g)) return 0;
+    return inv[g];
+  }
 };
 
 struct SharedTab {  // whole Cayley table staged in shared memory (small groups)

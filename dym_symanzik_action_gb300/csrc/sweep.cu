@@ -1,22 +1,20 @@
 // Metropolis sweep kernels: one thread per link of one colour phase.
 //
-// Two kernels implement the hit loop of dym-mod-metro.cpp:161-192:
+// Two kernels implement the hit loop of dym-mod-metro.cpp:161-192 with the
+// reference's FP64 arithmetic and order:
 //
-//  * k_sweep_direct  -- the reference's arithmetic verbatim: every hit gathers
-//    mult[bnew][staple] for all 24 staples (4D) from the L2-resident Cayley
-//    table and sums ReTr in FP64 in the reference's order.
+//  * k_sweep_direct -- any table, any proposal pool: every hit gathers
+//    mult[bnew][staple] for all 8(D-1) staples from the L2-resident Cayley
+//    table (358 gathers per link visit at 10 hits in 4D).
 //
-//  * k_sweep_fast    -- same decisions, restructured.  With u_j = s_j * b
-//    (staple times current link), Tr(bnew s_j) = Tr(b g s_j) = Tr(g s_j b)
-//    = Tr(g u_j): the proposal's terms depend only on (g, u_j).  For the
-//    nearest-to-identity pool (72 elements for S(1080)) the products u*g and
-//    their ReTr class fit in shared memory as one uint16 table sub[k][u] =
-//    (u*g_k) | class << shift (155 KB for S(1080)), so a hit is 24 shared
-//    loads instead of 24 L2 gathers; an accepted hit advances u_j <- u_j*g_k
-//    from the same entries.  dS is summed in FP32 from per-class values; a
-//    decision closer to its threshold than the proven error bound is
-//    re-evaluated in FP64 in the reference's order, so accepted
-//    configurations are identical to the FP64 path.
+//  * k_sweep_sub    -- class-constant tables, nearest-element pool: with
+//    u_j = s_j * b (staple times current link), Tr(bnew s_j) = Tr(b g s_j) =
+//    Tr(g s_j b) = Tr(u_j g), so a proposal's terms depend only on (g, u_j).
+//    The products u * g for the pool elements fit in shared memory as
+//    sub[k][u] = u * g_k (155 KB for S(1080)'s 72-element pool): a hit is
+//    8(D-1) shared-memory loads instead of L2 gathers, and an accepted hit
+//    advances u_j <- u_j * g_k from the same entries.  108 L2 gathers per
+//    link visit remain (staples and u_j).
 #include <cuda_runtime.h>
 
 #include "chain.h"
@@ -37,11 +35,6 @@ __device__ __forceinline__ void flush_counters(unsigned long long* ctr, unsigned
     if (accs) atomicAdd(ctr + 1, (unsigned long long)accs);
     if (rechecks) atomicAdd(ctr + 2, (unsigned long long)rechecks);
   }
-}
-
-// Max of non-negative doubles via their ordered bit patterns.
-__device__ __forceinline__ void atomic_max_nonneg(double* addr, double v) {
-  atomicMax((unsigned long long*)addr, (unsigned long long)__double_as_longlong(v));
 }
 
 template <int D, int DIR>
@@ -104,48 +97,36 @@ __global__ void __launch_bounds__(256) k_sweep_direct(SweepArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// Mixed-precision shared sub-table kernel.
+// Shared sub-table kernel (FP64, class-constant tables).  A minimal change of
+// k_sweep_direct: same launch shape, counters and FP64 arithmetic; only the
+// per-hit products come from sub[k][u] = u * g_k in shared memory instead of
+// mult[bnew][s_j] in L2.  With u_j = s_j * b, the element u_j * g_k =
+// s_j b g_k is conjugate to bnew s_j = b g_k s_j, so for a table whose ReTr
+// is the same double on every conjugacy class ReTr[u_j g_k] is bit-identical
+// to the reference's ReTr[mult[bnew][s_j]], summed in the same order.
 // ---------------------------------------------------------------------------
 template <int D, int DIR>
-__global__ void __launch_bounds__(512, 1) k_sweep_fast(SweepArgs a, FastTables ft, double* maxerr) {
+__global__ void __launch_bounds__(256) k_sweep_sub(SweepArgs a, const uint16_t* __restrict__ sub) {
   constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
   extern __shared__ __align__(16) unsigned char smem[];
-  const uint32_t P = a.P;
-  uint16_t* s_sub = reinterpret_cast<uint16_t*>(smem);                       // npool*P
-  double* s_retr = reinterpret_cast<double*>(smem + ((size_t)a.npool * P * 2 + 15) / 16 * 16);  // P
-  double* s_cv64 = s_retr + P;                                               // ncls
-  float* s_cv32 = reinterpret_cast<float*>(s_cv64 + ft.ncls);                // ncls
-  uint16_t* s_inv = reinterpret_cast<uint16_t*>(s_cv32 + ft.ncls);           // P
-  uint8_t* s_cls = reinterpret_cast<uint8_t*>(s_inv + P);                    // P
-
-  {
-    const uint4* src = reinterpret_cast<const uint4*>(ft.sub);
-    uint4* dst = reinterpret_cast<uint4*>(s_sub);
-    const uint32_t nsub = a.npool * P;
-    const uint32_t n16 = nsub / 8;
-    for (uint32_t t = threadIdx.x; t < n16; t += blockDim.x) dst[t] = __ldg(src + t);
-    for (uint32_t t = n16 * 8 + threadIdx.x; t < nsub; t += blockDim.x) s_sub[t] = ft.sub[t];
-    for (uint32_t t = threadIdx.x; t < P; t += blockDim.x) {
-      s_retr[t] = a.retr[t];
-      s_inv[t] = a.inv[t];
-      s_cls[t] = ft.cls[t];
-    }
-    for (uint32_t t = threadIdx.x; t < (uint32_t)ft.ncls; t += blockDim.x) {
-      s_cv64[t] = ft.cls_val64[t];
-      s_cv32[t] = ft.cls_val32[t];
-    }
+  double* s_retr = reinterpret_cast<double*>(smem);
+  uint16_t* s_inv = reinterpret_cast<uint16_t*>(s_retr + a.P);
+  uint16_t* s_sub = s_inv + a.P;
+  for (uint32_t t = threadIdx.x; t < a.P; t += blockDim.x) {
+    s_retr[t] = a.retr[t];
+    s_inv[t] = a.inv[t];
   }
+  const uint32_t nsub = a.npool * a.P;
+  for (uint32_t t = threadIdx.x; t < nsub; t += blockDim.x) s_sub[t] = sub[t];
   __syncthreads();
 
-  const uint32_t mask = (1u << ft.shift) - 1u;
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned hits = 0, accs = 0, rechecks = 0;
-  double lmaxerr = 0;
+  unsigned hits = 0, accs = 0;
   if (tid < a.n) {
     const uint32_t i = a.sites[tid];
     SiteGeo<D> geo;
     site_geo<D>(i, a.Nt, a.Nx, geo);
-    GlobalTab T{a.mult, s_inv, P};
+    GlobalTab T{a.mult, s_inv, a.P};
     const uint16_t* L = a.links;
     const uint32_t V = a.V;
     auto ld = [L, V](uint32_t s, int d) -> uint32_t { return __ldg(L + (size_t)d * V + s); };
@@ -157,82 +138,33 @@ __global__ void __launch_bounds__(512, 1) k_sweep_fast(SweepArgs a, FastTables f
     const uint32_t b0 = b;
 #pragma unroll
     for (int j = 0; j < NT; ++j) u[j] = T.mul(u[j], b);  // u_j = s_j * b
-    const float b1f = (float)a.beta1, b2f = (float)a.beta2;
-    float r1 = 0.f, m1 = 0.f;
+    double r1 = 0, m1 = 0;
 #pragma unroll
-    for (int j = 0; j < NS; ++j) r1 += s_cv32[s_cls[u[j]]];
+    for (int j = 0; j < NS; ++j) r1 = DYM_ADD(r1, s_retr[u[j]]);
 #pragma unroll
-    for (int j = NS; j < NT; ++j) m1 += s_cv32[s_cls[u[j]]];
-
+    for (int j = NS; j < NT; ++j) m1 = DYM_ADD(m1, s_retr[u[j]]);
     for (int h = 0; h < a.nhit; ++h) {
       const dym_u32x4 r = dym_hit_random(a.seed, a.sweep, i, DIR, (uint32_t)h, DYM_TAG_METRO);
-      const uint32_t k = dym_pick(r.v[0], a.npool);
-      const uint16_t* row = s_sub + k * P;
+      const uint16_t* row = s_sub + dym_pick(r.v[0], a.npool) * a.P;
       uint32_t e[NT];
+      double r1n = 0, m1n = 0;
 #pragma unroll
-      for (int j = 0; j < NT; ++j) e[j] = row[u[j]];
-      float r1n = 0.f, m1n = 0.f;
-#pragma unroll
-      for (int j = 0; j < NS; ++j) r1n += s_cv32[e[j] >> ft.shift];
-#pragma unroll
-      for (int j = NS; j < NT; ++j) m1n += s_cv32[e[j] >> ft.shift];
-      const float ds = b1f * (r1n - r1) + b2f * (m1n - m1);
-      const double u2 = dym_u53(r.v[1], r.v[2]);
-      const float epsf = (float)ft.eps;
-      int decision;  // 1 accept, 0 reject, -1 recheck
-      if (ds < -epsf) {
-        decision = 1;
-      } else if (ds > epsf) {
-        // __expf has at most 2 + 1.173|x| ulp of error; the rest of the
-        // margin covers rounding u2 and q*(1+-m) to FP32.
-        const float q = __expf(-ds);
-        const float m = 2.0f * epsf + (4.0f + 1.2f * ds) * 1.2e-7f + 1e-6f;
-        const float u2f = (float)u2;
-        if (u2f < q * (1.0f - m)) decision = 1;
-        else if (u2f > q * (1.0f + m)) decision = 0;
-        else decision = -1;
-      } else {
-        decision = -1;
+      for (int j = 0; j < NS; ++j) {
+        e[j] = row[u[j]];
+        r1n = DYM_ADD(r1n, s_retr[e[j]]);
       }
-      if (decision < 0) {
-        // FP64 re-evaluation in the reference's order (dym-mod-metro.cpp:166-187).
-        ++rechecks;
-        double r1d = 0, m1d = 0, r1nd = 0, m1nd = 0;
-        if (ft.exact) {
 #pragma unroll
-          for (int j = 0; j < NS; ++j) {
-            r1d = DYM_ADD(r1d, s_cv64[s_cls[u[j]]]);
-            r1nd = DYM_ADD(r1nd, s_cv64[e[j] >> ft.shift]);
-          }
-#pragma unroll
-          for (int j = NS; j < NT; ++j) {
-            m1d = DYM_ADD(m1d, s_cv64[s_cls[u[j]]]);
-            m1nd = DYM_ADD(m1nd, s_cv64[e[j] >> ft.shift]);
-          }
-        } else {
-          // ReTr of the exact elements b*s_j and bnew*s_j, s_j = u_j * b^-1.
-          const uint32_t bi = s_inv[b];
-          const uint32_t bnew = row[b] & mask;
-#pragma unroll
-          for (int j = 0; j < NT; ++j) {
-            const uint32_t s = T.mul(u[j], bi);
-            const double vo = s_retr[T.mul(b, s)];
-            const double vn = s_retr[T.mul(bnew, s)];
-            if (j < NS) { r1d = DYM_ADD(r1d, vo); r1nd = DYM_ADD(r1nd, vn); }
-            else { m1d = DYM_ADD(m1d, vo); m1nd = DYM_ADD(m1nd, vn); }
-          }
-        }
-        const double oldact = dym_action(a.beta0, a.beta1, a.beta2, r1d, m1d);
-        const double newact = dym_action(a.beta0, a.beta1, a.beta2, r1nd, m1nd);
-        decision = dym_accept(oldact, newact, u2) ? 1 : 0;
-        const double err = fabs((double)ds - DYM_SUB(newact, oldact));
-        lmaxerr = fmax(lmaxerr, err);
+      for (int j = NS; j < NT; ++j) {
+        e[j] = row[u[j]];
+        m1n = DYM_ADD(m1n, s_retr[e[j]]);
       }
+      const double oldact = dym_action(a.beta0, a.beta1, a.beta2, r1, m1);
+      const double newact = dym_action(a.beta0, a.beta1, a.beta2, r1n, m1n);
       ++hits;
-      if (decision) {
-        b = row[b] & mask;
+      if (dym_accept(oldact, newact, dym_u53(r.v[1], r.v[2]))) {
+        b = row[b];
 #pragma unroll
-        for (int j = 0; j < NT; ++j) u[j] = e[j] & mask;
+        for (int j = 0; j < NT; ++j) u[j] = e[j];
         r1 = r1n;
         m1 = m1n;
         ++accs;
@@ -240,8 +172,7 @@ __global__ void __launch_bounds__(512, 1) k_sweep_fast(SweepArgs a, FastTables f
     }
     if (b != b0) *own = (uint16_t)b;
   }
-  flush_counters(a.counters, hits, accs, rechecks);
-  if (lmaxerr > 0) atomic_max_nonneg(maxerr, lmaxerr);
+  flush_counters(a.counters, hits, accs, 0);
 }
 
 __global__ void k_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uint64_t seed) {
@@ -302,22 +233,23 @@ cudaError_t direct_dispatch(int dir, const SweepArgs& a, cudaStream_t s) {
 }
 
 template <int D>
-cudaError_t fast_dispatch(int dir, const SweepArgs& a, const FastTables& ft, double* maxerr, cudaStream_t s) {
-  const size_t smem = fast_smem_bytes(a.P, a.npool, ft.ncls);
-  const unsigned threads = 512;
-  const unsigned grid = (a.n + threads - 1) / threads;
-  void (*fn)(SweepArgs, FastTables, double*) = nullptr;
+cudaError_t sub_dispatch(int dir, const SweepArgs& a, const uint16_t* sub, cudaStream_t s) {
+  const size_t smem = sub_smem_bytes(a.P, a.npool);
+  const unsigned grid = (a.n + 255) / 256;
+  void (*fn)(SweepArgs, const uint16_t*) = nullptr;
   switch (dir) {
-    case 0: fn = k_sweep_fast<D, 0>; break;
-    case 1: fn = k_sweep_fast<D, 1>; break;
-    case 2: if (D > 2) fn = k_sweep_fast<D, (D > 2 ? 2 : 0)>; break;
-    case 3: if (D > 3) fn = k_sweep_fast<D, (D > 3 ? 3 : 0)>; break;
+    case 0: fn = k_sweep_sub<D, 0>; break;
+    case 1: fn = k_sweep_sub<D, 1>; break;
+    case 2: if (D > 2) fn = k_sweep_sub<D, (D > 2 ? 2 : 0)>; break;
+    case 3: if (D > 3) fn = k_sweep_sub<D, (D > 3 ? 3 : 0)>; break;
   }
   if (!fn) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
   if (grid == 0) return cudaSuccess;
-  fn<<<grid, threads, smem, s>>>(a, ft, maxerr);
+  fn<<<grid, 256, smem, s>>>(a, sub);
   return cudaGetLastError();
 }
 
@@ -339,9 +271,8 @@ cudaError_t staples_dispatch(int dir, const SweepArgs& a, const uint32_t* sites,
 
 }  // namespace
 
-size_t fast_smem_bytes(uint32_t P, uint32_t npool, int ncls) {
-  size_t sub = ((size_t)npool * P * 2 + 15) / 16 * 16;
-  return sub + (size_t)P * 8 + (size_t)ncls * 12 + (size_t)P * 3 + 16;
+size_t sub_smem_bytes(uint32_t P, uint32_t npool) {
+  return (size_t)P * 8 + (size_t)P * 2 + (size_t)npool * P * 2 + 16;
 }
 
 cudaError_t launch_sweep_direct(int D, int dir, const SweepArgs& a, cudaStream_t s) {
@@ -353,12 +284,11 @@ cudaError_t launch_sweep_direct(int D, int dir, const SweepArgs& a, cudaStream_t
   return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_sweep_fast(int D, int dir, const SweepArgs& a, const FastTables& ft, double* maxerr,
-                              cudaStream_t s) {
+cudaError_t launch_sweep_sub(int D, int dir, const SweepArgs& a, const uint16_t* sub, cudaStream_t s) {
   switch (D) {
-    case 2: return fast_dispatch<2>(dir, a, ft, maxerr, s);
-    case 3: return fast_dispatch<3>(dir, a, ft, maxerr, s);
-    case 4: return fast_dispatch<4>(dir, a, ft, maxerr, s);
+    case 2: return sub_dispatch<2>(dir, a, sub, s);
+    case 3: return sub_dispatch<3>(dir, a, sub, s);
+    case 4: return sub_dispatch<4>(dir, a, sub, s);
   }
   return cudaErrorInvalidValue;
 }

@@ -162,6 +162,54 @@ int dym_schedule_check(int32_t D, int32_t Nt, int32_t Nx, int32_t* nphase, uint6
 int dym_schedule_get(int32_t D, int32_t Nt, int32_t Nx, uint32_t* V, int32_t* nphase, int32_t* phase_dir,
                      uint32_t* phase_len, uint32_t* sites);
 
+/* ------------------------------------------------------------------- LLR --- */
+
+#define DYM_LLR_MAX_NRM 1024
+
+#define DYM_LLR_DRIVE 0      /* energy outside the window, greedy drive-in */
+#define DYM_LLR_SETTLE 1     /* entered the window during the current sweep */
+#define DYM_LLR_RM 2         /* Robbins-Monro iterations */
+#define DYM_LLR_DONE 3       /* all NRM iterations done */
+#define DYM_LLR_UNREACHED 4  /* drive-in cap reached outside the window */
+
+typedef struct {
+  int32_t axis;      /* 1: window on S1 (plaquettes), background bg on S2; 2: the reverse (llr.cpp:42-43, 286) */
+  double bg;         /* fixed background coupling BG (llr.cpp:43, 287) */
+  double ewin;       /* window centre */
+  double hw;         /* half-width: window [ewin-hw, ewin+hw], W = 2 hw (llr.cpp:236) */
+  double a0;         /* initial a (also the drive-in tilt, seed_window's a_guess, llr.cpp:223) */
+  int32_t K;         /* sweeps per Robbins-Monro iteration (llr.cpp:294, default 50) */
+  int32_t NRM;       /* Robbins-Monro iterations (llr.cpp:295, default 80), <= DYM_LLR_MAX_NRM */
+  int32_t nhit;      /* hits per link per visit (llr.cpp:32, NHIT 20) */
+  int32_t drive_cap; /* max drive-in sweeps (llr.cpp:225, CAP 20000) */
+} dym_llr_req;
+
+typedef struct {
+  double a;            /* final a_n */
+  double S1, S2;       /* energies at the end (exact class sums) */
+  int32_t status;      /* DYM_LLR_DONE or DYM_LLR_UNREACHED */
+  int32_t drive_sweeps;
+  int32_t sweeps;      /* sweeps run by this call */
+  uint64_t hits, accepts;
+  uint64_t phase_accepts, phase_rejects;  /* colour-class moves kept / reverted by the window */
+} dym_llr_result;
+
+/* Exact S1 = sum over plaquettes of ReTr and S2 = sum over 1x2 rectangles of
+ * ReTr of the current configuration (recompute_S1, recompute_S2 with
+ * RECT_MULT = 6: llr.cpp:46-55, 139-151). */
+int dym_llr_energy(dym_chain* c, double* S1, double* S2);
+
+/* One LLR window on the device: drive the windowed energy into
+ * [ewin-hw, ewin+hw] (seed_window, llr.cpp:223-231), then NRM Robbins-Monro
+ * iterations of K constrained sweeps, a += 12/(W^2 (m+1)) (<E> - ewin)
+ * (rm_solve, llr.cpp:234-250).  Sweeps are colour-parallel: every link of a
+ * colour class does nhit Metropolis hits of weight exp(-a dE_w - bg dE_bg)
+ * (llr.cpp:208-212) and the class move is kept iff the new windowed energy
+ * lies in the window, else reverted (outside the window: kept iff it moves the
+ * energy towards the centre).  a_hist (may be NULL) receives a after each of
+ * the NRM iterations. */
+int dym_llr_run(dym_chain* c, const dym_llr_req* req, dym_llr_result* out, double* a_hist);
+
 /* Roofline probe (no reference counterpart): random 2-byte gathers from an
  * L2-resident table of table_bytes bytes on `device`, as the sweep kernels
  * issue them; returns the sustained gather rate in 32-byte sectors per second

@@ -123,9 +123,6 @@ def test_full_size_hot_chain_matches_oracle(engine):
     assert (got == ol_obs).all()
 
 
-def test_mixed_precision_reports_rechecks(engine):
-    lat = engine.Lattice(group(engine, "S1080"), 4, 8, 8, 0.0, 1.5, 0.1, 3, precision="mixed")
-    st = lat.update(3, 10)
-    assert st.hits == lat.V * 4 * 10 * 3
-    assert 0 < st.rechecks < st.hits
-    assert 0 <= st.max_ds_err < 1e-3
+def test_shared_table_path_is_selected_for_generated_tables(engine):
+    for name in ("S1080", "BI", "BT"):
+        assert group(engine, name).fast_path, name

@@ -1,0 +1,89 @@
+"""Statistical parity with the unmodified reference, and the drop-in CLI.
+
+tests/golden/chains_1sigma.npz holds GMES/RMES series of the unmodified
+reference executable (its own mys1080-v4 table, NHIT 20, hot start, 4^4,
+beta = (0, 1.5, 0.1), K 10, N 100, Ntherm 100) for six seeds.  The engine
+runs the same protocol on the generated, trace-isomorphic S(1080) table with
+independent seeds.  Runs from different seeds are independent; the error of
+each side's mean is the spread of its per-run means / sqrt(runs).  Every
+observable must agree within 4 combined standard errors (21 comparisons), and
+at least half within 1."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from dym_symanzik_action_gb300 import tables
+
+pytestmark = pytest.mark.gpu
+
+
+def per_run_means(gmes, rmes):
+    # GMES: 999, ReP, ImP, plaq, W[0][0..3], ..., W[3][0..3]; RMES: plaq, rect
+    return np.concatenate([gmes[:, 1:].mean(0), rmes[:, 1:].mean(0)])
+
+
+def test_observables_agree_with_reference_chains(engine):
+    ref = golden("chains_1sigma.npz")
+    ref_runs = np.array([per_run_means(ref[f"gmes_{s}"], ref[f"rmes_{s}"]) for s in ref["seeds"]])
+    g = engine.load_group(tables.ensure_table("S1080"))
+    our_runs = []
+    for s in range(12):
+        lat = engine.Lattice(g, 4, 4, 4, 0.0, 1.5, 0.1, 900 + s, start="hot", pool="nearest")
+        lat.update(100, 20)
+        gm, rm = [], []
+        for n in range(100):
+            lat.update(10, 20)
+            m = lat.measure()
+            gm.append([999.0, m.poly_re, m.poly_im, m.plaq, *m.wloop.ravel()])
+            rm.append([m.plaq, m.rect])
+        our_runs.append(per_run_means(np.array(gm), np.array(rm)))
+    our_runs = np.array(our_runs)
+    mr, mo = ref_runs.mean(0), our_runs.mean(0)
+    se = np.sqrt(ref_runs.var(0, ddof=1) / len(ref_runs) + our_runs.var(0, ddof=1) / len(our_runs))
+    z = (mo - mr) / np.where(se > 0, se, 1)
+    print("z-scores (ours - reference) / combined error:", np.round(z, 2).tolist())
+    assert np.all(np.abs(z) < 4.0), z
+    assert np.mean(np.abs(z) < 1.0) >= 0.5
+
+
+def test_cli_matches_python_api(engine):
+    from dym_symanzik_action_gb300.build import CLI
+    path = tables.ensure_table("S1080")
+    r = subprocess.run([CLI, path, "4", "4", "4", "0", "1.5", "0.1", "7", "2", "3", "5"], stdout=subprocess.PIPE,
+                       stderr=subprocess.PIPE, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    out = r.stdout.splitlines()
+    assert out[0].startswith("PARAMS(grp,D,Nt,Nx,beta0,beta1,beta2,seed): ")
+    assert out[1] == "RUN(K,N,Ntherm,NHIT): 2 3 5 20"
+    assert "small group size: 72" in out and "START: hot" in out and "thermo done" in out
+    gmes = [l for l in out if l.startswith("GMES:")]
+    rmes = [l for l in out if l.startswith("RMES:")]
+    accl = [l for l in out if l.startswith("ACC:")]
+    assert len(gmes) == 3 and len(rmes) == 3 and len(accl) == 3
+    assert len(gmes[0].split()) == 1 + 4 + 16
+    assert sum(1 for l in out if re.match(r"TM_END:   update {15}", l)) == 3
+    g = engine.load_group(path)
+    lat = engine.Lattice(g, 4, 4, 4, 0.0, 1.5, 0.1, 7, start="hot")
+    lat.update(5, 20)
+    for n in range(3):
+        lat.update(2, 20)
+        m = lat.measure()
+        assert m.gmes_line() == gmes[n]
+        assert m.rmes_line() == rmes[n]
+        assert accl[n] == "ACC: %f" % (lat.acc / lat.hit)
+
+
+def test_cli_cold_start_and_wilson_restriction(engine):
+    from dym_symanzik_action_gb300.build import CLI
+    path = tables.ensure_table("S1080")
+    env = dict(os.environ, DYM_WLOOP_MAX="2x2", DYM_NHIT="10", DYM_PRECISION="fp64")
+    r = subprocess.run([CLI, path, "4", "4", "4", "0", "3.0", "-0.15", "3", "1", "2", "0", "cold"],
+                       stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=120, env=env)
+    assert r.returncode == 0, r.stderr
+    gm = [l for l in r.stdout.splitlines() if l.startswith("GMES:")]
+    assert "START: cold" in r.stdout and "RUN(K,N,Ntherm,NHIT): 1 2 0 10" in r.stdout
+    assert len(gm) == 2 and len(gm[0].split()) == 1 + 4 + 4
