@@ -156,6 +156,57 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def ensemble_bench(dym, device: int, sweeps: int = 5, nhit: int = 10) -> dict:
+    """Config 3: 256 chains of uneven size, 200 on S(1080) and 56 on BI, hot
+    starts, (beta1, beta2) on a 16x16 grid.  The single-chain GPU path runs
+    each chain's sweep with its own dym_sweep call, one chain after another;
+    the batched path updates all chains with one kernel per colour-phase slot
+    replayed as a CUDA graph, after autotuning.  Both are timed by the wall
+    clock around synchronised calls (and by device events)."""
+    from dym_symanzik_action_gb300 import tables
+    from dym_symanzik_action_gb300.batch import Batch
+    from dym_symanzik_action_gb300.workloads import ensemble
+    specs = ensemble()
+    groups = {n: dym.load_group(tables.ensure_table(n)) for n in ("S1080", "BI")}
+    chains = [dym.Lattice(groups[c.group], 4, c.Nt, c.Nx, *c.beta, c.seed, start="hot", device=device)
+              for c in specs]
+    links = sum(c.links for c in specs)
+    for lat in chains:
+        lat.update(1, nhit)  # warm-up
+    t0 = time.perf_counter()
+    single_dev_ms = 0.0
+    for _ in range(max(1, sweeps // 2)):
+        for lat in chains:
+            single_dev_ms += lat.update(1, nhit).device_ms
+    single_wall = time.perf_counter() - t0
+    single_sweeps = max(1, sweeps // 2)
+    b = Batch(device)
+    for lat in chains:
+        b.add(lat)
+    tuning = b.autotune(nhit=nhit, nsweeps_per_trial=1)
+    b.update(1, nhit)  # warm-up (graph already captured by the autotuner's last trial)
+    t0 = time.perf_counter()
+    st = b.update(sweeps, nhit)
+    batch_wall = time.perf_counter() - t0
+    n, nlinks, nslots = b.size
+    hits_single = links * nhit * single_sweeps
+    hits_batch = links * nhit * sweeps
+    assert st.hits == hits_batch
+    out = {"workload": "256 chains: Nx in {8..24}, Nt in {2,4,6,8}, 200 S(1080) + 56 BI, hot, 10 hits/link",
+           "chains": n, "links": nlinks, "colour_phase_slots": nslots, "sweeps_timed": sweeps,
+           "batched_link_hits_per_s": hits_batch / batch_wall,
+           "batched_device_link_hits_per_s": hits_batch / (st.device_ms * 1e-3),
+           "single_chain_link_hits_per_s": hits_single / single_wall,
+           "single_chain_device_link_hits_per_s": hits_single / (single_dev_ms * 1e-3),
+           "speedup_batched_vs_single": (hits_batch / batch_wall) / (hits_single / single_wall),
+           "tuning": {"tile": tuning.tile, "threads": tuning.threads, "grid_per_sm": tuning.grid_per_sm,
+                      "cuda_graph": tuning.use_graph}}
+    b.close()
+    for lat in chains:
+        lat.close()
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -280,6 +331,8 @@ def run_ours(args):
             "clocks": clocks,
             "wall_s_timed_region": t_wall,
         }
+        if not args.no_ensemble:
+            line["batched"] = ensemble_bench(dym, local)
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline()
         print(json.dumps(line), flush=True)
@@ -294,6 +347,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched 256-chain ensemble")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

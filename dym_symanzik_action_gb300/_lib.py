@@ -53,6 +53,24 @@ class Obs(C.Structure):
                 ("wl_nx", C.c_int32), ("wl_nt", C.c_int32)]
 
 
+class LlrReq(C.Structure):
+    _fields_ = [("axis", C.c_int32), ("bg", C.c_double), ("ewin", C.c_double), ("hw", C.c_double),
+                ("a0", C.c_double), ("K", C.c_int32), ("NRM", C.c_int32), ("nhit", C.c_int32),
+                ("drive_cap", C.c_int32)]
+
+
+class LlrResult(C.Structure):
+    _fields_ = [("a", C.c_double), ("S1", C.c_double), ("S2", C.c_double), ("status", C.c_int32),
+                ("drive_sweeps", C.c_int32), ("sweeps", C.c_int32), ("hits", C.c_uint64), ("accepts", C.c_uint64),
+                ("phase_accepts", C.c_uint64), ("phase_rejects", C.c_uint64)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("tile", C.c_int32), ("threads", C.c_int32), ("grid_per_sm", C.c_int32), ("use_graph", C.c_int32)]
+
+
+LLR_STATUS = {0: "drive", 1: "settle", 2: "rm", 3: "done", 4: "unreached"}
+
 _P = C.c_void_p
 _u16p = C.POINTER(C.c_uint16)
 _u32p = C.POINTER(C.c_uint32)
@@ -79,6 +97,17 @@ PROTOTYPES = {
     "dym_chain_staples": (C.c_int, [_P, C.c_int32, _u32p, C.c_int32, _u16p]),
     "dym_schedule_check": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _i32p, _u64p]),
     "dym_schedule_get": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _u32p, _i32p, _i32p, _u32p, _u32p]),
+    "dym_batch_create": (C.c_int, [C.c_int32, C.POINTER(_P)]),
+    "dym_batch_add": (C.c_int, [_P, _P]),
+    "dym_batch_size": (C.c_int, [_P, _i32p, _u64p, _i32p]),
+    "dym_batch_set_tuning": (C.c_int, [_P, C.POINTER(BatchTuning)]),
+    "dym_batch_get_tuning": (C.c_int, [_P, C.POINTER(BatchTuning)]),
+    "dym_batch_sweep": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(Stats)]),
+    "dym_batch_chain_counters": (C.c_int, [_P, C.c_int32, _u64p, _u64p]),
+    "dym_batch_autotune": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(BatchTuning)]),
+    "dym_batch_free": (C.c_int, [_P]),
+    "dym_llr_energy": (C.c_int, [_P, _f64p, _f64p]),
+    "dym_llr_run": (C.c_int, [_P, C.POINTER(LlrReq), C.POINTER(LlrResult), _f64p]),
     "dym_probe_l2_gather": (C.c_int, [C.c_int32, C.c_uint32, _f64p]),
 }
 

@@ -8,6 +8,7 @@
 #include <memory>
 #include <string>
 
+#include "batch.h"
 #include "chain.h"
 #include "dym_core.h"
 
@@ -538,6 +539,7 @@ int dym_llr_run(dym_chain* c, const dym_llr_req* req, dym_llr_result* out, doubl
   A.st = c->d_llr;
   A.oldv = c->d_oldv;
   const Schedule& s = c->sched;
+  const uint32_t sweep0 = c->sweep;
   const long max_sweeps = (long)req->drive_cap + (long)req->K * req->NRM + 2;
   int mode = st->mode;
   long sweeps = 0;
@@ -569,7 +571,8 @@ int dym_llr_run(dym_chain* c, const dym_llr_req* req, dym_llr_result* out, doubl
   out->S2 = st->E[1];
   out->status = st->mode;
   out->drive_sweeps = st->drive_sweeps;
-  out->sweeps = (int32_t)sweeps;
+  out->sweeps = st->sweeps;
+  c->sweep = sweep0 + (uint32_t)st->sweeps;  // sweeps after the state machine finished did nothing
   out->hits = c->h_counters[0];
   out->accepts = c->h_counters[1];
   out->phase_accepts = st->phase_acc;
@@ -583,6 +586,379 @@ int dym_probe_l2_gather(int32_t device, uint32_t table_bytes, double* sectors_pe
   if (!sectors_per_s || table_bytes < 1024) return fail(DYM_EINVAL, "dym_probe_l2_gather: bad argument");
   DYM_CUDA(cudaSetDevice(device), "cudaSetDevice");
   DYM_CUDA(probe_l2_gather(table_bytes, sectors_per_s), "L2 gather probe");
+  return DYM_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ batch --
+
+struct dym_batch {
+  int device = 0;
+  int D = 0;
+  std::vector<dym_chain*> chains;
+  std::vector<dym::Group*> groups;
+  std::vector<uint16_t*> d_group_sub;  // one sub-table per group (owned)
+  dym::BatchGroups bg{};
+  dym::BatchChainDev* d_chains = nullptr;
+  dym::BatchTile* d_tiles = nullptr;
+  uint32_t* d_sweeps = nullptr;
+  unsigned long long* d_ctr = nullptr;
+  std::vector<unsigned long long> h_ctr;
+  std::vector<uint32_t> slot_off, slot_cnt;
+  size_t smem = 0;
+  uint64_t nlinks = 0;
+  dym_batch_tuning tune{256, 256, 1, 1};
+  bool dirty = true;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int graph_nhit = -1;
+  int sms = 0;
+};
+
+namespace dym {
+
+static void batch_release_device(dym_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+  b->graph_nhit = -1;
+  cudaFree(b->d_chains);
+  cudaFree(b->d_tiles);
+  cudaFree(b->d_sweeps);
+  cudaFree(b->d_ctr);
+  b->d_chains = nullptr;
+  b->d_tiles = nullptr;
+  b->d_sweeps = nullptr;
+  b->d_ctr = nullptr;
+  for (auto p : b->d_group_sub) cudaFree(p);
+  b->d_group_sub.clear();
+}
+
+// Lay out tables, descriptors and per-slot tile lists for the current chains.
+static int batch_build(dym_batch* b) {
+  batch_release_device(b);
+  const size_t nc = b->chains.size();
+  b->bg = BatchGroups{};
+  b->bg.n = (int)b->groups.size();
+  size_t off = 0;
+  auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
+  for (size_t g = 0; g < b->groups.size(); ++g) {
+    const Group& G = *b->groups[g];
+    const auto& pool = G.pool_nearest;
+    std::vector<uint16_t> sub(pool.size() * (size_t)G.P);
+    for (size_t k = 0; k < pool.size(); ++k)
+      for (uint32_t u = 0; u < G.P; ++u) sub[k * G.P + u] = G.mult[(size_t)u * G.P + pool[k]];
+    uint16_t* d = nullptr;
+    DYM_CUDA(dmalloc(&d, sub.size()), "cudaMalloc(batch sub)");
+    b->d_group_sub.push_back(d);
+    DYM_CUDA(cudaMemcpy(d, sub.data(), sub.size() * 2, cudaMemcpyHostToDevice), "upload batch sub");
+    BatchGroupDev& bd = b->bg.g[g];
+    bd.mult = (const uint16_t*)G.d_mult;
+    bd.inv = (const uint16_t*)G.d_inv;
+    bd.retr = (const double*)G.d_retr;
+    bd.sub = d;
+    bd.P = G.P;
+    bd.npool = (uint32_t)pool.size();
+    bd.off_retr = (uint32_t)off;
+    off = up16(off + (size_t)G.P * 8);
+    bd.off_inv = (uint32_t)off;
+    off = up16(off + (size_t)G.P * 2);
+    bd.off_sub = (uint32_t)off;
+    off = up16(off + sub.size() * 2);
+  }
+  b->smem = off;
+  int optin = 0;
+  DYM_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device), "attribute");
+  if (b->smem > (size_t)optin)
+    return fail(DYM_ENOTSUP, "the batch's groups need " + std::to_string(b->smem) + " B of shared tables, more than " +
+                                 std::to_string(optin));
+  std::vector<BatchChainDev> cd(nc);
+  DYM_CUDA(dmalloc(&b->d_ctr, 2 * nc), "cudaMalloc(batch counters)");
+  b->nlinks = 0;
+  size_t maxph = 0;
+  for (size_t i = 0; i < nc; ++i) {
+    dym_chain* c = b->chains[i];
+    BatchChainDev& d = cd[i];
+    d.links = c->dev.links;
+    d.sites = c->dev.sites;
+    d.V = c->dev.V;
+    d.Nt = c->p.Nt;
+    d.Nx = c->p.Nx;
+    d.group = (int)(std::find(b->groups.begin(), b->groups.end(), c->grp->g) - b->groups.begin());
+    d.beta0 = c->p.beta0;
+    d.beta1 = c->p.beta1;
+    d.beta2 = c->p.beta2;
+    d.seed = c->p.seed;
+    d.ctr = b->d_ctr + 2 * i;
+    b->nlinks += (uint64_t)c->dev.V * c->p.D;
+    maxph = std::max(maxph, c->sched.phase_dir.size());
+  }
+  DYM_CUDA(dmalloc(&b->d_chains, nc), "cudaMalloc(batch chains)");
+  DYM_CUDA(cudaMemcpy(b->d_chains, cd.data(), nc * sizeof(BatchChainDev), cudaMemcpyHostToDevice), "upload chains");
+  DYM_CUDA(dmalloc(&b->d_sweeps, nc), "cudaMalloc(batch sweeps)");
+  // Tiles: slot k holds phase k of every chain, split into pieces of `tile`
+  // links; larger pieces first so the last blocks of a slot get small ones.
+  std::vector<BatchTile> tiles;
+  b->slot_off.assign(maxph, 0);
+  b->slot_cnt.assign(maxph, 0);
+  const uint32_t T = (uint32_t)std::max(32, b->tune.tile);
+  for (size_t k = 0; k < maxph; ++k) {
+    b->slot_off[k] = (uint32_t)tiles.size();
+    std::vector<BatchTile> slot;
+    for (size_t i = 0; i < nc; ++i) {
+      const Schedule& s = b->chains[i]->sched;
+      if (k >= s.phase_dir.size()) continue;
+      for (uint32_t j = 0; j < s.phase_len[k]; j += T)
+        slot.push_back(BatchTile{(uint32_t)i, s.phase_off[k] + j, std::min(T, s.phase_len[k] - j),
+                                 (uint32_t)s.phase_dir[k]});
+    }
+    std::stable_sort(slot.begin(), slot.end(), [](const BatchTile& x, const BatchTile& y) { return x.count > y.count; });
+    tiles.insert(tiles.end(), slot.begin(), slot.end());
+    b->slot_cnt[k] = (uint32_t)slot.size();
+  }
+  DYM_CUDA(dmalloc(&b->d_tiles, std::max<size_t>(tiles.size(), 1)), "cudaMalloc(batch tiles)");
+  DYM_CUDA(cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice),
+           "upload tiles");
+  void* fn = batch_kernel_for(b->D);
+  if (!fn) return fail(DYM_ENOTSUP, "batch: unsupported D");
+  DYM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem), "smem attribute");
+  b->dirty = false;
+  return DYM_OK;
+}
+
+static int batch_grid(dym_batch* b, unsigned* grid) {
+  int per_sm = 0;
+  DYM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel_for(b->D), b->tune.threads, b->smem),
+           "occupancy");
+  *grid = (unsigned)std::max(1, b->sms * std::max(1, std::min(per_sm, b->tune.grid_per_sm)));
+  return DYM_OK;
+}
+
+static int batch_enqueue_sweep(dym_batch* b, int nhit, unsigned grid) {
+  for (size_t k = 0; k < b->slot_cnt.size(); ++k) {
+    cudaError_t e = launch_batch_slot(b->D, b->d_tiles + b->slot_off[k], b->slot_cnt[k], b->d_chains, b->bg,
+                                      b->d_sweeps, nhit, std::min<unsigned>(grid, b->slot_cnt[k]),
+                                      (unsigned)b->tune.threads, b->smem, b->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "batch slot launch");
+  }
+  DYM_CUDA(launch_batch_advance(b->d_sweeps, (uint32_t)b->chains.size(), b->stream), "batch advance");
+  return DYM_OK;
+}
+
+}  // namespace dym
+
+extern "C" {
+
+int dym_batch_create(int32_t device, dym_batch** out) {
+  if (!out) return fail(DYM_EINVAL, "dym_batch_create: out is NULL");
+  *out = nullptr;
+  int ndev = 0;
+  DYM_CUDA(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
+  if (device < 0 || device >= ndev) return fail(DYM_EINVAL, "bad device ordinal");
+  DYM_CUDA(cudaSetDevice(device), "cudaSetDevice");
+  std::unique_ptr<dym_batch> b(new dym_batch);
+  b->device = device;
+  DYM_CUDA(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device), "attribute");
+  DYM_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  *out = b.release();
+  return DYM_OK;
+}
+
+int dym_batch_add(dym_batch* b, dym_chain* c) {
+  if (!b || !c) return fail(DYM_EINVAL, "dym_batch_add: null argument");
+  if (c->p.device != b->device) return fail(DYM_EINVAL, "chain and batch are on different devices");
+  if (!b->chains.empty() && c->p.D != b->D) return fail(DYM_EINVAL, "all chains of a batch must have the same D");
+  if (!c->dev.sub_ok) return fail(DYM_ENOTSUP, "batch chains need the shared-table path (nearest pool, mixed)");
+  if (std::find(b->chains.begin(), b->chains.end(), c) != b->chains.end())
+    return fail(DYM_EINVAL, "chain already in the batch");
+  Group* g = c->grp->g;
+  if (std::find(b->groups.begin(), b->groups.end(), g) == b->groups.end()) {
+    if ((int)b->groups.size() == kBatchMaxGroups) return fail(DYM_ENOTSUP, "a batch holds at most 4 groups");
+    b->groups.push_back(g);
+  }
+  b->D = c->p.D;
+  b->chains.push_back(c);
+  b->dirty = true;
+  return DYM_OK;
+}
+
+int dym_batch_size(const dym_batch* b, int32_t* nchains, uint64_t* nlinks, int32_t* nslots) {
+  if (!b) return fail(DYM_EINVAL, "dym_batch_size: null batch");
+  uint64_t links = 0;
+  size_t maxph = 0;
+  for (auto c : b->chains) {
+    links += (uint64_t)c->dev.V * c->p.D;
+    maxph = std::max(maxph, c->sched.phase_dir.size());
+  }
+  if (nchains) *nchains = (int32_t)b->chains.size();
+  if (nlinks) *nlinks = links;
+  if (nslots) *nslots = (int32_t)maxph;
+  return DYM_OK;
+}
+
+int dym_batch_set_tuning(dym_batch* b, const dym_batch_tuning* t) {
+  if (!b || !t) return fail(DYM_EINVAL, "dym_batch_set_tuning: null argument");
+  if (t->tile < 32 || t->tile % 32 || (t->threads != 128 && t->threads != 256) || t->grid_per_sm < 1)
+    return fail(DYM_EINVAL, "tuning: tile a multiple of 32, threads 128 or 256, grid_per_sm >= 1");
+  if (t->tile != b->tune.tile) b->dirty = true;
+  b->tune = *t;
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  if (b->graph) {
+    cudaGraphDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  b->graph_nhit = -1;
+  return DYM_OK;
+}
+
+int dym_batch_get_tuning(const dym_batch* b, dym_batch_tuning* t) {
+  if (!b || !t) return fail(DYM_EINVAL, "dym_batch_get_tuning: null argument");
+  *t = b->tune;
+  return DYM_OK;
+}
+
+int dym_batch_sweep(dym_batch* b, int32_t nsweeps, int32_t nhit, dym_stats* total) {
+  if (!b) return fail(DYM_EINVAL, "dym_batch_sweep: null batch");
+  if (nsweeps < 0 || nhit < 0 || nhit > (1 << 20)) return fail(DYM_EINVAL, "dym_batch_sweep: bad nsweeps or nhit");
+  DYM_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
+  if (b->chains.empty()) return fail(DYM_EINVAL, "empty batch");
+  if (b->dirty) {
+    int rc = batch_build(b);
+    if (rc) return rc;
+  }
+  const size_t nc = b->chains.size();
+  std::vector<uint32_t> sw(nc);
+  for (size_t i = 0; i < nc; ++i) sw[i] = b->chains[i]->sweep;
+  DYM_CUDA(cudaMemcpyAsync(b->d_sweeps, sw.data(), nc * 4, cudaMemcpyHostToDevice, b->stream), "upload sweeps");
+  DYM_CUDA(cudaMemsetAsync(b->d_ctr, 0, 2 * nc * sizeof(unsigned long long), b->stream), "reset counters");
+  unsigned grid = 1;
+  int grc = batch_grid(b, &grid);
+  if (grc) return grc;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  DYM_CUDA(cudaEventCreate(&e0), "cudaEventCreate");
+  DYM_CUDA(cudaEventCreate(&e1), "cudaEventCreate");
+  if (b->tune.use_graph && (!b->exec || b->graph_nhit != nhit)) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    DYM_CUDA(cudaStreamSynchronize(b->stream), "pre-capture sync");
+    DYM_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    int rc = batch_enqueue_sweep(b, nhit, grid);
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    DYM_CUDA(ce, "end capture");
+    b->graph = g;
+    DYM_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0), "graph instantiate");
+    b->graph_nhit = nhit;
+  }
+  DYM_CUDA(cudaEventRecord(e0, b->stream), "cudaEventRecord");
+  for (int k = 0; k < nsweeps; ++k) {
+    if (b->tune.use_graph) {
+      DYM_CUDA(cudaGraphLaunch(b->exec, b->stream), "graph launch");
+    } else {
+      int rc = batch_enqueue_sweep(b, nhit, grid);
+      if (rc) return rc;
+    }
+  }
+  DYM_CUDA(cudaEventRecord(e1, b->stream), "cudaEventRecord");
+  b->h_ctr.assign(2 * nc, 0);
+  DYM_CUDA(cudaMemcpyAsync(b->h_ctr.data(), b->d_ctr, 2 * nc * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                           b->stream),
+           "read counters");
+  DYM_CUDA(cudaStreamSynchronize(b->stream), "batch sweep");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (auto c : b->chains) c->sweep += (uint32_t)nsweeps;
+  if (total) {
+    std::memset(total, 0, sizeof *total);
+    for (size_t i = 0; i < nc; ++i) {
+      total->hits += b->h_ctr[2 * i];
+      total->accepts += b->h_ctr[2 * i + 1];
+    }
+    total->sweep = (uint32_t)nsweeps;
+    total->launches = (uint32_t)(nsweeps * (b->slot_cnt.size() + 1));
+    total->device_ms = ms;
+  }
+  return DYM_OK;
+}
+
+int dym_batch_chain_counters(const dym_batch* b, int32_t idx, uint64_t* hits, uint64_t* accepts) {
+  if (!b || idx < 0 || (size_t)idx >= b->chains.size()) return fail(DYM_EINVAL, "dym_batch_chain_counters: bad index");
+  if (b->h_ctr.size() != 2 * b->chains.size()) return fail(DYM_EINVAL, "no batch sweep yet");
+  if (hits) *hits = b->h_ctr[2 * idx];
+  if (accepts) *accepts = b->h_ctr[2 * idx + 1];
+  return DYM_OK;
+}
+
+int dym_batch_autotune(dym_batch* b, int32_t nhit, int32_t nsweeps_per_trial, dym_batch_tuning* best) {
+  if (!b || nsweeps_per_trial < 1) return fail(DYM_EINVAL, "dym_batch_autotune: bad argument");
+  if (b->chains.empty()) return fail(DYM_EINVAL, "empty batch");
+  DYM_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
+  // Save every chain's configuration and sweep counter.
+  std::vector<uint16_t*> saved;
+  std::vector<uint32_t> sw;
+  for (auto c : b->chains) {
+    uint16_t* p = nullptr;
+    const size_t n = (size_t)c->dev.V * c->p.D;
+    DYM_CUDA(dmalloc(&p, n), "cudaMalloc(autotune save)");
+    DYM_CUDA(cudaMemcpy(p, c->dev.links, n * 2, cudaMemcpyDeviceToDevice), "save links");
+    saved.push_back(p);
+    sw.push_back(c->sweep);
+  }
+  const dym_batch_tuning start = b->tune;
+  dym_batch_tuning win = start;
+  float win_ms = 1e30f;
+  int rc = DYM_OK;
+  for (int threads : {128, 256})
+    for (int tile : {128, 256, 512, 1024})
+      for (int gps : {1, 2}) {
+        if (rc) break;
+        dym_batch_tuning t{tile, threads, gps, 1};
+        rc = dym_batch_set_tuning(b, &t);
+        dym_stats st;
+        if (!rc) rc = dym_batch_sweep(b, 1, nhit, &st);  // warm-up, graph capture
+        if (!rc) rc = dym_batch_sweep(b, nsweeps_per_trial, nhit, &st);
+        if (!rc && st.device_ms < win_ms) {
+          win_ms = st.device_ms;
+          win = t;
+        }
+      }
+  for (size_t i = 0; i < b->chains.size(); ++i) {
+    dym_chain* c = b->chains[i];
+    cudaMemcpy(c->dev.links, saved[i], (size_t)c->dev.V * c->p.D * 2, cudaMemcpyDeviceToDevice);
+    cudaFree(saved[i]);
+    c->sweep = sw[i];
+  }
+  if (rc) {
+    dym_batch_set_tuning(b, &start);
+    return rc;
+  }
+  rc = dym_batch_set_tuning(b, &win);
+  b->h_ctr.clear();
+  if (best) *best = win;
+  return rc;
+}
+
+int dym_batch_free(dym_batch* b) {
+  if (!b) return DYM_OK;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  batch_release_device(b);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
   return DYM_OK;
 }
 

@@ -66,7 +66,7 @@ struct LlrState {
   long long h[2][kLlrMaxCls];
   long long d[2][2][kLlrMaxCls];  // [phase parity][plaquette|rectangle][class]
   double a_hist[DYM_LLR_MAX_NRM];
-  int axis, mode, k, m, K, NRM, drive_sweeps, drive_cap, ncls, pad;
+  int axis, mode, k, m, K, NRM, drive_sweeps, drive_cap, ncls, sweeps;
   unsigned long long phase_acc, phase_rej;
 };
 

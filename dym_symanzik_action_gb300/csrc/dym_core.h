@@ -152,3 +152,14 @@ DYM_HD int dym_accept(double oldact, double newact, double u2) {
   double probrat = (newact <= oldact) ? 1.0 : dym_exp(-DYM_SUB(newact, oldact));
   return probrat > u2;
 }
+
+// The same decision with the exponential skipped where it cannot matter: for
+// d = newact - oldact > 38, exp(-d) < 3.2e-17 (and dym_exp is within a few ulp
+// of it) while every nonzero u2 is >= 2^-53 = 1.1e-16, so the test can only
+// pass for u2 == 0, which is then decided by dym_exp itself.
+DYM_HD int dym_accept_fast(double oldact, double newact, double u2) {
+  if (newact <= oldact) return 1.0 > u2;
+  const double d = DYM_SUB(newact, oldact);
+  if (d > 38.0 && u2 != 0.0) return 0;
+  return dym_exp(-d) > u2;
+}

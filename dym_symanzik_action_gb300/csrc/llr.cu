@@ -9,7 +9,8 @@
 //     one colour share no plaquette or rectangle, so their energy changes add.
 //     Outside the window (drive-in) a hit is kept iff it moves the link's
 //     running energy towards the window centre (llr.cpp:208-209), and only a
-//     deterministic fraction q of the links takes part.  Each link's change of
+//     deterministic fraction q of the links takes part; after each phase q is
+//     set so that the expected move covers the remaining distance.  Each link's change of
 //     plaquette and rectangle classes is added to an integer histogram delta.
 //  2. k_llr_decide: the class move is kept iff the new windowed energy lies in
 //     [Elo, Ehi] (outside the window: iff it is closer to the centre);
@@ -182,6 +183,8 @@ __global__ void k_llr_commit(LlrArgs A, int last_in_sweep) {
   if (mode >= DYM_LLR_DONE) return;
   const int buf = A.buf, w = st->axis - 1;
   const bool ok = phase_ok(st, buf);
+  const double Eold = st->E[w];
+  const double dE = DYM_SUB(class_sum(st->h[w], st->d[buf][w], st->v, st->ncls), Eold);
   if (ok) {
     for (int c = 0; c < st->ncls; ++c) {
       st->h[0][c] += st->d[buf][0][c];
@@ -198,10 +201,14 @@ __global__ void k_llr_commit(LlrArgs A, int last_in_sweep) {
     st->d[buf][1][c] = 0;
   }
   if (mode == DYM_LLR_DRIVE) {
-    st->q = ok ? fmin(1.0, DYM_MUL(st->q, 2.0)) : fmax(DYM_MUL(st->q, 0.5), 0x1.0p-32);
+    // Aim the next phase's expected move at the remaining distance.
+    const double dist = fabs(DYM_SUB(st->emid, st->E[w]));
+    const double q = fabs(dE) > 0 ? DYM_MUL(st->q, dist / fabs(dE)) : DYM_MUL(st->q, 2.0);
+    st->q = fmin(1.0, fmax(q, 0x1.0p-32));
     if (st->E[w] >= st->elo && st->E[w] <= st->ehi) mode = DYM_LLR_SETTLE;
   }
   if (last_in_sweep) {
+    st->sweeps++;
     if (mode == DYM_LLR_DRIVE) {
       if (++st->drive_sweeps >= st->drive_cap) mode = DYM_LLR_UNREACHED;
     } else if (mode == DYM_LLR_SETTLE) {

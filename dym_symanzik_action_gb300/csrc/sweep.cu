@@ -17,25 +17,16 @@
 //    link visit remain (staples and u_j).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "chain.h"
 #include "dym_core.h"
 #include "staples.cuh"
+#include "visit.cuh"
 
 namespace dym {
 
 namespace {
-
-__device__ __forceinline__ void flush_counters(unsigned long long* ctr, unsigned hits, unsigned accs,
-                                               unsigned rechecks) {
-  hits = __reduce_add_sync(0xffffffffu, hits);
-  accs = __reduce_add_sync(0xffffffffu, accs);
-  rechecks = __reduce_add_sync(0xffffffffu, rechecks);
-  if ((threadIdx.x & 31) == 0) {
-    if (hits) atomicAdd(ctr + 0, (unsigned long long)hits);
-    if (accs) atomicAdd(ctr + 1, (unsigned long long)accs);
-    if (rechecks) atomicAdd(ctr + 2, (unsigned long long)rechecks);
-  }
-}
 
 template <int D, int DIR>
 __global__ void __launch_bounds__(256) k_sweep_direct(SweepArgs a) {
@@ -107,71 +98,17 @@ __global__ void __launch_bounds__(256) k_sweep_direct(SweepArgs a) {
 // ---------------------------------------------------------------------------
 template <int D, int DIR>
 __global__ void __launch_bounds__(256) k_sweep_sub(SweepArgs a, const uint16_t* __restrict__ sub) {
-  constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
   extern __shared__ __align__(16) unsigned char smem[];
   double* s_retr = reinterpret_cast<double*>(smem);
   uint16_t* s_inv = reinterpret_cast<uint16_t*>(s_retr + a.P);
   uint16_t* s_sub = s_inv + a.P;
-  for (uint32_t t = threadIdx.x; t < a.P; t += blockDim.x) {
-    s_retr[t] = a.retr[t];
-    s_inv[t] = a.inv[t];
-  }
-  const uint32_t nsub = a.npool * a.P;
-  for (uint32_t t = threadIdx.x; t < nsub; t += blockDim.x) s_sub[t] = sub[t];
+  stage_sub_tables(a.retr, a.inv, sub, a.P, a.npool, s_retr, s_inv, s_sub);
   __syncthreads();
 
-  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned hits = 0, accs = 0;
-  if (tid < a.n) {
-    const uint32_t i = a.sites[tid];
-    SiteGeo<D> geo;
-    site_geo<D>(i, a.Nt, a.Nx, geo);
-    GlobalTab T{a.mult, s_inv, a.P};
-    const uint16_t* L = a.links;
-    const uint32_t V = a.V;
-    auto ld = [L, V](uint32_t s, int d) -> uint32_t { return __ldg(L + (size_t)d * V + s); };
-    uint32_t u[NT];
-    build_staples<D, DIR>(i, geo, T, ld, u, u + NS);
-
-    uint16_t* own = a.links + (size_t)DIR * V + i;
-    uint32_t b = *own;
-    const uint32_t b0 = b;
-#pragma unroll
-    for (int j = 0; j < NT; ++j) u[j] = T.mul(u[j], b);  // u_j = s_j * b
-    double r1 = 0, m1 = 0;
-#pragma unroll
-    for (int j = 0; j < NS; ++j) r1 = DYM_ADD(r1, s_retr[u[j]]);
-#pragma unroll
-    for (int j = NS; j < NT; ++j) m1 = DYM_ADD(m1, s_retr[u[j]]);
-    for (int h = 0; h < a.nhit; ++h) {
-      const dym_u32x4 r = dym_hit_random(a.seed, a.sweep, i, DIR, (uint32_t)h, DYM_TAG_METRO);
-      const uint16_t* row = s_sub + dym_pick(r.v[0], a.npool) * a.P;
-      uint32_t e[NT];
-      double r1n = 0, m1n = 0;
-#pragma unroll
-      for (int j = 0; j < NS; ++j) {
-        e[j] = row[u[j]];
-        r1n = DYM_ADD(r1n, s_retr[e[j]]);
-      }
-#pragma unroll
-      for (int j = NS; j < NT; ++j) {
-        e[j] = row[u[j]];
-        m1n = DYM_ADD(m1n, s_retr[e[j]]);
-      }
-      const double oldact = dym_action(a.beta0, a.beta1, a.beta2, r1, m1);
-      const double newact = dym_action(a.beta0, a.beta1, a.beta2, r1n, m1n);
-      ++hits;
-      if (dym_accept(oldact, newact, dym_u53(r.v[1], r.v[2]))) {
-        b = row[b];
-#pragma unroll
-        for (int j = 0; j < NT; ++j) u[j] = e[j];
-        r1 = r1n;
-        m1 = m1n;
-        ++accs;
-      }
-    }
-    if (b != b0) *own = (uint16_t)b;
-  }
+  // One wave of blocks, each staging the table once and visiting several links.
+  for (uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x; tid < a.n; tid += gridDim.x * blockDim.x)
+    visit_sub<D, DIR>(a, a.sites[tid], a.sweep, s_retr, s_inv, s_sub, hits, accs);
   flush_counters(a.counters, hits, accs, 0);
 }
 
@@ -235,7 +172,6 @@ cudaError_t direct_dispatch(int dir, const SweepArgs& a, cudaStream_t s) {
 template <int D>
 cudaError_t sub_dispatch(int dir, const SweepArgs& a, const uint16_t* sub, cudaStream_t s) {
   const size_t smem = sub_smem_bytes(a.P, a.npool);
-  const unsigned grid = (a.n + 255) / 256;
   void (*fn)(SweepArgs, const uint16_t*) = nullptr;
   switch (dir) {
     case 0: fn = k_sweep_sub<D, 0>; break;
@@ -248,7 +184,14 @@ cudaError_t sub_dispatch(int dir, const SweepArgs& a, const uint16_t* sub, cudaS
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  if (grid == 0) return cudaSuccess;
+  const unsigned need = (a.n + 255) / 256;
+  if (need == 0) return cudaSuccess;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem);
+  if (e != cudaSuccess) return e;
+  const unsigned grid = std::min<unsigned>(need, (unsigned)std::max(1, sms * std::max(per_sm, 1)));
   fn<<<grid, 256, smem, s>>>(a, sub);
   return cudaGetLastError();
 }

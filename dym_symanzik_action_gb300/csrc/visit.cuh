@@ -1,0 +1,104 @@
+// Per-link Metropolis visit of the shared sub-table path, shared by the
+// single-chain kernel (sweep.cu) and the batched kernel (batch.cu).
+#pragma once
+#include <stdint.h>
+
+#include "chain.h"
+#include "dym_core.h"
+#include "staples.cuh"
+
+namespace dym {
+
+// Copy ReTr, the inverse table and the sub-table sub[k][u] = u * g_k into
+// shared memory (s_sub must be 4-byte aligned when P is even).
+__device__ __forceinline__ void stage_sub_tables(const double* retr, const uint16_t* inv, const uint16_t* sub,
+                                                 uint32_t P, uint32_t npool, double* s_retr, uint16_t* s_inv,
+                                                 uint16_t* s_sub) {
+  for (uint32_t t = threadIdx.x; t < P; t += blockDim.x) {
+    s_retr[t] = retr[t];
+    s_inv[t] = inv[t];
+  }
+  const uint32_t nsub = npool * P;
+  if ((P & 1u) == 0) {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(sub);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(s_sub);
+    const uint32_t nw = nsub / 2;
+#pragma unroll 8
+    for (uint32_t t = threadIdx.x; t < nw; t += blockDim.x) dst[t] = src[t];
+  } else {
+    for (uint32_t t = threadIdx.x; t < nsub; t += blockDim.x) s_sub[t] = sub[t];
+  }
+}
+
+// One visit of link (i, DIR): build the staples, then nhit hits with the
+// per-hit products read from the shared sub-table.  With u_j = s_j * b the
+// element u_j * g_k = s_j b g_k is conjugate to bnew s_j = b g_k s_j, so for a
+// table whose ReTr is one double per conjugacy class ReTr[u_j g_k] equals the
+// reference's ReTr[mult[bnew][s_j]] bit for bit, summed in the same order
+// (dym-mod-metro.cpp:166-192).
+template <int D, int DIR>
+__device__ __forceinline__ void visit_sub(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
+                                          const uint16_t* s_inv, const uint16_t* s_sub, unsigned& hits,
+                                          unsigned& accs) {
+  constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
+  SiteGeo<D> geo;
+  site_geo<D>(i, a.Nt, a.Nx, geo);
+  GlobalTab T{a.mult, s_inv, a.P};
+  const uint16_t* L = a.links;
+  const uint32_t V = a.V;
+  auto ld = [L, V](uint32_t s, int d) -> uint32_t { return __ldg(L + (size_t)d * V + s); };
+  uint32_t u[NT];
+  build_staples<D, DIR>(i, geo, T, ld, u, u + NS);
+
+  uint16_t* own = a.links + (size_t)DIR * V + i;
+  uint32_t b = *own;
+  const uint32_t b0 = b;
+#pragma unroll
+  for (int j = 0; j < NT; ++j) u[j] = T.mul(u[j], b);  // u_j = s_j * b
+  double r1 = 0, m1 = 0;
+#pragma unroll
+  for (int j = 0; j < NS; ++j) r1 = DYM_ADD(r1, s_retr[u[j]]);
+#pragma unroll
+  for (int j = NS; j < NT; ++j) m1 = DYM_ADD(m1, s_retr[u[j]]);
+  double oldact = dym_action(a.beta0, a.beta1, a.beta2, r1, m1);  // changes only on accept
+  for (int h = 0; h < a.nhit; ++h) {
+    const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_METRO);
+    const uint16_t* row = s_sub + dym_pick(r.v[0], a.npool) * a.P;
+    uint32_t e[NT];
+    double r1n = 0, m1n = 0;
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      e[j] = row[u[j]];
+      r1n = DYM_ADD(r1n, s_retr[e[j]]);
+    }
+#pragma unroll
+    for (int j = NS; j < NT; ++j) {
+      e[j] = row[u[j]];
+      m1n = DYM_ADD(m1n, s_retr[e[j]]);
+    }
+    const double newact = dym_action(a.beta0, a.beta1, a.beta2, r1n, m1n);
+    ++hits;
+    if (dym_accept_fast(oldact, newact, dym_u53(r.v[1], r.v[2]))) {
+      b = row[b];
+#pragma unroll
+      for (int j = 0; j < NT; ++j) u[j] = e[j];
+      oldact = newact;
+      ++accs;
+    }
+  }
+  if (b != b0) *own = (uint16_t)b;
+}
+
+__device__ __forceinline__ void flush_counters(unsigned long long* ctr, unsigned hits, unsigned accs,
+                                               unsigned rechecks) {
+  hits = __reduce_add_sync(0xffffffffu, hits);
+  accs = __reduce_add_sync(0xffffffffu, accs);
+  rechecks = __reduce_add_sync(0xffffffffu, rechecks);
+  if ((threadIdx.x & 31) == 0) {
+    if (hits) atomicAdd(ctr + 0, (unsigned long long)hits);
+    if (accs) atomicAdd(ctr + 1, (unsigned long long)accs);
+    if (rechecks) atomicAdd(ctr + 2, (unsigned long long)rechecks);
+  }
+}
+
+}  // namespace dym

@@ -108,6 +108,22 @@ class Measurement:
 
 
 @dataclass
+class LlrResult:
+    """One LLR window (seed_window + rm_solve, llr.cpp:223-250)."""
+    a: float
+    S1: float
+    S2: float
+    status: str
+    drive_sweeps: int
+    sweeps: int
+    hits: int
+    accepts: int
+    phase_accepts: int
+    phase_rejects: int
+    a_hist: np.ndarray = field(repr=False)
+
+
+@dataclass
 class SweepStats:
     hits: int
     accepts: int
@@ -202,6 +218,23 @@ class Lattice:
         out = np.zeros((s.size, 8 * (self.D - 1)), np.uint16)
         check(lib().dym_chain_staples(self._h, d, ptr(s, C.c_uint32), s.size, ptr(out, C.c_uint16)))
         return out
+
+    def llr_energy(self):
+        """(S1, S2): exact plaquette and rectangle action sums (llr.cpp:46-55, 139-151)."""
+        s1, s2 = C.c_double(), C.c_double()
+        check(lib().dym_llr_energy(self._h, C.byref(s1), C.byref(s2)))
+        return s1.value, s2.value
+
+    def llr_run(self, ewin: float, hw: float, a0: float, axis: int = 1, bg: float = 0.0, K: int = 50,
+                NRM: int = 80, nhit: int = 20, drive_cap: int = 20000) -> LlrResult:
+        """Drive into [ewin-hw, ewin+hw], then NRM Robbins-Monro iterations of K
+        constrained sweeps (llr.cpp:223-250); defaults are llr.cpp's."""
+        req = _lib.LlrReq(axis=axis, bg=bg, ewin=ewin, hw=hw, a0=a0, K=K, NRM=NRM, nhit=nhit, drive_cap=drive_cap)
+        res = _lib.LlrResult()
+        hist = np.zeros(max(NRM, 1))
+        check(lib().dym_llr_run(self._h, C.byref(req), C.byref(res), ptr(hist, C.c_double)))
+        return LlrResult(res.a, res.S1, res.S2, _lib.LLR_STATUS.get(res.status, str(res.status)), res.drive_sweeps,
+                         res.sweeps, res.hits, res.accepts, res.phase_accepts, res.phase_rejects, hist[:NRM].copy())
 
     def schedule(self):
         V = C.c_uint32()

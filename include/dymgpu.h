@@ -162,6 +162,39 @@ int dym_schedule_check(int32_t D, int32_t Nt, int32_t Nx, int32_t* nphase, uint6
 int dym_schedule_get(int32_t D, int32_t Nt, int32_t Nx, uint32_t* V, int32_t* nphase, int32_t* phase_dir,
                      uint32_t* phase_len, uint32_t* sites);
 
+/* ----------------------------------------------------------------- batch --- */
+
+/* An ensemble of independent chains updated together (no reference
+ * counterpart: the reference runs one process per chain, evermore.sh and
+ * jobs2run).  One kernel per colour-phase slot updates the slot's phase of
+ * every chain; each chain's configurations are bit-identical to running it
+ * alone with dym_sweep.  Chains stay owned by the caller and must outlive
+ * the batch; they must share D and the device, use DYM_POOL_NEAREST and
+ * DYM_PREC_MIXED with a table eligible for the shared-table path
+ * (dym_group_info.fast_path), at most 4 distinct groups. */
+typedef struct dym_batch dym_batch;
+
+typedef struct {
+  int32_t tile;         /* links per work tile (multiple of 32) */
+  int32_t threads;      /* threads per block (128 or 256) */
+  int32_t grid_per_sm;  /* blocks launched per SM per slot (>= 1) */
+  int32_t use_graph;    /* 1: replay each sweep as a captured CUDA graph */
+} dym_batch_tuning;
+
+int dym_batch_create(int32_t device, dym_batch** out);
+int dym_batch_add(dym_batch* b, dym_chain* c);
+int dym_batch_size(const dym_batch* b, int32_t* nchains, uint64_t* nlinks, int32_t* nslots);
+int dym_batch_set_tuning(dym_batch* b, const dym_batch_tuning* t);
+int dym_batch_get_tuning(const dym_batch* b, dym_batch_tuning* t);
+/* nsweeps sweeps of every chain (nhit hits per link); totals in `total`. */
+int dym_batch_sweep(dym_batch* b, int32_t nsweeps, int32_t nhit, dym_stats* total);
+/* Counters of chain `idx` (order of dym_batch_add) for the last dym_batch_sweep. */
+int dym_batch_chain_counters(const dym_batch* b, int32_t idx, uint64_t* hits, uint64_t* accepts);
+/* Time candidate tunings on the batch's own chains (their configurations,
+ * sweep counters and counters are restored afterwards) and keep the fastest. */
+int dym_batch_autotune(dym_batch* b, int32_t nhit, int32_t nsweeps_per_trial, dym_batch_tuning* best);
+int dym_batch_free(dym_batch* b);
+
 /* ------------------------------------------------------------------- LLR --- */
 
 #define DYM_LLR_MAX_NRM 1024

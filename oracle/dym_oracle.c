@@ -450,3 +450,196 @@ void or_measure(const or_lattice* L, int wl_nx, int wl_nt, double* out, uint64_t
   if (hist) memcpy(hist, h, slots * P * sizeof(uint64_t));
   free(h);
 }
+
+/* -------------------------------------------------------------------- LLR */
+/* Restatement of the engine's colour-parallel LLR (test oracle), following
+ * llr.cpp:178-250 of the reference for the per-hit rule, the drive-in rule
+ * and the Robbins-Monro step, with the class-level window test of the engine
+ * (a colour class's move is kept iff the new windowed energy is in the
+ * window; outside the window iff it is closer to the centre).  Energies are
+ * exact integer class histograms of plaquettes and rectangles. */
+
+#define OR_MAXCLS 32
+
+/* ReTr value classes: elements sorted by ReTr, a new class whenever a value
+ * exceeds the first value of the current class by more than 1e-9; the class
+ * value is the ReTr of the class's lowest-numbered element. */
+static int or_classes(const or_group* g, int* cls, double* val) {
+  const unsigned P = g->P;
+  int* ord = (int*)malloc(sizeof(int) * P);
+  for (unsigned i = 0; i < P; ++i) ord[i] = (int)i;
+  for (unsigned i = 1; i < P; ++i) { /* stable insertion sort by ReTr */
+    int x = ord[i];
+    int j = (int)i - 1;
+    while (j >= 0 && g->ReTr[ord[j]] > g->ReTr[x]) { ord[j + 1] = ord[j]; --j; }
+    ord[j + 1] = x;
+  }
+  int n = 0;
+  double first = 0;
+  for (unsigned k = 0; k < P; ++k) {
+    int i = ord[k];
+    if (k == 0 || g->ReTr[i] - first > 1e-9) { first = g->ReTr[i]; ++n; }
+    cls[i] = n - 1;
+  }
+  free(ord);
+  if (n > OR_MAXCLS) return -1;
+  for (int c = 0; c < n; ++c) {
+    for (unsigned i = 0; i < P; ++i)
+      if (cls[i] == c) { val[c] = g->ReTr[i]; break; }
+  }
+  return n;
+}
+
+static double or_class_sum(const long long* h, const long long* d, const double* v, int n) {
+  double s = 0;
+  for (int c = 0; c < n; ++c) s = s + (double)(h[c] + (d ? d[c] : 0)) * v[c];
+  return s;
+}
+
+enum { OR_DRIVE = 0, OR_SETTLE = 1, OR_RM = 2, OR_DONE = 3, OR_UNREACHED = 4 };
+
+/* out[0..3] = a, S1, S2, mode; iout[0..5] = drive_sweeps, sweeps, hits,
+ * accepts, phase_accepts, phase_rejects; a_hist[NRM]. */
+int or_llr_run(or_lattice* L, const int* phase_dir, const uint32_t* phase_len, const uint32_t* sites, int nphase,
+               int axis, double bg, double ewin, double hw, double a0, int K, int NRM, int nhit, int drive_cap,
+               uint64_t seed, uint32_t first_sweep, double* out, int64_t* iout, double* a_hist) {
+  const or_group* g = L->g;
+  const unsigned D = L->D, V = L->V;
+  int* cls = (int*)malloc(sizeof(int) * g->P);
+  double v[OR_MAXCLS];
+  const int ncls = or_classes(g, cls, v);
+  if (ncls < 0) { free(cls); return -6; }
+  long long h[2][OR_MAXCLS] = {{0}}, d[2][OR_MAXCLS];
+  for (unsigned i = 0; i < V; ++i) {
+    for (unsigned d1 = 0; d1 < D; ++d1)
+      for (unsigned d2 = d1 + 1; d2 < D; ++d2) h[0][cls[plaq_elem(L, i, d1, d2)]]++;
+    for (unsigned d1 = 0; d1 < D; ++d1)
+      for (unsigned d2 = 0; d2 < D; ++d2)
+        if (d1 != d2) h[1][cls[wilson_elem(L, i, d1, d2, 2, 1)]]++;
+  }
+  double E[2] = {or_class_sum(h[0], NULL, v, ncls), or_class_sum(h[1], NULL, v, ncls)};
+  const double W = 2 * hw, elo = ewin - hw, ehi = ewin + hw;
+  const double emid = 0.5 * (elo + ehi), w2 = W * W;
+  const int w = axis - 1;
+  double a = a0, q = 1.0, sumE = 0;
+  int mode = (E[w] >= elo && E[w] <= ehi) ? OR_RM : OR_DRIVE;
+  if (NRM == 0 && mode == OR_RM) mode = OR_DONE;
+  if (mode == OR_DRIVE && drive_cap == 0) mode = OR_UNREACHED;
+  int k = 0, m = 0, drive_sweeps = 0;
+  long long hits = 0, accs = 0, pacc = 0, prej = 0;
+  const long max_sweeps = (long)drive_cap + (long)K * NRM + 2;
+  long sweeps = 0;
+  const int ns = 2 * ((int)D - 1), nr = 6 * ((int)D - 1);
+  uint32_t* chg_site = (uint32_t*)malloc(sizeof(uint32_t) * V);
+  int* chg_old = (int*)malloc(sizeof(int) * V);
+  while (mode < OR_DONE && sweeps < max_sweeps) {
+    const uint32_t sweep = first_sweep + (uint32_t)sweeps;
+    size_t off = 0;
+    for (int p = 0; p < nphase && mode < OR_DONE; ++p) {
+      const unsigned dir = (unsigned)phase_dir[p];
+      memset(d, 0, sizeof d);
+      int nchg = 0;
+      const int drive = (mode == OR_DRIVE);
+      const double t = q * 4294967296.0;
+      const uint32_t qthr = drive ? (t >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)t) : 0u;
+      for (uint32_t kk = 0; kk < phase_len[p]; ++kk) {
+        const unsigned i = sites[off + kk];
+        int st[2 * 7], re[6 * 7];
+        or_staples(L, i, dir, st, re);
+        const int b0 = L->a[i * D + dir];
+        int b = b0;
+        double r1 = 0, m1 = 0;
+        for (int j = 0; j < ns; ++j) r1 += g->ReTr[g->mult[b][st[j]]];
+        for (int j = 0; j < nr; ++j) m1 += g->ReTr[g->mult[b][re[j]]];
+        int part = 1;
+        if (drive) {
+          dym_u32x4 r = dym_hit_random(seed, sweep, i, dir, 0xFFFFFu, DYM_TAG_LLR);
+          part = r.v[0] < qthr;
+        }
+        double cum = 0;
+        for (int hh = 0; part && hh < nhit; ++hh) {
+          dym_u32x4 r = dym_hit_random(seed, sweep, i, dir, (uint32_t)hh, DYM_TAG_LLR);
+          const double u1 = (double)r.v[0] * 0x1p-32;
+          const int bnew = g->mult[b][g->pool[(size_t)(g->npool * u1)]];
+          double r1n = 0, m1n = 0;
+          for (int j = 0; j < ns; ++j) r1n += g->ReTr[g->mult[bnew][st[j]]];
+          for (int j = 0; j < nr; ++j) m1n += g->ReTr[g->mult[bnew][re[j]]];
+          const double dS1 = r1n - r1, dS2 = m1n - m1;
+          const double dEw = axis == 1 ? dS1 : dS2, dEbg = axis == 1 ? dS2 : dS1;
+          int acc;
+          if (drive) {
+            const double Ec = E[w] + cum;
+            acc = fabs(Ec + dEw - emid) < fabs(Ec - emid);
+          } else {
+            acc = dym_exp(-a * dEw - bg * dEbg) > dym_u53(r.v[1], r.v[2]);
+          }
+          ++hits;
+          if (acc) { b = bnew; r1 = r1n; m1 = m1n; cum = cum + dEw; ++accs; }
+        }
+        if (b != b0) {
+          L->a[i * D + dir] = b;
+          chg_site[nchg] = i;
+          chg_old[nchg++] = b0;
+          for (int j = 0; j < ns; ++j) { d[0][cls[g->mult[b0][st[j]]]]--; d[0][cls[g->mult[b][st[j]]]]++; }
+          for (int j = 0; j < nr; ++j) { d[1][cls[g->mult[b0][re[j]]]]--; d[1][cls[g->mult[b][re[j]]]]++; }
+        }
+      }
+      off += phase_len[p];
+      const double En = or_class_sum(h[w], d[w], v, ncls);
+      const int ok = (mode == OR_DRIVE) ? (fabs(En - emid) < fabs(E[w] - emid)) : (En >= elo && En <= ehi);
+      const double dE = En - E[w];
+      if (ok) {
+        for (int c = 0; c < ncls; ++c) { h[0][c] += d[0][c]; h[1][c] += d[1][c]; }
+        E[0] = or_class_sum(h[0], NULL, v, ncls);
+        E[1] = or_class_sum(h[1], NULL, v, ncls);
+        ++pacc;
+      } else {
+        for (int c2 = 0; c2 < nchg; ++c2) L->a[chg_site[c2] * D + dir] = chg_old[c2];
+        ++prej;
+      }
+      if (mode == OR_DRIVE) {
+        const double dist = fabs(emid - E[w]);
+        const double qq = fabs(dE) > 0 ? q * (dist / fabs(dE)) : q * 2.0;
+        q = fmin(1.0, fmax(qq, 0x1.0p-32));
+        if (E[w] >= elo && E[w] <= ehi) mode = OR_SETTLE;
+      }
+      if (p == nphase - 1) {
+        if (mode == OR_DRIVE) {
+          if (++drive_sweeps >= drive_cap) mode = OR_UNREACHED;
+        } else if (mode == OR_SETTLE) {
+          mode = OR_RM; k = 0; m = 0; sumE = 0;
+        } else if (mode == OR_RM) {
+          sumE = sumE + E[w];
+          if (++k == K) {
+            const double gg = sumE / (double)K - ewin;
+            const double step = 12.0 / (w2 * (double)(m + 1));
+            a = a + step * gg;
+            if (a_hist) a_hist[m] = a;
+            ++m; k = 0; sumE = 0;
+            if (m >= NRM) mode = OR_DONE;
+          }
+        }
+      }
+    }
+    ++sweeps;
+  }
+  out[0] = a; out[1] = E[0]; out[2] = E[1]; out[3] = mode;
+  iout[0] = drive_sweeps; iout[1] = sweeps; iout[2] = hits; iout[3] = accs; iout[4] = pacc; iout[5] = prej;
+  free(cls); free(chg_site); free(chg_old);
+  return 0;
+}
+
+/* S1, S2 of the current configuration by the reference's loops (serial). */
+void or_energies(const or_lattice* L, double* S1, double* S2) {
+  const unsigned D = L->D, V = L->V;
+  double s1 = 0, s2 = 0;
+  for (unsigned i = 0; i < V; ++i) {
+    for (unsigned d1 = 0; d1 < D; ++d1)
+      for (unsigned d2 = d1 + 1; d2 < D; ++d2) s1 += L->g->ReTr[plaq_elem(L, i, d1, d2)];
+    for (unsigned d1 = 0; d1 < D; ++d1)
+      for (unsigned d2 = 0; d2 < D; ++d2)
+        if (d1 != d2) s2 += L->g->ReTr[wilson_elem(L, i, d1, d2, 2, 1)];
+  }
+  *S1 = s1;
+  *S2 = s2;
+}

@@ -59,6 +59,9 @@ def lib() -> C.CDLL:
             "or_philox": (None, [P(u32), P(u32), P(u32)]),
             "or_exp": (d, [d]),
             "or_pick": (u32, [u32, u32]),
+            "or_llr_run": (i, [vp, P(C.c_int), P(u32), P(u32), i, i, d, d, d, d, i, i, i, i, u64, u32, P(d),
+                               P(C.c_int64), P(d)]),
+            "or_energies": (None, [vp, P(d), P(d)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(l, name)
@@ -152,6 +155,27 @@ class OracleLattice:
         self.hits += int(ctr[0])
         self.accepts += int(ctr[1])
         return int(ctr[0]), int(ctr[1])
+
+    def energies(self):
+        s1, s2 = C.c_double(), C.c_double()
+        lib().or_energies(self.h, C.byref(s1), C.byref(s2))
+        return s1.value, s2.value
+
+    def llr_run(self, sched, ewin, hw, a0, axis=1, bg=0.0, K=50, NRM=80, nhit=20, drive_cap=20000, seed=0,
+                first_sweep=0):
+        pd, pl, sites = sched
+        out = np.zeros(4)
+        iout = np.zeros(6, np.int64)
+        hist = np.zeros(max(NRM, 1))
+        rc = lib().or_llr_run(self.h, _p(pd, C.c_int), _p(pl, C.c_uint32), _p(sites, C.c_uint32), len(pd), axis,
+                              float(bg), float(ewin), float(hw), float(a0), K, NRM, nhit, drive_cap, seed, first_sweep,
+                              _p(out, C.c_double), _p(iout, C.c_int64), _p(hist, C.c_double))
+        if rc:
+            raise ValueError(f"oracle llr failed ({rc})")
+        status = {0: "drive", 1: "settle", 2: "rm", 3: "done", 4: "unreached"}[int(out[3])]
+        return dict(a=out[0], S1=out[1], S2=out[2], status=status, drive_sweeps=int(iout[0]), sweeps=int(iout[1]),
+                    hits=int(iout[2]), accepts=int(iout[3]), phase_accepts=int(iout[4]),
+                    phase_rejects=int(iout[5]), a_hist=hist[:NRM].copy())
 
     def measure(self, wl_nx: int, wl_nt: int, want_hist: bool = False):
         out = np.zeros(4 + max(wl_nx, 0) * max(wl_nt, 0))
