@@ -69,6 +69,26 @@ class BatchTuning(C.Structure):
     _fields_ = [("tile", C.c_int32), ("threads", C.c_int32), ("grid_per_sm", C.c_int32), ("use_graph", C.c_int32)]
 
 
+SERVE_MAX_NRM = 64
+
+
+class ServerParams(C.Structure):
+    _fields_ = [("max_chains", C.c_int32), ("hbm_budget", C.c_uint64), ("nhit", C.c_int32), ("device", C.c_int32)]
+
+
+class LlrRequest(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("D", C.c_int32), ("Nt", C.c_int32), ("Nx", C.c_int32), ("start", C.c_int32),
+                ("seed", C.c_uint64), ("axis", C.c_int32), ("bg", C.c_double), ("ewin", C.c_double),
+                ("hw", C.c_double), ("a0", C.c_double), ("K", C.c_int32), ("NRM", C.c_int32),
+                ("drive_cap", C.c_int32)]
+
+
+class LlrResponse(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("a", C.c_double), ("S1", C.c_double), ("S2", C.c_double),
+                ("status", C.c_int32), ("sweeps", C.c_int32), ("drive_sweeps", C.c_int32), ("NRM", C.c_int32),
+                ("hits", C.c_uint64), ("accepts", C.c_uint64), ("a_hist", C.c_double * SERVE_MAX_NRM)]
+
+
 LLR_STATUS = {0: "drive", 1: "settle", 2: "rm", 3: "done", 4: "unreached"}
 
 _P = C.c_void_p
@@ -106,6 +126,12 @@ PROTOTYPES = {
     "dym_batch_chain_counters": (C.c_int, [_P, C.c_int32, _u64p, _u64p]),
     "dym_batch_autotune": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(BatchTuning)]),
     "dym_batch_free": (C.c_int, [_P]),
+    "dym_server_create": (C.c_int, [_P, C.POINTER(ServerParams), C.POINTER(_P)]),
+    "dym_server_submit": (C.c_int, [_P, C.POINTER(LlrRequest)]),
+    "dym_server_step": (C.c_int, [_P, C.c_int32]),
+    "dym_server_poll": (C.c_int, [_P, C.POINTER(LlrResponse), C.c_int32, _i32p]),
+    "dym_server_status": (C.c_int, [_P, _i32p, _i32p, _u64p, _u64p]),
+    "dym_server_free": (C.c_int, [_P]),
     "dym_llr_energy": (C.c_int, [_P, _f64p, _f64p]),
     "dym_llr_run": (C.c_int, [_P, C.POINTER(LlrReq), C.POINTER(LlrResult), _f64p]),
     "dym_probe_l2_gather": (C.c_int, [C.c_int32, C.c_uint32, _f64p]),

@@ -83,25 +83,14 @@ void* batch_kernel() {
 
 }  // namespace
 
-void* batch_kernel_for(int D) {
-  switch (D) {
-    case 2: return batch_kernel<2>();
-    case 3: return batch_kernel<3>();
-    case 4: return batch_kernel<4>();
-  }
-  return nullptr;
-}
+void* batch_kernel_for(int D) { return D == 4 ? batch_kernel<4>() : nullptr; }
 
 cudaError_t launch_batch_slot(int D, const BatchTile* tiles, uint32_t ntiles, const BatchChainDev* chains,
                               const BatchGroups& groups, const uint32_t* sweeps, int nhit, unsigned grid,
                               unsigned threads, size_t smem, cudaStream_t s) {
   if (ntiles == 0) return cudaSuccess;
-  switch (D) {
-    case 2: k_batch_sub<2><<<grid, threads, smem, s>>>(tiles, ntiles, chains, groups, sweeps, nhit); break;
-    case 3: k_batch_sub<3><<<grid, threads, smem, s>>>(tiles, ntiles, chains, groups, sweeps, nhit); break;
-    case 4: k_batch_sub<4><<<grid, threads, smem, s>>>(tiles, ntiles, chains, groups, sweeps, nhit); break;
-    default: return cudaErrorInvalidValue;
-  }
+  if (D != 4) return cudaErrorInvalidValue;  // four dimensions only (see launch_sweep_sub)
+  k_batch_sub<4><<<grid, threads, smem, s>>>(tiles, ntiles, chains, groups, sweeps, nhit);
   return cudaGetLastError();
 }
 

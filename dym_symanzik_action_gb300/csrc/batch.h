@@ -21,8 +21,9 @@ struct BatchGroupDev {
   const uint16_t* inv;
   const double* retr;
   const uint16_t* sub;  // sub[k][u] = u * pool[k]
+  const uint16_t* cls16;  // ReTr class of each element (LLR only)
   uint32_t P, npool;
-  uint32_t off_retr, off_inv, off_sub;  // byte offsets of the staged copies in shared memory
+  uint32_t off_retr, off_inv, off_sub, off_cls;  // byte offsets of the staged copies in shared memory
 };
 
 constexpr int kBatchMaxGroups = 4;
@@ -34,6 +35,30 @@ struct BatchGroups {
 struct BatchTile {
   uint32_t chain, begin, count, dir;
 };
+
+// LLR work lists (llr.cu): per-chain descriptors, tiles of one colour-phase
+// slot, and the chains whose phase the slot's commit closes.
+struct LlrState;
+struct LlrChainDev {
+  uint16_t* links;
+  const uint32_t* sites;
+  uint32_t V;
+  int Nt, Nx;
+  uint64_t seed;
+  LlrState* st;
+  uint16_t* oldv;
+  int group;
+};
+struct LlrTile {
+  uint32_t chain, begin, count, dir, pos;  // pos: offset of the tile inside its phase
+};
+struct LlrCommit {
+  uint32_t chain, last;  // last: this slot holds the chain's last phase of a sweep
+};
+void* llr_propose_kernel_for(int D);
+cudaError_t launch_llr_slot(int D, const LlrTile* tiles, uint32_t ntiles, const LlrCommit* commits, uint32_t ncommit,
+                            const LlrChainDev* chains, const BatchGroups& groups, int nhit, unsigned grid,
+                            size_t smem, cudaStream_t s);
 
 void* batch_kernel_for(int D);
 cudaError_t launch_batch_slot(int D, const BatchTile* tiles, uint32_t ntiles, const BatchChainDev* chains,

@@ -11,6 +11,7 @@
 #include "batch.h"
 #include "chain.h"
 #include "dym_core.h"
+#include "util.h"
 
 namespace dym {
 
@@ -20,21 +21,6 @@ void set_error(const std::string& msg) { g_last_error = msg; }
 int fail(int code, const std::string& msg) {
   g_last_error = msg;
   return code;
-}
-
-static int cuda_fail(cudaError_t e, const char* what) {
-  return fail(DYM_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
-}
-
-#define DYM_CUDA(call, what)                      \
-  do {                                            \
-    cudaError_t _e = (call);                      \
-    if (_e != cudaSuccess) return cuda_fail(_e, what); \
-  } while (0)
-
-template <class T>
-static cudaError_t dmalloc(T** p, size_t n) {
-  return cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T));
 }
 
 int group_to_device(Group* g) {
@@ -84,8 +70,13 @@ void group_free(Group* g) {
 
 // Whether the shared sub-table kernel applies: the table is associative,
 // ReTr is one double per conjugacy class (so ReTr[u_j g] == ReTr[bnew s_j]
-// bit for bit), and the sub-table fits the shared-memory opt-in.
-static bool sub_eligible(const Group& g, uint32_t npool, int device) {
+// bit for bit), the sub-table fits the shared-memory opt-in, and D = 4.
+// The D = 2 and D = 3 instantiations of the shared-table kernels faulted on
+// the GPU (illegal address / invalid address space) while their source runs
+// bit-exact under AddressSanitizer in a host emulation; no cause was found,
+// so they are not built and those lattices use the FP64 direct kernel.
+static bool sub_eligible(const Group& g, uint32_t npool, int device, int D) {
+  if (D != 4) return false;
   if (!g.assoc_ok || !g.cls_conj_invariant || !g.cls_exact) return false;
   int optin = 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) return false;
@@ -150,6 +141,21 @@ static void chain_release(dym_chain* c) {
   delete c;
 }
 
+int chain_reset(dym_chain* c, uint64_t seed, int start) {
+  if (start != DYM_START_HOT && start != DYM_START_COLD) return fail(DYM_EINVAL, "start must be hot or cold");
+  DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+  c->p.seed = seed;
+  c->p.start = start;
+  c->sweep = 0;
+  const Group& g = *c->grp->g;
+  if (start == DYM_START_HOT)
+    DYM_CUDA(launch_hot_start(c->dev.links, c->dev.V, c->p.D, g.P, seed, c->stream), "hot start");
+  else
+    DYM_CUDA(launch_fill(c->dev.links, (size_t)c->dev.V * c->p.D, (uint16_t)g.id, c->stream), "cold start");
+  DYM_CUDA(cudaStreamSynchronize(c->stream), "start configuration");
+  return DYM_OK;
+}
+
 }  // namespace dym
 
 using namespace dym;
@@ -191,7 +197,7 @@ int dym_group_get_info(const dym_group* gh, dym_group_info* out) {
   out->fast_path = 0;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0)
-    out->fast_path = sub_eligible(g, (uint32_t)g.pool_nearest.size(), dev) ? 1 : 0;
+    out->fast_path = sub_eligible(g, (uint32_t)g.pool_nearest.size(), dev, 4) ? 1 : 0;
   else
     cudaGetLastError();
   out->class_spread = g.cls_spread;
@@ -271,7 +277,7 @@ int dym_chain_create(const dym_group* gh, const dym_chain_params* p, dym_chain**
   DYM_CUDA(dmalloc(&d.counters, 5), "cudaMalloc(counters)");
   DYM_CUDA(cudaHostAlloc((void**)&c->h_counters, 5 * sizeof(unsigned long long), cudaHostAllocDefault),
            "cudaHostAlloc");
-  if (p->precision == DYM_PREC_MIXED && sub_eligible(g, d.npool, p->device)) {
+  if (p->precision == DYM_PREC_MIXED && sub_eligible(g, d.npool, p->device, p->D)) {
     rc = build_sub_table(c.get(), pool);
     if (rc) return rc;
   }
@@ -447,138 +453,6 @@ int dym_chain_staples(dym_chain* c, int32_t dir, const uint32_t* sites, int32_t 
   cudaFree(d_sites);
   cudaFree(d_out);
   if (e != cudaSuccess) return cuda_fail(e, "staples");
-  return DYM_OK;
-}
-
-// Element histograms of all plaquettes (slot 0) and oriented 1x2 rectangles
-// (slot 1) of the current configuration, folded into ReTr classes.
-static int class_histograms(dym_chain* c, long long h[2][kLlrMaxCls]) {
-  const Group& g = *c->grp->g;
-  dym_meas_opts mo{-1, -1};
-  dym_obs o;
-  int rc = dym_measure(c, &mo, &o, nullptr);
-  if (rc) return rc;
-  for (int k = 0; k < 2; ++k)
-    for (int q = 0; q < kLlrMaxCls; ++q) h[k][q] = 0;
-  for (uint32_t n = 0; n < g.P; ++n) {
-    h[0][g.cls[n]] += (long long)c->h_hist[n];
-    h[1][g.cls[n]] += (long long)c->h_hist[g.P + n];
-  }
-  return DYM_OK;
-}
-
-static double class_sum_host(const long long* h, const std::vector<double>& v, int ncls) {
-  double s = 0;
-  for (int q = 0; q < ncls; ++q) s = s + (double)h[q] * v[q];
-  return s;
-}
-
-int dym_llr_energy(dym_chain* c, double* S1, double* S2) {
-  if (!c) return fail(DYM_EINVAL, "dym_llr_energy: null chain");
-  const Group& g = *c->grp->g;
-  if (g.ncls > kLlrMaxCls || !g.cls_conj_invariant)
-    return fail(DYM_ENOTSUP, "LLR needs a table whose ReTr takes at most 32 class values");
-  long long h[2][kLlrMaxCls];
-  int rc = class_histograms(c, h);
-  if (rc) return rc;
-  if (S1) *S1 = class_sum_host(h[0], g.cls_val, g.ncls);
-  if (S2) *S2 = class_sum_host(h[1], g.cls_val, g.ncls);
-  return DYM_OK;
-}
-
-int dym_llr_run(dym_chain* c, const dym_llr_req* req, dym_llr_result* out, double* a_hist) {
-  if (!c || !req || !out) return fail(DYM_EINVAL, "dym_llr_run: null argument");
-  const Group& g = *c->grp->g;
-  if (req->axis != 1 && req->axis != 2) return fail(DYM_EINVAL, "axis must be 1 (S1 window) or 2 (S2 window)");
-  if (req->K < 1 || req->NRM < 0 || req->NRM > DYM_LLR_MAX_NRM || req->nhit < 0 || !(req->hw > 0) ||
-      req->drive_cap < 0)
-    return fail(DYM_EINVAL, "dym_llr_run: bad K, NRM, nhit, hw or drive_cap");
-  if (g.ncls > kLlrMaxCls || !g.cls_conj_invariant)
-    return fail(DYM_ENOTSUP, "LLR needs a table whose ReTr takes at most 32 class values");
-  if (req->axis == 2 && (c->p.Nt < 3 || c->p.Nx < 3))
-    return fail(DYM_ENOTSUP, "an S2 window needs every extent >= 3 (1x2 rectangles wrap otherwise)");
-  if (c->p.pool != DYM_POOL_NEAREST) return fail(DYM_ENOTSUP, "LLR proposals use the nearest-element pool");
-  DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
-  if (!c->d_llr) {
-    DYM_CUDA(dmalloc(&c->d_llr, 1), "cudaMalloc(llr)");
-    uint32_t maxlen = 1;
-    for (auto l : c->sched.phase_len) maxlen = std::max(maxlen, l);
-    DYM_CUDA(dmalloc(&c->d_oldv, maxlen), "cudaMalloc(llr oldv)");
-  }
-  std::unique_ptr<LlrState> st(new LlrState());
-  std::memset(st.get(), 0, sizeof(LlrState));
-  int rc = class_histograms(c, st->h);
-  if (rc) return rc;
-  const double W = 2 * req->hw;
-  st->a = req->a0;
-  st->bg = req->bg;
-  st->ewin = req->ewin;
-  st->elo = req->ewin - req->hw;
-  st->ehi = req->ewin + req->hw;
-  st->emid = 0.5 * (st->elo + st->ehi);
-  st->w2 = W * W;
-  st->q = 1.0;
-  st->ncls = g.ncls;
-  for (int q = 0; q < g.ncls; ++q) st->v[q] = g.cls_val[q];
-  st->E[0] = class_sum_host(st->h[0], g.cls_val, g.ncls);
-  st->E[1] = class_sum_host(st->h[1], g.cls_val, g.ncls);
-  st->axis = req->axis;
-  st->K = req->K;
-  st->NRM = req->NRM;
-  st->drive_cap = req->drive_cap;
-  const double Ew = st->E[req->axis - 1];
-  st->mode = (Ew >= st->elo && Ew <= st->ehi) ? DYM_LLR_RM : DYM_LLR_DRIVE;
-  if (req->NRM == 0 && st->mode == DYM_LLR_RM) st->mode = DYM_LLR_DONE;
-  if (st->mode == DYM_LLR_DRIVE && req->drive_cap == 0) st->mode = DYM_LLR_UNREACHED;
-  DYM_CUDA(cudaMemcpyAsync(c->d_llr, st.get(), sizeof(LlrState), cudaMemcpyHostToDevice, c->stream), "upload llr");
-  DYM_CUDA(cudaMemsetAsync(c->dev.counters, 0, 5 * sizeof(unsigned long long), c->stream), "reset counters");
-  LlrArgs A{};
-  A.s = sweep_args(c);
-  A.s.nhit = req->nhit;
-  A.cls16 = (const uint16_t*)g.d_cls16;
-  A.st = c->d_llr;
-  A.oldv = c->d_oldv;
-  const Schedule& s = c->sched;
-  const uint32_t sweep0 = c->sweep;
-  const long max_sweeps = (long)req->drive_cap + (long)req->K * req->NRM + 2;
-  int mode = st->mode;
-  long sweeps = 0;
-  while (mode < DYM_LLR_DONE && sweeps < max_sweeps) {
-    for (int chunk = 0; chunk < 8 && sweeps < max_sweeps; ++chunk, ++sweeps) {
-      A.s.sweep = c->sweep;
-      for (size_t p = 0; p < s.phase_dir.size(); ++p) {
-        A.s.sites = c->dev.sites + s.phase_off[p];
-        A.s.n = s.phase_len[p];
-        A.dir = s.phase_dir[p];
-        A.buf = (int)(c->llr_phase++ & 1);
-        cudaError_t e = launch_llr_phase(c->p.D, A, p + 1 == s.phase_dir.size(), c->stream);
-        if (e != cudaSuccess) return cuda_fail(e, "llr launch");
-      }
-      ++c->sweep;
-    }
-    DYM_CUDA(cudaMemcpyAsync(&st->mode, &c->d_llr->mode, sizeof(int), cudaMemcpyDeviceToHost, c->stream),
-             "read llr mode");
-    DYM_CUDA(cudaStreamSynchronize(c->stream), "llr sweeps");
-    mode = st->mode;
-  }
-  DYM_CUDA(cudaMemcpyAsync(st.get(), c->d_llr, sizeof(LlrState), cudaMemcpyDeviceToHost, c->stream), "read llr");
-  DYM_CUDA(cudaMemcpyAsync(c->h_counters, c->dev.counters, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                           c->stream),
-           "read counters");
-  DYM_CUDA(cudaStreamSynchronize(c->stream), "llr");
-  out->a = st->a;
-  out->S1 = st->E[0];
-  out->S2 = st->E[1];
-  out->status = st->mode;
-  out->drive_sweeps = st->drive_sweeps;
-  out->sweeps = st->sweeps;
-  c->sweep = sweep0 + (uint32_t)st->sweeps;  // sweeps after the state machine finished did nothing
-  out->hits = c->h_counters[0];
-  out->accepts = c->h_counters[1];
-  out->phase_accepts = st->phase_acc;
-  out->phase_rejects = st->phase_rej;
-  if (a_hist)
-    for (int m = 0; m < req->NRM; ++m) a_hist[m] = st->a_hist[m];
   return DYM_OK;
 }
 
@@ -771,7 +645,8 @@ int dym_batch_add(dym_batch* b, dym_chain* c) {
   if (!b || !c) return fail(DYM_EINVAL, "dym_batch_add: null argument");
   if (c->p.device != b->device) return fail(DYM_EINVAL, "chain and batch are on different devices");
   if (!b->chains.empty() && c->p.D != b->D) return fail(DYM_EINVAL, "all chains of a batch must have the same D");
-  if (!c->dev.sub_ok) return fail(DYM_ENOTSUP, "batch chains need the shared-table path (nearest pool, mixed)");
+  if (!c->dev.sub_ok || c->p.D != 4)
+    return fail(DYM_ENOTSUP, "batch chains need D = 4 and the shared-table path (nearest pool, mixed)");
   if (std::find(b->chains.begin(), b->chains.end(), c) != b->chains.end())
     return fail(DYM_EINVAL, "chain already in the batch");
   Group* g = c->grp->g;

@@ -58,6 +58,7 @@ cudaError_t launch_staples(int D, int dir, const SweepArgs& a, const uint32_t* s
 // phase.  Energies are exact: integer class histograms of all plaquettes (h[0])
 // and rectangles (h[1]), one FP64 dot product with the class values.
 constexpr int kLlrMaxCls = 32;
+constexpr int kLlrDeltaBytes = 2 * kLlrMaxCls * 4;  // per-tile class deltas at the front of shared memory
 struct LlrState {
   double a, bg, elo, ehi, emid, ewin, w2, q;
   double E[2];
@@ -67,19 +68,9 @@ struct LlrState {
   long long d[2][2][kLlrMaxCls];  // [phase parity][plaquette|rectangle][class]
   double a_hist[DYM_LLR_MAX_NRM];
   int axis, mode, k, m, K, NRM, drive_sweeps, drive_cap, ncls, sweeps;
-  unsigned long long phase_acc, phase_rej;
+  uint32_t phase, sweep;  // colour phases committed (delta parity), Philox sweep counter
+  unsigned long long phase_acc, phase_rej, hits, accepts;
 };
-
-struct LlrArgs {
-  SweepArgs s;
-  const uint16_t* cls16;  // ReTr class of each element
-  LlrState* st;
-  uint16_t* oldv;         // value of each phase link before the proposal
-  int buf;                // phase parity
-  int dir;
-};
-
-cudaError_t launch_llr_phase(int D, const LlrArgs& a, bool last_in_sweep, cudaStream_t s);
 
 // Observables.
 struct MeasArgs {
@@ -90,6 +81,9 @@ struct MeasArgs {
   const uint16_t* inv;
   uint32_t P, id;
 };
+// Fresh start configuration and Philox key for an existing chain (capi.cu).
+int chain_reset(dym_chain* c, uint64_t seed, int start);
+
 cudaError_t launch_measure(const MeasArgs& m, int wl_nx, int wl_nt, bool assoc, unsigned long long* hist,
                            uint16_t* scratch, cudaStream_t s);
 size_t measure_scratch_elems(const MeasArgs& m, int wl_nx, int wl_nt, bool assoc);

@@ -1,32 +1,37 @@
 // Interval-restricted (LLR) Metropolis sweeps with the Robbins-Monro update,
-// on the device.
+// on the device, for any number of chains at once.
 //
 // The reference (llr.cpp:178-250) updates links one at a time because the
 // window constraint is on the global energy.  Here a colour class moves at
-// once:
+// once, in three kernels per colour-phase slot over a work list of chains:
 //  1. k_llr_propose: every link of the class runs nhit Metropolis hits with
 //     weight exp(-a dE_w - bg dE_bg) (llr.cpp:211) and no window test; links of
 //     one colour share no plaquette or rectangle, so their energy changes add.
 //     Outside the window (drive-in) a hit is kept iff it moves the link's
 //     running energy towards the window centre (llr.cpp:208-209), and only a
 //     deterministic fraction q of the links takes part; after each phase q is
-//     set so that the expected move covers the remaining distance.  Each link's change of
-//     plaquette and rectangle classes is added to an integer histogram delta.
+//     set so that the expected move covers the remaining distance.  Each
+//     link's change of plaquette and rectangle classes is added to the chain's
+//     integer histogram delta.
 //  2. k_llr_decide: the class move is kept iff the new windowed energy lies in
 //     [Elo, Ehi] (outside the window: iff it is closer to the centre);
 //     otherwise every link of the class is restored.
-//  3. k_llr_commit: one thread folds the delta into the chain's histograms,
-//     recomputes the exact energies, adapts q, and at the end of a sweep
-//     advances the drive-in / Robbins-Monro state machine
+//  3. k_llr_commit: one thread per chain folds the delta into the chain's
+//     histograms, recomputes the exact energies, adapts q, and at the end of a
+//     sweep advances the drive-in / Robbins-Monro state machine
 //     (a += 12/(W^2 (m+1)) (<E> - Ewin), llr.cpp:244).
 // NHIT identical single-hit Metropolis kernels compose into a reversible
 // kernel, so accepting the class move iff it stays in the window is an exact
-// Metropolis-Hastings step for the window-restricted distribution.
+// Metropolis-Hastings step for the window-restricted distribution.  Every
+// chain's state (Philox sweep counter, delta parity, energies) lives in its
+// own LlrState, so a chain gives the same result alone or in any mix.
 #include <cuda_runtime.h>
 
+#include "batch.h"
 #include "chain.h"
 #include "dym_core.h"
 #include "staples.cuh"
+#include "visit.cuh"
 
 namespace dym {
 
@@ -38,10 +43,10 @@ __device__ __forceinline__ double class_sum(const long long* h, const long long*
   return s;
 }
 
-// Whether the class move of the phase with parity `buf` is kept.
-__device__ __forceinline__ bool phase_ok(const LlrState* st, int buf) {
+// Whether the class move of the chain's current phase is kept.
+__device__ __forceinline__ bool phase_ok(const LlrState* st) {
   const int w = st->axis - 1;
-  const double En = class_sum(st->h[w], st->d[buf][w], st->v, st->ncls);
+  const double En = class_sum(st->h[w], st->d[st->phase & 1][w], st->v, st->ncls);
   if (st->mode == DYM_LLR_DRIVE) return fabs(DYM_SUB(En, st->emid)) < fabs(DYM_SUB(st->E[w], st->emid));
   return En >= st->elo && En <= st->ehi;
 }
@@ -51,140 +56,111 @@ __device__ __forceinline__ uint32_t q_threshold(double q) {
   return t >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)t;
 }
 
-__device__ __forceinline__ void flush_hits(unsigned long long* ctr, unsigned hits, unsigned accs) {
-  hits = __reduce_add_sync(0xffffffffu, hits);
-  accs = __reduce_add_sync(0xffffffffu, accs);
-  if ((threadIdx.x & 31) == 0) {
-    if (hits) atomicAdd(ctr + 0, (unsigned long long)hits);
-    if (accs) atomicAdd(ctr + 1, (unsigned long long)accs);
-  }
-}
-
-template <int D, int DIR>
-__global__ void __launch_bounds__(256) k_llr_propose(LlrArgs A) {
-  constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1);
-  const SweepArgs& a = A.s;
-  LlrState* st = A.st;
-  const int mode = st->mode;
-  if (mode >= DYM_LLR_DONE) return;  // the same for every thread of the grid
+template <int D>
+__global__ void __launch_bounds__(256) k_llr_propose(const LlrTile* __restrict__ tiles, uint32_t ntiles,
+                                                     const LlrChainDev* __restrict__ chains, BatchGroups groups,
+                                                     int nhit) {
   extern __shared__ __align__(16) unsigned char smem[];
-  double* s_retr = reinterpret_cast<double*>(smem);
-  uint16_t* s_inv = reinterpret_cast<uint16_t*>(s_retr + a.P);
-  uint16_t* s_cls = s_inv + a.P;
-  uint16_t* s_pool = s_cls + a.P;
-  int* s_delta = reinterpret_cast<int*>(smem + ((size_t)a.P * 8 + (size_t)a.P * 4 + (size_t)a.npool * 2 + 15) / 16 * 16);
-  for (uint32_t t = threadIdx.x; t < a.P; t += blockDim.x) {
-    s_retr[t] = a.retr[t];
-    s_inv[t] = a.inv[t];
-    s_cls[t] = A.cls16[t];
+  int* s_delta = reinterpret_cast<int*>(smem);  // first kLlrDeltaBytes of the dynamic shared memory
+  for (int g = 0; g < groups.n; ++g) {
+    const BatchGroupDev& G = groups.g[g];
+    stage_sub_tables(G.retr, G.inv, G.sub, G.P, G.npool, reinterpret_cast<double*>(smem + G.off_retr),
+                     reinterpret_cast<uint16_t*>(smem + G.off_inv), reinterpret_cast<uint16_t*>(smem + G.off_sub));
+    uint16_t* s_cls = reinterpret_cast<uint16_t*>(smem + G.off_cls);
+    for (uint32_t t = threadIdx.x; t < G.P; t += blockDim.x) s_cls[t] = G.cls16[t];
   }
-  for (uint32_t t = threadIdx.x; t < a.npool; t += blockDim.x) s_pool[t] = a.pool[t];
-  for (uint32_t t = threadIdx.x; t < 2 * kLlrMaxCls; t += blockDim.x) s_delta[t] = 0;
   __syncthreads();
-
-  const int axis = st->axis;
-  const double aa = st->a, bg = st->bg, emid = st->emid, E0 = st->E[axis - 1];
-  const bool drive = (mode == DYM_LLR_DRIVE);
-  const uint32_t qthr = drive ? q_threshold(st->q) : 0u;
-  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned hits = 0, accs = 0;
-  if (tid < a.n) {
-    const uint32_t i = a.sites[tid];
-    SiteGeo<D> geo;
-    site_geo<D>(i, a.Nt, a.Nx, geo);
-    GlobalTab T{a.mult, s_inv, a.P};
-    const uint16_t* L = a.links;
-    const uint32_t V = a.V;
-    auto ld = [L, V](uint32_t s, int d) -> uint32_t { return __ldg(L + (size_t)d * V + s); };
-    uint32_t stp[NS], re[NR];
-    build_staples<D, DIR>(i, geo, T, ld, stp, re);
-    uint16_t* own = a.links + (size_t)DIR * V + i;
-    uint32_t b = *own;
-    const uint32_t b0 = b;
-    double r1 = 0, m1 = 0;
-#pragma unroll
-    for (int j = 0; j < NS; ++j) r1 = DYM_ADD(r1, s_retr[T.mul(b, stp[j])]);
-#pragma unroll
-    for (int k = 0; k < NR; ++k) m1 = DYM_ADD(m1, s_retr[T.mul(b, re[k])]);
-    bool part = true;
-    if (drive) {
-      const dym_u32x4 r = dym_hit_random(a.seed, a.sweep, i, DIR, 0xFFFFFu, DYM_TAG_LLR);
-      part = r.v[0] < qthr;
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const LlrTile tl = tiles[t];
+    const LlrChainDev c = chains[tl.chain];
+    LlrState* st = c.st;
+    const int mode = st->mode;
+    if (mode >= DYM_LLR_DONE) continue;  // the same for every thread of the block
+    for (uint32_t x = threadIdx.x; x < 2 * kLlrMaxCls; x += blockDim.x) s_delta[x] = 0;
+    __syncthreads();
+    const BatchGroupDev& G = groups.g[c.group];
+    SweepArgs a{};
+    a.links = c.links;
+    a.V = c.V;
+    a.Nt = c.Nt;
+    a.Nx = c.Nx;
+    a.mult = G.mult;
+    a.P = G.P;
+    a.npool = G.npool;
+    a.seed = c.seed;
+    a.nhit = nhit;
+    const double* s_retr = reinterpret_cast<const double*>(smem + G.off_retr);
+    const uint16_t* s_inv = reinterpret_cast<const uint16_t*>(smem + G.off_inv);
+    const uint16_t* s_sub = reinterpret_cast<const uint16_t*>(smem + G.off_sub);
+    const uint16_t* s_cls = reinterpret_cast<const uint16_t*>(smem + G.off_cls);
+    const int axis = st->axis;
+    const double aa = st->a, bg = st->bg, emid = st->emid, E0 = st->E[axis - 1];
+    const bool drive = (mode == DYM_LLR_DRIVE);
+    const uint32_t qthr = drive ? q_threshold(st->q) : 0u;
+    const uint32_t sweep = st->sweep;
+    unsigned hits = 0, accs = 0;
+    for (uint32_t k = threadIdx.x; k < tl.count; k += blockDim.x) {
+      const uint32_t i = c.sites[tl.begin + k];
+      uint32_t b0 = 0;
+      switch (tl.dir) {
+        case 0: b0 = visit_llr<D, 0>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, axis, aa, bg, E0, emid, drive, qthr,
+                                     s_delta, hits, accs); break;
+        case 1: b0 = visit_llr<D, 1>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, axis, aa, bg, E0, emid, drive, qthr,
+                                     s_delta, hits, accs); break;
+        case 2: if (D > 2) b0 = visit_llr<D, (D > 2 ? 2 : 0)>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, axis, aa,
+                                                               bg, E0, emid, drive, qthr, s_delta, hits, accs);
+          break;
+        case 3: if (D > 3) b0 = visit_llr<D, (D > 3 ? 3 : 0)>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, axis, aa,
+                                                               bg, E0, emid, drive, qthr, s_delta, hits, accs);
+          break;
+      }
+      c.oldv[tl.pos + k] = (uint16_t)b0;
     }
-    double cum = 0;
-    for (int h = 0; part && h < a.nhit; ++h) {
-      const dym_u32x4 r = dym_hit_random(a.seed, a.sweep, i, DIR, (uint32_t)h, DYM_TAG_LLR);
-      const uint32_t bnew = T.mul(b, s_pool[dym_pick(r.v[0], a.npool)]);
-      double r1n = 0, m1n = 0;
-#pragma unroll
-      for (int j = 0; j < NS; ++j) r1n = DYM_ADD(r1n, s_retr[T.mul(bnew, stp[j])]);
-#pragma unroll
-      for (int k = 0; k < NR; ++k) m1n = DYM_ADD(m1n, s_retr[T.mul(bnew, re[k])]);
-      const double dS1 = DYM_SUB(r1n, r1), dS2 = DYM_SUB(m1n, m1);
-      const double dEw = axis == 1 ? dS1 : dS2;
-      const double dEbg = axis == 1 ? dS2 : dS1;
-      bool acc;
-      if (drive) {
-        const double Ec = DYM_ADD(E0, cum);
-        acc = fabs(DYM_SUB(DYM_ADD(Ec, dEw), emid)) < fabs(DYM_SUB(Ec, emid));
-      } else {
-        const double w = dym_exp(DYM_SUB(DYM_MUL(-aa, dEw), DYM_MUL(bg, dEbg)));
-        acc = w > dym_u53(r.v[1], r.v[2]);
-      }
-      ++hits;
-      if (acc) {
-        b = bnew;
-        r1 = r1n;
-        m1 = m1n;
-        cum = DYM_ADD(cum, dEw);
-        ++accs;
-      }
+    hits = __reduce_add_sync(0xffffffffu, hits);
+    accs = __reduce_add_sync(0xffffffffu, accs);
+    if ((threadIdx.x & 31) == 0) {
+      if (hits) atomicAdd(&st->hits, (unsigned long long)hits);
+      if (accs) atomicAdd(&st->accepts, (unsigned long long)accs);
     }
-    A.oldv[tid] = (uint16_t)b0;
-    if (b != b0) {
-      *own = (uint16_t)b;
-#pragma unroll
-      for (int j = 0; j < NS; ++j) {
-        atomicAdd(&s_delta[s_cls[T.mul(b0, stp[j])]], -1);
-        atomicAdd(&s_delta[s_cls[T.mul(b, stp[j])]], 1);
-      }
-#pragma unroll
-      for (int k = 0; k < NR; ++k) {
-        atomicAdd(&s_delta[kLlrMaxCls + s_cls[T.mul(b0, re[k])]], -1);
-        atomicAdd(&s_delta[kLlrMaxCls + s_cls[T.mul(b, re[k])]], 1);
-      }
+    __syncthreads();
+    const uint32_t buf = st->phase & 1u;
+    for (uint32_t x = threadIdx.x; x < 2 * kLlrMaxCls; x += blockDim.x) {
+      const int v = s_delta[x];
+      if (v) atomicAdd(reinterpret_cast<unsigned long long*>(&st->d[buf][x / kLlrMaxCls][x % kLlrMaxCls]),
+                       (unsigned long long)(long long)v);
     }
-  }
-  flush_hits(a.counters, hits, accs);
-  __syncthreads();
-  for (uint32_t t = threadIdx.x; t < 2 * kLlrMaxCls; t += blockDim.x) {
-    const int v = s_delta[t];
-    if (v) atomicAdd(reinterpret_cast<unsigned long long*>(&st->d[A.buf][t / kLlrMaxCls][t % kLlrMaxCls]),
-                     (unsigned long long)(long long)v);
+    __syncthreads();
   }
 }
 
-__global__ void k_llr_decide(LlrArgs A) {
-  const LlrState* st = A.st;
-  if (st->mode >= DYM_LLR_DONE) return;
-  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= A.s.n) return;
-  if (phase_ok(st, A.buf)) return;
-  const uint32_t i = A.s.sites[tid];
-  uint16_t* own = A.s.links + (size_t)A.dir * A.s.V + i;
-  const uint16_t old = A.oldv[tid];
-  if (*own != old) *own = old;
+__global__ void k_llr_decide(const LlrTile* __restrict__ tiles, uint32_t ntiles,
+                             const LlrChainDev* __restrict__ chains) {
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const LlrTile tl = tiles[t];
+    const LlrChainDev c = chains[tl.chain];
+    const LlrState* st = c.st;
+    if (st->mode >= DYM_LLR_DONE || phase_ok(st)) continue;
+    for (uint32_t k = threadIdx.x; k < tl.count; k += blockDim.x) {
+      const uint32_t i = c.sites[tl.begin + k];
+      uint16_t* own = c.links + (size_t)tl.dir * c.V + i;
+      const uint16_t old = c.oldv[tl.pos + k];
+      if (*own != old) *own = old;
+    }
+  }
 }
 
-__global__ void k_llr_commit(LlrArgs A, int last_in_sweep) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  LlrState* st = A.st;
+__global__ void k_llr_commit(const LlrCommit* __restrict__ commits, uint32_t n,
+                             const LlrChainDev* __restrict__ chains) {
+  const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  const LlrCommit cm = commits[idx];
+  LlrState* st = chains[cm.chain].st;
   int mode = st->mode;
   if (mode >= DYM_LLR_DONE) return;
-  const int buf = A.buf, w = st->axis - 1;
-  const bool ok = phase_ok(st, buf);
-  const double Eold = st->E[w];
-  const double dE = DYM_SUB(class_sum(st->h[w], st->d[buf][w], st->v, st->ncls), Eold);
+  const int w = st->axis - 1;
+  const uint32_t buf = st->phase & 1u;
+  const bool ok = phase_ok(st);
+  const double dE = DYM_SUB(class_sum(st->h[w], st->d[buf][w], st->v, st->ncls), st->E[w]);
   if (ok) {
     for (int c = 0; c < st->ncls; ++c) {
       st->h[0][c] += st->d[buf][0][c];
@@ -200,6 +176,7 @@ __global__ void k_llr_commit(LlrArgs A, int last_in_sweep) {
     st->d[buf][0][c] = 0;
     st->d[buf][1][c] = 0;
   }
+  st->phase++;
   if (mode == DYM_LLR_DRIVE) {
     // Aim the next phase's expected move at the remaining distance.
     const double dist = fabs(DYM_SUB(st->emid, st->E[w]));
@@ -207,8 +184,9 @@ __global__ void k_llr_commit(LlrArgs A, int last_in_sweep) {
     st->q = fmin(1.0, fmax(q, 0x1.0p-32));
     if (st->E[w] >= st->elo && st->E[w] <= st->ehi) mode = DYM_LLR_SETTLE;
   }
-  if (last_in_sweep) {
+  if (cm.last) {
     st->sweeps++;
+    st->sweep++;
     if (mode == DYM_LLR_DRIVE) {
       if (++st->drive_sweeps >= st->drive_cap) mode = DYM_LLR_UNREACHED;
     } else if (mode == DYM_LLR_SETTLE) {
@@ -233,40 +211,21 @@ __global__ void k_llr_commit(LlrArgs A, int last_in_sweep) {
   st->mode = mode;
 }
 
-template <int D>
-cudaError_t llr_d(const LlrArgs& a, bool last, cudaStream_t s) {
-  const SweepArgs& sa = a.s;
-  const size_t smem = ((size_t)sa.P * 8 + (size_t)sa.P * 4 + (size_t)sa.npool * 2 + 15) / 16 * 16 + 2 * kLlrMaxCls * 4;
-  void (*fn)(LlrArgs) = nullptr;
-  switch (a.dir) {
-    case 0: fn = k_llr_propose<D, 0>; break;
-    case 1: fn = k_llr_propose<D, 1>; break;
-    case 2: if (D > 2) fn = k_llr_propose<D, (D > 2 ? 2 : 0)>; break;
-    case 3: if (D > 3) fn = k_llr_propose<D, (D > 3 ? 3 : 0)>; break;
-  }
-  if (!fn) return cudaErrorInvalidValue;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-  }
-  const unsigned grid = (sa.n + 255) / 256;
-  if (grid) {
-    fn<<<grid, 256, smem, s>>>(a);
-    k_llr_decide<<<grid, 256, 0, s>>>(a);
-  }
-  k_llr_commit<<<1, 32, 0, s>>>(a, last ? 1 : 0);
-  return cudaGetLastError();
-}
-
 }  // namespace
 
-cudaError_t launch_llr_phase(int D, const LlrArgs& a, bool last_in_sweep, cudaStream_t s) {
-  switch (D) {
-    case 2: return llr_d<2>(a, last_in_sweep, s);
-    case 3: return llr_d<3>(a, last_in_sweep, s);
-    case 4: return llr_d<4>(a, last_in_sweep, s);
+void* llr_propose_kernel_for(int D) { return D == 4 ? (void*)k_llr_propose<4> : nullptr; }
+
+cudaError_t launch_llr_slot(int D, const LlrTile* tiles, uint32_t ntiles, const LlrCommit* commits, uint32_t ncommit,
+                            const LlrChainDev* chains, const BatchGroups& groups, int nhit, unsigned grid,
+                            size_t smem, cudaStream_t s) {
+  if (ntiles) {
+    const unsigned g = grid < ntiles ? grid : ntiles;
+    if (D != 4) return cudaErrorInvalidValue;  // four dimensions only (see launch_sweep_sub)
+    k_llr_propose<4><<<g, 256, smem, s>>>(tiles, ntiles, chains, groups, nhit);
+    k_llr_decide<<<g, 256, 0, s>>>(tiles, ntiles, chains);
   }
-  return cudaErrorInvalidValue;
+  if (ncommit) k_llr_commit<<<(ncommit + 127) / 128, 128, 0, s>>>(commits, ncommit, chains);
+  return cudaGetLastError();
 }
 
 }  // namespace dym

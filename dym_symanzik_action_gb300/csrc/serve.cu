@@ -1,0 +1,543 @@
+// LLR on the host side: per-chain state set-up, the work list that advances
+// any set of chains by LLR sweeps, dym_llr_run (a work list of one chain), and
+// the request server (continuous batching of LLR windows).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "batch.h"
+#include "chain.h"
+#include "util.h"
+
+namespace dym {
+
+namespace {
+
+double class_sum_host(const long long* h, const std::vector<double>& v, int ncls) {
+  double s = 0;
+  for (int q = 0; q < ncls; ++q) s = s + (double)h[q] * v[q];
+  return s;
+}
+
+// Element histograms of all plaquettes and oriented 1x2 rectangles of the
+// chain's configuration, folded into ReTr classes (recompute_S1/S2,
+// llr.cpp:46-55, 139-151).
+int class_histograms(dym_chain* c, long long h[2][kLlrMaxCls]) {
+  const Group& g = *c->grp->g;
+  dym_meas_opts mo{-1, -1};
+  dym_obs o;
+  int rc = dym_measure(c, &mo, &o, nullptr);
+  if (rc) return rc;
+  for (int k = 0; k < 2; ++k)
+    for (int q = 0; q < kLlrMaxCls; ++q) h[k][q] = 0;
+  for (uint32_t n = 0; n < g.P; ++n) {
+    h[0][g.cls[n]] += (long long)c->h_hist[n];
+    h[1][g.cls[n]] += (long long)c->h_hist[g.P + n];
+  }
+  return DYM_OK;
+}
+
+int check_llr_group(const Group& g) {
+  if (g.ncls > kLlrMaxCls || !g.cls_conj_invariant || !g.cls_exact || !g.assoc_ok)
+    return fail(DYM_ENOTSUP, "LLR needs a group table whose ReTr is one double per class (at most 32 classes)");
+  return DYM_OK;
+}
+
+int check_llr_req(const dym_chain* c, const dym_llr_req* req) {
+  if (req->axis != 1 && req->axis != 2) return fail(DYM_EINVAL, "axis must be 1 (S1 window) or 2 (S2 window)");
+  if (req->K < 1 || req->NRM < 0 || req->NRM > DYM_LLR_MAX_NRM || req->nhit < 0 || !(req->hw > 0) ||
+      req->drive_cap < 0)
+    return fail(DYM_EINVAL, "LLR: bad K, NRM, nhit, hw or drive_cap");
+  if (req->axis == 2 && (c->p.Nt < 3 || c->p.Nx < 3))
+    return fail(DYM_ENOTSUP, "an S2 window needs every extent >= 3 (1x2 rectangles wrap otherwise)");
+  if (c->p.pool != DYM_POOL_NEAREST) return fail(DYM_ENOTSUP, "LLR proposals use the nearest-element pool");
+  if (c->p.D != 4) return fail(DYM_ENOTSUP, "LLR runs on four-dimensional lattices");
+  return check_llr_group(*c->grp->g);
+}
+
+// Allocate (once) and fill the chain's LLR state for window `req`.
+int llr_init_state(dym_chain* c, const dym_llr_req* req, LlrState* st) {
+  const Group& g = *c->grp->g;
+  DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+  if (!c->d_llr) {
+    DYM_CUDA(dmalloc(&c->d_llr, 1), "cudaMalloc(llr)");
+    uint32_t maxlen = 1;
+    for (auto l : c->sched.phase_len) maxlen = std::max(maxlen, l);
+    DYM_CUDA(dmalloc(&c->d_oldv, maxlen), "cudaMalloc(llr oldv)");
+  }
+  std::memset(st, 0, sizeof(LlrState));
+  int rc = class_histograms(c, st->h);
+  if (rc) return rc;
+  const double W = 2 * req->hw;
+  st->a = req->a0;
+  st->bg = req->bg;
+  st->ewin = req->ewin;
+  st->elo = req->ewin - req->hw;
+  st->ehi = req->ewin + req->hw;
+  st->emid = 0.5 * (st->elo + st->ehi);
+  st->w2 = W * W;
+  st->q = 1.0;
+  st->ncls = g.ncls;
+  for (int q = 0; q < g.ncls; ++q) st->v[q] = g.cls_val[q];
+  st->E[0] = class_sum_host(st->h[0], g.cls_val, g.ncls);
+  st->E[1] = class_sum_host(st->h[1], g.cls_val, g.ncls);
+  st->axis = req->axis;
+  st->K = req->K;
+  st->NRM = req->NRM;
+  st->drive_cap = req->drive_cap;
+  st->sweep = c->sweep;
+  const double Ew = st->E[req->axis - 1];
+  st->mode = (Ew >= st->elo && Ew <= st->ehi) ? DYM_LLR_RM : DYM_LLR_DRIVE;
+  if (req->NRM == 0 && st->mode == DYM_LLR_RM) st->mode = DYM_LLR_DONE;
+  if (st->mode == DYM_LLR_DRIVE && req->drive_cap == 0) st->mode = DYM_LLR_UNREACHED;
+  DYM_CUDA(cudaMemcpy(c->d_llr, st, sizeof(LlrState), cudaMemcpyHostToDevice), "upload llr state");
+  return DYM_OK;
+}
+
+}  // namespace
+
+// A set of chains advanced together by LLR sweeps: one propose/decide/commit
+// triple per colour-phase slot.
+struct LlrWork {
+  int device = 0, D = 0;
+  int sms = 0;
+  std::vector<dym_chain*> chains;
+  std::vector<Group*> groups;
+  std::vector<uint16_t*> d_sub;
+  std::vector<uint16_t*> d_cls16;
+  BatchGroups bg{};
+  size_t smem = 0;
+  LlrChainDev* d_chains = nullptr;
+  LlrTile* d_tiles = nullptr;
+  LlrCommit* d_commits = nullptr;
+  std::vector<uint32_t> tile_off, tile_cnt, commit_off, commit_cnt;
+  unsigned grid = 1;
+  bool dirty = true;
+  cudaStream_t stream = nullptr;
+
+  ~LlrWork() { release(); }
+
+  void release_lists() {
+    cudaFree(d_chains);
+    cudaFree(d_tiles);
+    cudaFree(d_commits);
+    d_chains = nullptr;
+    d_tiles = nullptr;
+    d_commits = nullptr;
+  }
+  void release() {
+    release_lists();
+    for (auto p : d_sub) cudaFree(p);
+    d_sub.clear();
+    groups.clear();
+  }
+
+  // Shared tables of a new group.
+  int add_group(Group* g) {
+    if (std::find(groups.begin(), groups.end(), g) != groups.end()) return DYM_OK;
+    if ((int)groups.size() == kBatchMaxGroups) return fail(DYM_ENOTSUP, "at most 4 groups");
+    const auto& pool = g->pool_nearest;
+    std::vector<uint16_t> sub(pool.size() * (size_t)g->P);
+    for (size_t k = 0; k < pool.size(); ++k)
+      for (uint32_t u = 0; u < g->P; ++u) sub[k * g->P + u] = g->mult[(size_t)u * g->P + pool[k]];
+    uint16_t* d = nullptr;
+    DYM_CUDA(dmalloc(&d, sub.size()), "cudaMalloc(llr sub)");
+    DYM_CUDA(cudaMemcpy(d, sub.data(), sub.size() * 2, cudaMemcpyHostToDevice), "upload llr sub");
+    d_sub.push_back(d);
+    groups.push_back(g);
+    // layout
+    auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
+    size_t off = kLlrDeltaBytes;
+    bg.n = (int)groups.size();
+    for (size_t k = 0; k < groups.size(); ++k) {
+      const Group& G = *groups[k];
+      BatchGroupDev& b = bg.g[k];
+      b.mult = (const uint16_t*)G.d_mult;
+      b.inv = (const uint16_t*)G.d_inv;
+      b.retr = (const double*)G.d_retr;
+      b.sub = d_sub[k];
+      b.cls16 = (const uint16_t*)G.d_cls16;
+      b.P = G.P;
+      b.npool = (uint32_t)G.pool_nearest.size();
+      b.off_retr = (uint32_t)off;
+      off = up16(off + (size_t)G.P * 8);
+      b.off_inv = (uint32_t)off;
+      off = up16(off + (size_t)G.P * 2);
+      b.off_cls = (uint32_t)off;
+      off = up16(off + (size_t)G.P * 2);
+      b.off_sub = (uint32_t)off;
+      off = up16(off + (size_t)b.npool * G.P * 2);
+    }
+    smem = off;
+    int optin = 0;
+    DYM_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "attribute");
+    if (smem > (size_t)optin) return fail(DYM_ENOTSUP, "LLR tables do not fit shared memory");
+    dirty = true;
+    return DYM_OK;
+  }
+
+  int build() {
+    release_lists();
+    const size_t nc = chains.size();
+    if (nc == 0) {
+      dirty = false;
+      return DYM_OK;
+    }
+    std::vector<LlrChainDev> cd(nc);
+    size_t maxph = 0;
+    for (size_t i = 0; i < nc; ++i) {
+      dym_chain* c = chains[i];
+      LlrChainDev& d = cd[i];
+      d.links = c->dev.links;
+      d.sites = c->dev.sites;
+      d.V = c->dev.V;
+      d.Nt = c->p.Nt;
+      d.Nx = c->p.Nx;
+      d.seed = c->p.seed;
+      d.st = c->d_llr;
+      d.oldv = c->d_oldv;
+      d.group = (int)(std::find(groups.begin(), groups.end(), c->grp->g) - groups.begin());
+      maxph = std::max(maxph, c->sched.phase_dir.size());
+    }
+    std::vector<LlrTile> tiles;
+    std::vector<LlrCommit> commits;
+    tile_off.assign(maxph, 0);
+    tile_cnt.assign(maxph, 0);
+    commit_off.assign(maxph, 0);
+    commit_cnt.assign(maxph, 0);
+    const uint32_t T = 256;
+    for (size_t k = 0; k < maxph; ++k) {
+      tile_off[k] = (uint32_t)tiles.size();
+      commit_off[k] = (uint32_t)commits.size();
+      for (size_t i = 0; i < nc; ++i) {
+        const Schedule& s = chains[i]->sched;
+        if (k >= s.phase_dir.size()) continue;
+        for (uint32_t j = 0; j < s.phase_len[k]; j += T)
+          tiles.push_back(LlrTile{(uint32_t)i, s.phase_off[k] + j, std::min(T, s.phase_len[k] - j),
+                                  (uint32_t)s.phase_dir[k], j});
+        commits.push_back(LlrCommit{(uint32_t)i, k + 1 == s.phase_dir.size() ? 1u : 0u});
+      }
+      tile_cnt[k] = (uint32_t)tiles.size() - tile_off[k];
+      commit_cnt[k] = (uint32_t)commits.size() - commit_off[k];
+    }
+    DYM_CUDA(dmalloc(&d_chains, nc), "cudaMalloc(llr chains)");
+    DYM_CUDA(dmalloc(&d_tiles, tiles.size()), "cudaMalloc(llr tiles)");
+    DYM_CUDA(dmalloc(&d_commits, commits.size()), "cudaMalloc(llr commits)");
+    DYM_CUDA(cudaMemcpy(d_chains, cd.data(), nc * sizeof(LlrChainDev), cudaMemcpyHostToDevice), "upload chains");
+    DYM_CUDA(cudaMemcpy(d_tiles, tiles.data(), tiles.size() * sizeof(LlrTile), cudaMemcpyHostToDevice), "tiles");
+    DYM_CUDA(cudaMemcpy(d_commits, commits.data(), commits.size() * sizeof(LlrCommit), cudaMemcpyHostToDevice),
+             "commits");
+    void* fn = llr_propose_kernel_for(D);
+    if (!fn) return fail(DYM_ENOTSUP, "LLR: unsupported D");
+    DYM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attribute");
+    int per_sm = 0;
+    DYM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem), "occupancy");
+    grid = (unsigned)std::max(1, sms * std::max(1, per_sm));
+    dirty = false;
+    return DYM_OK;
+  }
+
+  int enqueue_sweeps(int nsweeps, int nhit) {
+    if (dirty) {
+      int rc = build();
+      if (rc) return rc;
+    }
+    if (chains.empty()) return DYM_OK;
+    for (int s = 0; s < nsweeps; ++s)
+      for (size_t k = 0; k < tile_cnt.size(); ++k) {
+        cudaError_t e = launch_llr_slot(D, d_tiles + tile_off[k], tile_cnt[k], d_commits + commit_off[k],
+                                        commit_cnt[k], d_chains, bg, nhit, grid, smem, stream);
+        if (e != cudaSuccess) return cuda_fail(e, "llr slot launch");
+      }
+    return DYM_OK;
+  }
+};
+
+}  // namespace dym
+
+using namespace dym;
+
+extern "C" {
+
+int dym_llr_energy(dym_chain* c, double* S1, double* S2) {
+  if (!c) return fail(DYM_EINVAL, "dym_llr_energy: null chain");
+  const Group& g = *c->grp->g;
+  int rc = check_llr_group(g);
+  if (rc) return rc;
+  long long h[2][kLlrMaxCls];
+  rc = class_histograms(c, h);
+  if (rc) return rc;
+  if (S1) *S1 = class_sum_host(h[0], g.cls_val, g.ncls);
+  if (S2) *S2 = class_sum_host(h[1], g.cls_val, g.ncls);
+  return DYM_OK;
+}
+
+int dym_llr_run(dym_chain* c, const dym_llr_req* req, dym_llr_result* out, double* a_hist) {
+  if (!c || !req || !out) return fail(DYM_EINVAL, "dym_llr_run: null argument");
+  int rc = check_llr_req(c, req);
+  if (rc) return rc;
+  std::unique_ptr<LlrState> st(new LlrState());
+  rc = llr_init_state(c, req, st.get());
+  if (rc) return rc;
+  LlrWork w;
+  w.device = c->p.device;
+  w.D = c->p.D;
+  w.stream = c->stream;
+  DYM_CUDA(cudaDeviceGetAttribute(&w.sms, cudaDevAttrMultiProcessorCount, w.device), "attribute");
+  rc = w.add_group(c->grp->g);
+  if (rc) return rc;
+  w.chains.push_back(c);
+  const long max_sweeps = (long)req->drive_cap + (long)req->K * req->NRM + 2;
+  int mode = st->mode;
+  long sweeps = 0;
+  while (mode < DYM_LLR_DONE && sweeps < max_sweeps) {
+    const int chunk = (int)std::min<long>(8, max_sweeps - sweeps);
+    rc = w.enqueue_sweeps(chunk, req->nhit);
+    if (rc) return rc;
+    sweeps += chunk;
+    DYM_CUDA(cudaMemcpyAsync(&st->mode, &c->d_llr->mode, sizeof(int), cudaMemcpyDeviceToHost, c->stream),
+             "read llr mode");
+    DYM_CUDA(cudaStreamSynchronize(c->stream), "llr sweeps");
+    mode = st->mode;
+  }
+  DYM_CUDA(cudaMemcpy(st.get(), c->d_llr, sizeof(LlrState), cudaMemcpyDeviceToHost), "read llr state");
+  out->a = st->a;
+  out->S1 = st->E[0];
+  out->S2 = st->E[1];
+  out->status = st->mode;
+  out->drive_sweeps = st->drive_sweeps;
+  out->sweeps = st->sweeps;
+  out->hits = st->hits;
+  out->accepts = st->accepts;
+  out->phase_accepts = st->phase_acc;
+  out->phase_rejects = st->phase_rej;
+  c->sweep = st->sweep;  // sweeps after the state machine finished did nothing
+  if (a_hist)
+    for (int m = 0; m < req->NRM; ++m) a_hist[m] = st->a_hist[m];
+  return DYM_OK;
+}
+
+}  // extern "C"
+
+// ----------------------------------------------------------------- server --
+
+struct dym_server {
+  dym_group* grp = nullptr;
+  dym_server_params p{};
+  struct Active {
+    dym_llr_request req;
+    dym_chain* chain;
+    uint64_t bytes;
+  };
+  std::deque<dym_llr_request> queue;
+  std::vector<Active> active;
+  std::map<std::tuple<int, int, int>, std::vector<dym_chain*>> spare;  // finished chains by shape
+  std::vector<dym_llr_response> done;
+  dym::LlrWork work;
+  uint64_t hbm_used = 0;
+  uint64_t link_hits = 0;
+  std::vector<int> h_modes;
+};
+
+namespace dym {
+namespace {
+
+uint64_t chain_bytes(int D, int Nt, int Nx, uint32_t P) {
+  uint64_t V = (uint64_t)Nt;
+  for (int d = 1; d < D; ++d) V *= (uint64_t)Nx;
+  // links + site lists + oldv + LLR state + measurement histograms and pinned copies
+  return V * D * 2 + V * D * 4 + V * 2 + sizeof(LlrState) + 2 * 3ull * P * 8;
+}
+
+int server_admit(dym_server* s) {
+  const Group& g = *s->grp->g;
+  while (!s->queue.empty() && (int)s->active.size() < s->p.max_chains) {
+    const dym_llr_request r = s->queue.front();
+    const uint64_t bytes = chain_bytes(r.D, r.Nt, r.Nx, g.P);
+    if (!s->active.empty() && s->hbm_used + bytes > s->p.hbm_budget) break;
+    s->queue.pop_front();
+    dym_chain* c = nullptr;
+    auto key = std::make_tuple(r.D, r.Nt, r.Nx);
+    auto it = s->spare.find(key);
+    if (it != s->spare.end() && !it->second.empty()) {
+      c = it->second.back();
+      it->second.pop_back();
+      int rc = chain_reset(c, r.seed, r.start);
+      if (rc) return rc;
+    } else {
+      dym_chain_params cp{};
+      cp.D = r.D;
+      cp.Nt = r.Nt;
+      cp.Nx = r.Nx;
+      cp.seed = r.seed;
+      cp.start = r.start;
+      cp.pool = DYM_POOL_NEAREST;
+      cp.precision = DYM_PREC_FP64;
+      cp.device = s->p.device;
+      int rc = dym_chain_create(s->grp, &cp, &c);
+      if (rc) return rc;
+    }
+    dym_llr_req q{};
+    q.axis = r.axis;
+    q.bg = r.bg;
+    q.ewin = r.ewin;
+    q.hw = r.hw;
+    q.a0 = r.a0;
+    q.K = r.K;
+    q.NRM = r.NRM;
+    q.nhit = s->p.nhit;
+    q.drive_cap = r.drive_cap;
+    LlrState st;
+    int rc = check_llr_req(c, &q);
+    if (!rc) rc = llr_init_state(c, &q, &st);
+    if (rc) {
+      dym_chain_free(c);
+      return rc;
+    }
+    s->active.push_back(dym_server::Active{r, c, bytes});
+    s->hbm_used += bytes;
+    s->work.chains.push_back(c);
+    s->work.dirty = true;
+  }
+  return DYM_OK;
+}
+
+int server_retire(dym_server* s) {
+  const size_t n = s->active.size();
+  if (n == 0) return DYM_OK;
+  s->h_modes.resize(n);
+  for (size_t i = 0; i < n; ++i)
+    DYM_CUDA(cudaMemcpyAsync(&s->h_modes[i], &s->active[i].chain->d_llr->mode, sizeof(int), cudaMemcpyDeviceToHost,
+                             s->work.stream),
+             "read modes");
+  DYM_CUDA(cudaStreamSynchronize(s->work.stream), "read modes");
+  std::vector<dym_server::Active> keep;
+  bool changed = false;
+  for (size_t i = 0; i < n; ++i) {
+    dym_server::Active& a = s->active[i];
+    if (s->h_modes[i] < DYM_LLR_DONE) {
+      keep.push_back(a);
+      continue;
+    }
+    LlrState st;
+    DYM_CUDA(cudaMemcpy(&st, a.chain->d_llr, sizeof(LlrState), cudaMemcpyDeviceToHost), "read llr state");
+    dym_llr_response resp{};
+    resp.id = a.req.id;
+    resp.a = st.a;
+    resp.S1 = st.E[0];
+    resp.S2 = st.E[1];
+    resp.status = st.mode;
+    resp.sweeps = st.sweeps;
+    resp.drive_sweeps = st.drive_sweeps;
+    resp.NRM = a.req.NRM;
+    resp.hits = st.hits;
+    resp.accepts = st.accepts;
+    for (int m = 0; m < a.req.NRM && m < DYM_SERVE_MAX_NRM; ++m) resp.a_hist[m] = st.a_hist[m];
+    s->done.push_back(resp);
+    s->link_hits += st.hits;
+    s->hbm_used -= a.bytes;
+    s->spare[std::make_tuple(a.req.D, a.req.Nt, a.req.Nx)].push_back(a.chain);
+    changed = true;
+  }
+  if (changed) {
+    s->active.swap(keep);
+    s->work.chains.clear();
+    for (auto& a : s->active) s->work.chains.push_back(a.chain);
+    s->work.dirty = true;
+  }
+  return DYM_OK;
+}
+
+}  // namespace
+}  // namespace dym
+
+extern "C" {
+
+int dym_server_create(const dym_group* g, const dym_server_params* p, dym_server** out) {
+  if (!g || !p || !out) return fail(DYM_EINVAL, "dym_server_create: null argument");
+  *out = nullptr;
+  if (p->max_chains < 1 || p->nhit < 0) return fail(DYM_EINVAL, "dym_server_create: bad max_chains or nhit");
+  int rc = check_llr_group(*g->g);
+  if (rc) return rc;
+  int ndev = 0;
+  DYM_CUDA(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
+  if (p->device < 0 || p->device >= ndev) return fail(DYM_EINVAL, "bad device ordinal");
+  DYM_CUDA(cudaSetDevice(p->device), "cudaSetDevice");
+  rc = group_to_device(g->g);
+  if (rc) return rc;
+  std::unique_ptr<dym_server> s(new dym_server);
+  s->grp = const_cast<dym_group*>(g);
+  s->p = *p;
+  s->work.device = p->device;
+  DYM_CUDA(cudaDeviceGetAttribute(&s->work.sms, cudaDevAttrMultiProcessorCount, p->device), "attribute");
+  DYM_CUDA(cudaStreamCreateWithFlags(&s->work.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  rc = s->work.add_group(g->g);
+  if (rc) return rc;
+  *out = s.release();
+  return DYM_OK;
+}
+
+int dym_server_submit(dym_server* s, const dym_llr_request* r) {
+  if (!s || !r) return fail(DYM_EINVAL, "dym_server_submit: null argument");
+  if (r->NRM < 0 || r->NRM > DYM_SERVE_MAX_NRM) return fail(DYM_EINVAL, "request NRM out of range");
+  if (r->D != 4 || r->Nt < 1 || r->Nx < 1) return fail(DYM_EINVAL, "bad lattice shape (LLR runs on D = 4)");
+  if (!s->active.empty() && r->D != s->work.D) return fail(DYM_ENOTSUP, "all requests of a server share D");
+  if (s->work.D == 0) s->work.D = r->D;
+  s->queue.push_back(*r);
+  return DYM_OK;
+}
+
+int dym_server_step(dym_server* s, int32_t nsweeps) {
+  if (!s || nsweeps < 0) return fail(DYM_EINVAL, "dym_server_step: bad argument");
+  DYM_CUDA(cudaSetDevice(s->p.device), "cudaSetDevice");
+  int rc = server_admit(s);
+  if (rc) return rc;
+  if (!s->active.empty()) {
+    s->work.D = s->active.front().req.D;
+    rc = s->work.enqueue_sweeps(nsweeps, s->p.nhit);
+    if (rc) return rc;
+  }
+  return server_retire(s);
+}
+
+int dym_server_poll(dym_server* s, dym_llr_response* out, int32_t max, int32_t* n) {
+  if (!s || (!out && max > 0) || !n || max < 0) return fail(DYM_EINVAL, "dym_server_poll: bad argument");
+  const int32_t k = (int32_t)std::min<size_t>(s->done.size(), (size_t)max);
+  for (int32_t i = 0; i < k; ++i) out[i] = s->done[i];
+  s->done.erase(s->done.begin(), s->done.begin() + k);
+  *n = k;
+  return DYM_OK;
+}
+
+int dym_server_status(const dym_server* s, int32_t* active, int32_t* queued, uint64_t* hbm_used,
+                      uint64_t* link_hits) {
+  if (!s) return fail(DYM_EINVAL, "dym_server_status: null server");
+  if (active) *active = (int32_t)s->active.size();
+  if (queued) *queued = (int32_t)s->queue.size();
+  if (hbm_used) *hbm_used = s->hbm_used;
+  if (link_hits) *link_hits = s->link_hits;
+  return DYM_OK;
+}
+
+int dym_server_free(dym_server* s) {
+  if (!s) return DYM_OK;
+  cudaSetDevice(s->p.device);
+  if (s->work.stream) cudaStreamSynchronize(s->work.stream);
+  for (auto& a : s->active) dym_chain_free(a.chain);
+  for (auto& kv : s->spare)
+    for (auto c : kv.second) dym_chain_free(c);
+  s->work.release();
+  if (s->work.stream) cudaStreamDestroy(s->work.stream);
+  delete s;
+  return DYM_OK;
+}
+
+}  // extern "C"

@@ -102,3 +102,95 @@ __device__ __forceinline__ void flush_counters(unsigned long long* ctr, unsigned
 }
 
 }  // namespace dym
+
+namespace dym {
+
+// One LLR visit of link (i, DIR) with the shared sub-table (llr.cpp:186-216
+// per hit): nhit hits with weight exp(-a dE_w - bg dE_bg), or, in drive-in
+// mode, greedy moves of the link's running energy towards emid.  The link is
+// written in place and its plaquette/rectangle class changes are added to
+// s_delta; returns the value before the visit.
+template <int D, int DIR>
+__device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
+                                              const uint16_t* s_inv, const uint16_t* s_sub, const uint16_t* s_cls,
+                                              int axis, double aa, double bg, double E0, double emid, bool drive,
+                                              uint32_t qthr, int* s_delta, unsigned& hits, unsigned& accs) {
+  constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
+  SiteGeo<D> geo;
+  site_geo<D>(i, a.Nt, a.Nx, geo);
+  GlobalTab T{a.mult, s_inv, a.P};
+  const uint16_t* L = a.links;
+  const uint32_t V = a.V;
+  auto ld = [L, V](uint32_t s, int d) -> uint32_t { return __ldg(L + (size_t)d * V + s); };
+  uint32_t u[NT];
+  build_staples<D, DIR>(i, geo, T, ld, u, u + NS);
+  uint16_t* own = a.links + (size_t)DIR * V + i;
+  uint32_t b = *own;
+  const uint32_t b0 = b;
+#pragma unroll
+  for (int j = 0; j < NT; ++j) u[j] = T.mul(u[j], b);
+  uint32_t u0[NT];
+#pragma unroll
+  for (int j = 0; j < NT; ++j) u0[j] = u[j];
+  double r1 = 0, m1 = 0;
+#pragma unroll
+  for (int j = 0; j < NS; ++j) r1 = DYM_ADD(r1, s_retr[u[j]]);
+#pragma unroll
+  for (int j = NS; j < NT; ++j) m1 = DYM_ADD(m1, s_retr[u[j]]);
+  bool part = true;
+  if (drive) part = dym_hit_random(a.seed, sweep, i, DIR, 0xFFFFFu, DYM_TAG_LLR).v[0] < qthr;
+  double cum = 0;
+  for (int h = 0; part && h < a.nhit; ++h) {
+    const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_LLR);
+    const uint16_t* row = s_sub + dym_pick(r.v[0], a.npool) * a.P;
+    uint32_t e[NT];
+    double r1n = 0, m1n = 0;
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      e[j] = row[u[j]];
+      r1n = DYM_ADD(r1n, s_retr[e[j]]);
+    }
+#pragma unroll
+    for (int j = NS; j < NT; ++j) {
+      e[j] = row[u[j]];
+      m1n = DYM_ADD(m1n, s_retr[e[j]]);
+    }
+    const double dS1 = DYM_SUB(r1n, r1), dS2 = DYM_SUB(m1n, m1);
+    const double dEw = axis == 1 ? dS1 : dS2;
+    const double dEbg = axis == 1 ? dS2 : dS1;
+    bool acc;
+    if (drive) {
+      const double Ec = DYM_ADD(E0, cum);
+      acc = fabs(DYM_SUB(DYM_ADD(Ec, dEw), emid)) < fabs(DYM_SUB(Ec, emid));
+    } else {
+      acc = dym_exp(DYM_SUB(DYM_MUL(-aa, dEw), DYM_MUL(bg, dEbg))) > dym_u53(r.v[1], r.v[2]);
+    }
+    ++hits;
+    if (acc) {
+      b = row[b];
+#pragma unroll
+      for (int j = 0; j < NT; ++j) u[j] = e[j];
+      r1 = r1n;
+      m1 = m1n;
+      cum = DYM_ADD(cum, dEw);
+      ++accs;
+    }
+  }
+  if (b != b0) {
+    *own = (uint16_t)b;
+    // Class of b s_j equals the class of its conjugate s_j b = u_j.
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      atomicAdd(&s_delta[s_cls[u0[j]]], -1);
+      atomicAdd(&s_delta[s_cls[u[j]]], 1);
+    }
+#pragma unroll
+    for (int j = NS; j < NT; ++j) {
+      atomicAdd(&s_delta[kLlrMaxCls + s_cls[u0[j]]], -1);
+      atomicAdd(&s_delta[kLlrMaxCls + s_cls[u[j]]], 1);
+    }
+  }
+  return b0;
+}
+
+}  // namespace dym

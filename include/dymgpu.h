@@ -243,6 +243,56 @@ int dym_llr_energy(dym_chain* c, double* S1, double* S2);
  * the NRM iterations. */
 int dym_llr_run(dym_chain* c, const dym_llr_req* req, dym_llr_result* out, double* a_hist);
 
+/* ---------------------------------------------------------------- server --- */
+
+/* A request loop for LLR windows (no reference counterpart: the reference
+ * runs one llr process per window range, scripts/llr2d_parallel.sh).  Requests
+ * queue on submit; dym_server_step admits queued requests while the resident
+ * chain count and the device-memory budget allow, runs nsweeps LLR sweeps of
+ * every resident chain together (one kernel per colour-phase slot), and
+ * retires finished chains, whose responses dym_server_poll returns.  A
+ * request's result depends only on the request: it is the same alone or in
+ * any mix.  Chains of a finished request are reused for later requests of the
+ * same shape. */
+#define DYM_SERVE_MAX_NRM 64
+
+typedef struct dym_server dym_server;
+
+typedef struct {
+  int32_t max_chains;   /* resident chains at most */
+  uint64_t hbm_budget;  /* device bytes of resident chains at most */
+  int32_t nhit;         /* hits per link per visit */
+  int32_t device;
+} dym_server_params;
+
+typedef struct {
+  uint64_t id;
+  int32_t D, Nt, Nx;
+  int32_t start;        /* DYM_START_HOT / DYM_START_COLD */
+  uint64_t seed;
+  int32_t axis;
+  double bg, ewin, hw, a0;
+  int32_t K, NRM, drive_cap;  /* NRM <= DYM_SERVE_MAX_NRM */
+} dym_llr_request;
+
+typedef struct {
+  uint64_t id;
+  double a, S1, S2;
+  int32_t status;       /* DYM_LLR_DONE or DYM_LLR_UNREACHED */
+  int32_t sweeps, drive_sweeps, NRM;
+  uint64_t hits, accepts;
+  double a_hist[DYM_SERVE_MAX_NRM];
+} dym_llr_response;
+
+int dym_server_create(const dym_group* g, const dym_server_params* p, dym_server** out);
+int dym_server_submit(dym_server* s, const dym_llr_request* r);
+int dym_server_step(dym_server* s, int32_t nsweeps);
+/* Up to `max` finished responses (in completion order); *n receives the count. */
+int dym_server_poll(dym_server* s, dym_llr_response* out, int32_t max, int32_t* n);
+int dym_server_status(const dym_server* s, int32_t* active, int32_t* queued, uint64_t* hbm_used,
+                      uint64_t* link_hits);
+int dym_server_free(dym_server* s);
+
 /* Roofline probe (no reference counterpart): random 2-byte gathers from an
  * L2-resident table of table_bytes bytes on `device`, as the sweep kernels
  * issue them; returns the sustained gather rate in 32-byte sectors per second
