@@ -111,6 +111,7 @@ PROTOTYPES = {
     "dym_chain_set_beta": (C.c_int, [_P, C.c_double, C.c_double, C.c_double]),
     "dym_sweep": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(Stats)]),
     "dym_measure": (C.c_int, [_P, C.POINTER(MeasOpts), C.POINTER(Obs), _f64p]),
+    "dym_measure_noalloc": (C.c_int, [_P, C.POINTER(MeasOpts), C.POINTER(Obs), _f64p]),
     "dym_links_get": (C.c_int, [_P, _u16p]),
     "dym_links_set": (C.c_int, [_P, _u16p]),
     "dym_chain_get_schedule": (C.c_int, [_P, _u32p, _i32p, _i32p, _u32p, _u32p]),

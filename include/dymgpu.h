@@ -137,6 +137,32 @@ typedef struct {
  * histograms over group elements followed by one FP64 dot product. */
 int dym_measure(dym_chain* c, const dym_meas_opts* opts, dym_obs* out, double* wloop);
 
+/* Same observables as dym_measure, with no memory allocation (no reference
+ * counterpart: the reference measures on the host).  For callers that must not
+ * allocate while they run, e.g. a server whose device-memory budget is all
+ * given to resident chains, or a caller whose other streams cudaMalloc and
+ * cudaFree would stall by synchronising the device.  dym_measure allocates
+ * per-chain histogram buffers (device and pinned host) on first use; this call
+ * uses instead one fixed device array of DYM_NOALLOC_HIST_BINS 64-bit bins
+ * (1 MiB) plus room for DYM_NOALLOC_MAX_LOOPS Wilson loops, built into the
+ * library's device code, walks Wilson loops link by link instead of building
+ * lattice-sized line-product tables, takes the dot products on the device and
+ * copies only the results, into *out and wloop.  Results are identical to
+ * dym_measure's.
+ * Limits: (3 + wl_nx*wl_nt) * P <= DYM_NOALLOC_HIST_BINS and
+ * wl_nx*wl_nt <= DYM_NOALLOC_MAX_LOOPS (S(1080): up to 118 loops, e.g. the 8x8
+ * grid); larger requests return DYM_ERANGE before any device work.
+ * The array is per device and shared by all chains on it; every call clears
+ * the bins it uses (they must start at zero), so calls whose device work
+ * overlaps -- from several host threads, or on chains of one device -- race
+ * and must be serialised by the caller.  The first call on each device looks
+ * up the array's device address (which may load the library's device code);
+ * make that first call before any stream capture begins.  On success nothing
+ * is allocated, host or device; an error records its message as every call. */
+#define DYM_NOALLOC_HIST_BINS 131072
+#define DYM_NOALLOC_MAX_LOOPS 1024
+int dym_measure_noalloc(dym_chain* c, const dym_meas_opts* opts, dym_obs* out, double* wloop);
+
 /* Host <-> device copies of the configuration (layout in the header comment). */
 int dym_links_get(dym_chain* c, uint16_t* host_out);
 int dym_links_set(dym_chain* c, const uint16_t* host_in);
