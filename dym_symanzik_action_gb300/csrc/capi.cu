@@ -36,16 +36,16 @@ int group_to_device(Group* g) {
   DYM_CUDA(dmalloc((uint8_t**)&g->d_cls, P), "cudaMalloc(cls)");
   DYM_CUDA(dmalloc((uint16_t**)&g->d_cls16, P), "cudaMalloc(cls16)");
   DYM_CUDA(dmalloc((double**)&g->d_clsval, std::max(g->ncls, 1)), "cudaMalloc(clsval)");
-  DYM_CUDA(cudaMemcpy(g->d_mult, g->mult.data(), P * P * 2, cudaMemcpyHostToDevice), "upload mult");
-  DYM_CUDA(cudaMemcpy(g->d_inv, g->inv.data(), P * 2, cudaMemcpyHostToDevice), "upload inv");
-  DYM_CUDA(cudaMemcpy(g->d_retr, g->retr.data(), P * 8, cudaMemcpyHostToDevice), "upload retr");
-  DYM_CUDA(cudaMemcpy(g->d_imtr, g->imtr.data(), P * 8, cudaMemcpyHostToDevice), "upload imtr");
-  DYM_CUDA(cudaMemcpy(g->d_cls, g->cls.data(), P, cudaMemcpyHostToDevice), "upload cls");
+  DYM_CUDA(copy_sync(g->d_mult, g->mult.data(), P * P * 2, cudaMemcpyHostToDevice, cudaStreamLegacy), "upload mult");
+  DYM_CUDA(copy_sync(g->d_inv, g->inv.data(), P * 2, cudaMemcpyHostToDevice, cudaStreamLegacy), "upload inv");
+  DYM_CUDA(copy_sync(g->d_retr, g->retr.data(), P * 8, cudaMemcpyHostToDevice, cudaStreamLegacy), "upload retr");
+  DYM_CUDA(copy_sync(g->d_imtr, g->imtr.data(), P * 8, cudaMemcpyHostToDevice, cudaStreamLegacy), "upload imtr");
+  DYM_CUDA(copy_sync(g->d_cls, g->cls.data(), P, cudaMemcpyHostToDevice, cudaStreamLegacy), "upload cls");
   {
     std::vector<uint16_t> c16(g->cls.begin(), g->cls.end());
-    DYM_CUDA(cudaMemcpy(g->d_cls16, c16.data(), P * 2, cudaMemcpyHostToDevice), "upload cls16");
+    DYM_CUDA(copy_sync(g->d_cls16, c16.data(), P * 2, cudaMemcpyHostToDevice, cudaStreamLegacy), "upload cls16");
   }
-  DYM_CUDA(cudaMemcpy(g->d_clsval, g->cls_val.data(), g->ncls * 8, cudaMemcpyHostToDevice), "upload clsval");
+  DYM_CUDA(copy_sync(g->d_clsval, g->cls_val.data(), g->ncls * 8, cudaMemcpyHostToDevice, cudaStreamLegacy), "upload clsval");
   g->device = dev;
   return DYM_OK;
 }
@@ -90,7 +90,7 @@ static int build_sub_table(dym_chain* c, const std::vector<uint16_t>& pool) {
   for (uint32_t k = 0; k < np; ++k)
     for (uint32_t u = 0; u < P; ++u) sub[(size_t)k * P + u] = g.mult[(size_t)u * P + pool[k]];
   DYM_CUDA(dmalloc(&c->dev.sub, sub.size()), "cudaMalloc(sub)");
-  DYM_CUDA(cudaMemcpy(c->dev.sub, sub.data(), sub.size() * 2, cudaMemcpyHostToDevice), "upload sub");
+  DYM_CUDA(copy_sync(c->dev.sub, sub.data(), sub.size() * 2, cudaMemcpyHostToDevice, c->stream), "upload sub");
   c->dev.sub_ok = true;
   return DYM_OK;
 }
@@ -266,14 +266,14 @@ int dym_chain_create(const dym_group* gh, const dym_chain_params* p, dym_chain**
   DYM_CUDA(cudaEventCreate(&c->ev1), "cudaEventCreate");
   DYM_CUDA(dmalloc(&d.links, (size_t)V * p->D), "cudaMalloc(links)");
   DYM_CUDA(dmalloc(&d.sites, c->sched.sites.size()), "cudaMalloc(sites)");
-  DYM_CUDA(cudaMemcpy(d.sites, c->sched.sites.data(), c->sched.sites.size() * 4, cudaMemcpyHostToDevice),
+  DYM_CUDA(copy_sync(d.sites, c->sched.sites.data(), c->sched.sites.size() * 4, cudaMemcpyHostToDevice, c->stream),
            "upload sites");
   std::vector<uint16_t> pool;
   if (p->pool == DYM_POOL_NEAREST) pool = g.pool_nearest;
   else for (uint32_t k = 0; k < g.P; ++k) pool.push_back((uint16_t)k);
   d.npool = (uint32_t)pool.size();
   DYM_CUDA(dmalloc(&d.pool, pool.size()), "cudaMalloc(pool)");
-  DYM_CUDA(cudaMemcpy(d.pool, pool.data(), pool.size() * 2, cudaMemcpyHostToDevice), "upload pool");
+  DYM_CUDA(copy_sync(d.pool, pool.data(), pool.size() * 2, cudaMemcpyHostToDevice, c->stream), "upload pool");
   DYM_CUDA(dmalloc(&d.counters, 5), "cudaMalloc(counters)");
   DYM_CUDA(cudaHostAlloc((void**)&c->h_counters, 5 * sizeof(unsigned long long), cudaHostAllocDefault),
            "cudaHostAlloc");
@@ -528,7 +528,7 @@ static int batch_build(dym_batch* b) {
     uint16_t* d = nullptr;
     DYM_CUDA(dmalloc(&d, sub.size()), "cudaMalloc(batch sub)");
     b->d_group_sub.push_back(d);
-    DYM_CUDA(cudaMemcpy(d, sub.data(), sub.size() * 2, cudaMemcpyHostToDevice), "upload batch sub");
+    DYM_CUDA(copy_sync(d, sub.data(), sub.size() * 2, cudaMemcpyHostToDevice, b->stream), "upload batch sub");
     BatchGroupDev& bd = b->bg.g[g];
     bd.mult = (const uint16_t*)G.d_mult;
     bd.inv = (const uint16_t*)G.d_inv;
@@ -571,7 +571,7 @@ static int batch_build(dym_batch* b) {
     maxph = std::max(maxph, c->sched.phase_dir.size());
   }
   DYM_CUDA(dmalloc(&b->d_chains, nc), "cudaMalloc(batch chains)");
-  DYM_CUDA(cudaMemcpy(b->d_chains, cd.data(), nc * sizeof(BatchChainDev), cudaMemcpyHostToDevice), "upload chains");
+  DYM_CUDA(copy_sync(b->d_chains, cd.data(), nc * sizeof(BatchChainDev), cudaMemcpyHostToDevice, b->stream), "upload chains");
   DYM_CUDA(dmalloc(&b->d_sweeps, nc), "cudaMalloc(batch sweeps)");
   // Tiles: slot k holds phase k of every chain, split into pieces of `tile`
   // links; larger pieces first so the last blocks of a slot get small ones.
@@ -594,7 +594,7 @@ static int batch_build(dym_batch* b) {
     b->slot_cnt[k] = (uint32_t)slot.size();
   }
   DYM_CUDA(dmalloc(&b->d_tiles, std::max<size_t>(tiles.size(), 1)), "cudaMalloc(batch tiles)");
-  DYM_CUDA(cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice),
+  DYM_CUDA(copy_sync(b->d_tiles, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice, b->stream),
            "upload tiles");
   void* fn = batch_kernel_for(b->D);
   if (!fn) return fail(DYM_ENOTSUP, "batch: unsupported D");
@@ -789,7 +789,7 @@ int dym_batch_autotune(dym_batch* b, int32_t nhit, int32_t nsweeps_per_trial, dy
     uint16_t* p = nullptr;
     const size_t n = (size_t)c->dev.V * c->p.D;
     DYM_CUDA(dmalloc(&p, n), "cudaMalloc(autotune save)");
-    DYM_CUDA(cudaMemcpy(p, c->dev.links, n * 2, cudaMemcpyDeviceToDevice), "save links");
+    DYM_CUDA(copy_sync(p, c->dev.links, n * 2, cudaMemcpyDeviceToDevice, b->stream), "save links");
     saved.push_back(p);
     sw.push_back(c->sweep);
   }
@@ -813,7 +813,7 @@ int dym_batch_autotune(dym_batch* b, int32_t nhit, int32_t nsweeps_per_trial, dy
       }
   for (size_t i = 0; i < b->chains.size(); ++i) {
     dym_chain* c = b->chains[i];
-    cudaMemcpy(c->dev.links, saved[i], (size_t)c->dev.V * c->p.D * 2, cudaMemcpyDeviceToDevice);
+    copy_sync(c->dev.links, saved[i], (size_t)c->dev.V * c->p.D * 2, cudaMemcpyDeviceToDevice, b->stream);
     cudaFree(saved[i]);
     c->sweep = sw[i];
   }

@@ -98,7 +98,7 @@ int llr_init_state(dym_chain* c, const dym_llr_req* req, LlrState* st) {
   st->mode = (Ew >= st->elo && Ew <= st->ehi) ? DYM_LLR_RM : DYM_LLR_DRIVE;
   if (req->NRM == 0 && st->mode == DYM_LLR_RM) st->mode = DYM_LLR_DONE;
   if (st->mode == DYM_LLR_DRIVE && req->drive_cap == 0) st->mode = DYM_LLR_UNREACHED;
-  DYM_CUDA(cudaMemcpy(c->d_llr, st, sizeof(LlrState), cudaMemcpyHostToDevice), "upload llr state");
+  DYM_CUDA(copy_sync(c->d_llr, st, sizeof(LlrState), cudaMemcpyHostToDevice, c->stream), "upload llr state");
   return DYM_OK;
 }
 
@@ -150,7 +150,7 @@ struct LlrWork {
       for (uint32_t u = 0; u < g->P; ++u) sub[k * g->P + u] = g->mult[(size_t)u * g->P + pool[k]];
     uint16_t* d = nullptr;
     DYM_CUDA(dmalloc(&d, sub.size()), "cudaMalloc(llr sub)");
-    DYM_CUDA(cudaMemcpy(d, sub.data(), sub.size() * 2, cudaMemcpyHostToDevice), "upload llr sub");
+    DYM_CUDA(copy_sync(d, sub.data(), sub.size() * 2, cudaMemcpyHostToDevice, stream), "upload llr sub");
     d_sub.push_back(d);
     groups.push_back(g);
     // layout
@@ -231,9 +231,9 @@ struct LlrWork {
     DYM_CUDA(dmalloc(&d_chains, nc), "cudaMalloc(llr chains)");
     DYM_CUDA(dmalloc(&d_tiles, tiles.size()), "cudaMalloc(llr tiles)");
     DYM_CUDA(dmalloc(&d_commits, commits.size()), "cudaMalloc(llr commits)");
-    DYM_CUDA(cudaMemcpy(d_chains, cd.data(), nc * sizeof(LlrChainDev), cudaMemcpyHostToDevice), "upload chains");
-    DYM_CUDA(cudaMemcpy(d_tiles, tiles.data(), tiles.size() * sizeof(LlrTile), cudaMemcpyHostToDevice), "tiles");
-    DYM_CUDA(cudaMemcpy(d_commits, commits.data(), commits.size() * sizeof(LlrCommit), cudaMemcpyHostToDevice),
+    DYM_CUDA(copy_sync(d_chains, cd.data(), nc * sizeof(LlrChainDev), cudaMemcpyHostToDevice, stream), "upload chains");
+    DYM_CUDA(copy_sync(d_tiles, tiles.data(), tiles.size() * sizeof(LlrTile), cudaMemcpyHostToDevice, stream), "tiles");
+    DYM_CUDA(copy_sync(d_commits, commits.data(), commits.size() * sizeof(LlrCommit), cudaMemcpyHostToDevice, stream),
              "commits");
     void* fn = llr_propose_kernel_for(D);
     if (!fn) return fail(DYM_ENOTSUP, "LLR: unsupported D");
@@ -308,7 +308,7 @@ int dym_llr_run(dym_chain* c, const dym_llr_req* req, dym_llr_result* out, doubl
     DYM_CUDA(cudaStreamSynchronize(c->stream), "llr sweeps");
     mode = st->mode;
   }
-  DYM_CUDA(cudaMemcpy(st.get(), c->d_llr, sizeof(LlrState), cudaMemcpyDeviceToHost), "read llr state");
+  DYM_CUDA(copy_sync(st.get(), c->d_llr, sizeof(LlrState), cudaMemcpyDeviceToHost, c->stream), "read llr state");
   out->a = st->a;
   out->S1 = st->E[0];
   out->S2 = st->E[1];
@@ -428,7 +428,7 @@ int server_retire(dym_server* s) {
       continue;
     }
     LlrState st;
-    DYM_CUDA(cudaMemcpy(&st, a.chain->d_llr, sizeof(LlrState), cudaMemcpyDeviceToHost), "read llr state");
+    DYM_CUDA(copy_sync(&st, a.chain->d_llr, sizeof(LlrState), cudaMemcpyDeviceToHost, s->work.stream), "read llr state");
     dym_llr_response resp{};
     resp.id = a.req.id;
     resp.a = st.a;
