@@ -17,7 +17,7 @@ ERRORS = {-1: "DYM_EINVAL", -2: "DYM_EIO", -3: "DYM_EFORMAT", -4: "DYM_ENOMEM", 
           -6: "DYM_ENOTSUP", -7: "DYM_ETIMEDOUT", -8: "DYM_ERANGE"}
 START = {"hot": 0, "cold": 1}
 POOL = {"nearest": 0, "all": 1}
-PRECISION = {"fp64": 0, "mixed": 1}
+PRECISION = {"fp64": 0, "mixed": 1, "shared": 2}
 
 
 class DymError(RuntimeError):

@@ -95,6 +95,67 @@ static int build_sub_table(dym_chain* c, const std::vector<uint16_t>& pool) {
   return DYM_OK;
 }
 
+// The mixed-precision kernel applies on top of the sub-table path when element
+// ids fit 11 bits and classes 5 bits of a packed entry, and its shared tables
+// fit the opt-in limit.
+static bool mixed_eligible(const Group& g, uint32_t npool, int device) {
+  if (g.P > kMixedMaxP || g.ncls > kMixedMaxCls || g.ncls < 1) return false;
+  int optin = 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) return false;
+  return mixed_smem_bytes(g.P, npool) <= (size_t)optin;
+}
+
+// Fixed-point scale 2^S of the class values: the largest S <= 24 for which a
+// difference of two sums of NR rectangle terms, each |c| 2^S + 1/2 at most,
+// stays inside int32.
+static int fix_shift(const Group& g, int D) {
+  const double NR = 6.0 * (D - 1);
+  const double amax = std::max(g.max_abs_retr, 1e-3);
+  const double lim = (2147483647.0 - 2.0 * NR) / (2.0 * NR * amax);
+  int S = 24;
+  while (S > 0 && std::ldexp(1.0, S) > lim) --S;
+  return S;
+}
+
+// Bound on |dS_fast - dS_fp64| for the mixed kernel at the chain's couplings:
+// class values rounded to 2^-(S+1) (plus the class spread) in each of the
+// 2(NS + NR) terms of a difference, four FP32 roundings (betas, conversions,
+// product, sum) of the scaled difference, and the reference's own FP64
+// rounding of both actions; doubled, plus 1e-7.
+static float mixed_margin(const Group& g, int D, int S, double b0, double b1, double b2) {
+  const double NS = 2.0 * (D - 1), NR = 6.0 * (D - 1);
+  const double q = std::ldexp(1.0, -(S + 1)) + g.cls_spread;
+  const double w = std::fabs(b1) * 2.0 * NS + std::fabs(b2) * 2.0 * NR;
+  const double quant = w * q;
+  const double feval = std::ldexp(1.0, -22) * w * (g.max_abs_retr + q);
+  const double rref = std::ldexp(1.0, -45) * (std::fabs(b0) + (std::fabs(b1) * NS + std::fabs(b2) * NR) * g.max_abs_retr + 1.0);
+  const double m = 2.0 * (quant + feval + rref) + 1e-7;
+  return std::nextafter((float)m, INFINITY);
+}
+
+static int build_mixed_tables(dym_chain* c, const std::vector<uint16_t>& pool) {
+  const Group& g = *c->grp->g;
+  const uint32_t P = g.P, np = (uint32_t)pool.size();
+  std::vector<uint16_t> psub((size_t)np * P);
+  for (uint32_t k = 0; k < np; ++k)
+    for (uint32_t u = 0; u < P; ++u) {
+      const uint16_t e = g.mult[(size_t)u * P + pool[k]];
+      psub[(size_t)k * P + u] = (uint16_t)(e | (g.cls[e] << 11));
+    }
+  const int S = fix_shift(g, c->p.D);
+  std::vector<int32_t> cfix(kMixedMaxCls, 0);
+  for (int k = 0; k < g.ncls; ++k) cfix[k] = (int32_t)std::llrint(std::ldexp(g.cls_val[k], S));
+  DYM_CUDA(dmalloc(&c->dev.psub, psub.size()), "cudaMalloc(psub)");
+  DYM_CUDA(dmalloc(&c->dev.cls8, (size_t)P), "cudaMalloc(cls8)");
+  DYM_CUDA(dmalloc(&c->dev.cfix, (size_t)kMixedMaxCls), "cudaMalloc(cfix)");
+  DYM_CUDA(copy_sync(c->dev.psub, psub.data(), psub.size() * 2, cudaMemcpyHostToDevice, c->stream), "upload psub");
+  DYM_CUDA(copy_sync(c->dev.cls8, g.cls.data(), P, cudaMemcpyHostToDevice, c->stream), "upload cls8");
+  DYM_CUDA(copy_sync(c->dev.cfix, cfix.data(), kMixedMaxCls * 4, cudaMemcpyHostToDevice, c->stream), "upload cfix");
+  c->dev.fix_shift = S;
+  c->dev.mixed_ok = true;
+  return DYM_OK;
+}
+
 static SweepArgs sweep_args(dym_chain* c) {
   const Group& g = *c->grp->g;
   SweepArgs a{};
@@ -114,6 +175,14 @@ static SweepArgs sweep_args(dym_chain* c) {
   a.beta2 = c->p.beta2;
   a.seed = c->p.seed;
   a.counters = c->dev.counters;
+  if (c->dev.mixed_ok) {
+    a.cls8 = c->dev.cls8;
+    a.cfix = c->dev.cfix;
+    a.b1f = (float)c->p.beta1;
+    a.b2f = (float)c->p.beta2;
+    a.dscale = std::ldexp(1.0f, -c->dev.fix_shift);
+    a.dmargin = mixed_margin(g, c->p.D, c->dev.fix_shift, c->p.beta0, c->p.beta1, c->p.beta2);
+  }
 #ifdef DYM_BOUNDS_CHECK
   a.status = c->dev.counters + 4;
 #endif
@@ -129,6 +198,9 @@ static void chain_release(dym_chain* c) {
   cudaFree(c->dev.pool);
   cudaFree(c->dev.counters);
   cudaFree(c->dev.sub);
+  cudaFree(c->dev.psub);
+  cudaFree(c->dev.cls8);
+  cudaFree(c->dev.cfix);
   cudaFree(c->d_hist);
   cudaFree(c->d_meas_scratch);
   cudaFree(c->d_llr);
@@ -243,7 +315,8 @@ int dym_chain_create(const dym_group* gh, const dym_chain_params* p, dym_chain**
   *out = nullptr;
   if (p->start != DYM_START_HOT && p->start != DYM_START_COLD) return fail(DYM_EINVAL, "start must be hot or cold");
   if (p->pool != DYM_POOL_NEAREST && p->pool != DYM_POOL_ALL) return fail(DYM_EINVAL, "unknown proposal pool");
-  if (p->precision != DYM_PREC_FP64 && p->precision != DYM_PREC_MIXED) return fail(DYM_EINVAL, "unknown precision");
+  if (p->precision != DYM_PREC_FP64 && p->precision != DYM_PREC_MIXED && p->precision != DYM_PREC_SHARED)
+    return fail(DYM_EINVAL, "unknown precision");
   std::unique_ptr<dym_chain, void (*)(dym_chain*)> c(new dym_chain, chain_release);
   c->grp = const_cast<dym_group*>(gh);
   c->p = *p;
@@ -277,9 +350,13 @@ int dym_chain_create(const dym_group* gh, const dym_chain_params* p, dym_chain**
   DYM_CUDA(dmalloc(&d.counters, 5), "cudaMalloc(counters)");
   DYM_CUDA(cudaHostAlloc((void**)&c->h_counters, 5 * sizeof(unsigned long long), cudaHostAllocDefault),
            "cudaHostAlloc");
-  if (p->precision == DYM_PREC_MIXED && sub_eligible(g, d.npool, p->device, p->D)) {
+  if (p->precision != DYM_PREC_FP64 && sub_eligible(g, d.npool, p->device, p->D)) {
     rc = build_sub_table(c.get(), pool);
     if (rc) return rc;
+    if (p->precision == DYM_PREC_MIXED && mixed_eligible(g, d.npool, p->device)) {
+      rc = build_mixed_tables(c.get(), pool);
+      if (rc) return rc;
+    }
   }
   if (p->start == DYM_START_HOT)
     DYM_CUDA(launch_hot_start(d.links, V, p->D, g.P, p->seed, c->stream), "hot start");
@@ -317,8 +394,9 @@ int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
     for (size_t p = 0; p < s.phase_dir.size(); ++p) {
       a.sites = c->dev.sites + s.phase_off[p];
       a.n = s.phase_len[p];
-      cudaError_t e = c->dev.sub_ok ? launch_sweep_sub(c->p.D, s.phase_dir[p], a, c->dev.sub, c->stream)
-                                    : launch_sweep_direct(c->p.D, s.phase_dir[p], a, c->stream);
+      cudaError_t e = c->dev.mixed_ok ? launch_sweep_mixed(c->p.D, s.phase_dir[p], a, c->dev.psub, c->stream)
+                      : c->dev.sub_ok ? launch_sweep_sub(c->p.D, s.phase_dir[p], a, c->dev.sub, c->stream)
+                                      : launch_sweep_direct(c->p.D, s.phase_dir[p], a, c->stream);
       if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
     }
     ++c->sweep;

@@ -27,8 +27,14 @@ struct SweepArgs {
   uint64_t seed;
   uint32_t sweep;
   int nhit;
-  unsigned long long* counters;  // [0] hits, [1] accepts, [2] rechecks
+  unsigned long long* counters;  // [0] hits, [1] accepts, [2] rechecks, [3] low word: max |dS error| (FP32 bits)
   unsigned long long* status;    // self-checking build only: first bad index
+  // Mixed-precision kernel (k_sweep_mixed): class of each element, class
+  // values in fixed point (ReTr * 2^fix_shift, rounded), FP32 betas, 2^-fix_shift
+  // and the bound on |dS_fast - dS_fp64| within which a decision is re-evaluated.
+  const uint8_t* cls8;
+  const int32_t* cfix;
+  float b1f, b2f, dscale, dmargin;
 };
 
 struct ChainDev {
@@ -41,6 +47,12 @@ struct ChainDev {
   unsigned long long* counters = nullptr;
   uint16_t* sub = nullptr;     // sub[k*P + u] = u * pool[k] (shared sub-table kernel)
   bool sub_ok = false;
+  // Mixed-precision kernel: psub[k*P + u] = (u * pool[k]) | class << 11.
+  uint16_t* psub = nullptr;
+  uint8_t* cls8 = nullptr;
+  int32_t* cfix = nullptr;
+  int fix_shift = 0;
+  bool mixed_ok = false;
 };
 
 // Launch one colour phase of the FP64 direct sweep.
@@ -48,6 +60,11 @@ cudaError_t launch_sweep_direct(int D, int dir, const SweepArgs& a, cudaStream_t
 // Launch one colour phase of the shared sub-table sweep.
 cudaError_t launch_sweep_sub(int D, int dir, const SweepArgs& a, const uint16_t* sub, cudaStream_t s);
 size_t sub_smem_bytes(uint32_t P, uint32_t npool);
+// Launch one colour phase of the mixed-precision shared sub-table sweep.
+cudaError_t launch_sweep_mixed(int D, int dir, const SweepArgs& a, const uint16_t* psub, cudaStream_t s);
+size_t mixed_smem_bytes(uint32_t P, uint32_t npool);
+constexpr int kMixedMaxCls = 32;    // classes addressable by the 5 high bits of a psub entry
+constexpr uint32_t kMixedMaxP = 2048;  // element ids in the 11 low bits
 cudaError_t launch_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uint64_t seed, cudaStream_t s);
 cudaError_t launch_fill(uint16_t* links, size_t n, uint16_t v, cudaStream_t s);
 cudaError_t launch_staples(int D, int dir, const SweepArgs& a, const uint32_t* sites, uint32_t n, uint16_t* out,

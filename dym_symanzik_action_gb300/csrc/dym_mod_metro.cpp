@@ -8,7 +8,7 @@
 // TM_END) as the reference.  Extensions, all optional:
 //   argv[13] or DYM_NHIT      hits per link (the reference fixes NHIT at compile time)
 //   DYM_POOL=nearest|all      proposal pool (default nearest, as the reference)
-//   DYM_PRECISION=mixed|fp64  accept arithmetic (default mixed; decisions identical)
+//   DYM_PRECISION=mixed|shared|fp64  accept arithmetic (default mixed; decisions identical)
 //   DYM_WLOOP_MAX=KxL         Wilson grid 1..K by 1..L (default the full Nx x Nt grid)
 //   DYM_DEVICE=n              CUDA device
 //   DYM_PERF=1                add PERF lines (link-hits/s and sweeps/s per block)
@@ -119,7 +119,9 @@ int main(int argc, char* argv[]) {
   p.seed = (uint64_t)(int64_t)iseed;
   p.start = coldstart ? DYM_START_COLD : DYM_START_HOT;
   p.pool = pool_all ? DYM_POOL_ALL : DYM_POOL_NEAREST;
-  p.precision = (prec_s && strcmp(prec_s, "fp64") == 0) ? DYM_PREC_FP64 : DYM_PREC_MIXED;
+  p.precision = DYM_PREC_MIXED;
+  if (prec_s && strcmp(prec_s, "fp64") == 0) p.precision = DYM_PREC_FP64;
+  if (prec_s && strcmp(prec_s, "shared") == 0) p.precision = DYM_PREC_SHARED;
   p.device = getenv("DYM_DEVICE") ? atoi(getenv("DYM_DEVICE")) : 0;
   printf("Initializing nearest neighbours [%d:%d]... \n", Nt, Nx);
   dym_chain* c = nullptr;

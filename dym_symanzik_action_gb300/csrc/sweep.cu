@@ -15,6 +15,11 @@
 //    8(D-1) shared-memory loads instead of L2 gathers, and an accepted hit
 //    advances u_j <- u_j * g_k from the same entries.  108 L2 gathers per
 //    link visit remain (staples and u_j).
+//
+//  * k_sweep_mixed  -- k_sweep_sub's decisions with exact integer sums of
+//    fixed-point class values and an FP32 threshold test; FP64 only for the
+//    hits within a proven bound of the threshold (visit_mixed), so the
+//    configurations are the FP64 path's bit for bit.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -112,6 +117,30 @@ __global__ void __launch_bounds__(256) k_sweep_sub(SweepArgs a, const uint16_t* 
   flush_counters(a.counters, hits, accs, 0);
 }
 
+// Shared memory: ReTr (FP64) | class values (int32 fixed point) | inverses |
+// packed sub-table | element classes.
+template <int D, int DIR>
+__global__ void __launch_bounds__(256) k_sweep_mixed(SweepArgs a, const uint16_t* __restrict__ psub) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  double* s_retr = reinterpret_cast<double*>(smem);
+  int32_t* s_cfix = reinterpret_cast<int32_t*>(s_retr + a.P);
+  uint16_t* s_inv = reinterpret_cast<uint16_t*>(s_cfix + kMixedMaxCls);
+  uint16_t* s_psub = s_inv + a.P;
+  uint8_t* s_cls = reinterpret_cast<uint8_t*>(s_psub + (size_t)a.npool * a.P);
+  stage_sub_tables(a.retr, a.inv, psub, a.P, a.npool, s_retr, s_inv, s_psub);
+  for (uint32_t t = threadIdx.x; t < a.P; t += blockDim.x) s_cls[t] = a.cls8[t];
+  if (threadIdx.x < kMixedMaxCls) s_cfix[threadIdx.x] = a.cfix[threadIdx.x];
+  __syncthreads();
+
+  unsigned hits = 0, accs = 0, rechecks = 0;
+  float max_err = 0.0f;
+  for (uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x; tid < a.n; tid += gridDim.x * blockDim.x)
+    visit_mixed<D, DIR>(a, a.sites[tid], a.sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks,
+                        max_err);
+  flush_counters(a.counters, hits, accs, rechecks);
+  flush_max_err(a.counters + 3, max_err);
+}
+
 __global__ void k_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uint64_t seed) {
   const size_t n = (size_t)V * D;
   for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
@@ -197,6 +226,33 @@ cudaError_t sub_dispatch(int dir, const SweepArgs& a, const uint16_t* sub, cudaS
 }
 
 template <int D>
+cudaError_t mixed_dispatch(int dir, const SweepArgs& a, const uint16_t* psub, cudaStream_t s) {
+  const size_t smem = mixed_smem_bytes(a.P, a.npool);
+  void (*fn)(SweepArgs, const uint16_t*) = nullptr;
+  switch (dir) {
+    case 0: fn = k_sweep_mixed<D, 0>; break;
+    case 1: fn = k_sweep_mixed<D, 1>; break;
+    case 2: if (D > 2) fn = k_sweep_mixed<D, (D > 2 ? 2 : 0)>; break;
+    case 3: if (D > 3) fn = k_sweep_mixed<D, (D > 3 ? 3 : 0)>; break;
+  }
+  if (!fn) return cudaErrorInvalidValue;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  const unsigned need = (a.n + 255) / 256;
+  if (need == 0) return cudaSuccess;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem);
+  if (e != cudaSuccess) return e;
+  const unsigned grid = std::min<unsigned>(need, (unsigned)std::max(1, sms * std::max(per_sm, 1)));
+  fn<<<grid, 256, smem, s>>>(a, psub);
+  return cudaGetLastError();
+}
+
+template <int D>
 cudaError_t staples_dispatch(int dir, const SweepArgs& a, const uint32_t* sites, uint32_t n, uint16_t* out,
                              cudaStream_t s) {
   void (*fn)(SweepArgs, const uint32_t*, uint32_t, uint16_t*) = nullptr;
@@ -216,6 +272,15 @@ cudaError_t staples_dispatch(int dir, const SweepArgs& a, const uint32_t* sites,
 
 size_t sub_smem_bytes(uint32_t P, uint32_t npool) {
   return (size_t)P * 8 + (size_t)P * 2 + (size_t)npool * P * 2 + 16;
+}
+
+size_t mixed_smem_bytes(uint32_t P, uint32_t npool) {
+  return (size_t)P * 8 + kMixedMaxCls * 4 + (size_t)P * 2 + (size_t)npool * P * 2 + (size_t)P + 16;
+}
+
+cudaError_t launch_sweep_mixed(int D, int dir, const SweepArgs& a, const uint16_t* psub, cudaStream_t s) {
+  if (D == 4) return mixed_dispatch<4>(dir, a, psub, s);  // four dimensions only, as launch_sweep_sub
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_sweep_direct(int D, int dir, const SweepArgs& a, cudaStream_t s) {

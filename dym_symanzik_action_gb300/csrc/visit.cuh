@@ -89,6 +89,112 @@ __device__ __forceinline__ void visit_sub(const SweepArgs& a, uint32_t i, uint32
   if (b != b0) *own = (uint16_t)b;
 }
 
+// Mixed-precision visit of link (i, DIR): the decisions of visit_sub, taken
+// without FP64 arithmetic except near the threshold.
+//
+// A packed sub-table entry holds the element (11 low bits) and its ReTr class
+// (5 high bits); the class values are staged as int32 fixed point c * 2^S.  A
+// proposal's action change is then dS_fast = (b1 dR + b2 dM) 2^-S with dR, dM
+// exact integer differences of the plaquette and rectangle sums, evaluated in
+// FP32.  a.dmargin bounds |dS_fast - dS_fp64| (class-value rounding, FP32
+// rounding, and the reference's own FP64 rounding), and t = -log(u2) is
+// computed in FP32 with a bound of 2^-19 + 2^-20 t.  The reference accepts iff
+// dS <= 0 or exp(-dS) > u2, i.e. iff dS < t (dym_exp is within an ulp of exp),
+// so dS_fast < t - band accepts, dS_fast > t + band rejects, and only the hits
+// in between are re-evaluated exactly as visit_sub does (FP64 sums in the
+// reference's order, dym_accept_fast).  The configurations are therefore those
+// of the FP64 path bit for bit.  The exact action of the current link is
+// rebuilt lazily when a re-evaluation needs it after fast accepts.
+template <int D, int DIR>
+__device__ __forceinline__ void visit_mixed(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
+                                            const uint16_t* s_inv, const uint16_t* s_psub, const uint8_t* s_cls,
+                                            const int32_t* s_cfix, unsigned& hits, unsigned& accs,
+                                            unsigned& rechecks, float& max_err) {
+  constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
+  SiteGeo<D> geo;
+  site_geo<D>(i, a.Nt, a.Nx, geo);
+  GlobalTab T{a.mult, s_inv, a.P};
+  const uint16_t* L = a.links;
+  const uint32_t V = a.V;
+  auto ld = [L, V](uint32_t s, int d) -> uint32_t { return __ldg(L + (size_t)d * V + s); };
+  uint32_t u[NT];
+  build_staples<D, DIR>(i, geo, T, ld, u, u + NS);
+
+  uint16_t* own = a.links + (size_t)DIR * V + i;
+  uint32_t b = *own;
+  const uint32_t b0 = b;
+#pragma unroll
+  for (int j = 0; j < NT; ++j) u[j] = T.mul(u[j], b);  // u_j = s_j * b
+  uint32_t R = 0, M = 0;  // fixed-point sums, modular (differences are exact)
+#pragma unroll
+  for (int j = 0; j < NS; ++j) R += (uint32_t)s_cfix[s_cls[u[j]]];
+#pragma unroll
+  for (int j = NS; j < NT; ++j) M += (uint32_t)s_cfix[s_cls[u[j]]];
+  double oldact = 0.0;
+  bool old_ok = false;
+  for (int h = 0; h < a.nhit; ++h) {
+    const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_METRO);
+    const uint16_t* row = s_psub + dym_pick(r.v[0], a.npool) * a.P;
+    uint32_t e[NT];
+    uint32_t Rn = 0, Mn = 0;
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      e[j] = row[u[j]];
+      Rn += (uint32_t)s_cfix[e[j] >> 11];
+    }
+#pragma unroll
+    for (int j = NS; j < NT; ++j) {
+      e[j] = row[u[j]];
+      Mn += (uint32_t)s_cfix[e[j] >> 11];
+    }
+    const float dR = (float)(int32_t)(Rn - R), dM = (float)(int32_t)(Mn - M);
+    const float ds = __fmaf_rn(a.b2f, dM, __fmul_rn(a.b1f, dR)) * a.dscale;
+    // u2 = (r1 * 2^21 + (r2 >> 11)) * 2^-53 to within a relative 2^-22.
+    const float u2f = __fmaf_rn((float)r.v[1], 0x1p-32f, (float)(r.v[2] >> 11) * 0x1p-53f);
+    const float t = -__logf(u2f);
+    const float band = a.dmargin + __fmaf_rn(t, 0x1p-20f, 0x1p-19f);
+    bool acc;
+    bool exact = false;
+    if (ds < t - band) {
+      acc = true;
+    } else if (ds > t + band) {
+      acc = false;
+    } else {  // too close to call (also u2 == 0, where t - band is NaN)
+      if (!old_ok) {
+        double r1 = 0, m1 = 0;
+#pragma unroll
+        for (int j = 0; j < NS; ++j) r1 = DYM_ADD(r1, s_retr[u[j]]);
+#pragma unroll
+        for (int j = NS; j < NT; ++j) m1 = DYM_ADD(m1, s_retr[u[j]]);
+        oldact = dym_action(a.beta0, a.beta1, a.beta2, r1, m1);
+        old_ok = true;
+      }
+      double r1n = 0, m1n = 0;
+#pragma unroll
+      for (int j = 0; j < NS; ++j) r1n = DYM_ADD(r1n, s_retr[e[j] & 0x7FFu]);
+#pragma unroll
+      for (int j = NS; j < NT; ++j) m1n = DYM_ADD(m1n, s_retr[e[j] & 0x7FFu]);
+      const double newact = dym_action(a.beta0, a.beta1, a.beta2, r1n, m1n);
+      acc = dym_accept_fast(oldact, newact, dym_u53(r.v[1], r.v[2]));
+      max_err = fmaxf(max_err, fabsf(ds - (float)DYM_SUB(newact, oldact)));
+      ++rechecks;
+      exact = true;
+      if (acc) oldact = newact;
+    }
+    ++hits;
+    if (acc) {
+      b = row[b] & 0x7FFu;
+#pragma unroll
+      for (int j = 0; j < NT; ++j) u[j] = e[j] & 0x7FFu;
+      R = Rn;
+      M = Mn;
+      old_ok = exact;
+      ++accs;
+    }
+  }
+  if (b != b0) *own = (uint16_t)b;
+}
+
 __device__ __forceinline__ void flush_counters(unsigned long long* ctr, unsigned hits, unsigned accs,
                                                unsigned rechecks) {
   hits = __reduce_add_sync(0xffffffffu, hits);
@@ -99,6 +205,13 @@ __device__ __forceinline__ void flush_counters(unsigned long long* ctr, unsigned
     if (accs) atomicAdd(ctr + 1, (unsigned long long)accs);
     if (rechecks) atomicAdd(ctr + 2, (unsigned long long)rechecks);
   }
+}
+
+// Largest |dS_fast - dS_fp64| seen at a re-evaluation, into the low word of
+// *ctr (non-negative floats order like their bit patterns).
+__device__ __forceinline__ void flush_max_err(unsigned long long* ctr, float err) {
+  const unsigned bits = __reduce_max_sync(0xffffffffu, __float_as_uint(err));
+  if ((threadIdx.x & 31) == 0 && bits) atomicMax(reinterpret_cast<unsigned int*>(ctr), bits);
 }
 
 }  // namespace dym

@@ -47,8 +47,14 @@ extern "C" {
 #define DYM_POOL_ALL 1     /* uniform over the whole group */
 
 #define DYM_PREC_FP64 0    /* every accept test in FP64, as the reference */
-#define DYM_PREC_MIXED 1   /* FP32 dS with FP64 re-evaluation near the threshold;
-                              accept decisions identical to DYM_PREC_FP64 */
+#define DYM_PREC_MIXED 1   /* dS from exact int32 sums of fixed-point class values,
+                              scaled and tested against -log(u2) in FP32; FP64
+                              re-evaluation within a proven bound of the threshold.
+                              Decisions identical to DYM_PREC_FP64 (four dimensions,
+                              tables with P <= 2048 and <= 32 ReTr classes; else
+                              as DYM_PREC_SHARED) */
+#define DYM_PREC_SHARED 2  /* FP64 decisions, hit loop served from the shared
+                              sub-table (four dimensions, class-constant tables) */
 
 typedef struct dym_group dym_group;
 typedef struct dym_chain dym_chain;
@@ -93,7 +99,7 @@ typedef struct {
   uint64_t seed;                 /* Philox key (reference: per-site minstd seeds) */
   int32_t start;                 /* DYM_START_HOT / DYM_START_COLD */
   int32_t pool;                  /* DYM_POOL_NEAREST / DYM_POOL_ALL */
-  int32_t precision;             /* DYM_PREC_FP64 / DYM_PREC_MIXED */
+  int32_t precision;             /* DYM_PREC_FP64 / DYM_PREC_MIXED / DYM_PREC_SHARED */
   int32_t device;                /* CUDA device ordinal */
 } dym_chain_params;
 
@@ -196,7 +202,7 @@ int dym_schedule_get(int32_t D, int32_t Nt, int32_t Nx, uint32_t* V, int32_t* np
  * every chain; each chain's configurations are bit-identical to running it
  * alone with dym_sweep.  Chains stay owned by the caller and must outlive
  * the batch; they must share D and the device, use DYM_POOL_NEAREST and
- * DYM_PREC_MIXED with a table eligible for the shared-table path
+ * DYM_PREC_MIXED or DYM_PREC_SHARED with a table eligible for the shared-table path
  * (dym_group_info.fast_path), at most 4 distinct groups. */
 typedef struct dym_batch dym_batch;
 

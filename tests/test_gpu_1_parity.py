@@ -3,9 +3,11 @@ and the oracle.
 
 Bar: link configurations and hit/accept counts bit-exact after every sweep;
 observables bit-exact against the oracle's histogram sums and within 1e-12
-of the reference's site-order sums.  Both accept paths are covered: FP64
-(every decision as the reference) and mixed (FP32 dS with FP64 re-evaluation
-near the threshold), which must give identical configurations."""
+of the reference's site-order sums.  All three accept paths are covered:
+fp64 (direct kernel, every decision as the reference), shared (FP64
+decisions with the shared sub-table) and mixed (exact fixed-point dS with an
+FP32 threshold test and FP64 re-evaluation near the threshold); all must give
+identical configurations."""
 import numpy as np
 import pytest
 
@@ -34,7 +36,7 @@ def test_staples_match_reference(engine):
         assert (st == g["staples"][d]).all(), d
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "shared", "mixed"])
 @pytest.mark.parametrize("name", list(sweep_cases().keys()))
 def test_sweeps_match_reference(engine, sweeps_golden, name, precision):
     gname, D, Nt, Nx, beta, start, seed, nhit, pool_all, nsw, wx, wt = sweep_cases()[name]
@@ -75,7 +77,7 @@ def test_random_configs_match_oracle(engine, case):
     seed = 1000 + Nt * 7 + Nx
     og = OracleGroup(tables.ensure_table(gname))
     sched = schedule(D, Nt, Nx)
-    for precision in ("fp64", "mixed"):
+    for precision in ("fp64", "shared", "mixed"):
         lat = engine.Lattice(group(engine, gname), D, Nt, Nx, *beta, seed, start=start, pool=pool,
                              precision=precision)
         ol = OracleLattice(og, D, Nt, Nx)
@@ -89,18 +91,19 @@ def test_random_configs_match_oracle(engine, case):
 
 def test_full_size_cold_chain_matches_oracle(engine):
     """32^3 x 8 (1,048,576 links), cold start at beta = (0, 3, -0.15), NHIT 10:
-    two sweeps bit-exact against the oracle, both accept paths."""
+    two sweeps bit-exact against the oracle, all three accept paths."""
     D, Nt, Nx, beta, nhit = 4, 8, 32, (0.0, 3.0, -0.15), 10
     og = OracleGroup(tables.ensure_table("S1080"))
     sched = schedule(D, Nt, Nx)
     ol = OracleLattice(og, D, Nt, Nx)
     res = {}
-    for precision in ("mixed", "fp64"):
+    for precision in ("mixed", "shared", "fp64"):
         lat = engine.Lattice(group(engine, "S1080"), D, Nt, Nx, *beta, 20261203, start="cold", precision=precision)
         st = lat.update(2, nhit)
         assert st.hits == lat.V * D * nhit * 2
         res[precision] = (lat.links.ravel(), st.accepts)
-    assert (res["mixed"][0] == res["fp64"][0]).all() and res["mixed"][1] == res["fp64"][1]
+    for p in ("mixed", "shared"):
+        assert (res[p][0] == res["fp64"][0]).all() and res[p][1] == res["fp64"][1], p
     h, a = ol.sweep(sched, beta, 20261203, 0, 2, nhit)
     assert a == res["fp64"][1]
     assert (ol.links == res["fp64"][0]).all()
@@ -126,3 +129,20 @@ def test_full_size_hot_chain_matches_oracle(engine):
 def test_shared_table_path_is_selected_for_generated_tables(engine):
     for name in ("S1080", "BI", "BT"):
         assert group(engine, name).fast_path, name
+
+
+def test_mixed_precision_reports_rechecks(engine):
+    """Hot S(1080) 8^4 at beta = (0, 2, -0.1): the mixed kernel re-evaluates a
+    small fraction of hits in FP64, reports the largest |dS_fast - dS_fp64|
+    seen there (below its bound), and gives the fp64 kernel's configuration."""
+    D, Nt, Nx, beta, nhit = 4, 8, 8, (0.0, 2.0, -0.1), 10
+    res = {}
+    for precision in ("mixed", "fp64"):
+        lat = engine.Lattice(group(engine, "S1080"), D, Nt, Nx, *beta, 4242, start="hot", precision=precision)
+        st = lat.update(5, nhit)
+        res[precision] = (lat.links.ravel(), st)
+    (lm, sm), (lf, sf) = res["mixed"], res["fp64"]
+    assert (lm == lf).all() and sm.accepts == sf.accepts
+    assert sf.rechecks == 0
+    assert 0 < sm.rechecks < 1e-3 * sm.hits
+    assert 0.0 <= sm.max_ds_err < 1e-3
