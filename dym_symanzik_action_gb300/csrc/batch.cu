@@ -71,6 +71,67 @@ __global__ void __launch_bounds__(256) k_batch_sub(const BatchTile* __restrict__
   }
 }
 
+// The same work list with the mixed-precision visit (visit_mixed): every group
+// of the batch stages ReTr, inverses, packed sub-table, element classes and
+// fixed-point class values.
+template <int D>
+__global__ void __launch_bounds__(kMixedMaxThreads, 1) k_batch_mixed(const BatchTile* __restrict__ tiles, uint32_t ntiles,
+                                                     const BatchChainDev* __restrict__ chains, BatchGroups groups,
+                                                     const uint32_t* __restrict__ sweeps, int nhit) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  for (int g = 0; g < groups.n; ++g) {
+    const BatchGroupDev& G = groups.g[g];
+    stage_sub_tables(G.retr, G.inv, G.sub, G.P, G.npool, reinterpret_cast<double*>(smem + G.off_retr),
+                     reinterpret_cast<uint16_t*>(smem + G.off_inv), reinterpret_cast<uint16_t*>(smem + G.off_sub));
+    uint8_t* s_cls = smem + G.off_cls8;
+    for (uint32_t t = threadIdx.x; t < G.P; t += blockDim.x) s_cls[t] = G.cls8[t];
+    if (threadIdx.x < kMixedMaxCls) reinterpret_cast<int32_t*>(smem + G.off_cfix)[threadIdx.x] = G.cfix[threadIdx.x];
+  }
+  __syncthreads();
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const BatchTile tl = tiles[t];
+    const BatchChainDev c = chains[tl.chain];
+    const BatchGroupDev& G = groups.g[c.group];
+    SweepArgs a{};
+    a.links = c.links;
+    a.V = c.V;
+    a.Nt = c.Nt;
+    a.Nx = c.Nx;
+    a.mult = G.mult;
+    a.P = G.P;
+    a.npool = G.npool;
+    a.beta0 = c.beta0;
+    a.beta1 = c.beta1;
+    a.beta2 = c.beta2;
+    a.seed = c.seed;
+    a.nhit = nhit;
+    a.b1f = c.b1f;
+    a.b2f = c.b2f;
+    a.dscale = G.dscale;
+    a.dmargin = c.dmargin;
+    const uint32_t sweep = sweeps[tl.chain];
+    const double* s_retr = reinterpret_cast<const double*>(smem + G.off_retr);
+    const uint16_t* s_inv = reinterpret_cast<const uint16_t*>(smem + G.off_inv);
+    const uint16_t* s_psub = reinterpret_cast<const uint16_t*>(smem + G.off_sub);
+    const uint8_t* s_cls = smem + G.off_cls8;
+    const int32_t* s_cfix = reinterpret_cast<const int32_t*>(smem + G.off_cfix);
+    unsigned hits = 0, accs = 0, rechecks = 0;
+    float max_err = 0.0f;
+    for (uint32_t k = threadIdx.x; k < tl.count; k += blockDim.x) {
+      const uint32_t i = c.sites[tl.begin + k];
+      const uint32_t xyz = c.xyz[tl.begin + k];
+      switch (tl.dir) {
+        case 0: visit_mixed<D, 0>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
+        case 1: visit_mixed<D, 1>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
+        case 2: visit_mixed<D, 2>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
+        case 3: visit_mixed<D, 3>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
+      }
+    }
+    flush_counters(c.ctr, hits, accs, rechecks);
+    flush_max_err(c.ctr + 3, max_err);
+  }
+}
+
 __global__ void k_batch_advance(uint32_t* sweeps, uint32_t n) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) sweeps[i] += 1;
@@ -83,14 +144,20 @@ void* batch_kernel() {
 
 }  // namespace
 
-void* batch_kernel_for(int D) { return D == 4 ? batch_kernel<4>() : nullptr; }
+void* batch_kernel_for(int D, bool mixed) {
+  if (D != 4) return nullptr;
+  return mixed ? (void*)k_batch_mixed<4> : batch_kernel<4>();
+}
 
-cudaError_t launch_batch_slot(int D, const BatchTile* tiles, uint32_t ntiles, const BatchChainDev* chains,
+cudaError_t launch_batch_slot(int D, bool mixed, const BatchTile* tiles, uint32_t ntiles, const BatchChainDev* chains,
                               const BatchGroups& groups, const uint32_t* sweeps, int nhit, unsigned grid,
                               unsigned threads, size_t smem, cudaStream_t s) {
   if (ntiles == 0) return cudaSuccess;
   if (D != 4) return cudaErrorInvalidValue;  // four dimensions only (see launch_sweep_sub)
-  k_batch_sub<4><<<grid, threads, smem, s>>>(tiles, ntiles, chains, groups, sweeps, nhit);
+  if (mixed)
+    k_batch_mixed<4><<<grid, threads, smem, s>>>(tiles, ntiles, chains, groups, sweeps, nhit);
+  else
+    k_batch_sub<4><<<grid, threads, smem, s>>>(tiles, ntiles, chains, groups, sweeps, nhit);
   return cudaGetLastError();
 }
 

@@ -13,7 +13,9 @@ struct BatchChainDev {
   int group;
   double beta0, beta1, beta2;
   uint64_t seed;
-  unsigned long long* ctr;  // [hits, accepts] of this chain
+  unsigned long long* ctr;  // [hits, accepts, rechecks, max |dS error| bits] of this chain
+  float b1f, b2f, dmargin;  // mixed-precision kernel: FP32 betas, error bound at these betas
+  const uint32_t* xyz;      // mixed-precision kernel: packed coordinates of sites[k]
 };
 
 struct BatchGroupDev {
@@ -24,6 +26,12 @@ struct BatchGroupDev {
   const uint16_t* cls16;  // ReTr class of each element (LLR only)
   uint32_t P, npool;
   uint32_t off_retr, off_inv, off_sub, off_cls;  // byte offsets of the staged copies in shared memory
+  // Mixed-precision kernel: sub holds packed entries (element | class << 11),
+  // cls8 the class of each element, cfix the fixed-point class values.
+  const uint8_t* cls8;
+  const int32_t* cfix;
+  float dscale;
+  uint32_t off_cls8, off_cfix;
 };
 
 constexpr int kBatchMaxGroups = 4;
@@ -60,8 +68,8 @@ cudaError_t launch_llr_slot(int D, const LlrTile* tiles, uint32_t ntiles, const 
                             const LlrChainDev* chains, const BatchGroups& groups, int nhit, unsigned grid,
                             size_t smem, cudaStream_t s);
 
-void* batch_kernel_for(int D);
-cudaError_t launch_batch_slot(int D, const BatchTile* tiles, uint32_t ntiles, const BatchChainDev* chains,
+void* batch_kernel_for(int D, bool mixed);
+cudaError_t launch_batch_slot(int D, bool mixed, const BatchTile* tiles, uint32_t ntiles, const BatchChainDev* chains,
                               const BatchGroups& groups, const uint32_t* sweeps, int nhit, unsigned grid,
                               unsigned threads, size_t smem, cudaStream_t s);
 cudaError_t launch_batch_advance(uint32_t* sweeps, uint32_t n, cudaStream_t s);

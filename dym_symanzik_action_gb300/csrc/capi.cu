@@ -151,6 +151,20 @@ static int build_mixed_tables(dym_chain* c, const std::vector<uint16_t>& pool) {
   DYM_CUDA(copy_sync(c->dev.psub, psub.data(), psub.size() * 2, cudaMemcpyHostToDevice, c->stream), "upload psub");
   DYM_CUDA(copy_sync(c->dev.cls8, g.cls.data(), P, cudaMemcpyHostToDevice, c->stream), "upload cls8");
   DYM_CUDA(copy_sync(c->dev.cfix, cfix.data(), kMixedMaxCls * 4, cudaMemcpyHostToDevice, c->stream), "upload cfix");
+  // Packed coordinates of every schedule entry (8 bits per axis).
+  const Schedule& sc = c->sched;
+  std::vector<uint32_t> xyz(sc.sites.size());
+  for (size_t k = 0; k < sc.sites.size(); ++k) {
+    uint32_t i = sc.sites[k], w = 0;
+    for (int b = 0; b < c->p.D; ++b) {
+      const uint32_t N = (uint32_t)(b == 0 ? c->p.Nt : c->p.Nx);
+      w |= (i % N) << (8 * b);
+      i /= N;
+    }
+    xyz[k] = w;
+  }
+  DYM_CUDA(dmalloc(&c->dev.xyz, xyz.size()), "cudaMalloc(xyz)");
+  DYM_CUDA(copy_sync(c->dev.xyz, xyz.data(), xyz.size() * 4, cudaMemcpyHostToDevice, c->stream), "upload xyz");
   c->dev.fix_shift = S;
   c->dev.mixed_ok = true;
   return DYM_OK;
@@ -201,6 +215,7 @@ static void chain_release(dym_chain* c) {
   cudaFree(c->dev.psub);
   cudaFree(c->dev.cls8);
   cudaFree(c->dev.cfix);
+  cudaFree(c->dev.xyz);
   cudaFree(c->d_hist);
   cudaFree(c->d_meas_scratch);
   cudaFree(c->d_llr);
@@ -353,7 +368,8 @@ int dym_chain_create(const dym_group* gh, const dym_chain_params* p, dym_chain**
   if (p->precision != DYM_PREC_FP64 && sub_eligible(g, d.npool, p->device, p->D)) {
     rc = build_sub_table(c.get(), pool);
     if (rc) return rc;
-    if (p->precision == DYM_PREC_MIXED && mixed_eligible(g, d.npool, p->device)) {
+    if (p->precision == DYM_PREC_MIXED && mixed_eligible(g, d.npool, p->device) && p->Nt <= kMixedMaxExtent &&
+        p->Nx <= kMixedMaxExtent) {
       rc = build_mixed_tables(c.get(), pool);
       if (rc) return rc;
     }
@@ -393,6 +409,7 @@ int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
     a.sweep = c->sweep;
     for (size_t p = 0; p < s.phase_dir.size(); ++p) {
       a.sites = c->dev.sites + s.phase_off[p];
+      a.xyz = c->dev.xyz ? c->dev.xyz + s.phase_off[p] : nullptr;
       a.n = s.phase_len[p];
       cudaError_t e = c->dev.mixed_ok ? launch_sweep_mixed(c->p.D, s.phase_dir[p], a, c->dev.psub, c->stream)
                       : c->dev.sub_ok ? launch_sweep_sub(c->p.D, s.phase_dir[p], a, c->dev.sub, c->stream)
@@ -550,7 +567,9 @@ struct dym_batch {
   int D = 0;
   std::vector<dym_chain*> chains;
   std::vector<dym::Group*> groups;
-  std::vector<uint16_t*> d_group_sub;  // one sub-table per group (owned)
+  std::vector<uint16_t*> d_group_sub;  // one sub-table per group (owned; packed when mixed)
+  std::vector<int32_t*> d_group_cfix;  // fixed-point class values per group (mixed only)
+  bool mixed = false;                  // every chain runs the mixed-precision visit
   dym::BatchGroups bg{};
   dym::BatchChainDev* d_chains = nullptr;
   dym::BatchTile* d_tiles = nullptr;
@@ -587,6 +606,8 @@ static void batch_release_device(dym_batch* b) {
   b->d_ctr = nullptr;
   for (auto p : b->d_group_sub) cudaFree(p);
   b->d_group_sub.clear();
+  for (auto p : b->d_group_cfix) cudaFree(p);
+  b->d_group_cfix.clear();
 }
 
 // Lay out tables, descriptors and per-slot tile lists for the current chains.
@@ -597,12 +618,17 @@ static int batch_build(dym_batch* b) {
   b->bg.n = (int)b->groups.size();
   size_t off = 0;
   auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
+  b->mixed = std::all_of(b->chains.begin(), b->chains.end(), [](const dym_chain* c) { return c->dev.mixed_ok; });
+  std::vector<int> shift(b->groups.size(), 0);
   for (size_t g = 0; g < b->groups.size(); ++g) {
     const Group& G = *b->groups[g];
     const auto& pool = G.pool_nearest;
     std::vector<uint16_t> sub(pool.size() * (size_t)G.P);
     for (size_t k = 0; k < pool.size(); ++k)
-      for (uint32_t u = 0; u < G.P; ++u) sub[k * G.P + u] = G.mult[(size_t)u * G.P + pool[k]];
+      for (uint32_t u = 0; u < G.P; ++u) {
+        const uint16_t e = G.mult[(size_t)u * G.P + pool[k]];
+        sub[k * G.P + u] = b->mixed ? (uint16_t)(e | (G.cls[e] << 11)) : e;
+      }
     uint16_t* d = nullptr;
     DYM_CUDA(dmalloc(&d, sub.size()), "cudaMalloc(batch sub)");
     b->d_group_sub.push_back(d);
@@ -620,6 +646,22 @@ static int batch_build(dym_batch* b) {
     off = up16(off + (size_t)G.P * 2);
     bd.off_sub = (uint32_t)off;
     off = up16(off + sub.size() * 2);
+    if (b->mixed) {
+      shift[g] = fix_shift(G, b->D);
+      std::vector<int32_t> cfix(kMixedMaxCls, 0);
+      for (int k = 0; k < G.ncls; ++k) cfix[k] = (int32_t)std::llrint(std::ldexp(G.cls_val[k], shift[g]));
+      int32_t* dc = nullptr;
+      DYM_CUDA(dmalloc(&dc, (size_t)kMixedMaxCls), "cudaMalloc(batch cfix)");
+      b->d_group_cfix.push_back(dc);
+      DYM_CUDA(copy_sync(dc, cfix.data(), kMixedMaxCls * 4, cudaMemcpyHostToDevice, b->stream), "upload batch cfix");
+      bd.cls8 = (const uint8_t*)G.d_cls;
+      bd.cfix = dc;
+      bd.dscale = std::ldexp(1.0f, -shift[g]);
+      bd.off_cls8 = (uint32_t)off;
+      off = up16(off + G.P);
+      bd.off_cfix = (uint32_t)off;
+      off = up16(off + kMixedMaxCls * 4);
+    }
   }
   b->smem = off;
   int optin = 0;
@@ -628,7 +670,7 @@ static int batch_build(dym_batch* b) {
     return fail(DYM_ENOTSUP, "the batch's groups need " + std::to_string(b->smem) + " B of shared tables, more than " +
                                  std::to_string(optin));
   std::vector<BatchChainDev> cd(nc);
-  DYM_CUDA(dmalloc(&b->d_ctr, 2 * nc), "cudaMalloc(batch counters)");
+  DYM_CUDA(dmalloc(&b->d_ctr, 4 * nc), "cudaMalloc(batch counters)");
   b->nlinks = 0;
   size_t maxph = 0;
   for (size_t i = 0; i < nc; ++i) {
@@ -644,7 +686,13 @@ static int batch_build(dym_batch* b) {
     d.beta1 = c->p.beta1;
     d.beta2 = c->p.beta2;
     d.seed = c->p.seed;
-    d.ctr = b->d_ctr + 2 * i;
+    d.ctr = b->d_ctr + 4 * i;
+    d.xyz = c->dev.xyz;
+    if (b->mixed) {
+      d.b1f = (float)c->p.beta1;
+      d.b2f = (float)c->p.beta2;
+      d.dmargin = mixed_margin(*c->grp->g, b->D, shift[d.group], c->p.beta0, c->p.beta1, c->p.beta2);
+    }
     b->nlinks += (uint64_t)c->dev.V * c->p.D;
     maxph = std::max(maxph, c->sched.phase_dir.size());
   }
@@ -674,7 +722,7 @@ static int batch_build(dym_batch* b) {
   DYM_CUDA(dmalloc(&b->d_tiles, std::max<size_t>(tiles.size(), 1)), "cudaMalloc(batch tiles)");
   DYM_CUDA(copy_sync(b->d_tiles, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice, b->stream),
            "upload tiles");
-  void* fn = batch_kernel_for(b->D);
+  void* fn = batch_kernel_for(b->D, b->mixed);
   if (!fn) return fail(DYM_ENOTSUP, "batch: unsupported D");
   DYM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem), "smem attribute");
   b->dirty = false;
@@ -683,7 +731,7 @@ static int batch_build(dym_batch* b) {
 
 static int batch_grid(dym_batch* b, unsigned* grid) {
   int per_sm = 0;
-  DYM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel_for(b->D), b->tune.threads, b->smem),
+  DYM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel_for(b->D, b->mixed), b->tune.threads, b->smem),
            "occupancy");
   *grid = (unsigned)std::max(1, b->sms * std::max(1, std::min(per_sm, b->tune.grid_per_sm)));
   return DYM_OK;
@@ -691,7 +739,7 @@ static int batch_grid(dym_batch* b, unsigned* grid) {
 
 static int batch_enqueue_sweep(dym_batch* b, int nhit, unsigned grid) {
   for (size_t k = 0; k < b->slot_cnt.size(); ++k) {
-    cudaError_t e = launch_batch_slot(b->D, b->d_tiles + b->slot_off[k], b->slot_cnt[k], b->d_chains, b->bg,
+    cudaError_t e = launch_batch_slot(b->D, b->mixed, b->d_tiles + b->slot_off[k], b->slot_cnt[k], b->d_chains, b->bg,
                                       b->d_sweeps, nhit, std::min<unsigned>(grid, b->slot_cnt[k]),
                                       (unsigned)b->tune.threads, b->smem, b->stream);
     if (e != cudaSuccess) return cuda_fail(e, "batch slot launch");
@@ -754,8 +802,12 @@ int dym_batch_size(const dym_batch* b, int32_t* nchains, uint64_t* nlinks, int32
 
 int dym_batch_set_tuning(dym_batch* b, const dym_batch_tuning* t) {
   if (!b || !t) return fail(DYM_EINVAL, "dym_batch_set_tuning: null argument");
-  if (t->tile < 32 || t->tile % 32 || (t->threads != 128 && t->threads != 256) || t->grid_per_sm < 1)
-    return fail(DYM_EINVAL, "tuning: tile a multiple of 32, threads 128 or 256, grid_per_sm >= 1");
+  if (t->tile < 32 || t->tile % 32 || (t->threads != 128 && t->threads != 256 && t->threads != 512) ||
+      t->grid_per_sm < 1)
+    return fail(DYM_EINVAL, "tuning: tile a multiple of 32, threads 128, 256 or 512, grid_per_sm >= 1");
+  if (t->threads == 512 && !b->mixed && !b->chains.empty() &&
+      !std::all_of(b->chains.begin(), b->chains.end(), [](const dym_chain* c) { return c->dev.mixed_ok; }))
+    return fail(DYM_EINVAL, "tuning: 512 threads need the mixed-precision batch kernel");
   if (t->tile != b->tune.tile) b->dirty = true;
   b->tune = *t;
   if (b->exec) {
@@ -789,7 +841,7 @@ int dym_batch_sweep(dym_batch* b, int32_t nsweeps, int32_t nhit, dym_stats* tota
   std::vector<uint32_t> sw(nc);
   for (size_t i = 0; i < nc; ++i) sw[i] = b->chains[i]->sweep;
   DYM_CUDA(cudaMemcpyAsync(b->d_sweeps, sw.data(), nc * 4, cudaMemcpyHostToDevice, b->stream), "upload sweeps");
-  DYM_CUDA(cudaMemsetAsync(b->d_ctr, 0, 2 * nc * sizeof(unsigned long long), b->stream), "reset counters");
+  DYM_CUDA(cudaMemsetAsync(b->d_ctr, 0, 4 * nc * sizeof(unsigned long long), b->stream), "reset counters");
   unsigned grid = 1;
   int grc = batch_grid(b, &grid);
   if (grc) return grc;
@@ -825,8 +877,8 @@ int dym_batch_sweep(dym_batch* b, int32_t nsweeps, int32_t nhit, dym_stats* tota
     }
   }
   DYM_CUDA(cudaEventRecord(e1, b->stream), "cudaEventRecord");
-  b->h_ctr.assign(2 * nc, 0);
-  DYM_CUDA(cudaMemcpyAsync(b->h_ctr.data(), b->d_ctr, 2 * nc * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+  b->h_ctr.assign(4 * nc, 0);
+  DYM_CUDA(cudaMemcpyAsync(b->h_ctr.data(), b->d_ctr, 4 * nc * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                            b->stream),
            "read counters");
   DYM_CUDA(cudaStreamSynchronize(b->stream), "batch sweep");
@@ -838,8 +890,13 @@ int dym_batch_sweep(dym_batch* b, int32_t nsweeps, int32_t nhit, dym_stats* tota
   if (total) {
     std::memset(total, 0, sizeof *total);
     for (size_t i = 0; i < nc; ++i) {
-      total->hits += b->h_ctr[2 * i];
-      total->accepts += b->h_ctr[2 * i + 1];
+      total->hits += b->h_ctr[4 * i];
+      total->accepts += b->h_ctr[4 * i + 1];
+      total->rechecks += b->h_ctr[4 * i + 2];
+      float me;
+      const uint32_t bits = (uint32_t)(b->h_ctr[4 * i + 3] & 0xFFFFFFFFull);
+      std::memcpy(&me, &bits, 4);
+      total->max_ds_err = std::max(total->max_ds_err, (double)me);
     }
     total->sweep = (uint32_t)nsweeps;
     total->launches = (uint32_t)(nsweeps * (b->slot_cnt.size() + 1));
@@ -850,9 +907,9 @@ int dym_batch_sweep(dym_batch* b, int32_t nsweeps, int32_t nhit, dym_stats* tota
 
 int dym_batch_chain_counters(const dym_batch* b, int32_t idx, uint64_t* hits, uint64_t* accepts) {
   if (!b || idx < 0 || (size_t)idx >= b->chains.size()) return fail(DYM_EINVAL, "dym_batch_chain_counters: bad index");
-  if (b->h_ctr.size() != 2 * b->chains.size()) return fail(DYM_EINVAL, "no batch sweep yet");
-  if (hits) *hits = b->h_ctr[2 * idx];
-  if (accepts) *accepts = b->h_ctr[2 * idx + 1];
+  if (b->h_ctr.size() != 4 * b->chains.size()) return fail(DYM_EINVAL, "no batch sweep yet");
+  if (hits) *hits = b->h_ctr[4 * idx];
+  if (accepts) *accepts = b->h_ctr[4 * idx + 1];
   return DYM_OK;
 }
 
@@ -875,10 +932,13 @@ int dym_batch_autotune(dym_batch* b, int32_t nhit, int32_t nsweeps_per_trial, dy
   dym_batch_tuning win = start;
   float win_ms = 1e30f;
   int rc = DYM_OK;
-  for (int threads : {128, 256})
+  const bool all_mixed =
+      std::all_of(b->chains.begin(), b->chains.end(), [](const dym_chain* c) { return c->dev.mixed_ok; });
+  for (int threads : {128, 256, 512})
     for (int tile : {128, 256, 512, 1024})
       for (int gps : {1, 2}) {
         if (rc) break;
+        if (threads == 512 && !all_mixed) continue;
         dym_batch_tuning t{tile, threads, gps, 1};
         rc = dym_batch_set_tuning(b, &t);
         dym_stats st;

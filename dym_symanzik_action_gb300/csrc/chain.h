@@ -35,6 +35,7 @@ struct SweepArgs {
   const uint8_t* cls8;
   const int32_t* cfix;
   float b1f, b2f, dscale, dmargin;
+  const uint32_t* xyz;  // coordinates of sites[k], 8 bits per axis (already offset)
 };
 
 struct ChainDev {
@@ -53,6 +54,7 @@ struct ChainDev {
   int32_t* cfix = nullptr;
   int fix_shift = 0;
   bool mixed_ok = false;
+  uint32_t* xyz = nullptr;     // packed coordinates of sites[k] (mixed kernel)
 };
 
 // Launch one colour phase of the FP64 direct sweep.
@@ -65,6 +67,8 @@ cudaError_t launch_sweep_mixed(int D, int dir, const SweepArgs& a, const uint16_
 size_t mixed_smem_bytes(uint32_t P, uint32_t npool);
 constexpr int kMixedMaxCls = 32;    // classes addressable by the 5 high bits of a psub entry
 constexpr uint32_t kMixedMaxP = 2048;  // element ids in the 11 low bits
+constexpr int kMixedMaxExtent = 256;   // coordinates packed 8 bits per axis
+constexpr int kMixedMaxThreads = 512;
 cudaError_t launch_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uint64_t seed, cudaStream_t s);
 cudaError_t launch_fill(uint16_t* links, size_t n, uint16_t v, cudaStream_t s);
 cudaError_t launch_staples(int D, int dir, const SweepArgs& a, const uint32_t* sites, uint32_t n, uint16_t* out,

@@ -15,22 +15,48 @@ struct SiteGeo {
   int off[D][5];
 };
 
+// Periodic wrap of c = x + s, 0 <= x < N, |s| <= 2 (two corrections each way
+// cover N = 1).
+__device__ __forceinline__ int wrap_near(int c, int N) {
+  if (c < 0) c += N;
+  if (c < 0) c += N;
+  if (c >= N) c -= N;
+  if (c >= N) c -= N;
+  return c;
+}
+
+// Offsets from the site's coordinates x[0..D-1] (x[0] temporal).
 template <int D>
-__device__ __forceinline__ void site_geo(uint32_t i, int Nt, int Nx, SiteGeo<D>& g) {
+__device__ __forceinline__ void site_geo_xyz(const int* x, int Nt, int Nx, SiteGeo<D>& g) {
   int stride = 1;
 #pragma unroll
   for (int b = 0; b < D; ++b) {
     const int N = (b == 0) ? Nt : Nx;
-    const int xb = (int)(i % (uint32_t)N);
-    i /= (uint32_t)N;
 #pragma unroll
-    for (int k = 0; k < 5; ++k) {
-      int c = xb + k - 2;
-      c = ((c % N) + N) % N;
-      g.off[b][k] = (c - xb) * stride;
-    }
+    for (int k = 0; k < 5; ++k) g.off[b][k] = (wrap_near(x[b] + k - 2, N) - x[b]) * stride;
     stride *= N;
   }
+}
+
+template <int D>
+__device__ __forceinline__ void site_geo(uint32_t i, int Nt, int Nx, SiteGeo<D>& g) {
+  int x[D];
+#pragma unroll
+  for (int b = 0; b < D; ++b) {
+    const uint32_t N = (uint32_t)((b == 0) ? Nt : Nx);
+    x[b] = (int)(i % N);
+    i /= N;
+  }
+  site_geo_xyz<D>(x, Nt, Nx, g);
+}
+
+// Coordinates packed 8 bits per axis (x[0] in the low byte), extents <= 256.
+template <int D>
+__device__ __forceinline__ void site_geo_packed(uint32_t xyz, int Nt, int Nx, SiteGeo<D>& g) {
+  int x[D];
+#pragma unroll
+  for (int b = 0; b < D; ++b) x[b] = (int)((xyz >> (8 * b)) & 0xFFu);
+  site_geo_xyz<D>(x, Nt, Nx, g);
 }
 
 // Table access policies.  `Tab` provides mul(g, h), inv(g) for uint32 ids.

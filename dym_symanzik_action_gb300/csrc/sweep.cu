@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(256) k_sweep_sub(SweepArgs a, const uint16_t* 
 // Shared memory: ReTr (FP64) | class values (int32 fixed point) | inverses |
 // packed sub-table | element classes.
 template <int D, int DIR>
-__global__ void __launch_bounds__(256) k_sweep_mixed(SweepArgs a, const uint16_t* __restrict__ psub) {
+__global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_mixed(SweepArgs a, const uint16_t* __restrict__ psub) {
   extern __shared__ __align__(16) unsigned char smem[];
   double* s_retr = reinterpret_cast<double*>(smem);
   int32_t* s_cfix = reinterpret_cast<int32_t*>(s_retr + a.P);
@@ -135,8 +135,8 @@ __global__ void __launch_bounds__(256) k_sweep_mixed(SweepArgs a, const uint16_t
   unsigned hits = 0, accs = 0, rechecks = 0;
   float max_err = 0.0f;
   for (uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x; tid < a.n; tid += gridDim.x * blockDim.x)
-    visit_mixed<D, DIR>(a, a.sites[tid], a.sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks,
-                        max_err);
+    visit_mixed<D, DIR>(a, a.sites[tid], a.xyz[tid], a.sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs,
+                        rechecks, max_err);
   flush_counters(a.counters, hits, accs, rechecks);
   flush_max_err(a.counters + 3, max_err);
 }
@@ -240,15 +240,17 @@ cudaError_t mixed_dispatch(int dir, const SweepArgs& a, const uint16_t* psub, cu
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  const unsigned need = (a.n + 255) / 256;
-  if (need == 0) return cudaSuccess;
-  int dev = 0, sms = 0, per_sm = 0;
+  if (a.n == 0) return cudaSuccess;
+  // One block per SM (the shared tables allow no more), as many warps per
+  // block as the phase fills evenly across the SMs, 128..512 threads.
+  int dev = 0, sms = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem);
   if (e != cudaSuccess) return e;
-  const unsigned grid = std::min<unsigned>(need, (unsigned)std::max(1, sms * std::max(per_sm, 1)));
-  fn<<<grid, 256, smem, s>>>(a, psub);
+  const uint32_t per = (a.n + (uint32_t)sms - 1) / (uint32_t)sms;
+  const unsigned threads = std::min<unsigned>(kMixedMaxThreads, std::max<unsigned>(128, (per + 31) / 32 * 32));
+  const unsigned grid = (a.n + threads - 1) / threads;
+  fn<<<grid, threads, smem, s>>>(a, psub);
   return cudaGetLastError();
 }
 

@@ -106,13 +106,13 @@ __device__ __forceinline__ void visit_sub(const SweepArgs& a, uint32_t i, uint32
 // of the FP64 path bit for bit.  The exact action of the current link is
 // rebuilt lazily when a re-evaluation needs it after fast accepts.
 template <int D, int DIR>
-__device__ __forceinline__ void visit_mixed(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
-                                            const uint16_t* s_inv, const uint16_t* s_psub, const uint8_t* s_cls,
-                                            const int32_t* s_cfix, unsigned& hits, unsigned& accs,
-                                            unsigned& rechecks, float& max_err) {
+__device__ __forceinline__ void visit_mixed(const SweepArgs& a, uint32_t i, uint32_t xyz, uint32_t sweep,
+                                            const double* s_retr, const uint16_t* s_inv, const uint16_t* s_psub,
+                                            const uint8_t* s_cls, const int32_t* s_cfix, unsigned& hits,
+                                            unsigned& accs, unsigned& rechecks, float& max_err) {
   constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
   SiteGeo<D> geo;
-  site_geo<D>(i, a.Nt, a.Nx, geo);
+  site_geo_packed<D>(xyz, a.Nt, a.Nx, geo);  // i's coordinates, packed
   GlobalTab T{a.mult, s_inv, a.P};
   const uint16_t* L = a.links;
   const uint32_t V = a.V;

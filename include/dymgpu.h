@@ -208,7 +208,7 @@ typedef struct dym_batch dym_batch;
 
 typedef struct {
   int32_t tile;         /* links per work tile (multiple of 32) */
-  int32_t threads;      /* threads per block (128 or 256) */
+  int32_t threads;      /* threads per block (128, 256; 512 when every chain is DYM_PREC_MIXED) */
   int32_t grid_per_sm;  /* blocks launched per SM per slot (>= 1) */
   int32_t use_graph;    /* 1: replay each sweep as a captured CUDA graph */
 } dym_batch_tuning;
