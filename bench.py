@@ -47,17 +47,35 @@ def gathers_per_link_hit(nhit: int) -> float:
     return 25.0 + 108.0 / nhit
 
 
-# L2 work of the mixed shared-table kernel in 4D: per link visit 84 staple
-# products + 24 u_j = s_j * b products, each a random 2-byte gather (one
+# L2 work per link visit in 4D.  Shared-table kernels (mixed, shared): 84
+# staple products + 24 u_j = s_j * b products, each a random 2-byte gather (one
 # 32-byte sector) from the L2-resident Cayley table; the hits run from shared
-# memory.  Per launch every block also stages its shared tables from L2.
-KERNEL_GATHERS_PER_VISIT = 108
+# memory.  Direct kernel (fp64): the same 108 plus 25 per hit.  Per launch
+# every block also stages its shared tables from L2.
+# dram__bytes_read.sum + dram__bytes_write.sum of one sweep launch of this
+# workload, from the ncu --set full captures summarised in
+# profiles/sweep_mixed_s1080_32x32x32x8_ncu.md and
+# profiles/sweep_sub_s1080_32x32x32x8_ncu.md (cold cache after ncu's flush).
+DRAM_BYTES_PER_LAUNCH = {"mixed": 2830336, "shared": 2563584}
+
+PRECISION_DTYPE = {"mixed": "u16/i32+f32 (f64 rechecks)", "shared": "u16/f64", "fp64": "u16/f64"}
+PRECISION_TEXT = {
+    "mixed": "mixed: exact int32 fixed-point dS, FP32 threshold test, FP64 re-evaluation within the error bound "
+             "(decisions identical to FP64)",
+    "shared": "fp64 decisions, hit loop from the shared sub-table",
+    "fp64": "fp64 decisions, direct table gathers (reference arithmetic)"}
 
 
-def mixed_smem_bytes(P: int, npool: int) -> int:
-    """Shared tables of k_sweep_mixed: ReTr, class values, inverses, packed
-    sub-table, element classes (sweep.cu mixed_smem_bytes)."""
-    return P * 8 + 32 * 4 + P * 2 + npool * P * 2 + P + 16
+def kernel_model(precision: str, P: int, npool: int, nhit: int, links_per_launch: int, sms: int):
+    """(kernel name, table gathers per link visit, blocks, staged bytes per block)."""
+    if precision == "mixed":  # sweep.cu mixed_smem_bytes; 128..512 threads, one block per SM
+        per = -(-links_per_launch // sms)
+        threads = min(512, max(128, -(-per // 32) * 32))
+        return ("k_sweep_mixed", 108, -(-links_per_launch // threads),
+                P * 8 + 32 * 4 + P * 2 + npool * P * 2 + P + 16)
+    if precision == "shared":  # sweep.cu sub_smem_bytes; one wave of 256-thread blocks
+        return ("k_sweep_sub", 108, min(sms, -(-links_per_launch // 256)), P * 8 + P * 2 + npool * P * 2 + 16)
+    return ("k_sweep_direct", 108 + 25 * nhit, -(-links_per_launch // 256), P * 8 + P * 2 + npool * 2 + 16)
 
 
 class Clocks:
@@ -74,7 +92,7 @@ class Clocks:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -265,6 +283,38 @@ def serving_bench(dym, device: int, n_requests: int, nhit: int = 20, step_sweeps
             "unreached": sum(1 for v in status.values() if v != "done"), "max_resident_chains": max_chains}
 
 
+def mixed_precision_scan(dym, device: int, sweeps: int = 300, nhit: int = 10) -> dict:
+    """S(1080) 48^3 x 12 (5,308,416 links), hot start, beta1 in {2.0, 2.5, 3.0},
+    beta2 = -0.1: the mixed kernel against the all-FP64 shared-table kernel from
+    the same start, configuration compared every 50 sweeps; recheck fraction
+    and largest |dS_fast - dS_fp64| seen at a recheck."""
+    import numpy as np
+    from dym_symanzik_action_gb300 import tables
+    g = dym.load_group(tables.ensure_table("S1080"))
+    out = []
+    for b1 in (2.0, 2.5, 3.0):
+        lm = dym.Lattice(g, 4, 12, 48, 0.0, b1, -0.1, 4848, start="hot", precision="mixed", device=device)
+        lf = dym.Lattice(g, 4, 12, 48, 0.0, b1, -0.1, 4848, start="hot", precision="shared", device=device)
+        same, hits, acc, rechecks, max_err, ms_m, ms_f = True, 0, 0, 0, 0.0, 0.0, 0.0
+        for _ in range(sweeps // 50):
+            sm = lm.update(50, nhit)
+            sf = lf.update(50, nhit)
+            hits += sm.hits
+            acc += sm.accepts
+            rechecks += sm.rechecks
+            max_err = max(max_err, sm.max_ds_err)
+            ms_m += sm.device_ms
+            ms_f += sf.device_ms
+            same = same and sm.accepts == sf.accepts and bool(np.array_equal(lm.links, lf.links))
+        out.append({"beta1": b1, "beta2": -0.1, "sweeps": sweeps, "identical_to_fp64": same,
+                    "acceptance": acc / hits, "recheck_fraction": rechecks / hits, "max_ds_err": max_err,
+                    "mixed_link_hits_per_s": hits / (ms_m * 1e-3), "fp64_link_hits_per_s": hits / (ms_f * 1e-3)})
+        lm.close()
+        lf.close()
+    return {"workload": "S(1080) 48^3x12 hot, beta2=-0.1, 10 hits/link; mixed vs all-FP64 shared-table kernel",
+            "scan": out}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -283,7 +333,7 @@ def run_ours(args):
     w = WORKLOAD
     g = dym.load_group(tables.ensure_table(w["group"]))
     lat = dym.Lattice(g, w["D"], w["Nt"], w["Nx"], *w["beta"], w["seed"] + rank, start=w["start"],
-                      precision="mixed", device=local)
+                      precision=args.precision, device=local)
     links_per_sweep = lat.V * w["D"]
     hits_per_step = links_per_sweep * w["nhit"]
     nphase = len(lat.schedule()[0])
@@ -354,9 +404,10 @@ def run_ours(args):
     avg_launch_s = dev_ms * 1e-3 / max(launches, 1)
     sms = torch.cuda.get_device_properties(local).multi_processor_count
     links_per_launch = links_per_sweep / nphase
-    blocks = min(sms, -(-int(links_per_launch) // 256))  # one wave, one 167 KB block per SM
-    stage_bytes = blocks * mixed_smem_bytes(g.P, len(g.smallgroup))
-    alg_bytes_per_launch = links_per_launch * KERNEL_GATHERS_PER_VISIT * 32 + stage_bytes
+    kname, gathers, blocks, block_bytes = kernel_model(args.precision, g.P, len(g.smallgroup), w["nhit"],
+                                                       int(links_per_launch), sms)
+    stage_bytes = blocks * block_bytes
+    alg_bytes_per_launch = links_per_launch * gathers * 32 + stage_bytes
     achieved = alg_bytes_per_launch / avg_launch_s / 1e9
     ref_equiv = hits_per_step / nphase * G_ref * 32 / avg_launch_s / 1e9
     hbm_bytes = links_per_sweep * 2 * 2  # every link read and written once per sweep
@@ -366,27 +417,23 @@ def run_ours(args):
     except Exception:
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    traffic = None
-    try:
-        traffic = json.load(open(os.path.join(ROOT, "profiles", "sweep_traffic.json"))).get("dram_bytes_per_launch")
-    except Exception:
-        pass
+    traffic = DRAM_BYTES_PER_LAUNCH.get(args.precision)
 
     if rank == 0:
         line = {
             "metric": "link-hits/s", "value": value, "unit": "link-hits/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16/i32+f32 (f64 rechecks)",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": PRECISION_DTYPE[args.precision],
             "data": "synthetic",
             "config": {"workload": WORKLOAD_NAME, "links": links_per_sweep, "nhit": w["nhit"],
-                       "colour_phases": nphase, "precision": "mixed: exact int32 fixed-point dS, FP32 threshold test, FP64 re-evaluation within the error bound (decisions identical to FP64)",
+                       "colour_phases": nphase, "precision": PRECISION_TEXT[args.precision],
                        "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "l2", "achieved": achieved, "peak": l2_peak_gbs, "unit": "GB/s",
                          "frac": achieved / l2_peak_gbs, "traffic": traffic,
                          "peak_source": "measured live: random 2-byte L2 gathers (dym_probe_l2_gather), 32 B/sector",
-                         "algorithmic": (f"k_sweep_mixed: {KERNEL_GATHERS_PER_VISIT} table gathers x 32 B per link visit "
-                                         f"({KERNEL_GATHERS_PER_VISIT / w['nhit']:.1f} per link-hit) + {blocks} blocks x "
-                                         f"{mixed_smem_bytes(g.P, len(g.smallgroup))} B table staging per launch"),
+                         "algorithmic": (f"{kname}: {gathers} table gathers x 32 B per link visit "
+                                         f"({gathers / w['nhit']:.1f} per link-hit) + {blocks} blocks x "
+                                         f"{block_bytes} B table staging per launch"),
                          "reference_algorithm_equivalent": {
                              "gathers_per_link_hit": G_ref, "achieved": ref_equiv, "unit": "GB/s",
                              "note": "the reference algorithm's gathers at this rate (hits from shared memory here)"},
@@ -403,6 +450,8 @@ def run_ours(args):
             line["batched"] = ensemble_bench(dym, local)
         if args.serve_requests > 0:
             line["serving"] = serving_bench(dym, local, args.serve_requests)
+        if not args.no_mixed_scan:
+            line["mixed_precision"] = mixed_precision_scan(dym, local)
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline()
         print(json.dumps(line), flush=True)
@@ -417,7 +466,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", choices=["mixed", "shared", "fp64"], default="mixed",
+                    help="single-chain kernel: mixed (default), shared (FP64 shared-table), fp64 (direct)")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched 256-chain ensemble")
+    ap.add_argument("--no-mixed-scan", action="store_true", help="skip the 48^3x12 mixed-vs-FP64 scan")
     ap.add_argument("--serve-requests", type=int, default=60,
                     help="requests of the served LLR stream to run (2000 = the whole stream; 0 = skip)")
     args = ap.parse_args()
