@@ -80,8 +80,9 @@ cudaError_t launch_staples(int D, int dir, const SweepArgs& a, const uint32_t* s
 // and rectangles (h[1]), one FP64 dot product with the class values.
 constexpr int kLlrMaxCls = 32;
 constexpr int kLlrDeltaBytes = 2 * kLlrMaxCls * 4;  // per-tile class deltas at the front of shared memory
+constexpr int kLlrMaxPhases = 256;                   // colour phases per sweep with their own drive-in fraction
 struct LlrState {
-  double a, bg, elo, ehi, emid, ewin, w2, q;
+  double a, bg, elo, ehi, emid, ewin, w2;
   double E[2];
   double sumE;
   double v[kLlrMaxCls];
@@ -91,6 +92,10 @@ struct LlrState {
   int axis, mode, k, m, K, NRM, drive_sweeps, drive_cap, ncls, sweeps;
   uint32_t phase, sweep;  // colour phases committed (delta parity), Philox sweep counter
   unsigned long long phase_acc, phase_rej, hits, accepts;
+  // Drive-in: fraction of each colour phase's links that take part, adapted
+  // per phase (the links able to move towards the window differ by class).
+  int nphase;
+  double qp[kLlrMaxPhases];
 };
 
 // Observables.

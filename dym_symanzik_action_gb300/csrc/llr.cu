@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(256) k_llr_propose(const LlrTile* __restrict__
     const int axis = st->axis;
     const double aa = st->a, bg = st->bg, emid = st->emid, E0 = st->E[axis - 1];
     const bool drive = (mode == DYM_LLR_DRIVE);
-    const uint32_t qthr = drive ? q_threshold(st->q) : 0u;
+    const uint32_t qthr = drive ? q_threshold(st->qp[st->phase % (uint32_t)st->nphase]) : 0u;
     const uint32_t sweep = st->sweep;
     unsigned hits = 0, accs = 0;
     for (uint32_t k = threadIdx.x; k < tl.count; k += blockDim.x) {
@@ -176,12 +176,14 @@ __global__ void k_llr_commit(const LlrCommit* __restrict__ commits, uint32_t n,
     st->d[buf][0][c] = 0;
     st->d[buf][1][c] = 0;
   }
+  const uint32_t pidx = st->phase % (uint32_t)st->nphase;
   st->phase++;
   if (mode == DYM_LLR_DRIVE) {
-    // Aim the next phase's expected move at the remaining distance.
+    // Aim this phase's next expected move at the remaining distance.
     const double dist = fabs(DYM_SUB(st->emid, st->E[w]));
-    const double q = fabs(dE) > 0 ? DYM_MUL(st->q, dist / fabs(dE)) : DYM_MUL(st->q, 2.0);
-    st->q = fmin(1.0, fmax(q, 0x1.0p-32));
+    const double qo = st->qp[pidx];
+    const double q = fabs(dE) > 0 ? DYM_MUL(qo, dist / fabs(dE)) : DYM_MUL(qo, 2.0);
+    st->qp[pidx] = fmin(1.0, fmax(q, 0x1.0p-32));
     if (st->E[w] >= st->elo && st->E[w] <= st->ehi) mode = DYM_LLR_SETTLE;
   }
   if (cm.last) {

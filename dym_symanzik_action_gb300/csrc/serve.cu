@@ -60,6 +60,8 @@ int check_llr_req(const dym_chain* c, const dym_llr_req* req) {
     return fail(DYM_ENOTSUP, "an S2 window needs every extent >= 3 (1x2 rectangles wrap otherwise)");
   if (c->p.pool != DYM_POOL_NEAREST) return fail(DYM_ENOTSUP, "LLR proposals use the nearest-element pool");
   if (c->p.D != 4) return fail(DYM_ENOTSUP, "LLR runs on four-dimensional lattices");
+  if (c->sched.phase_dir.size() > (size_t)kLlrMaxPhases)
+    return fail(DYM_ENOTSUP, "LLR: the lattice's colour schedule has more than 256 phases");
   return check_llr_group(*c->grp->g);
 }
 
@@ -84,7 +86,8 @@ int llr_init_state(dym_chain* c, const dym_llr_req* req, LlrState* st) {
   st->ehi = req->ewin + req->hw;
   st->emid = 0.5 * (st->elo + st->ehi);
   st->w2 = W * W;
-  st->q = 1.0;
+  st->nphase = (int)c->sched.phase_dir.size();
+  for (int p = 0; p < st->nphase; ++p) st->qp[p] = 1.0;
   st->ncls = g.ncls;
   for (int q = 0; q < g.ncls; ++q) st->v[q] = g.cls_val[q];
   st->E[0] = class_sum_host(st->h[0], g.cls_val, g.ncls);

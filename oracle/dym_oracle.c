@@ -521,7 +521,9 @@ int or_llr_run(or_lattice* L, const int* phase_dir, const uint32_t* phase_len, c
   const double W = 2 * hw, elo = ewin - hw, ehi = ewin + hw;
   const double emid = 0.5 * (elo + ehi), w2 = W * W;
   const int w = axis - 1;
-  double a = a0, q = 1.0, sumE = 0;
+  double a = a0, sumE = 0;
+  double* qv = (double*)malloc(sizeof(double) * (size_t)(nphase > 0 ? nphase : 1));
+  for (int p = 0; p < nphase; ++p) qv[p] = 1.0;  /* drive-in fraction per colour phase */
   int mode = (E[w] >= elo && E[w] <= ehi) ? OR_RM : OR_DRIVE;
   if (NRM == 0 && mode == OR_RM) mode = OR_DONE;
   if (mode == OR_DRIVE && drive_cap == 0) mode = OR_UNREACHED;
@@ -540,7 +542,7 @@ int or_llr_run(or_lattice* L, const int* phase_dir, const uint32_t* phase_len, c
       memset(d, 0, sizeof d);
       int nchg = 0;
       const int drive = (mode == OR_DRIVE);
-      const double t = q * 4294967296.0;
+      const double t = qv[p] * 4294967296.0;
       const uint32_t qthr = drive ? (t >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)t) : 0u;
       for (uint32_t kk = 0; kk < phase_len[p]; ++kk) {
         const unsigned i = sites[off + kk];
@@ -599,8 +601,8 @@ int or_llr_run(or_lattice* L, const int* phase_dir, const uint32_t* phase_len, c
       }
       if (mode == OR_DRIVE) {
         const double dist = fabs(emid - E[w]);
-        const double qq = fabs(dE) > 0 ? q * (dist / fabs(dE)) : q * 2.0;
-        q = fmin(1.0, fmax(qq, 0x1.0p-32));
+        const double qq = fabs(dE) > 0 ? qv[p] * (dist / fabs(dE)) : qv[p] * 2.0;
+        qv[p] = fmin(1.0, fmax(qq, 0x1.0p-32));
         if (E[w] >= elo && E[w] <= ehi) mode = OR_SETTLE;
       }
       if (p == nphase - 1) {
@@ -625,7 +627,7 @@ int or_llr_run(or_lattice* L, const int* phase_dir, const uint32_t* phase_len, c
   }
   out[0] = a; out[1] = E[0]; out[2] = E[1]; out[3] = mode;
   iout[0] = drive_sweeps; iout[1] = sweeps; iout[2] = hits; iout[3] = accs; iout[4] = pacc; iout[5] = prej;
-  free(cls); free(chg_site); free(chg_old);
+  free(cls); free(chg_site); free(chg_old); free(qv);
   return 0;
 }
 
