@@ -105,34 +105,6 @@ static bool mixed_eligible(const Group& g, uint32_t npool, int device) {
   return mixed_smem_bytes(g.P, npool) <= (size_t)optin;
 }
 
-// Fixed-point scale 2^S of the class values: the largest S <= 24 for which a
-// difference of two sums of NR rectangle terms, each |c| 2^S + 1/2 at most,
-// stays inside int32.
-static int fix_shift(const Group& g, int D) {
-  const double NR = 6.0 * (D - 1);
-  const double amax = std::max(g.max_abs_retr, 1e-3);
-  const double lim = (2147483647.0 - 2.0 * NR) / (2.0 * NR * amax);
-  int S = 24;
-  while (S > 0 && std::ldexp(1.0, S) > lim) --S;
-  return S;
-}
-
-// Bound on |dS_fast - dS_fp64| for the mixed kernel at the chain's couplings:
-// class values rounded to 2^-(S+1) (plus the class spread) in each of the
-// 2(NS + NR) terms of a difference, four FP32 roundings (betas, conversions,
-// product, sum) of the scaled difference, and the reference's own FP64
-// rounding of both actions; doubled, plus 1e-7.
-static float mixed_margin(const Group& g, int D, int S, double b0, double b1, double b2) {
-  const double NS = 2.0 * (D - 1), NR = 6.0 * (D - 1);
-  const double q = std::ldexp(1.0, -(S + 1)) + g.cls_spread;
-  const double w = std::fabs(b1) * 2.0 * NS + std::fabs(b2) * 2.0 * NR;
-  const double quant = w * q;
-  const double feval = std::ldexp(1.0, -22) * w * (g.max_abs_retr + q);
-  const double rref = std::ldexp(1.0, -45) * (std::fabs(b0) + (std::fabs(b1) * NS + std::fabs(b2) * NR) * g.max_abs_retr + 1.0);
-  const double m = 2.0 * (quant + feval + rref) + 1e-7;
-  return std::nextafter((float)m, INFINITY);
-}
-
 static int build_mixed_tables(dym_chain* c, const std::vector<uint16_t>& pool) {
   const Group& g = *c->grp->g;
   const uint32_t P = g.P, np = (uint32_t)pool.size();

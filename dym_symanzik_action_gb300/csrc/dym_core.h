@@ -157,6 +157,23 @@ DYM_HD int dym_accept(double oldact, double newact, double u2) {
 // d = newact - oldact > 38, exp(-d) < 3.2e-17 (and dym_exp is within a few ulp
 // of it) while every nonzero u2 is >= 2^-53 = 1.1e-16, so the test can only
 // pass for u2 == 0, which is then decided by dym_exp itself.
+/* Mixed-precision decisions.  Bound on |x_fast - x_fp64| for
+ *   x = c0 + c1 dE1 + c2 dE2  (dE1 a difference of two sums of n1 class values,
+ *                              dE2 of two sums of n2)
+ * when x_fast comes from exact integer sums of class values rounded to the
+ * fixed point (error q per term: half a unit plus the class spread, |value| <=
+ * amax) scaled in FP32 (four roundings of 2^-24 relative), and x_fp64 is the
+ * FP64 evaluation of the same expression in the reference's order; doubled,
+ * plus 1e-7.  A decision x < t whose |x_fast - t| exceeds this bound plus the
+ * error of t is the FP64 decision. */
+DYM_HD double dym_mixed_margin(double c0, double c1, double n1, double c2, double n2, double q, double amax) {
+  const double w = fabs(c1) * 2.0 * n1 + fabs(c2) * 2.0 * n2;
+  const double quant = w * q;
+  const double feval = 0x1p-22 * w * (amax + q);
+  const double rref = 0x1p-45 * (fabs(c0) + (fabs(c1) * n1 + fabs(c2) * n2) * amax + 1.0);
+  return 2.0 * (quant + feval + rref) + 1e-7;
+}
+
 DYM_HD int dym_accept_fast(double oldact, double newact, double u2) {
   if (newact <= oldact) return 1.0 > u2;
   const double d = DYM_SUB(newact, oldact);

@@ -3,8 +3,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <string>
 
+#include "dym_core.h"
 #include "engine.h"
 
 namespace dym {
@@ -27,6 +29,29 @@ inline cudaError_t copy_sync(void* dst, const void* src, size_t bytes, cudaMemcp
   cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   return e;
+}
+
+// Fixed-point scale 2^S of the class values for the mixed-precision kernels:
+// the largest S <= 24 for which a difference of two sums of NR = 6(D-1)
+// rectangle terms, each at most |c| 2^S + 1/2, stays inside int32.
+inline int fix_shift(const Group& g, int D) {
+  const double NR = 6.0 * (D - 1);
+  const double amax = std::max(g.max_abs_retr, 1e-3);
+  const double lim = (2147483647.0 - 2.0 * NR) / (2.0 * NR * amax);
+  int S = 24;
+  while (S > 0 && std::ldexp(1.0, S) > lim) --S;
+  return S;
+}
+
+// Rounding error of one fixed-point class value: half a unit plus the spread
+// of ReTr inside a class.
+inline double fix_q(const Group& g, int S) { return std::ldexp(1.0, -(S + 1)) + g.cls_spread; }
+
+// dym_mixed_margin for a Metropolis sweep at couplings (b0, b1, b2), rounded up
+// to FP32.
+inline float mixed_margin(const Group& g, int D, int S, double b0, double b1, double b2) {
+  const double m = dym_mixed_margin(b0, b1, 2.0 * (D - 1), b2, 6.0 * (D - 1), fix_q(g, S), g.max_abs_retr);
+  return std::nextafter((float)m, INFINITY);
 }
 
 }  // namespace dym
