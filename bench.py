@@ -239,7 +239,7 @@ def ensemble_bench(dym, device: int, sweeps: int = 5, nhit: int = 10) -> dict:
 
 
 def serving_bench(dym, device: int, n_requests: int, nhit: int = 20, step_sweeps: int = 5,
-                  max_chains: int = 256) -> dict:
+                  max_chains: int = 256, max_links: int = 0) -> dict:
     """Config 5: LLR windows arriving as a Poisson stream (200/s) on S(1080)
     lattices Nx in {6,8,12,16}, Nt in {2,4}, beta2 in {0,-0.1}; each request one
     window of 0.5% of the plaquette-energy range, 20 Robbins-Monro iterations of
@@ -252,7 +252,7 @@ def serving_bench(dym, device: int, n_requests: int, nhit: int = 20, step_sweeps
     from dym_symanzik_action_gb300.workloads import llr_requests
     reqs = llr_requests(n=2000)[:n_requests]
     g = dym.load_group(tables.ensure_table("S1080"))
-    srv = Server(g, max_chains=max_chains, hbm_budget=8 << 30, nhit=nhit, device=device)
+    srv = Server(g, max_chains=max_chains, hbm_budget=8 << 30, nhit=nhit, device=device, max_links=max_links)
     lat = {}
     status = {}
     i = 0
@@ -280,7 +280,8 @@ def serving_bench(dym, device: int, n_requests: int, nhit: int = 20, step_sweeps
                         f"Nt in {{2,4}}, 20 RM x 50 sweeps, {nhit} hits/link",
             "requests": len(reqs), "wall_s": wall, "link_hits_per_s": hits / wall,
             "latency_p50_s": float(np.percentile(L, 50)), "latency_p99_s": float(np.percentile(L, 99)),
-            "unreached": sum(1 for v in status.values() if v != "done"), "max_resident_chains": max_chains}
+            "unreached": sum(1 for v in status.values() if v != "done"), "max_resident_chains": max_chains,
+            "max_resident_links": max_links}
 
 
 def mixed_precision_scan(dym, device: int, sweeps: int = 300, nhit: int = 10) -> dict:

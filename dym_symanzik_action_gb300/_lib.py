@@ -73,7 +73,8 @@ SERVE_MAX_NRM = 64
 
 
 class ServerParams(C.Structure):
-    _fields_ = [("max_chains", C.c_int32), ("hbm_budget", C.c_uint64), ("nhit", C.c_int32), ("device", C.c_int32)]
+    _fields_ = [("max_chains", C.c_int32), ("hbm_budget", C.c_uint64), ("nhit", C.c_int32), ("device", C.c_int32),
+                ("max_links", C.c_uint64)]
 
 
 class LlrRequest(C.Structure):

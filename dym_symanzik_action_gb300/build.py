@@ -24,6 +24,7 @@ BINDIR = os.path.join(PKG, "bin")
 OBJDIR = os.path.join(PKG, "_build")
 LIB = os.path.join(LIBDIR, "libdymgpu.so")
 CLI = os.path.join(BINDIR, "dym-mod-metro")
+LLR_CLI = os.path.join(BINDIR, "dym-llr")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # DYM_BOUNDS_CHECK=1 builds the self-checking kernels (every index checked,
@@ -98,10 +99,11 @@ def build(verbose: bool = False) -> str:
         _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs])
         with open(flavor_file, "w") as f:
             f.write(flavor)
-    cli_src = os.path.join(CSRC, "dym_mod_metro.cpp")
-    if os.path.exists(cli_src) and (_stale(CLI, [cli_src, LIB] + hdrs)):
-        _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", *inc, cli_src, "-o", CLI,
-              "-L", LIBDIR, "-ldymgpu", "-Wl,-rpath,$ORIGIN/../lib"])
+    for name, exe in (("dym_mod_metro.cpp", CLI), ("dym_llr.cpp", LLR_CLI)):
+        cli_src = os.path.join(CSRC, name)
+        if os.path.exists(cli_src) and (_stale(exe, [cli_src, LIB] + hdrs)):
+            _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", "-pthread", *inc, cli_src, "-o", exe,
+                  "-L", LIBDIR, "-ldymgpu", "-Wl,-rpath,$ORIGIN/../lib"])
     return LIB
 
 

@@ -338,7 +338,7 @@ struct dym_server {
   struct Active {
     dym_llr_request req;
     dym_chain* chain;
-    uint64_t bytes;
+    uint64_t bytes, links;
   };
   std::deque<dym_llr_request> queue;
   std::vector<Active> active;
@@ -346,6 +346,7 @@ struct dym_server {
   std::vector<dym_llr_response> done;
   dym::LlrWork work;
   uint64_t hbm_used = 0;
+  uint64_t links_used = 0;
   uint64_t link_hits = 0;
   std::vector<int> h_modes;
 };
@@ -365,7 +366,10 @@ int server_admit(dym_server* s) {
   while (!s->queue.empty() && (int)s->active.size() < s->p.max_chains) {
     const dym_llr_request r = s->queue.front();
     const uint64_t bytes = chain_bytes(r.D, r.Nt, r.Nx, g.P);
+    uint64_t links = (uint64_t)r.D * (uint64_t)r.Nt;
+    for (int d = 1; d < r.D; ++d) links *= (uint64_t)r.Nx;
     if (!s->active.empty() && s->hbm_used + bytes > s->p.hbm_budget) break;
+    if (!s->active.empty() && s->p.max_links && s->links_used + links > s->p.max_links) break;
     s->queue.pop_front();
     dym_chain* c = nullptr;
     auto key = std::make_tuple(r.D, r.Nt, r.Nx);
@@ -405,8 +409,9 @@ int server_admit(dym_server* s) {
       dym_chain_free(c);
       return rc;
     }
-    s->active.push_back(dym_server::Active{r, c, bytes});
+    s->active.push_back(dym_server::Active{r, c, bytes, links});
     s->hbm_used += bytes;
+    s->links_used += links;
     s->work.chains.push_back(c);
     s->work.dirty = true;
   }
@@ -447,6 +452,7 @@ int server_retire(dym_server* s) {
     s->done.push_back(resp);
     s->link_hits += st.hits;
     s->hbm_used -= a.bytes;
+    s->links_used -= a.links;
     s->spare[std::make_tuple(a.req.D, a.req.Nt, a.req.Nx)].push_back(a.chain);
     changed = true;
   }

@@ -33,8 +33,9 @@ class Response:
 
 class Server:
     def __init__(self, group: Group, max_chains: int = 64, hbm_budget: int = 8 << 30, nhit: int = 20,
-                 device: int = 0):
-        p = _lib.ServerParams(max_chains=max_chains, hbm_budget=hbm_budget, nhit=nhit, device=device)
+                 device: int = 0, max_links: int = 0):
+        p = _lib.ServerParams(max_chains=max_chains, hbm_budget=hbm_budget, nhit=nhit, device=device,
+                              max_links=max_links)
         h = C.c_void_p()
         check(lib().dym_server_create(group._h, C.byref(p), C.byref(h)))
         self._h = h

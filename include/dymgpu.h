@@ -295,6 +295,9 @@ typedef struct {
   uint64_t hbm_budget;  /* device bytes of resident chains at most */
   int32_t nhit;         /* hits per link per visit */
   int32_t device;
+  uint64_t max_links;   /* links of resident chains at most (0: no limit).  All resident chains
+                           advance together, so a smaller limit lets the oldest requests finish
+                           sooner; a larger one keeps more work per kernel. */
 } dym_server_params;
 
 typedef struct {
