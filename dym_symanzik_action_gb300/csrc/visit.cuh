@@ -105,11 +105,13 @@ __device__ __forceinline__ void visit_sub(const SweepArgs& a, uint32_t i, uint32
 // reference's order, dym_accept_fast).  The configurations are therefore those
 // of the FP64 path bit for bit.  The exact action of the current link is
 // rebuilt lazily when a re-evaluation needs it after fast accepts.
+// First half of a mixed-precision visit of link (i, DIR): the staples,
+// u_j = s_j * b and the fixed-point sums R, M of the current link (bound by
+// global-memory latency).
 template <int D, int DIR>
-__device__ __forceinline__ void visit_mixed(const SweepArgs& a, uint32_t i, uint32_t xyz, uint32_t sweep,
-                                            const double* s_retr, const uint16_t* s_inv, const uint16_t* s_psub,
-                                            const uint8_t* s_cls, const int32_t* s_cfix, unsigned& hits,
-                                            unsigned& accs, unsigned& rechecks, float& max_err) {
+__device__ __forceinline__ void mixed_prepare(const SweepArgs& a, uint32_t i, uint32_t xyz, const uint16_t* s_inv,
+                                              const uint8_t* s_cls, const int32_t* s_cfix, uint32_t* u,
+                                              uint32_t& b, uint32_t& R, uint32_t& M) {
   constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
   SiteGeo<D> geo;
   site_geo_packed<D>(xyz, a.Nt, a.Nx, geo);  // i's coordinates, packed
@@ -117,19 +119,27 @@ __device__ __forceinline__ void visit_mixed(const SweepArgs& a, uint32_t i, uint
   const uint16_t* L = a.links;
   const uint32_t V = a.V;
   auto ld = [L, V](uint32_t s, int d) -> uint32_t { return __ldg(L + (size_t)d * V + s); };
-  uint32_t u[NT];
   build_staples<D, DIR>(i, geo, T, ld, u, u + NS);
-
-  uint16_t* own = a.links + (size_t)DIR * V + i;
-  uint32_t b = *own;
-  const uint32_t b0 = b;
+  b = a.links[(size_t)DIR * V + i];
 #pragma unroll
   for (int j = 0; j < NT; ++j) u[j] = T.mul(u[j], b);  // u_j = s_j * b
-  uint32_t R = 0, M = 0;  // fixed-point sums, modular (differences are exact)
+  R = 0;
+  M = 0;  // fixed-point sums, modular (differences are exact)
 #pragma unroll
   for (int j = 0; j < NS; ++j) R += (uint32_t)s_cfix[s_cls[u[j]]];
 #pragma unroll
   for (int j = NS; j < NT; ++j) M += (uint32_t)s_cfix[s_cls[u[j]]];
+}
+
+// Second half: the nhit hits of link (i, DIR) from the shared tables, starting
+// from mixed_prepare's state; the link is written when it changed.
+template <int D, int DIR>
+__device__ __forceinline__ void mixed_hits(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
+                                           const uint16_t* s_psub, const int32_t* s_cfix, uint32_t* u, uint32_t b,
+                                           uint32_t R, uint32_t M, unsigned& hits, unsigned& accs,
+                                           unsigned& rechecks, float& max_err) {
+  constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
+  const uint32_t b0 = b;
   double oldact = 0.0;
   bool old_ok = false;
   for (int h = 0; h < a.nhit; ++h) {
@@ -192,7 +202,7 @@ __device__ __forceinline__ void visit_mixed(const SweepArgs& a, uint32_t i, uint
       ++accs;
     }
   }
-  if (b != b0) *own = (uint16_t)b;
+  if (b != b0) a.links[(size_t)DIR * a.V + i] = (uint16_t)b;
 }
 
 __device__ __forceinline__ void flush_counters(unsigned long long* ctr, unsigned hits, unsigned accs,
@@ -205,6 +215,19 @@ __device__ __forceinline__ void flush_counters(unsigned long long* ctr, unsigned
     if (accs) atomicAdd(ctr + 1, (unsigned long long)accs);
     if (rechecks) atomicAdd(ctr + 2, (unsigned long long)rechecks);
   }
+}
+
+
+template <int D, int DIR>
+__device__ __forceinline__ void visit_mixed(const SweepArgs& a, uint32_t i, uint32_t xyz, uint32_t sweep,
+                                            const double* s_retr, const uint16_t* s_inv, const uint16_t* s_psub,
+                                            const uint8_t* s_cls, const int32_t* s_cfix, unsigned& hits,
+                                            unsigned& accs, unsigned& rechecks, float& max_err) {
+  constexpr int NT = 8 * (D - 1);
+  uint32_t u[NT];
+  uint32_t b, R, M;
+  mixed_prepare<D, DIR>(a, i, xyz, s_inv, s_cls, s_cfix, u, b, R, M);
+  mixed_hits<D, DIR>(a, i, sweep, s_retr, s_psub, s_cfix, u, b, R, M, hits, accs, rechecks, max_err);
 }
 
 // Largest |dS_fast - dS_fp64| seen at a re-evaluation, into the low word of
