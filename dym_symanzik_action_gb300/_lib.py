@@ -65,6 +65,18 @@ class LlrResult(C.Structure):
                 ("phase_accepts", C.c_uint64), ("phase_rejects", C.c_uint64)]
 
 
+class Llr2dReq(C.Structure):
+    _fields_ = [("E1", C.c_double), ("hw1", C.c_double), ("E2", C.c_double), ("hw2", C.c_double),
+                ("a1", C.c_double), ("a2", C.c_double), ("K", C.c_int32), ("NRM", C.c_int32), ("nhit", C.c_int32),
+                ("drive_cap", C.c_int32)]
+
+
+class Llr2dResult(C.Structure):
+    _fields_ = [("a1", C.c_double), ("a2", C.c_double), ("S1", C.c_double), ("S2", C.c_double),
+                ("status", C.c_int32), ("drive_sweeps", C.c_int32), ("sweeps", C.c_int32), ("hits", C.c_uint64),
+                ("accepts", C.c_uint64), ("phase_accepts", C.c_uint64), ("phase_rejects", C.c_uint64)]
+
+
 class BatchTuning(C.Structure):
     _fields_ = [("tile", C.c_int32), ("threads", C.c_int32), ("grid_per_sm", C.c_int32), ("use_graph", C.c_int32)]
 
@@ -136,6 +148,7 @@ PROTOTYPES = {
     "dym_server_free": (C.c_int, [_P]),
     "dym_llr_energy": (C.c_int, [_P, _f64p, _f64p]),
     "dym_llr_run": (C.c_int, [_P, C.POINTER(LlrReq), C.POINTER(LlrResult), _f64p]),
+    "dym_llr2d_run": (C.c_int, [_P, C.POINTER(Llr2dReq), C.POINTER(Llr2dResult), _f64p]),
     "dym_probe_l2_gather": (C.c_int, [C.c_int32, C.c_uint32, _f64p]),
 }
 

@@ -96,6 +96,21 @@ struct LlrState {
   // per phase (the links able to move towards the window differ by class).
   int nphase;
   double qp[kLlrMaxPhases];
+  // Two-dimensional cells (dims == 2, llr2d.cpp:178-259): S1 in [elo, ehi] and
+  // S2 in [elo2, ehi2] (axis is 1); a is a1 and bg is a2, both updated by
+  // Robbins-Monro; ihw are the reciprocal half-widths of the normalised
+  // distance to the cell centre used by the drive-in.
+  int dims;
+  double elo2, ehi2, emid2, ewin2, w2b, sumE2;
+  double ihw[2];
+  double a2_hist[DYM_LLR_MAX_NRM];
+};
+
+// Drive-in parameters of a two-dimensional cell, as the propose kernel passes
+// them to visit_llr.
+struct LlrDrive2 {
+  int dims;
+  double E0b, emid2, ihw0, ihw1;
 };
 
 // Observables.

@@ -43,8 +43,26 @@ __device__ __forceinline__ double class_sum(const long long* h, const long long*
   return s;
 }
 
+// Squared normalised distance of (e1, e2) to a two-dimensional cell's centre
+// (the reference compares hypot() of the same terms, llr2d.cpp:207-209).
+__device__ __forceinline__ double norm_sq(const LlrState* st, double e1, double e2) {
+  const double x = DYM_MUL(DYM_SUB(e1, st->emid), st->ihw[0]);
+  const double y = DYM_MUL(DYM_SUB(e2, st->emid2), st->ihw[1]);
+  return DYM_ADD(DYM_MUL(x, x), DYM_MUL(y, y));
+}
+
+__device__ __forceinline__ bool in_box(const LlrState* st, double e1, double e2) {
+  return e1 >= st->elo && e1 <= st->ehi && e2 >= st->elo2 && e2 <= st->ehi2;
+}
+
 // Whether the class move of the chain's current phase is kept.
 __device__ __forceinline__ bool phase_ok(const LlrState* st) {
+  if (st->dims == 2) {
+    const double En1 = class_sum(st->h[0], st->d[st->phase & 1][0], st->v, st->ncls);
+    const double En2 = class_sum(st->h[1], st->d[st->phase & 1][1], st->v, st->ncls);
+    if (st->mode == DYM_LLR_DRIVE) return norm_sq(st, En1, En2) < norm_sq(st, st->E[0], st->E[1]);
+    return in_box(st, En1, En2);
+  }
   const int w = st->axis - 1;
   const double En = class_sum(st->h[w], st->d[st->phase & 1][w], st->v, st->ncls);
   if (st->mode == DYM_LLR_DRIVE) return fabs(DYM_SUB(En, st->emid)) < fabs(DYM_SUB(st->E[w], st->emid));
@@ -95,6 +113,7 @@ __global__ void __launch_bounds__(256) k_llr_propose(const LlrTile* __restrict__
     const uint16_t* s_cls = reinterpret_cast<const uint16_t*>(smem + G.off_cls);
     const int axis = st->axis;
     const double aa = st->a, bg = st->bg, emid = st->emid, E0 = st->E[axis - 1];
+    const LlrDrive2 d2{st->dims, st->E[1], st->emid2, st->ihw[0], st->ihw[1]};
     const bool drive = (mode == DYM_LLR_DRIVE);
     const uint32_t qthr = drive ? q_threshold(st->qp[st->phase % (uint32_t)st->nphase]) : 0u;
     const uint32_t sweep = st->sweep;
@@ -103,15 +122,15 @@ __global__ void __launch_bounds__(256) k_llr_propose(const LlrTile* __restrict__
       const uint32_t i = c.sites[tl.begin + k];
       uint32_t b0 = 0;
       switch (tl.dir) {
-        case 0: b0 = visit_llr<D, 0>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, axis, aa, bg, E0, emid, drive, qthr,
+        case 0: b0 = visit_llr<D, 0>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, axis, aa, bg, E0, emid, d2, drive, qthr,
                                      s_delta, hits, accs); break;
-        case 1: b0 = visit_llr<D, 1>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, axis, aa, bg, E0, emid, drive, qthr,
+        case 1: b0 = visit_llr<D, 1>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, axis, aa, bg, E0, emid, d2, drive, qthr,
                                      s_delta, hits, accs); break;
         case 2: if (D > 2) b0 = visit_llr<D, (D > 2 ? 2 : 0)>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, axis, aa,
-                                                               bg, E0, emid, drive, qthr, s_delta, hits, accs);
+                                                               bg, E0, emid, d2, drive, qthr, s_delta, hits, accs);
           break;
         case 3: if (D > 3) b0 = visit_llr<D, (D > 3 ? 3 : 0)>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, axis, aa,
-                                                               bg, E0, emid, drive, qthr, s_delta, hits, accs);
+                                                               bg, E0, emid, d2, drive, qthr, s_delta, hits, accs);
           break;
       }
       c.oldv[tl.pos + k] = (uint16_t)b0;
@@ -161,6 +180,7 @@ __global__ void k_llr_commit(const LlrCommit* __restrict__ commits, uint32_t n,
   const uint32_t buf = st->phase & 1u;
   const bool ok = phase_ok(st);
   const double dE = DYM_SUB(class_sum(st->h[w], st->d[buf][w], st->v, st->ncls), st->E[w]);
+  const double dE2 = DYM_SUB(class_sum(st->h[1], st->d[buf][1], st->v, st->ncls), st->E[1]);
   if (ok) {
     for (int c = 0; c < st->ncls; ++c) {
       st->h[0][c] += st->d[buf][0][c];
@@ -179,12 +199,22 @@ __global__ void k_llr_commit(const LlrCommit* __restrict__ commits, uint32_t n,
   const uint32_t pidx = st->phase % (uint32_t)st->nphase;
   st->phase++;
   if (mode == DYM_LLR_DRIVE) {
-    // Aim this phase's next expected move at the remaining distance.
-    const double dist = fabs(DYM_SUB(st->emid, st->E[w]));
+    // Aim this phase's next expected move at the remaining distance (in a
+    // two-dimensional cell: normalised distance and normalised move).
+    double dist, move;
+    if (st->dims == 2) {
+      dist = sqrt(norm_sq(st, st->E[0], st->E[1]));
+      const double x = DYM_MUL(dE, st->ihw[0]), y = DYM_MUL(dE2, st->ihw[1]);
+      move = sqrt(DYM_ADD(DYM_MUL(x, x), DYM_MUL(y, y)));
+    } else {
+      dist = fabs(DYM_SUB(st->emid, st->E[w]));
+      move = fabs(dE);
+    }
     const double qo = st->qp[pidx];
-    const double q = fabs(dE) > 0 ? DYM_MUL(qo, dist / fabs(dE)) : DYM_MUL(qo, 2.0);
+    const double q = move > 0 ? DYM_MUL(qo, dist / move) : DYM_MUL(qo, 2.0);
     st->qp[pidx] = fmin(1.0, fmax(q, 0x1.0p-32));
-    if (st->E[w] >= st->elo && st->E[w] <= st->ehi) mode = DYM_LLR_SETTLE;
+    const bool in = st->dims == 2 ? in_box(st, st->E[0], st->E[1]) : (st->E[w] >= st->elo && st->E[w] <= st->ehi);
+    if (in) mode = DYM_LLR_SETTLE;
   }
   if (cm.last) {
     st->sweeps++;
@@ -192,20 +222,29 @@ __global__ void k_llr_commit(const LlrCommit* __restrict__ commits, uint32_t n,
     if (mode == DYM_LLR_DRIVE) {
       if (++st->drive_sweeps >= st->drive_cap) mode = DYM_LLR_UNREACHED;
     } else if (mode == DYM_LLR_SETTLE) {
-      mode = DYM_LLR_RM;
+      mode = st->NRM > 0 ? DYM_LLR_RM : DYM_LLR_DONE;  // NRM = 0: drive-in only (seed_cell)
       st->k = 0;
       st->m = 0;
       st->sumE = 0;
+      st->sumE2 = 0;
     } else if (mode == DYM_LLR_RM) {
       st->sumE = DYM_ADD(st->sumE, st->E[w]);
+      if (st->dims == 2) st->sumE2 = DYM_ADD(st->sumE2, st->E[1]);
       if (++st->k == st->K) {
         const double g = DYM_SUB(st->sumE / (double)st->K, st->ewin);
         const double step = 12.0 / DYM_MUL(st->w2, (double)(st->m + 1));
         st->a = DYM_ADD(st->a, DYM_MUL(step, g));
         st->a_hist[st->m] = st->a;
+        if (st->dims == 2) {  // llr2d.cpp:252-253
+          const double g2 = DYM_SUB(st->sumE2 / (double)st->K, st->ewin2);
+          const double step2 = 12.0 / DYM_MUL(st->w2b, (double)(st->m + 1));
+          st->bg = DYM_ADD(st->bg, DYM_MUL(step2, g2));
+          st->a2_hist[st->m] = st->bg;
+        }
         st->m++;
         st->k = 0;
         st->sumE = 0;
+        st->sumE2 = 0;
         if (st->m >= st->NRM) mode = DYM_LLR_DONE;
       }
     }

@@ -65,8 +65,14 @@ int check_llr_req(const dym_chain* c, const dym_llr_req* req) {
   return check_llr_group(*c->grp->g);
 }
 
-// Allocate (once) and fill the chain's LLR state for window `req`.
-int llr_init_state(dym_chain* c, const dym_llr_req* req, LlrState* st) {
+// A two-dimensional cell: S2 window and the initial a2 (a1 is req->a0).
+struct Llr2dCell {
+  double ewin2, hw2, a2;
+};
+
+// Allocate (once) and fill the chain's LLR state for window `req` (and, for a
+// two-dimensional cell, its S2 window `cell`; req->axis is then 1).
+int llr_init_state(dym_chain* c, const dym_llr_req* req, LlrState* st, const Llr2dCell* cell = nullptr) {
   const Group& g = *c->grp->g;
   DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
   if (!c->d_llr) {
@@ -99,6 +105,20 @@ int llr_init_state(dym_chain* c, const dym_llr_req* req, LlrState* st) {
   st->sweep = c->sweep;
   const double Ew = st->E[req->axis - 1];
   st->mode = (Ew >= st->elo && Ew <= st->ehi) ? DYM_LLR_RM : DYM_LLR_DRIVE;
+  st->dims = 1;
+  if (cell) {
+    st->dims = 2;
+    st->bg = cell->a2;
+    st->ewin2 = cell->ewin2;
+    st->elo2 = cell->ewin2 - cell->hw2;
+    st->ehi2 = cell->ewin2 + cell->hw2;
+    st->emid2 = 0.5 * (st->elo2 + st->ehi2);
+    st->w2b = (2 * cell->hw2) * (2 * cell->hw2);
+    st->ihw[0] = 1.0 / req->hw;
+    st->ihw[1] = 1.0 / cell->hw2;
+    const bool in = st->E[0] >= st->elo && st->E[0] <= st->ehi && st->E[1] >= st->elo2 && st->E[1] <= st->ehi2;
+    st->mode = in ? DYM_LLR_RM : DYM_LLR_DRIVE;
+  }
   if (req->NRM == 0 && st->mode == DYM_LLR_RM) st->mode = DYM_LLR_DONE;
   if (st->mode == DYM_LLR_DRIVE && req->drive_cap == 0) st->mode = DYM_LLR_UNREACHED;
   DYM_CUDA(copy_sync(c->d_llr, st, sizeof(LlrState), cudaMemcpyHostToDevice, c->stream), "upload llr state");
@@ -283,27 +303,27 @@ int dym_llr_energy(dym_chain* c, double* S1, double* S2) {
   return DYM_OK;
 }
 
-int dym_llr_run(dym_chain* c, const dym_llr_req* req, dym_llr_result* out, double* a_hist) {
-  if (!c || !req || !out) return fail(DYM_EINVAL, "dym_llr_run: null argument");
-  int rc = check_llr_req(c, req);
-  if (rc) return rc;
-  std::unique_ptr<LlrState> st(new LlrState());
-  rc = llr_init_state(c, req, st.get());
-  if (rc) return rc;
+}  // extern "C"
+
+namespace dym {
+namespace {
+
+// Run the chain's LLR state machine to the end (or max_sweeps); st holds the
+// initial state on entry and the final state on return.
+int llr_run_state(dym_chain* c, LlrState* st, int nhit, long max_sweeps) {
   LlrWork w;
   w.device = c->p.device;
   w.D = c->p.D;
   w.stream = c->stream;
   DYM_CUDA(cudaDeviceGetAttribute(&w.sms, cudaDevAttrMultiProcessorCount, w.device), "attribute");
-  rc = w.add_group(c->grp->g);
+  int rc = w.add_group(c->grp->g);
   if (rc) return rc;
   w.chains.push_back(c);
-  const long max_sweeps = (long)req->drive_cap + (long)req->K * req->NRM + 2;
   int mode = st->mode;
   long sweeps = 0;
   while (mode < DYM_LLR_DONE && sweeps < max_sweeps) {
     const int chunk = (int)std::min<long>(8, max_sweeps - sweeps);
-    rc = w.enqueue_sweeps(chunk, req->nhit);
+    rc = w.enqueue_sweeps(chunk, nhit);
     if (rc) return rc;
     sweeps += chunk;
     DYM_CUDA(cudaMemcpyAsync(&st->mode, &c->d_llr->mode, sizeof(int), cudaMemcpyDeviceToHost, c->stream),
@@ -311,7 +331,25 @@ int dym_llr_run(dym_chain* c, const dym_llr_req* req, dym_llr_result* out, doubl
     DYM_CUDA(cudaStreamSynchronize(c->stream), "llr sweeps");
     mode = st->mode;
   }
-  DYM_CUDA(copy_sync(st.get(), c->d_llr, sizeof(LlrState), cudaMemcpyDeviceToHost, c->stream), "read llr state");
+  DYM_CUDA(copy_sync(st, c->d_llr, sizeof(LlrState), cudaMemcpyDeviceToHost, c->stream), "read llr state");
+  c->sweep = st->sweep;  // sweeps after the state machine finished did nothing
+  return DYM_OK;
+}
+
+}  // namespace
+}  // namespace dym
+
+extern "C" {
+
+int dym_llr_run(dym_chain* c, const dym_llr_req* req, dym_llr_result* out, double* a_hist) {
+  if (!c || !req || !out) return fail(DYM_EINVAL, "dym_llr_run: null argument");
+  int rc = check_llr_req(c, req);
+  if (rc) return rc;
+  std::unique_ptr<LlrState> st(new LlrState());
+  rc = llr_init_state(c, req, st.get());
+  if (rc) return rc;
+  rc = llr_run_state(c, st.get(), req->nhit, (long)req->drive_cap + (long)req->K * req->NRM + 2);
+  if (rc) return rc;
   out->a = st->a;
   out->S1 = st->E[0];
   out->S2 = st->E[1];
@@ -322,9 +360,50 @@ int dym_llr_run(dym_chain* c, const dym_llr_req* req, dym_llr_result* out, doubl
   out->accepts = st->accepts;
   out->phase_accepts = st->phase_acc;
   out->phase_rejects = st->phase_rej;
-  c->sweep = st->sweep;  // sweeps after the state machine finished did nothing
   if (a_hist)
     for (int m = 0; m < req->NRM; ++m) a_hist[m] = st->a_hist[m];
+  return DYM_OK;
+}
+
+int dym_llr2d_run(dym_chain* c, const dym_llr2d_req* req, dym_llr2d_result* out, double* a_hist) {
+  if (!c || !req || !out) return fail(DYM_EINVAL, "dym_llr2d_run: null argument");
+  dym_llr_req q{};
+  q.axis = 1;
+  q.bg = req->a2;
+  q.ewin = req->E1;
+  q.hw = req->hw1;
+  q.a0 = req->a1;
+  q.K = req->K;
+  q.NRM = req->NRM;
+  q.nhit = req->nhit;
+  q.drive_cap = req->drive_cap;
+  int rc = check_llr_req(c, &q);
+  if (rc) return rc;
+  if (!(req->hw2 > 0)) return fail(DYM_EINVAL, "dym_llr2d_run: hw2 must be positive");
+  if (c->p.Nt < 3 || c->p.Nx < 3)
+    return fail(DYM_ENOTSUP, "an S2 window needs every extent >= 3 (1x2 rectangles wrap otherwise)");
+  const Llr2dCell cell{req->E2, req->hw2, req->a2};
+  std::unique_ptr<LlrState> st(new LlrState());
+  rc = llr_init_state(c, &q, st.get(), &cell);
+  if (rc) return rc;
+  rc = llr_run_state(c, st.get(), req->nhit, (long)req->drive_cap + (long)req->K * req->NRM + 2);
+  if (rc) return rc;
+  out->a1 = st->a;
+  out->a2 = st->bg;
+  out->S1 = st->E[0];
+  out->S2 = st->E[1];
+  out->status = st->mode;
+  out->drive_sweeps = st->drive_sweeps;
+  out->sweeps = st->sweeps;
+  out->hits = st->hits;
+  out->accepts = st->accepts;
+  out->phase_accepts = st->phase_acc;
+  out->phase_rejects = st->phase_rej;
+  if (a_hist)
+    for (int m = 0; m < req->NRM; ++m) {
+      a_hist[2 * m] = st->a_hist[m];
+      a_hist[2 * m + 1] = st->a2_hist[m];
+    }
   return DYM_OK;
 }
 

@@ -249,8 +249,9 @@ namespace dym {
 template <int D, int DIR>
 __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
                                               const uint16_t* s_inv, const uint16_t* s_sub, const uint16_t* s_cls,
-                                              int axis, double aa, double bg, double E0, double emid, bool drive,
-                                              uint32_t qthr, int* s_delta, unsigned& hits, unsigned& accs) {
+                                              int axis, double aa, double bg, double E0, double emid,
+                                              const LlrDrive2& d2, bool drive, uint32_t qthr, int* s_delta,
+                                              unsigned& hits, unsigned& accs) {
   constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
   SiteGeo<D> geo;
   site_geo<D>(i, a.Nt, a.Nx, geo);
@@ -275,7 +276,7 @@ __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, ui
   for (int j = NS; j < NT; ++j) m1 = DYM_ADD(m1, s_retr[u[j]]);
   bool part = true;
   if (drive) part = dym_hit_random(a.seed, sweep, i, DIR, 0xFFFFFu, DYM_TAG_LLR).v[0] < qthr;
-  double cum = 0;
+  double cum = 0, cum2 = 0;
   for (int h = 0; part && h < a.nhit; ++h) {
     const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_LLR);
     const uint16_t* row = s_sub + dym_pick(r.v[0], a.npool) * a.P;
@@ -295,7 +296,13 @@ __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, ui
     const double dEw = axis == 1 ? dS1 : dS2;
     const double dEbg = axis == 1 ? dS2 : dS1;
     bool acc;
-    if (drive) {
+    if (drive && d2.dims == 2) {  // closer to the cell centre in normalised distance (llr2d.cpp:206-209)
+      const double c1 = DYM_ADD(E0, cum), c2 = DYM_ADD(d2.E0b, cum2);
+      const double x1 = DYM_MUL(DYM_SUB(c1, emid), d2.ihw0), y1 = DYM_MUL(DYM_SUB(c2, d2.emid2), d2.ihw1);
+      const double x2 = DYM_MUL(DYM_SUB(DYM_ADD(c1, dS1), emid), d2.ihw0);
+      const double y2 = DYM_MUL(DYM_SUB(DYM_ADD(c2, dS2), d2.emid2), d2.ihw1);
+      acc = DYM_ADD(DYM_MUL(x2, x2), DYM_MUL(y2, y2)) < DYM_ADD(DYM_MUL(x1, x1), DYM_MUL(y1, y1));
+    } else if (drive) {
       const double Ec = DYM_ADD(E0, cum);
       acc = fabs(DYM_SUB(DYM_ADD(Ec, dEw), emid)) < fabs(DYM_SUB(Ec, emid));
     } else {
@@ -309,6 +316,7 @@ __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, ui
       r1 = r1n;
       m1 = m1n;
       cum = DYM_ADD(cum, dEw);
+      cum2 = DYM_ADD(cum2, dS2);
       ++accs;
     }
   }

@@ -124,6 +124,23 @@ class LlrResult:
 
 
 @dataclass
+class Llr2dResult:
+    """One two-dimensional LLR cell (seed_cell + rm_solve2d, llr2d.cpp:225-259)."""
+    a1: float
+    a2: float
+    S1: float
+    S2: float
+    status: str
+    drive_sweeps: int
+    sweeps: int
+    hits: int
+    accepts: int
+    phase_accepts: int
+    phase_rejects: int
+    a_hist: np.ndarray = field(repr=False)  # [NRM, 2]: (a1, a2) after each iteration
+
+
+@dataclass
 class SweepStats:
     hits: int
     accepts: int
@@ -235,6 +252,20 @@ class Lattice:
         check(lib().dym_llr_run(self._h, C.byref(req), C.byref(res), ptr(hist, C.c_double)))
         return LlrResult(res.a, res.S1, res.S2, _lib.LLR_STATUS.get(res.status, str(res.status)), res.drive_sweeps,
                          res.sweeps, res.hits, res.accepts, res.phase_accepts, res.phase_rejects, hist[:NRM].copy())
+
+    def llr2d_run(self, E1: float, hw1: float, E2: float, hw2: float, a1: float, a2: float, K: int = 40,
+                  NRM: int = 70, nhit: int = 20, drive_cap: int = 4000) -> Llr2dResult:
+        """Drive (S1, S2) into the cell [E1 +- hw1] x [E2 +- hw2], then NRM pairs of
+        Robbins-Monro iterations of K constrained sweeps (llr2d.cpp:225-259);
+        defaults are llr2d.cpp's (K 40, NRM 70, drive-in cap 4000)."""
+        req = _lib.Llr2dReq(E1=E1, hw1=hw1, E2=E2, hw2=hw2, a1=a1, a2=a2, K=K, NRM=NRM, nhit=nhit,
+                            drive_cap=drive_cap)
+        res = _lib.Llr2dResult()
+        hist = np.zeros(2 * max(NRM, 1))
+        check(lib().dym_llr2d_run(self._h, C.byref(req), C.byref(res), ptr(hist, C.c_double)))
+        return Llr2dResult(res.a1, res.a2, res.S1, res.S2, _lib.LLR_STATUS.get(res.status, str(res.status)),
+                           res.drive_sweeps, res.sweeps, res.hits, res.accepts, res.phase_accepts, res.phase_rejects,
+                           hist[: 2 * NRM].reshape(NRM, 2).copy())
 
     def schedule(self):
         V = C.c_uint32()

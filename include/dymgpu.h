@@ -244,7 +244,8 @@ typedef struct {
   double hw;         /* half-width: window [ewin-hw, ewin+hw], W = 2 hw (llr.cpp:236) */
   double a0;         /* initial a (also the drive-in tilt, seed_window's a_guess, llr.cpp:223) */
   int32_t K;         /* sweeps per Robbins-Monro iteration (llr.cpp:294, default 50) */
-  int32_t NRM;       /* Robbins-Monro iterations (llr.cpp:295, default 80), <= DYM_LLR_MAX_NRM */
+  int32_t NRM;       /* Robbins-Monro iterations (llr.cpp:295, default 80), <= DYM_LLR_MAX_NRM;
+                        0: drive into the window only (seed_window) */
   int32_t nhit;      /* hits per link per visit (llr.cpp:32, NHIT 20) */
   int32_t drive_cap; /* max drive-in sweeps (llr.cpp:225, CAP 20000) */
 } dym_llr_req;
@@ -274,6 +275,32 @@ int dym_llr_energy(dym_chain* c, double* S1, double* S2);
  * energy towards the centre).  a_hist (may be NULL) receives a after each of
  * the NRM iterations. */
 int dym_llr_run(dym_chain* c, const dym_llr_req* req, dym_llr_result* out, double* a_hist);
+
+/* Two-dimensional LLR cell (replaces update_constrained2d, seed_cell and
+ * rm_solve2d, llr2d.cpp:178-259): both actions windowed, S1 in [E1-hw1, E1+hw1]
+ * and S2 in [E2-hw2, E2+hw2], weight exp(-a1 dS1 - a2 dS2) inside the cell;
+ * drive-in moves closer to the cell centre in normalised distance; two
+ * Robbins-Monro recursions a_i += 12/(W_i^2 (m+1)) (<S_i> - E_i).  Same
+ * colour-parallel rule as dym_llr_run.  Every extent must be >= 3. */
+typedef struct {
+  double E1, hw1;    /* S1 window */
+  double E2, hw2;    /* S2 window */
+  double a1, a2;     /* initial (a1, a2): drive-in tilt and Robbins-Monro start */
+  int32_t K, NRM;    /* sweeps per iteration, iterations (<= DYM_LLR_MAX_NRM) */
+  int32_t nhit, drive_cap;
+} dym_llr2d_req;
+
+typedef struct {
+  double a1, a2;
+  double S1, S2;
+  int32_t status;    /* DYM_LLR_DONE or DYM_LLR_UNREACHED */
+  int32_t drive_sweeps, sweeps;
+  uint64_t hits, accepts;
+  uint64_t phase_accepts, phase_rejects;
+} dym_llr2d_result;
+
+/* a_hist (may be NULL) receives 2*NRM doubles: (a1, a2) after each iteration. */
+int dym_llr2d_run(dym_chain* c, const dym_llr2d_req* req, dym_llr2d_result* out, double* a_hist);
 
 /* ---------------------------------------------------------------- server --- */
 

@@ -500,9 +500,13 @@ enum { OR_DRIVE = 0, OR_SETTLE = 1, OR_RM = 2, OR_DONE = 3, OR_UNREACHED = 4 };
 
 /* out[0..3] = a, S1, S2, mode; iout[0..5] = drive_sweeps, sweeps, hits,
  * accepts, phase_accepts, phase_rejects; a_hist[NRM]. */
-int or_llr_run(or_lattice* L, const int* phase_dir, const uint32_t* phase_len, const uint32_t* sites, int nphase,
-               int axis, double bg, double ewin, double hw, double a0, int K, int NRM, int nhit, int drive_cap,
-               uint64_t seed, uint32_t first_sweep, double* out, int64_t* iout, double* a_hist) {
+/* dims == 2: a two-dimensional cell (llr2d.cpp:178-259), axis 1, S2 window
+ * [ewin2 - hw2, ewin2 + hw2], bg is a2 and is Robbins-Monro updated too, a2_hist
+ * receives it; drive-in compares squared normalised distances to the centre. */
+static int llr_impl(or_lattice* L, const int* phase_dir, const uint32_t* phase_len, const uint32_t* sites,
+                    int nphase, int axis, double bg, double ewin, double hw, double a0, int K, int NRM, int nhit,
+                    int drive_cap, uint64_t seed, uint32_t first_sweep, double* out, int64_t* iout, double* a_hist,
+                    int dims, double ewin2, double hw2, double* a2_hist) {
   const or_group* g = L->g;
   const unsigned D = L->D, V = L->V;
   int* cls = (int*)malloc(sizeof(int) * g->P);
@@ -520,11 +524,16 @@ int or_llr_run(or_lattice* L, const int* phase_dir, const uint32_t* phase_len, c
   double E[2] = {or_class_sum(h[0], NULL, v, ncls), or_class_sum(h[1], NULL, v, ncls)};
   const double W = 2 * hw, elo = ewin - hw, ehi = ewin + hw;
   const double emid = 0.5 * (elo + ehi), w2 = W * W;
+  const double elo2 = ewin2 - hw2, ehi2 = ewin2 + hw2, emid2 = 0.5 * (elo2 + ehi2), w2b = (2 * hw2) * (2 * hw2);
+  const double ihw0 = dims == 2 ? 1.0 / hw : 0, ihw1 = dims == 2 ? 1.0 / hw2 : 0;
+#define OR_NSQ(e1, e2) ((((e1) - emid) * ihw0) * (((e1) - emid) * ihw0) + (((e2) - emid2) * ihw1) * (((e2) - emid2) * ihw1))
+#define OR_INBOX(e1, e2) ((e1) >= elo && (e1) <= ehi && (e2) >= elo2 && (e2) <= ehi2)
   const int w = axis - 1;
-  double a = a0, sumE = 0;
+  double a = a0, sumE = 0, sumE2 = 0;
   double* qv = (double*)malloc(sizeof(double) * (size_t)(nphase > 0 ? nphase : 1));
   for (int p = 0; p < nphase; ++p) qv[p] = 1.0;  /* drive-in fraction per colour phase */
   int mode = (E[w] >= elo && E[w] <= ehi) ? OR_RM : OR_DRIVE;
+  if (dims == 2) mode = OR_INBOX(E[0], E[1]) ? OR_RM : OR_DRIVE;
   if (NRM == 0 && mode == OR_RM) mode = OR_DONE;
   if (mode == OR_DRIVE && drive_cap == 0) mode = OR_UNREACHED;
   int k = 0, m = 0, drive_sweeps = 0;
@@ -558,7 +567,7 @@ int or_llr_run(or_lattice* L, const int* phase_dir, const uint32_t* phase_len, c
           dym_u32x4 r = dym_hit_random(seed, sweep, i, dir, 0xFFFFFu, DYM_TAG_LLR);
           part = r.v[0] < qthr;
         }
-        double cum = 0;
+        double cum = 0, cum2 = 0;
         for (int hh = 0; part && hh < nhit; ++hh) {
           dym_u32x4 r = dym_hit_random(seed, sweep, i, dir, (uint32_t)hh, DYM_TAG_LLR);
           const double u1 = (double)r.v[0] * 0x1p-32;
@@ -569,14 +578,19 @@ int or_llr_run(or_lattice* L, const int* phase_dir, const uint32_t* phase_len, c
           const double dS1 = r1n - r1, dS2 = m1n - m1;
           const double dEw = axis == 1 ? dS1 : dS2, dEbg = axis == 1 ? dS2 : dS1;
           int acc;
-          if (drive) {
+          if (drive && dims == 2) {
+            const double c1 = E[0] + cum, c2 = E[1] + cum2;
+            const double x1 = (c1 - emid) * ihw0, y1 = (c2 - emid2) * ihw1;
+            const double x2 = ((c1 + dS1) - emid) * ihw0, y2 = ((c2 + dS2) - emid2) * ihw1;
+            acc = (x2 * x2 + y2 * y2) < (x1 * x1 + y1 * y1);
+          } else if (drive) {
             const double Ec = E[w] + cum;
             acc = fabs(Ec + dEw - emid) < fabs(Ec - emid);
           } else {
             acc = dym_exp(-a * dEw - bg * dEbg) > dym_u53(r.v[1], r.v[2]);
           }
           ++hits;
-          if (acc) { b = bnew; r1 = r1n; m1 = m1n; cum = cum + dEw; ++accs; }
+          if (acc) { b = bnew; r1 = r1n; m1 = m1n; cum = cum + dEw; cum2 = cum2 + dS2; ++accs; }
         }
         if (b != b0) {
           L->a[i * D + dir] = b;
@@ -588,8 +602,10 @@ int or_llr_run(or_lattice* L, const int* phase_dir, const uint32_t* phase_len, c
       }
       off += phase_len[p];
       const double En = or_class_sum(h[w], d[w], v, ncls);
-      const int ok = (mode == OR_DRIVE) ? (fabs(En - emid) < fabs(E[w] - emid)) : (En >= elo && En <= ehi);
-      const double dE = En - E[w];
+      const double En2 = or_class_sum(h[1], d[1], v, ncls);
+      int ok = (mode == OR_DRIVE) ? (fabs(En - emid) < fabs(E[w] - emid)) : (En >= elo && En <= ehi);
+      if (dims == 2) ok = (mode == OR_DRIVE) ? (OR_NSQ(En, En2) < OR_NSQ(E[0], E[1])) : OR_INBOX(En, En2);
+      const double dE = En - E[w], dE2 = En2 - E[1];
       if (ok) {
         for (int c = 0; c < ncls; ++c) { h[0][c] += d[0][c]; h[1][c] += d[1][c]; }
         E[0] = or_class_sum(h[0], NULL, v, ncls);
@@ -600,24 +616,36 @@ int or_llr_run(or_lattice* L, const int* phase_dir, const uint32_t* phase_len, c
         ++prej;
       }
       if (mode == OR_DRIVE) {
-        const double dist = fabs(emid - E[w]);
-        const double qq = fabs(dE) > 0 ? qv[p] * (dist / fabs(dE)) : qv[p] * 2.0;
+        double dist = fabs(emid - E[w]), move = fabs(dE);
+        if (dims == 2) {
+          dist = sqrt(OR_NSQ(E[0], E[1]));
+          const double x = dE * ihw0, y = dE2 * ihw1;
+          move = sqrt(x * x + y * y);
+        }
+        const double qq = move > 0 ? qv[p] * (dist / move) : qv[p] * 2.0;
         qv[p] = fmin(1.0, fmax(qq, 0x1.0p-32));
-        if (E[w] >= elo && E[w] <= ehi) mode = OR_SETTLE;
+        if (dims == 2 ? OR_INBOX(E[0], E[1]) : (E[w] >= elo && E[w] <= ehi)) mode = OR_SETTLE;
       }
       if (p == nphase - 1) {
         if (mode == OR_DRIVE) {
           if (++drive_sweeps >= drive_cap) mode = OR_UNREACHED;
         } else if (mode == OR_SETTLE) {
-          mode = OR_RM; k = 0; m = 0; sumE = 0;
+          mode = NRM > 0 ? OR_RM : OR_DONE; k = 0; m = 0; sumE = 0; sumE2 = 0;
         } else if (mode == OR_RM) {
           sumE = sumE + E[w];
+          if (dims == 2) sumE2 = sumE2 + E[1];
           if (++k == K) {
             const double gg = sumE / (double)K - ewin;
             const double step = 12.0 / (w2 * (double)(m + 1));
             a = a + step * gg;
             if (a_hist) a_hist[m] = a;
-            ++m; k = 0; sumE = 0;
+            if (dims == 2) {
+              const double g2 = sumE2 / (double)K - ewin2;
+              const double step2 = 12.0 / (w2b * (double)(m + 1));
+              bg = bg + step2 * g2;
+              if (a2_hist) a2_hist[m] = bg;
+            }
+            ++m; k = 0; sumE = 0; sumE2 = 0;
             if (m >= NRM) mode = OR_DONE;
           }
         }
@@ -628,7 +656,27 @@ int or_llr_run(or_lattice* L, const int* phase_dir, const uint32_t* phase_len, c
   out[0] = a; out[1] = E[0]; out[2] = E[1]; out[3] = mode;
   iout[0] = drive_sweeps; iout[1] = sweeps; iout[2] = hits; iout[3] = accs; iout[4] = pacc; iout[5] = prej;
   free(cls); free(chg_site); free(chg_old); free(qv);
+  if (dims == 2) out[4] = bg;
   return 0;
+#undef OR_NSQ
+#undef OR_INBOX
+}
+
+int or_llr_run(or_lattice* L, const int* phase_dir, const uint32_t* phase_len, const uint32_t* sites, int nphase,
+               int axis, double bg, double ewin, double hw, double a0, int K, int NRM, int nhit, int drive_cap,
+               uint64_t seed, uint32_t first_sweep, double* out, int64_t* iout, double* a_hist) {
+  return llr_impl(L, phase_dir, phase_len, sites, nphase, axis, bg, ewin, hw, a0, K, NRM, nhit, drive_cap, seed,
+                  first_sweep, out, iout, a_hist, 1, 0.0, 1.0, NULL);
+}
+
+/* Two-dimensional cell; out[0] a1, out[4] a2 (llr2d.cpp:178-259 with the
+ * colour-parallel rule of or_llr_run). */
+int or_llr2d_run(or_lattice* L, const int* phase_dir, const uint32_t* phase_len, const uint32_t* sites, int nphase,
+                 double E1, double hw1, double E2, double hw2, double a1, double a2, int K, int NRM, int nhit,
+                 int drive_cap, uint64_t seed, uint32_t first_sweep, double* out, int64_t* iout, double* a1_hist,
+                 double* a2_hist) {
+  return llr_impl(L, phase_dir, phase_len, sites, nphase, 1, a2, E1, hw1, a1, K, NRM, nhit, drive_cap, seed,
+                  first_sweep, out, iout, a1_hist, 2, E2, hw2, a2_hist);
 }
 
 /* S1, S2 of the current configuration by the reference's loops (serial). */

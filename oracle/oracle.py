@@ -61,6 +61,8 @@ def lib() -> C.CDLL:
             "or_pick": (u32, [u32, u32]),
             "or_llr_run": (i, [vp, P(C.c_int), P(u32), P(u32), i, i, d, d, d, d, i, i, i, i, u64, u32, P(d),
                                P(C.c_int64), P(d)]),
+            "or_llr2d_run": (i, [vp, P(C.c_int), P(u32), P(u32), i, d, d, d, d, d, d, i, i, i, i, u64, u32, P(d),
+                                 P(C.c_int64), P(d), P(d)]),
             "or_energies": (None, [vp, P(d), P(d)]),
         }
         for name, (res, args) in sig.items():
@@ -176,6 +178,25 @@ class OracleLattice:
         return dict(a=out[0], S1=out[1], S2=out[2], status=status, drive_sweeps=int(iout[0]), sweeps=int(iout[1]),
                     hits=int(iout[2]), accepts=int(iout[3]), phase_accepts=int(iout[4]),
                     phase_rejects=int(iout[5]), a_hist=hist[:NRM].copy())
+
+    def llr2d_run(self, sched, E1, hw1, E2, hw2, a1, a2, K=40, NRM=70, nhit=20, drive_cap=4000, seed=0,
+                  first_sweep=0):
+        """Two-dimensional cell with the colour-parallel rule (llr2d.cpp:178-259)."""
+        pd, pl, sites = sched
+        out = np.zeros(5)
+        iout = np.zeros(6, np.int64)
+        h1 = np.zeros(max(NRM, 1))
+        h2 = np.zeros(max(NRM, 1))
+        rc = lib().or_llr2d_run(self.h, _p(pd, C.c_int), _p(pl, C.c_uint32), _p(sites, C.c_uint32), len(pd),
+                                float(E1), float(hw1), float(E2), float(hw2), float(a1), float(a2), K, NRM, nhit,
+                                drive_cap, seed, first_sweep, _p(out, C.c_double), _p(iout, C.c_int64),
+                                _p(h1, C.c_double), _p(h2, C.c_double))
+        if rc:
+            raise ValueError(f"oracle llr2d failed ({rc})")
+        status = {0: "drive", 1: "settle", 2: "rm", 3: "done", 4: "unreached"}[int(out[3])]
+        return dict(a1=out[0], a2=out[4], S1=out[1], S2=out[2], status=status, drive_sweeps=int(iout[0]),
+                    sweeps=int(iout[1]), hits=int(iout[2]), accepts=int(iout[3]), phase_accepts=int(iout[4]),
+                    phase_rejects=int(iout[5]), a_hist=np.stack([h1[:NRM], h2[:NRM]], axis=1))
 
     def measure(self, wl_nx: int, wl_nt: int, want_hist: bool = False):
         out = np.zeros(4 + max(wl_nx, 0) * max(wl_nt, 0))

@@ -26,3 +26,38 @@ def test_gpu_llr_matches_oracle(engine, case):
     assert (lat.links.ravel() == L.links).all()
     s1, s2 = lat.llr_energy()
     assert s1 == res.S1 and s2 == res.S2
+
+
+CASES_2D = [
+    # name, group, Nt, Nx, start, seed, S1 centre / NPLAQ, S2 centre / NRECT, a1, a2, K, NRM, nhit, cap
+    ("s1080_4444_2d_cold", "S1080", 4, 4, "cold", 8, -2.5, -2.2, 3.0, 0.5, 4, 5, 10, 300),
+    ("bi_4444_2d_hot", "BI", 4, 4, "hot", 5, -0.6, -0.4, 1.0, 0.5, 4, 5, 10, 300),
+    ("s1080_3444_2d_hot", "S1080", 3, 4, "hot", 11, -1.0, -0.7, 2.0, 0.0, 4, 5, 10, 300),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES_2D, ids=[c[0] for c in CASES_2D])
+def test_gpu_llr2d_matches_oracle(engine, case):
+    from dym_symanzik_action_gb300.schedule import schedule
+    from oracle.oracle import OracleGroup, OracleLattice
+    name, gname, Nt, Nx, start, seed, c1, c2, a1, a2, K, NRM, nhit, cap = case
+    og = OracleGroup(tables.ensure_table(gname))
+    L = OracleLattice(og, 4, Nt, Nx)
+    if start == "hot":
+        L.hot_start(seed)
+    else:
+        L.links = np.full(4 * L.V, og.id, np.uint16)
+    n1 = L.V * 6
+    cell = (c1 * n1, 0.0225 * n1 / 2, c2 * 2 * n1, 0.0225 * 2 * n1 / 2)
+    r = L.llr2d_run(schedule(4, Nt, Nx), *cell, a1, a2, K=K, NRM=NRM, nhit=nhit, drive_cap=cap, seed=seed)
+    g = engine.load_group(tables.ensure_table(gname))
+    lat = engine.Lattice(g, 4, Nt, Nx, 0.0, 0.0, 0.0, seed, start=start)
+    res = lat.llr2d_run(*cell, a1, a2, K=K, NRM=NRM, nhit=nhit, drive_cap=cap)
+    assert res.status == r["status"] == "done"
+    assert (res.a_hist == r["a_hist"]).all()
+    assert (res.a1, res.a2, res.S1, res.S2) == (r["a1"], r["a2"], r["S1"], r["S2"])
+    assert (res.drive_sweeps, res.sweeps, res.hits, res.accepts) == (r["drive_sweeps"], r["sweeps"], r["hits"],
+                                                                     r["accepts"])
+    assert (res.phase_accepts, res.phase_rejects) == (r["phase_accepts"], r["phase_rejects"])
+    assert (lat.links.ravel() == L.links).all()
