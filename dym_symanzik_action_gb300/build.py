@@ -26,6 +26,7 @@ LIB = os.path.join(LIBDIR, "libdymgpu.so")
 CLI = os.path.join(BINDIR, "dym-mod-metro")
 LLR_CLI = os.path.join(BINDIR, "dym-llr")
 LLR2D_CLI = os.path.join(BINDIR, "dym-llr2d")
+SAVECFG_CLI = os.path.join(BINDIR, "dym-mod-metro-savecfg")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # DYM_BOUNDS_CHECK=1 builds the self-checking kernels (every index checked,
@@ -100,7 +101,8 @@ def build(verbose: bool = False) -> str:
         _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs])
         with open(flavor_file, "w") as f:
             f.write(flavor)
-    for name, exe in (("dym_mod_metro.cpp", CLI), ("dym_llr.cpp", LLR_CLI), ("dym_llr2d.cpp", LLR2D_CLI)):
+    for name, exe in (("dym_mod_metro.cpp", CLI), ("dym_llr.cpp", LLR_CLI), ("dym_llr2d.cpp", LLR2D_CLI),
+                      ("dym_mod_metro_savecfg.cpp", SAVECFG_CLI)):
         cli_src = os.path.join(CSRC, name)
         if os.path.exists(cli_src) and (_stale(exe, [cli_src, LIB] + hdrs)):
             _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", "-pthread", *inc, cli_src, "-o", exe,

@@ -7,6 +7,10 @@ Writes Cayley tables in the plain-text group format the reference loader reads
     ReTr[0] .. ReTr[P-1]        real part of  -Tr(U_n)
     ImTr[0] .. ImTr[P-1]        imag part of  -Tr(U_n)
     mult[0][0] .. mult[P-1][P-1]
+    [3x3 groups: the matrix of every element, 18 doubles each: Re, Im of
+     U[0][0], U[0][1], ..., U[2][2] -- the layout the reference's
+     configuration writer reads after the table (dym-mod-metro-savecfg.cpp:47,
+     248-265); loaders ignore these trailing tokens]
 
 The sign convention (minus the trace) follows the reference's generators, so the
 identity has the smallest ReTr.
@@ -160,6 +164,9 @@ def write_table(tab: GroupTable, path: str) -> None:
         f.write(" ".join(repr(float(x)) for x in tab.imtr) + "\n")
         for row in tab.mult:
             f.write(" ".join(map(str, row.tolist())) + "\n")
+        if tab.mats.shape[1] == 3:
+            for m in tab.mats:
+                f.write(" ".join(repr(float(v)) for z in m.ravel() for v in (z.real, z.imag)) + "\n")
     os.replace(tmp, path)
 
 
@@ -174,7 +181,8 @@ def ensure_table(name: str, cache_dir: str | None = None) -> str:
     """Path of the generated table file for `name`, generating it on first use."""
     cache_dir = cache_dir or default_cache_dir()
     os.makedirs(cache_dir, exist_ok=True)
-    path = os.path.join(cache_dir, name)
+    path = os.path.join(cache_dir, "v2", name)  # v2: SU(3) matrices appended
+    os.makedirs(os.path.dirname(path), exist_ok=True)
     if not os.path.exists(path):
         write_table(generate(name), path)
     return path
