@@ -56,7 +56,7 @@ def gathers_per_link_hit(nhit: int) -> float:
 # workload, from the ncu --set full captures summarised in
 # profiles/sweep_mixed_s1080_32x32x32x8_ncu.md and
 # profiles/sweep_sub_s1080_32x32x32x8_ncu.md (cold cache after ncu's flush).
-DRAM_BYTES_PER_LAUNCH = {"mixed": 2830336, "shared": 2563584}
+DRAM_BYTES_PER_LAUNCH = {"k_sweep_mixed": 2830336, "k_sweep_sub": 2563584}
 
 PRECISION_DTYPE = {"mixed": "u16/i32+f32 (f64 rechecks)", "shared": "u16/f64", "fp64": "u16/f64"}
 PRECISION_TEXT = {
@@ -66,14 +66,20 @@ PRECISION_TEXT = {
     "fp64": "fp64 decisions, direct table gathers (reference arithmetic)"}
 
 
-def kernel_model(precision: str, P: int, npool: int, nhit: int, links_per_launch: int, sms: int):
-    """(kernel name, table gathers per link visit, blocks, staged bytes per block)."""
-    if precision == "mixed":  # sweep.cu mixed_smem_bytes; 128..512 threads, one block per SM
+def kernel_model(kernel: int, P: int, npool: int, nhit: int, links_per_launch: int, sms: int):
+    """(kernel name, table gathers per link visit, blocks, staged bytes per block) of the
+    sweep kernel dym_sweep reported (DYM_KERNEL_*)."""
+    if kernel == 4:  # value table (sweep.cu vt_smem_bytes); accepted moves add 25 gathers each
+        per = -(-links_per_launch // sms)
+        threads = min(512, max(128, -(-per // 32) * 32))
+        return ("k_sweep_vt", 108, -(-links_per_launch // threads),
+                P * 8 + P * 2 + npool * P * 2 + P * 2 + npool * 2 + 16)
+    if kernel == 3:  # sweep.cu mixed_smem_bytes; 128..512 threads, one block per SM
         per = -(-links_per_launch // sms)
         threads = min(512, max(128, -(-per // 32) * 32))
         return ("k_sweep_mixed", 108, -(-links_per_launch // threads),
                 P * 8 + 32 * 4 + P * 2 + npool * P * 2 + P + 16)
-    if precision == "shared":  # sweep.cu sub_smem_bytes; one wave of 256-thread blocks
+    if kernel == 2:  # sweep.cu sub_smem_bytes; one wave of 256-thread blocks
         return ("k_sweep_sub", 108, min(sms, -(-links_per_launch // 256)), P * 8 + P * 2 + npool * P * 2 + 16)
     return ("k_sweep_direct", 108 + 25 * nhit, -(-links_per_launch // 256), P * 8 + P * 2 + npool * 2 + 16)
 
@@ -365,6 +371,7 @@ def run_ours(args):
             flush.fill_(k & 0xFF)
             torch.cuda.synchronize()
             st = lat.update(1, w["nhit"])
+            kernel_used = st.kernel
             dev_ms += st.device_ms
             launches += st.launches
             acc += st.accepts
@@ -405,7 +412,7 @@ def run_ours(args):
     avg_launch_s = dev_ms * 1e-3 / max(launches, 1)
     sms = torch.cuda.get_device_properties(local).multi_processor_count
     links_per_launch = links_per_sweep / nphase
-    kname, gathers, blocks, block_bytes = kernel_model(args.precision, g.P, len(g.smallgroup), w["nhit"],
+    kname, gathers, blocks, block_bytes = kernel_model(kernel_used, g.P, len(g.smallgroup), w["nhit"],
                                                        int(links_per_launch), sms)
     stage_bytes = blocks * block_bytes
     alg_bytes_per_launch = links_per_launch * gathers * 32 + stage_bytes
@@ -418,7 +425,7 @@ def run_ours(args):
     except Exception:
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    traffic = DRAM_BYTES_PER_LAUNCH.get(args.precision)
+    traffic = DRAM_BYTES_PER_LAUNCH.get(kname)
 
     if rank == 0:
         line = {
@@ -427,7 +434,7 @@ def run_ours(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": PRECISION_DTYPE[args.precision],
             "data": "synthetic",
             "config": {"workload": WORKLOAD_NAME, "links": links_per_sweep, "nhit": w["nhit"],
-                       "colour_phases": nphase, "precision": PRECISION_TEXT[args.precision],
+                       "colour_phases": nphase, "precision": PRECISION_TEXT[args.precision], "kernel": kname,
                        "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "l2", "achieved": achieved, "peak": l2_peak_gbs, "unit": "GB/s",
                          "frac": achieved / l2_peak_gbs, "traffic": traffic,

@@ -41,7 +41,7 @@ class ChainParams(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("hits", C.c_uint64), ("accepts", C.c_uint64), ("rechecks", C.c_uint64),
                 ("max_ds_err", C.c_double), ("sweep", C.c_uint32), ("launches", C.c_uint32),
-                ("device_ms", C.c_float)]
+                ("device_ms", C.c_float), ("kernel", C.c_int32)]
 
 
 class MeasOpts(C.Structure):

@@ -142,7 +142,37 @@ static int build_mixed_tables(dym_chain* c, const std::vector<uint16_t>& pool) {
   return DYM_OK;
 }
 
-static SweepArgs sweep_args(dym_chain* c) {
+// Value-table kernel tables: int16 fixed-point ReTr of u * g_k and of u, at
+// the largest scale 2^S for which |ReTr| 2^S fits int16.
+static int build_vt_tables(dym_chain* c, const std::vector<uint16_t>& pool) {
+  const Group& g = *c->grp->g;
+  const uint32_t P = g.P, np = (uint32_t)pool.size();
+  int S = 14;
+  while (S > 0 && std::ldexp(std::max(g.max_abs_retr, 1e-3), S) > 32767.0) --S;
+  std::vector<int16_t> vsub((size_t)np * P), val((size_t)P);
+  for (uint32_t u = 0; u < P; ++u) val[u] = (int16_t)std::lrint(std::ldexp(g.cls_val[g.cls[u]], S));
+  for (uint32_t k = 0; k < np; ++k)
+    for (uint32_t u = 0; u < P; ++u) vsub[(size_t)k * P + u] = val[g.mult[(size_t)u * P + pool[k]]];
+  DYM_CUDA(dmalloc(&c->dev.vsub, vsub.size()), "cudaMalloc(vsub)");
+  DYM_CUDA(dmalloc(&c->dev.val16, (size_t)P), "cudaMalloc(val16)");
+  DYM_CUDA(copy_sync(c->dev.vsub, vsub.data(), vsub.size() * 2, cudaMemcpyHostToDevice, c->stream), "upload vsub");
+  DYM_CUDA(copy_sync(c->dev.val16, val.data(), P * 2, cudaMemcpyHostToDevice, c->stream), "upload val16");
+  c->dev.vt_shift = S;
+  c->dev.vt_ok = true;
+  return DYM_OK;
+}
+
+// The kernel dym_sweep runs for this call (DYM_KERNEL_*).  Both mixed kernels
+// take the same decisions; the value-table one is faster while accepted moves
+// are rare, since each accepted move fetches its 25 new elements from L2.
+static int sweep_kernel(const dym_chain* c) {
+  if (c->dev.vt_ok && c->dev.last_acc < 0.01) return DYM_KERNEL_MIXED_VALUES;
+  if (c->dev.mixed_ok) return DYM_KERNEL_MIXED;
+  if (c->dev.sub_ok) return DYM_KERNEL_SHARED;
+  return DYM_KERNEL_DIRECT;
+}
+
+static SweepArgs sweep_args(dym_chain* c, int kernel = DYM_KERNEL_MIXED) {
   const Group& g = *c->grp->g;
   SweepArgs a{};
   a.links = c->dev.links;
@@ -169,6 +199,11 @@ static SweepArgs sweep_args(dym_chain* c) {
     a.dscale = std::ldexp(1.0f, -c->dev.fix_shift);
     a.dmargin = mixed_margin(g, c->p.D, c->dev.fix_shift, c->p.beta0, c->p.beta1, c->p.beta2);
   }
+  if (kernel == DYM_KERNEL_MIXED_VALUES) {
+    a.val16 = c->dev.val16;
+    a.dscale = std::ldexp(1.0f, -c->dev.vt_shift);
+    a.dmargin = mixed_margin(g, c->p.D, c->dev.vt_shift, c->p.beta0, c->p.beta1, c->p.beta2);
+  }
 #ifdef DYM_BOUNDS_CHECK
   a.status = c->dev.counters + 4;
 #endif
@@ -188,6 +223,8 @@ static void chain_release(dym_chain* c) {
   cudaFree(c->dev.cls8);
   cudaFree(c->dev.cfix);
   cudaFree(c->dev.xyz);
+  cudaFree(c->dev.vsub);
+  cudaFree(c->dev.val16);
   cudaFree(c->d_hist);
   cudaFree(c->d_meas_scratch);
   cudaFree(c->d_llr);
@@ -206,6 +243,7 @@ int chain_reset(dym_chain* c, uint64_t seed, int start) {
   c->p.seed = seed;
   c->p.start = start;
   c->sweep = 0;
+  c->dev.last_acc = 1.0;
   const Group& g = *c->grp->g;
   if (start == DYM_START_HOT)
     DYM_CUDA(launch_hot_start(c->dev.links, c->dev.V, c->p.D, g.P, seed, c->stream), "hot start");
@@ -344,6 +382,12 @@ int dym_chain_create(const dym_group* gh, const dym_chain_params* p, dym_chain**
         p->Nx <= kMixedMaxExtent) {
       rc = build_mixed_tables(c.get(), pool);
       if (rc) return rc;
+      int optin = 0;
+      DYM_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device), "attribute");
+      if (vt_smem_bytes(g.P, d.npool) <= (size_t)optin) {
+        rc = build_vt_tables(c.get(), pool);
+        if (rc) return rc;
+      }
     }
   }
   if (p->start == DYM_START_HOT)
@@ -373,7 +417,8 @@ int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
   if (nsweeps < 0 || nhit < 0 || nhit > (1 << 20)) return fail(DYM_EINVAL, "dym_sweep: bad nsweeps or nhit");
   DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
   DYM_CUDA(cudaMemsetAsync(c->dev.counters, 0, 5 * sizeof(unsigned long long), c->stream), "reset counters");
-  SweepArgs a = sweep_args(c);
+  const int kernel = sweep_kernel(c);
+  SweepArgs a = sweep_args(c, kernel);
   a.nhit = nhit;
   const Schedule& s = c->sched;
   DYM_CUDA(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
@@ -383,9 +428,13 @@ int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
       a.sites = c->dev.sites + s.phase_off[p];
       a.xyz = c->dev.xyz ? c->dev.xyz + s.phase_off[p] : nullptr;
       a.n = s.phase_len[p];
-      cudaError_t e = c->dev.mixed_ok ? launch_sweep_mixed(c->p.D, s.phase_dir[p], a, c->dev.psub, c->stream)
-                      : c->dev.sub_ok ? launch_sweep_sub(c->p.D, s.phase_dir[p], a, c->dev.sub, c->stream)
-                                      : launch_sweep_direct(c->p.D, s.phase_dir[p], a, c->stream);
+      cudaError_t e;
+      switch (kernel) {
+        case DYM_KERNEL_MIXED_VALUES: e = launch_sweep_vt(c->p.D, s.phase_dir[p], a, c->dev.vsub, c->stream); break;
+        case DYM_KERNEL_MIXED: e = launch_sweep_mixed(c->p.D, s.phase_dir[p], a, c->dev.psub, c->stream); break;
+        case DYM_KERNEL_SHARED: e = launch_sweep_sub(c->p.D, s.phase_dir[p], a, c->dev.sub, c->stream); break;
+        default: e = launch_sweep_direct(c->p.D, s.phase_dir[p], a, c->stream);
+      }
       if (e != cudaSuccess) return cuda_fail(e, "sweep launch");
     }
     ++c->sweep;
@@ -398,7 +447,9 @@ int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
   if (c->h_counters[4])
     return fail(DYM_ECUDA, "bounds check: code " + std::to_string(c->h_counters[4] >> 32) + " value " +
                                std::to_string(c->h_counters[4] & 0xFFFFFFFFull));
+  if (c->h_counters[0]) c->dev.last_acc = (double)c->h_counters[1] / (double)c->h_counters[0];
   if (out) {
+    out->kernel = kernel;
     out->hits = c->h_counters[0];
     out->accepts = c->h_counters[1];
     out->rechecks = c->h_counters[2];

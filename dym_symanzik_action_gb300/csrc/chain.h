@@ -36,6 +36,7 @@ struct SweepArgs {
   const int32_t* cfix;
   float b1f, b2f, dscale, dmargin;
   const uint32_t* xyz;  // coordinates of sites[k], 8 bits per axis (already offset)
+  const int16_t* val16;  // value-table kernel: fixed-point ReTr of every element
 };
 
 struct ChainDev {
@@ -55,6 +56,11 @@ struct ChainDev {
   int fix_shift = 0;
   bool mixed_ok = false;
   uint32_t* xyz = nullptr;     // packed coordinates of sites[k] (mixed kernel)
+  int16_t* vsub = nullptr;     // value-table kernel: vsub[k*P + u] = ReTr(u * pool[k]) * 2^vt_shift
+  int16_t* val16 = nullptr;    // ReTr(u) * 2^vt_shift
+  int vt_shift = 0;
+  bool vt_ok = false;
+  double last_acc = 1.0;       // acceptance of the chain's previous dym_sweep call (kernel choice)
 };
 
 // Launch one colour phase of the FP64 direct sweep.
@@ -65,6 +71,8 @@ size_t sub_smem_bytes(uint32_t P, uint32_t npool);
 // Launch one colour phase of the mixed-precision shared sub-table sweep.
 cudaError_t launch_sweep_mixed(int D, int dir, const SweepArgs& a, const uint16_t* psub, cudaStream_t s);
 size_t mixed_smem_bytes(uint32_t P, uint32_t npool);
+cudaError_t launch_sweep_vt(int D, int dir, const SweepArgs& a, const int16_t* vsub, cudaStream_t s);
+size_t vt_smem_bytes(uint32_t P, uint32_t npool);
 constexpr int kMixedMaxCls = 32;    // classes addressable by the 5 high bits of a psub entry
 constexpr uint32_t kMixedMaxP = 2048;  // element ids in the 11 low bits
 constexpr int kMixedMaxExtent = 256;   // coordinates packed 8 bits per axis

@@ -141,6 +141,35 @@ __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_mixed(SweepArgs a
   flush_max_err(a.counters + 3, max_err);
 }
 
+// Value-table form of k_sweep_mixed (visit.cuh vt_prepare/vt_hits).  Shared
+// memory: ReTr (FP64) | inverses | value table | element values | pool.
+template <int D, int DIR>
+__global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_vt(SweepArgs a, const int16_t* __restrict__ vsub) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  double* s_retr = reinterpret_cast<double*>(smem);
+  uint16_t* s_inv = reinterpret_cast<uint16_t*>(s_retr + a.P);
+  int16_t* s_vsub = reinterpret_cast<int16_t*>(s_inv + a.P);
+  int16_t* s_val = s_vsub + (size_t)a.npool * a.P;
+  uint16_t* s_pool = reinterpret_cast<uint16_t*>(s_val + a.P);
+  stage_sub_tables(a.retr, a.inv, reinterpret_cast<const uint16_t*>(vsub), a.P, a.npool, s_retr, s_inv,
+                   reinterpret_cast<uint16_t*>(s_vsub));
+  for (uint32_t t = threadIdx.x; t < a.P; t += blockDim.x) s_val[t] = a.val16[t];
+  for (uint32_t t = threadIdx.x; t < a.npool; t += blockDim.x) s_pool[t] = a.pool[t];
+  __syncthreads();
+  constexpr int NT = 8 * (D - 1);
+  unsigned hits = 0, accs = 0, rechecks = 0;
+  float max_err = 0.0f;
+  for (uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x; tid < a.n; tid += gridDim.x * blockDim.x) {
+    uint32_t u[NT], b;
+    int32_t R, M;
+    const uint32_t i = a.sites[tid];
+    vt_prepare<D, DIR>(a, i, a.xyz[tid], s_inv, s_val, u, b, R, M);
+    vt_hits<D, DIR>(a, i, a.sweep, s_retr, s_vsub, s_pool, u, b, R, M, hits, accs, rechecks, max_err);
+  }
+  flush_counters(a.counters, hits, accs, rechecks);
+  flush_max_err(a.counters + 3, max_err);
+}
+
 __global__ void k_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uint64_t seed) {
   const size_t n = (size_t)V * D;
   for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
@@ -255,6 +284,30 @@ cudaError_t mixed_dispatch(int dir, const SweepArgs& a, const uint16_t* psub, cu
 }
 
 template <int D>
+cudaError_t vt_dispatch(int dir, const SweepArgs& a, const int16_t* vsub, cudaStream_t s) {
+  const size_t smem = vt_smem_bytes(a.P, a.npool);
+  void (*fn)(SweepArgs, const int16_t*) = nullptr;
+  switch (dir) {
+    case 0: fn = k_sweep_vt<D, 0>; break;
+    case 1: fn = k_sweep_vt<D, 1>; break;
+    case 2: if (D > 2) fn = k_sweep_vt<D, (D > 2 ? 2 : 0)>; break;
+    case 3: if (D > 3) fn = k_sweep_vt<D, (D > 3 ? 3 : 0)>; break;
+  }
+  if (!fn) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  if (a.n == 0) return cudaSuccess;
+  int dev = 0, sms = 0;
+  e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const uint32_t per = (a.n + (uint32_t)sms - 1) / (uint32_t)sms;
+  const unsigned threads = std::min<unsigned>(kMixedMaxThreads, std::max<unsigned>(128, (per + 31) / 32 * 32));
+  fn<<<(a.n + threads - 1) / threads, threads, smem, s>>>(a, vsub);
+  return cudaGetLastError();
+}
+
+template <int D>
 cudaError_t staples_dispatch(int dir, const SweepArgs& a, const uint32_t* sites, uint32_t n, uint16_t* out,
                              cudaStream_t s) {
   void (*fn)(SweepArgs, const uint32_t*, uint32_t, uint16_t*) = nullptr;
@@ -278,6 +331,15 @@ size_t sub_smem_bytes(uint32_t P, uint32_t npool) {
 
 size_t mixed_smem_bytes(uint32_t P, uint32_t npool) {
   return (size_t)P * 8 + kMixedMaxCls * 4 + (size_t)P * 2 + (size_t)npool * P * 2 + (size_t)P + 16;
+}
+
+size_t vt_smem_bytes(uint32_t P, uint32_t npool) {
+  return (size_t)P * 8 + (size_t)P * 2 + (size_t)npool * P * 2 + (size_t)P * 2 + (size_t)npool * 2 + 16;
+}
+
+cudaError_t launch_sweep_vt(int D, int dir, const SweepArgs& a, const int16_t* vsub, cudaStream_t s) {
+  if (D == 4) return vt_dispatch<4>(dir, a, vsub, s);
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_sweep_mixed(int D, int dir, const SweepArgs& a, const uint16_t* psub, cudaStream_t s) {

@@ -230,6 +230,111 @@ __device__ __forceinline__ void visit_mixed(const SweepArgs& a, uint32_t i, uint
   mixed_hits<D, DIR>(a, i, sweep, s_retr, s_psub, s_cfix, u, b, R, M, hits, accs, rechecks, max_err);
 }
 
+// Value-table form of the mixed visit.  The shared table holds, for pool
+// element g_k and element u, the int16 fixed-point value of ReTr(u * g_k)
+// (scale 2^S) rather than the element, so a hit is 24 shared loads and
+// integer adds; the new elements of an accepted (or re-evaluated) proposal,
+// u_j * g_k, come from the L2-resident Cayley table.  Decisions as visit_mixed.
+template <int D, int DIR>
+__device__ __forceinline__ void vt_prepare(const SweepArgs& a, uint32_t i, uint32_t xyz, const uint16_t* s_inv,
+                                           const int16_t* s_val, uint32_t* u, uint32_t& b, int32_t& R, int32_t& M) {
+  constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
+  SiteGeo<D> geo;
+  site_geo_packed<D>(xyz, a.Nt, a.Nx, geo);
+  GlobalTab T{a.mult, s_inv, a.P};
+  const uint16_t* L = a.links;
+  const uint32_t V = a.V;
+  auto ld = [L, V](uint32_t s, int d) -> uint32_t { return __ldg(L + (size_t)d * V + s); };
+  build_staples<D, DIR>(i, geo, T, ld, u, u + NS);
+  b = a.links[(size_t)DIR * V + i];
+#pragma unroll
+  for (int j = 0; j < NT; ++j) u[j] = T.mul(u[j], b);  // u_j = s_j * b
+  R = 0;
+  M = 0;
+#pragma unroll
+  for (int j = 0; j < NS; ++j) R += s_val[u[j]];
+#pragma unroll
+  for (int j = NS; j < NT; ++j) M += s_val[u[j]];
+}
+
+template <int D, int DIR>
+__device__ __forceinline__ void vt_hits(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
+                                        const int16_t* s_vsub, const uint16_t* s_pool, uint32_t* u, uint32_t b,
+                                        int32_t R, int32_t M, unsigned& hits, unsigned& accs, unsigned& rechecks,
+                                        float& max_err) {
+  constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
+  const uint32_t b0 = b;
+  const uint16_t* __restrict__ mult = a.mult;
+  const uint32_t P = a.P;
+  double oldact = 0.0;
+  bool old_ok = false;
+  for (int h = 0; h < a.nhit; ++h) {
+    const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_METRO);
+    const uint32_t k = dym_pick(r.v[0], a.npool);
+    const int16_t* row = s_vsub + k * P;
+    int32_t Rn = 0, Mn = 0;
+#pragma unroll
+    for (int j = 0; j < NS; ++j) Rn += row[u[j]];
+#pragma unroll
+    for (int j = NS; j < NT; ++j) Mn += row[u[j]];
+    const float ds = __fmaf_rn(a.b2f, (float)(Mn - M), __fmul_rn(a.b1f, (float)(Rn - R))) * a.dscale;
+    const float u2f = __fmaf_rn((float)r.v[1], 0x1p-32f, (float)(r.v[2] >> 11) * 0x1p-53f);
+    const float t = -__logf(u2f);
+    const float band = a.dmargin + __fmaf_rn(t, 0x1p-20f, 0x1p-19f);
+    bool acc;
+    bool exact = false;
+    uint32_t e[NT];
+    bool have_e = false;
+    if (ds < t - band) {
+      acc = true;
+    } else if (ds > t + band) {
+      acc = false;
+    } else {
+      const uint32_t g = s_pool[k];
+#pragma unroll
+      for (int j = 0; j < NT; ++j) e[j] = __ldg(mult + u[j] * P + g);
+      have_e = true;
+      if (!old_ok) {
+        double r1 = 0, m1 = 0;
+#pragma unroll
+        for (int j = 0; j < NS; ++j) r1 = DYM_ADD(r1, s_retr[u[j]]);
+#pragma unroll
+        for (int j = NS; j < NT; ++j) m1 = DYM_ADD(m1, s_retr[u[j]]);
+        oldact = dym_action(a.beta0, a.beta1, a.beta2, r1, m1);
+        old_ok = true;
+      }
+      double r1n = 0, m1n = 0;
+#pragma unroll
+      for (int j = 0; j < NS; ++j) r1n = DYM_ADD(r1n, s_retr[e[j]]);
+#pragma unroll
+      for (int j = NS; j < NT; ++j) m1n = DYM_ADD(m1n, s_retr[e[j]]);
+      const double newact = dym_action(a.beta0, a.beta1, a.beta2, r1n, m1n);
+      acc = dym_accept_fast(oldact, newact, dym_u53(r.v[1], r.v[2]));
+      max_err = fmaxf(max_err, fabsf(ds - (float)DYM_SUB(newact, oldact)));
+      ++rechecks;
+      exact = true;
+      if (acc) oldact = newact;
+    }
+    ++hits;
+    if (acc) {
+      const uint32_t g = s_pool[k];
+      b = __ldg(mult + b * P + g);
+      if (have_e) {
+#pragma unroll
+        for (int j = 0; j < NT; ++j) u[j] = e[j];
+      } else {
+#pragma unroll
+        for (int j = 0; j < NT; ++j) u[j] = __ldg(mult + u[j] * P + g);
+      }
+      R = Rn;
+      M = Mn;
+      old_ok = exact;
+      ++accs;
+    }
+  }
+  if (b != b0) a.links[(size_t)DIR * a.V + i] = (uint16_t)b;
+}
+
 // Largest |dS_fast - dS_fp64| seen at a re-evaluation, into the low word of
 // *ctr (non-negative floats order like their bit patterns).
 __device__ __forceinline__ void flush_max_err(unsigned long long* ctr, float err) {

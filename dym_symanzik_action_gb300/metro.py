@@ -149,6 +149,7 @@ class SweepStats:
     sweep: int
     launches: int
     device_ms: float
+    kernel: int = 0  # DYM_KERNEL_*: 1 direct, 2 shared, 3 mixed, 4 mixed with the value table
 
 
 class Lattice:
@@ -200,7 +201,8 @@ class Lattice:
         self.rechecks += st.rechecks
         self.max_ds_err = max(self.max_ds_err, st.max_ds_err)
         self.sweeps = st.sweep
-        return SweepStats(st.hits, st.accepts, st.rechecks, st.max_ds_err, st.sweep, st.launches, st.device_ms)
+        return SweepStats(st.hits, st.accepts, st.rechecks, st.max_ds_err, st.sweep, st.launches, st.device_ms,
+                          st.kernel)
 
     def measure(self, wl_nx: int = 0, wl_nt: int = 0) -> Measurement:
         """Observables (dym-mod-metro.cpp:282-318); wl_nx/wl_nt 0 = full Nx x Nt

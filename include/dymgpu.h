@@ -118,7 +118,15 @@ typedef struct {
   uint32_t sweep;       /* sweeps done by the chain so far */
   uint32_t launches;    /* sweep kernels launched by this call */
   float device_ms;      /* device time of those launches (CUDA events on the chain's stream) */
+  int32_t kernel;       /* sweep kernel of this call: DYM_KERNEL_* (batches: 0) */
 } dym_stats;
+
+#define DYM_KERNEL_DIRECT 1   /* FP64, table gathers for every hit (DYM_PREC_FP64) */
+#define DYM_KERNEL_SHARED 2   /* FP64, hits from the shared sub-table (DYM_PREC_SHARED) */
+#define DYM_KERNEL_MIXED 3    /* DYM_PREC_MIXED, shared (element | class) table */
+#define DYM_KERNEL_MIXED_VALUES 4  /* DYM_PREC_MIXED, shared table of fixed-point values: chosen for a
+                                      call when the chain's previous call accepted under 1% of its hits
+                                      (accepted moves then fetch their elements from the Cayley table) */
 
 /* nsweeps full sweeps with nhit hits per link (replaces update(),
  * dym-mod-metro.cpp:146-197, called nsweeps times).  Counters in `out`

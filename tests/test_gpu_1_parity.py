@@ -146,3 +146,23 @@ def test_mixed_precision_reports_rechecks(engine):
     assert sf.rechecks == 0
     assert 0 < sm.rechecks < 1e-3 * sm.hits
     assert 0.0 <= sm.max_ds_err < 1e-3
+
+
+def test_value_table_kernel_takes_over_when_moves_are_rare(engine):
+    """Cold S(1080) 8^4 at beta = (0, 3, -0.15): almost nothing is accepted, so
+    after its first call the mixed chain runs the value-table kernel
+    (DYM_KERNEL_MIXED_VALUES = 4); every configuration equals the FP64 kernel's.
+    A hot chain at beta1 = 1 keeps the element-table kernel (3)."""
+    D, Nt, Nx, beta, nhit = 4, 8, 8, (0.0, 3.0, -0.15), 10
+    lm = engine.Lattice(group(engine, "S1080"), D, Nt, Nx, *beta, 31, start="cold", precision="mixed")
+    lf = engine.Lattice(group(engine, "S1080"), D, Nt, Nx, *beta, 31, start="cold", precision="fp64")
+    kernels = []
+    for call in range(4):
+        sm = lm.update(2, nhit)
+        sf = lf.update(2, nhit)
+        kernels.append(sm.kernel)
+        assert sf.kernel == 1
+        assert sm.accepts == sf.accepts and (lm.links == lf.links).all(), call
+    assert kernels[0] == 3 and kernels[1:] == [4, 4, 4]
+    lh = engine.Lattice(group(engine, "S1080"), D, Nt, Nx, 0.0, 1.0, 0.0, 32, start="hot", precision="mixed")
+    assert [lh.update(1, nhit).kernel for _ in range(3)] == [3, 3, 3]
