@@ -54,9 +54,9 @@ def gathers_per_link_hit(nhit: int) -> float:
 # every block also stages its shared tables from L2.
 # dram__bytes_read.sum + dram__bytes_write.sum of one sweep launch of this
 # workload, from the ncu --set full captures summarised in
-# profiles/sweep_mixed_s1080_32x32x32x8_ncu.md and
-# profiles/sweep_sub_s1080_32x32x32x8_ncu.md (cold cache after ncu's flush).
-DRAM_BYTES_PER_LAUNCH = {"k_sweep_mixed": 2830336, "k_sweep_sub": 2563584}
+# profiles/sweep_vt_s1080_32x32x32x8_ncu.md, profiles/sweep_mixed_s1080_32x32x32x8_ncu.md
+# and profiles/sweep_sub_s1080_32x32x32x8_ncu.md (cold cache after ncu's flush).
+DRAM_BYTES_PER_LAUNCH = {"k_sweep_vt": 2834432, "k_sweep_mixed": 2830336, "k_sweep_sub": 2563584}
 
 PRECISION_DTYPE = {"mixed": "u16/i32+f32 (f64 rechecks)", "shared": "u16/f64", "fp64": "u16/f64"}
 PRECISION_TEXT = {
