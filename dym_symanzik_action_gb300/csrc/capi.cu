@@ -229,6 +229,7 @@ static void chain_release(dym_chain* c) {
   cudaFree(c->d_meas_scratch);
   cudaFree(c->d_llr);
   cudaFree(c->d_oldv);
+  cudaFree(c->d_stage);
   if (c->h_counters) cudaFreeHost(c->h_counters);
   if (c->h_hist) cudaFreeHost(c->h_hist);
   if (c->ev0) cudaEventDestroy(c->ev0);
@@ -531,10 +532,20 @@ int dym_links_set(dym_chain* c, const uint16_t* host_in) {
   if (!c || !host_in) return fail(DYM_EINVAL, "dym_links_set: null argument");
   const uint32_t P = c->grp->g->P;
   const size_t n = (size_t)c->dev.V * c->p.D;
-  for (size_t k = 0; k < n; ++k)
-    if (host_in[k] >= P) return fail(DYM_EINVAL, "dym_links_set: element id out of range at " + std::to_string(k));
   DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
-  DYM_CUDA(cudaMemcpyAsync(c->dev.links, host_in, n * 2, cudaMemcpyHostToDevice, c->stream), "upload links");
+  if (!c->d_stage) DYM_CUDA(dmalloc(&c->d_stage, n), "cudaMalloc(links stage)");
+  // Upload into the stage while the host checks the ids (a branch-free maximum
+  // that vectorises); the chain's links change only if every id is in range.
+  DYM_CUDA(cudaMemcpyAsync(c->d_stage, host_in, n * 2, cudaMemcpyHostToDevice, c->stream), "upload links");
+  uint16_t mx = 0;
+  for (size_t k = 0; k < n; ++k) mx = host_in[k] > mx ? host_in[k] : mx;
+  if (mx >= P) {
+    size_t k = 0;
+    while (host_in[k] < P) ++k;
+    cudaStreamSynchronize(c->stream);
+    return fail(DYM_EINVAL, "dym_links_set: element id out of range at " + std::to_string(k));
+  }
+  DYM_CUDA(cudaMemcpyAsync(c->dev.links, c->d_stage, n * 2, cudaMemcpyDeviceToDevice, c->stream), "copy links");
   DYM_CUDA(cudaStreamSynchronize(c->stream), "upload links");
   return DYM_OK;
 }

@@ -160,4 +160,5 @@ struct dym_chain {
   dym::LlrState* d_llr = nullptr;
   uint16_t* d_oldv = nullptr;
   uint64_t llr_phase = 0;  // colour phases run by LLR sweeps (delta-buffer parity)
+  uint16_t* d_stage = nullptr;  // dym_links_set: upload buffer, copied into the links once checked
 };

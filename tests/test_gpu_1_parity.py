@@ -166,3 +166,19 @@ def test_value_table_kernel_takes_over_when_moves_are_rare(engine):
     assert kernels[0] == 3 and kernels[1:] == [4, 4, 4]
     lh = engine.Lattice(group(engine, "S1080"), D, Nt, Nx, 0.0, 1.0, 0.0, 32, start="hot", precision="mixed")
     assert [lh.update(1, nhit).kernel for _ in range(3)] == [3, 3, 3]
+
+
+def test_links_set_rejects_out_of_range_ids(engine):
+    """dym_links_set refuses an element id >= P, names the first bad index and
+    leaves the chain's configuration as it was."""
+    from dym_symanzik_action_gb300._lib import DymError
+    lat = engine.Lattice(group(engine, "BT"), 4, 4, 4, 0.0, 1.0, 0.0, 3, start="hot")
+    before = lat.links.copy()
+    bad = before.copy().ravel()
+    bad[777] = lat.group.P
+    with pytest.raises(DymError, match="at 777"):
+        lat.links = bad
+    assert (lat.links == before).all()
+    good = np.roll(before.ravel(), 5)
+    lat.links = good
+    assert (lat.links.ravel() == good).all()
