@@ -174,6 +174,16 @@ DYM_HD double dym_mixed_margin(double c0, double c1, double n1, double c2, doubl
   return 2.0 * (quant + feval + rref) + 1e-7;
 }
 
+/* The LLR weighted test exp(x) > u2 (llr.cpp:211-212, x = -a dE_w - bg dE_bg)
+ * with the exponential evaluated only where it can change the outcome: x >= 0
+ * accepts (exp(x) >= 1 > u2), x < -38 rejects unless u2 == 0 (exp(x) < 3.2e-17
+ * while every nonzero u2 is >= 2^-53); otherwise dym_exp(x) > u2. */
+DYM_HD int dym_weight_accept(double x, double u2) {
+  if (x >= 0.0) return 1;
+  if (x < -38.0 && u2 != 0.0) return 0;
+  return dym_exp(x) > u2;
+}
+
 DYM_HD int dym_accept_fast(double oldact, double newact, double u2) {
   if (newact <= oldact) return 1.0 > u2;
   const double d = DYM_SUB(newact, oldact);

@@ -411,7 +411,7 @@ __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, ui
       const double Ec = DYM_ADD(E0, cum);
       acc = fabs(DYM_SUB(DYM_ADD(Ec, dEw), emid)) < fabs(DYM_SUB(Ec, emid));
     } else {
-      acc = dym_exp(DYM_SUB(DYM_MUL(-aa, dEw), DYM_MUL(bg, dEbg))) > dym_u53(r.v[1], r.v[2]);
+      acc = dym_weight_accept(DYM_SUB(DYM_MUL(-aa, dEw), DYM_MUL(bg, dEbg)), dym_u53(r.v[1], r.v[2]));
     }
     ++hits;
     if (acc) {

@@ -587,7 +587,7 @@ static int llr_impl(or_lattice* L, const int* phase_dir, const uint32_t* phase_l
             const double Ec = E[w] + cum;
             acc = fabs(Ec + dEw - emid) < fabs(Ec - emid);
           } else {
-            acc = dym_exp(-a * dEw - bg * dEbg) > dym_u53(r.v[1], r.v[2]);
+            acc = dym_weight_accept(-a * dEw - bg * dEbg, dym_u53(r.v[1], r.v[2]));
           }
           ++hits;
           if (acc) { b = bnew; r1 = r1n; m1 = m1n; cum = cum + dEw; cum2 = cum2 + dS2; ++accs; }
