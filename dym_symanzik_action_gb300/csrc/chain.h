@@ -87,7 +87,11 @@ cudaError_t launch_staples(int D, int dir, const SweepArgs& a, const uint32_t* s
 // phase.  Energies are exact: integer class histograms of all plaquettes (h[0])
 // and rectangles (h[1]), one FP64 dot product with the class values.
 constexpr int kLlrMaxCls = 32;
-constexpr int kLlrDeltaBytes = 2 * kLlrMaxCls * 4;  // per-tile class deltas at the front of shared memory
+// The LLR propose kernel runs 256-thread blocks whose warps take 32-link tiles
+// independently; each warp's class deltas sit at the front of shared memory.
+constexpr int kLlrWarps = 8;
+constexpr int kLlrTile = 32;
+constexpr int kLlrDeltaBytes = kLlrWarps * 2 * kLlrMaxCls * 4;
 constexpr int kLlrMaxPhases = 256;                   // colour phases per sweep with their own drive-in fraction
 struct LlrState {
   double a, bg, elo, ehi, emid, ewin, w2;
@@ -109,6 +113,7 @@ struct LlrState {
   // Robbins-Monro; ihw are the reciprocal half-widths of the normalised
   // distance to the cell centre used by the drive-in.
   int dims;
+  int restore;  // set by the commit: the phase's class move was refused, restore its links
   double elo2, ehi2, emid2, ewin2, w2b, sumE2;
   double ihw[2];
   double a2_hist[DYM_LLR_MAX_NRM];

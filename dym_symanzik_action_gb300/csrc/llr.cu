@@ -12,14 +12,15 @@
 //     deterministic fraction q of the links takes part; after each phase q is
 //     set so that the expected move covers the remaining distance.  Each
 //     link's change of plaquette and rectangle classes is added to the chain's
-//     integer histogram delta.
-//  2. k_llr_decide: the class move is kept iff the new windowed energy lies in
-//     [Elo, Ehi] (outside the window: iff it is closer to the centre);
-//     otherwise every link of the class is restored.
-//  3. k_llr_commit: one thread per chain folds the delta into the chain's
-//     histograms, recomputes the exact energies, adapts q, and at the end of a
-//     sweep advances the drive-in / Robbins-Monro state machine
-//     (a += 12/(W^2 (m+1)) (<E> - Ewin), llr.cpp:244).
+//     integer histogram delta.  A warp takes a tile of 32 links, so a short
+//     work list still reaches every SM (the FP64 pipe bounds this kernel).
+//  2. k_llr_commit: one warp per chain forms the energies after the class
+//     move from the histograms plus the delta and keeps the move iff the new
+//     windowed energy lies in [Elo, Ehi] (outside the window: iff it is closer
+//     to the centre); it folds a kept delta into the histograms, adapts q, and
+//     at the end of a sweep advances the drive-in / Robbins-Monro state
+//     machine (a += 12/(W^2 (m+1)) (<E> - Ewin), llr.cpp:244).
+//  3. k_llr_restore: the links of a refused class move get their old values.
 // NHIT identical single-hit Metropolis kernels compose into a reversible
 // kernel, so accepting the class move iff it stays in the window is an exact
 // Metropolis-Hastings step for the window-restricted distribution.  Every
@@ -37,12 +38,6 @@ namespace dym {
 
 namespace {
 
-__device__ __forceinline__ double class_sum(const long long* h, const long long* d, const double* v, int ncls) {
-  double s = 0;
-  for (int c = 0; c < ncls; ++c) s = DYM_ADD(s, DYM_MUL((double)(h[c] + (d ? d[c] : 0)), v[c]));
-  return s;
-}
-
 // Squared normalised distance of (e1, e2) to a two-dimensional cell's centre
 // (the reference compares hypot() of the same terms, llr2d.cpp:207-209).
 __device__ __forceinline__ double norm_sq(const LlrState* st, double e1, double e2) {
@@ -55,31 +50,19 @@ __device__ __forceinline__ bool in_box(const LlrState* st, double e1, double e2)
   return e1 >= st->elo && e1 <= st->ehi && e2 >= st->elo2 && e2 <= st->ehi2;
 }
 
-// Whether the class move of the chain's current phase is kept.
-__device__ __forceinline__ bool phase_ok(const LlrState* st) {
-  if (st->dims == 2) {
-    const double En1 = class_sum(st->h[0], st->d[st->phase & 1][0], st->v, st->ncls);
-    const double En2 = class_sum(st->h[1], st->d[st->phase & 1][1], st->v, st->ncls);
-    if (st->mode == DYM_LLR_DRIVE) return norm_sq(st, En1, En2) < norm_sq(st, st->E[0], st->E[1]);
-    return in_box(st, En1, En2);
-  }
-  const int w = st->axis - 1;
-  const double En = class_sum(st->h[w], st->d[st->phase & 1][w], st->v, st->ncls);
-  if (st->mode == DYM_LLR_DRIVE) return fabs(DYM_SUB(En, st->emid)) < fabs(DYM_SUB(st->E[w], st->emid));
-  return En >= st->elo && En <= st->ehi;
-}
-
 __device__ __forceinline__ uint32_t q_threshold(double q) {
   const double t = DYM_MUL(q, 4294967296.0);
   return t >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)t;
 }
 
 template <int D>
-__global__ void __launch_bounds__(256) k_llr_propose(const LlrTile* __restrict__ tiles, uint32_t ntiles,
-                                                     const LlrChainDev* __restrict__ chains, BatchGroups groups,
-                                                     int nhit) {
+__global__ void __launch_bounds__(kLlrWarps * 32) k_llr_propose(const LlrTile* __restrict__ tiles, uint32_t ntiles,
+                                                                const LlrChainDev* __restrict__ chains,
+                                                                BatchGroups groups, int nhit) {
   extern __shared__ __align__(16) unsigned char smem[];
-  int* s_delta = reinterpret_cast<int*>(smem);  // first kLlrDeltaBytes of the dynamic shared memory
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  int* s_delta = reinterpret_cast<int*>(smem) + warp * 2 * kLlrMaxCls;  // this warp's class deltas
+  for (uint32_t x = lane; x < 2 * kLlrMaxCls; x += 32) s_delta[x] = 0;
   for (int g = 0; g < groups.n; ++g) {
     const BatchGroupDev& G = groups.g[g];
     stage_sub_tables(G.retr, G.inv, G.sub, G.P, G.npool, reinterpret_cast<double*>(smem + G.off_retr),
@@ -88,14 +71,15 @@ __global__ void __launch_bounds__(256) k_llr_propose(const LlrTile* __restrict__
     for (uint32_t t = threadIdx.x; t < G.P; t += blockDim.x) s_cls[t] = G.cls16[t];
   }
   __syncthreads();
-  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+  // Tile t goes to warp t / gridDim.x of block t % gridDim.x: a short list
+  // spreads over the SMs (one warp each) before any SM takes a second tile.
+  const uint32_t stride = (blockDim.x >> 5) * gridDim.x;
+  for (uint32_t t = warp * gridDim.x + blockIdx.x; t < ntiles; t += stride) {
     const LlrTile tl = tiles[t];
     const LlrChainDev c = chains[tl.chain];
     LlrState* st = c.st;
     const int mode = st->mode;
-    if (mode >= DYM_LLR_DONE) continue;  // the same for every thread of the block
-    for (uint32_t x = threadIdx.x; x < 2 * kLlrMaxCls; x += blockDim.x) s_delta[x] = 0;
-    __syncthreads();
+    if (mode >= DYM_LLR_DONE) continue;  // the same for every lane of the warp
     const BatchGroupDev& G = groups.g[c.group];
     SweepArgs a{};
     a.links = c.links;
@@ -118,8 +102,8 @@ __global__ void __launch_bounds__(256) k_llr_propose(const LlrTile* __restrict__
     const uint32_t qthr = drive ? q_threshold(st->qp[st->phase % (uint32_t)st->nphase]) : 0u;
     const uint32_t sweep = st->sweep;
     unsigned hits = 0, accs = 0;
-    for (uint32_t k = threadIdx.x; k < tl.count; k += blockDim.x) {
-      const uint32_t i = c.sites[tl.begin + k];
+    if (lane < tl.count) {
+      const uint32_t i = c.sites[tl.begin + lane];
       uint32_t b0 = 0;
       switch (tl.dir) {
         case 0: b0 = visit_llr<D, 0>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, axis, aa, bg, E0, emid, d2, drive, qthr,
@@ -133,68 +117,102 @@ __global__ void __launch_bounds__(256) k_llr_propose(const LlrTile* __restrict__
                                                                bg, E0, emid, d2, drive, qthr, s_delta, hits, accs);
           break;
       }
-      c.oldv[tl.pos + k] = (uint16_t)b0;
+      c.oldv[tl.pos + lane] = (uint16_t)b0;
     }
     hits = __reduce_add_sync(0xffffffffu, hits);
     accs = __reduce_add_sync(0xffffffffu, accs);
-    if ((threadIdx.x & 31) == 0) {
+    if (lane == 0) {
       if (hits) atomicAdd(&st->hits, (unsigned long long)hits);
       if (accs) atomicAdd(&st->accepts, (unsigned long long)accs);
     }
-    __syncthreads();
+    __syncwarp();  // every lane's shared-memory deltas are in
     const uint32_t buf = st->phase & 1u;
-    for (uint32_t x = threadIdx.x; x < 2 * kLlrMaxCls; x += blockDim.x) {
+    for (uint32_t x = lane; x < 2 * kLlrMaxCls; x += 32) {
       const int v = s_delta[x];
-      if (v) atomicAdd(reinterpret_cast<unsigned long long*>(&st->d[buf][x / kLlrMaxCls][x % kLlrMaxCls]),
-                       (unsigned long long)(long long)v);
+      if (v) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&st->d[buf][x / kLlrMaxCls][x % kLlrMaxCls]),
+                  (unsigned long long)(long long)v);
+        s_delta[x] = 0;
+      }
     }
-    __syncthreads();
+    __syncwarp();
   }
 }
 
-__global__ void k_llr_decide(const LlrTile* __restrict__ tiles, uint32_t ntiles,
-                             const LlrChainDev* __restrict__ chains) {
-  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+// After the commit: the links of a refused class move get their old values.
+__global__ void k_llr_restore(const LlrTile* __restrict__ tiles, uint32_t ntiles,
+                              const LlrChainDev* __restrict__ chains) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t stride = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntiles; t += stride) {
     const LlrTile tl = tiles[t];
     const LlrChainDev c = chains[tl.chain];
-    const LlrState* st = c.st;
-    if (st->mode >= DYM_LLR_DONE || phase_ok(st)) continue;
-    for (uint32_t k = threadIdx.x; k < tl.count; k += blockDim.x) {
-      const uint32_t i = c.sites[tl.begin + k];
-      uint16_t* own = c.links + (size_t)tl.dir * c.V + i;
-      const uint16_t old = c.oldv[tl.pos + k];
-      if (*own != old) *own = old;
-    }
+    if (!c.st->restore || lane >= tl.count) continue;
+    const uint32_t i = c.sites[tl.begin + lane];
+    uint16_t* own = c.links + (size_t)tl.dir * c.V + i;
+    const uint16_t old = c.oldv[tl.pos + lane];
+    if (*own != old) *own = old;
   }
 }
 
+// One warp per chain whose phase the slot closes.  The lanes form the class
+// products (h + d) v of both histograms at once; lane 0 sums them in class
+// order, which gives the oracle's class sums bit for bit, decides the class
+// move from them, and runs the chain's state machine.
 __global__ void k_llr_commit(const LlrCommit* __restrict__ commits, uint32_t n,
                              const LlrChainDev* __restrict__ chains) {
-  const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= n) return;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (idx >= n) return;  // the same for every lane of the warp
   const LlrCommit cm = commits[idx];
   LlrState* st = chains[cm.chain].st;
   int mode = st->mode;
-  if (mode >= DYM_LLR_DONE) return;
-  const int w = st->axis - 1;
+  if (mode >= DYM_LLR_DONE) {
+    if (lane == 0) st->restore = 0;
+    return;
+  }
   const uint32_t buf = st->phase & 1u;
-  const bool ok = phase_ok(st);
-  const double dE = DYM_SUB(class_sum(st->h[w], st->d[buf][w], st->v, st->ncls), st->E[w]);
-  const double dE2 = DYM_SUB(class_sum(st->h[1], st->d[buf][1], st->v, st->ncls), st->E[1]);
+  const int ncls = st->ncls;
+  double p1 = 0, p2 = 0;
+  long long n1 = 0, n2 = 0;
+  if ((int)lane < ncls) {
+    n1 = st->h[0][lane] + st->d[buf][0][lane];
+    n2 = st->h[1][lane] + st->d[buf][1][lane];
+    p1 = DYM_MUL((double)n1, st->v[lane]);
+    p2 = DYM_MUL((double)n2, st->v[lane]);
+  }
+  double En1 = 0, En2 = 0;  // the energies after the class move
+  for (int c = 0; c < ncls; ++c) {
+    En1 = DYM_ADD(En1, __shfl_sync(0xffffffffu, p1, c));
+    En2 = DYM_ADD(En2, __shfl_sync(0xffffffffu, p2, c));
+  }
+  const int w = st->axis - 1;
+  const double Eo1 = st->E[0], Eo2 = st->E[1];
+  const double Enw = w ? En2 : En1, Eow = w ? Eo2 : Eo1;
+  bool ok;
+  if (st->dims == 2) {
+    ok = mode == DYM_LLR_DRIVE ? norm_sq(st, En1, En2) < norm_sq(st, Eo1, Eo2) : in_box(st, En1, En2);
+  } else {
+    ok = mode == DYM_LLR_DRIVE ? fabs(DYM_SUB(Enw, st->emid)) < fabs(DYM_SUB(Eow, st->emid))
+                               : (Enw >= st->elo && Enw <= st->ehi);
+  }
+  if (ok && (int)lane < ncls) {
+    st->h[0][lane] = n1;
+    st->h[1][lane] = n2;
+  }
+  for (uint32_t x = lane; x < (uint32_t)kLlrMaxCls; x += 32) {
+    st->d[buf][0][x] = 0;
+    st->d[buf][1][x] = 0;
+  }
+  if (lane != 0) return;
+  const double dE = DYM_SUB(Enw, Eow), dE2 = DYM_SUB(En2, Eo2);
+  st->restore = ok ? 0 : 1;
   if (ok) {
-    for (int c = 0; c < st->ncls; ++c) {
-      st->h[0][c] += st->d[buf][0][c];
-      st->h[1][c] += st->d[buf][1][c];
-    }
-    st->E[0] = class_sum(st->h[0], nullptr, st->v, st->ncls);
-    st->E[1] = class_sum(st->h[1], nullptr, st->v, st->ncls);
+    st->E[0] = En1;
+    st->E[1] = En2;
     st->phase_acc++;
   } else {
     st->phase_rej++;
-  }
-  for (int c = 0; c < kLlrMaxCls; ++c) {
-    st->d[buf][0][c] = 0;
-    st->d[buf][1][c] = 0;
   }
   const uint32_t pidx = st->phase % (uint32_t)st->nphase;
   st->phase++;
@@ -259,13 +277,13 @@ void* llr_propose_kernel_for(int D) { return D == 4 ? (void*)k_llr_propose<4> : 
 cudaError_t launch_llr_slot(int D, const LlrTile* tiles, uint32_t ntiles, const LlrCommit* commits, uint32_t ncommit,
                             const LlrChainDev* chains, const BatchGroups& groups, int nhit, unsigned grid,
                             size_t smem, cudaStream_t s) {
+  if (D != 4) return cudaErrorInvalidValue;  // four dimensions only (see launch_sweep_sub)
   if (ntiles) {
     const unsigned g = grid < ntiles ? grid : ntiles;
-    if (D != 4) return cudaErrorInvalidValue;  // four dimensions only (see launch_sweep_sub)
-    k_llr_propose<4><<<g, 256, smem, s>>>(tiles, ntiles, chains, groups, nhit);
-    k_llr_decide<<<g, 256, 0, s>>>(tiles, ntiles, chains);
+    k_llr_propose<4><<<g, kLlrWarps * 32, smem, s>>>(tiles, ntiles, chains, groups, nhit);
   }
-  if (ncommit) k_llr_commit<<<(ncommit + 127) / 128, 128, 0, s>>>(commits, ncommit, chains);
+  if (ncommit) k_llr_commit<<<(ncommit + 3) / 4, 128, 0, s>>>(commits, ncommit, chains);
+  if (ntiles) k_llr_restore<<<(ntiles + 7) / 8, 256, 0, s>>>(tiles, ntiles, chains);
   return cudaGetLastError();
 }
 

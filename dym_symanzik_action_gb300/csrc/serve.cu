@@ -236,7 +236,7 @@ struct LlrWork {
     tile_cnt.assign(maxph, 0);
     commit_off.assign(maxph, 0);
     commit_cnt.assign(maxph, 0);
-    const uint32_t T = 256;
+    const uint32_t T = kLlrTile;  // one warp's tile
     for (size_t k = 0; k < maxph; ++k) {
       tile_off[k] = (uint32_t)tiles.size();
       commit_off[k] = (uint32_t)commits.size();
@@ -262,7 +262,7 @@ struct LlrWork {
     if (!fn) return fail(DYM_ENOTSUP, "LLR: unsupported D");
     DYM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attribute");
     int per_sm = 0;
-    DYM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem), "occupancy");
+    DYM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kLlrWarps * 32, smem), "occupancy");
     grid = (unsigned)std::max(1, sms * std::max(1, per_sm));
     dirty = false;
     return DYM_OK;

@@ -346,6 +346,28 @@ __device__ __forceinline__ void flush_max_err(unsigned long long* ctr, float err
 
 namespace dym {
 
+// dym_weight_accept(x, u2) with u2 = dym_u53(r1, r2), deciding most hits in
+// FP32.  For -38 <= x < 0, ef = __expf((float)x) is within a relative
+// 2^-17 of exp(x) (the conversion of x costs |x| 2^-24 <= 2^-18.7, __expf at
+// most 2 + floor(1.173 |x|) <= 46 ulp = 2^-17.5), u2f within 2^-22 of u2
+// (exact when r1 == 0; every nonzero u2 is >= 2^-53, a normal float) and
+// dym_exp within an ulp of exp; so ef above u2f (1 + 2^-10) implies
+// dym_exp(x) > u2, ef below u2f (1 - 2^-10) implies the opposite, and only the
+// hits in between evaluate dym_exp.  The decision is dym_weight_accept's, bit
+// for bit, and the FP64 pipe (the limit of the LLR sweep on this part)
+// evaluates the exponential for at most 2^-9 of the hits with x < 0 instead of
+// for all of them.
+__device__ __forceinline__ bool llr_weight_accept(double x, uint32_t r1, uint32_t r2) {
+  if (x >= 0.0) return true;
+  const bool u2_zero = (r1 | (r2 >> 11)) == 0u;
+  if (x < -38.0) return u2_zero && dym_exp(x) > 0.0;
+  const float ef = __expf(__double2float_rn(x));
+  const float u2f = __fmaf_rn((float)r1, 0x1p-32f, (float)(r2 >> 11) * 0x1p-53f);
+  if (ef > __fmul_rn(u2f, 1.0f + 0x1p-10f)) return true;
+  if (ef < __fmul_rn(u2f, 1.0f - 0x1p-10f)) return false;
+  return dym_exp(x) > dym_u53(r1, r2);
+}
+
 // One LLR visit of link (i, DIR) with the shared sub-table (llr.cpp:186-216
 // per hit): nhit hits with weight exp(-a dE_w - bg dE_bg), or, in drive-in
 // mode, greedy moves of the link's running energy towards emid.  The link is
@@ -411,7 +433,7 @@ __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, ui
       const double Ec = DYM_ADD(E0, cum);
       acc = fabs(DYM_SUB(DYM_ADD(Ec, dEw), emid)) < fabs(DYM_SUB(Ec, emid));
     } else {
-      acc = dym_weight_accept(DYM_SUB(DYM_MUL(-aa, dEw), DYM_MUL(bg, dEbg)), dym_u53(r.v[1], r.v[2]));
+      acc = llr_weight_accept(DYM_SUB(DYM_MUL(-aa, dEw), DYM_MUL(bg, dEbg)), r.v[1], r.v[2]);
     }
     ++hits;
     if (acc) {
