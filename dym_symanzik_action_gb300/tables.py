@@ -26,6 +26,15 @@ Groups generated here, each as a matrix group closed under multiplication:
 * ``BI``     -- the binary icosahedral group (order 120) in SU(2): the unit
   quaternions generated by i, j, (1+i+j+k)/2 and (i + j/phi + phi k)/2.
 * ``BT``     -- the binary tetrahedral group (order 24) in SU(2).
+* ``BO``     -- the binary octahedral group (order 48) in SU(2): BT and the
+  quaternion (1 + i)/sqrt2.
+* ``BIxBO``  -- an SU(4) subgroup of order 2880: the Kronecker products g (x) h
+  of g in BI and h in BO, i.e. (BI x BO)/{(1,1), (-1,-1)} acting on C^2 (x) C^2.
+  It has the order of the reference's largest shipped SU(4) table and is the
+  case P > 2048 of the engine (element ids beyond 11 bits).  Built from the
+  two SU(2) tables (no 4x4 products): Tr(g (x) h) = Tr g Tr h, so
+  ReTr = -(Tr g)(Tr h) from the two snapped traces, bit-identical within a
+  class and across machines.
 
 Differences from the reference's tables (on purpose):
 
@@ -51,7 +60,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-__all__ = ["GroupTable", "generate", "write_table", "ensure_table", "GROUPS"]
+__all__ = ["GroupTable", "generate", "write_table", "ensure_table", "GROUPS", "PRODUCTS"]
 
 
 @dataclass
@@ -90,33 +99,70 @@ def _bt_generators():
     return [_quat(0, 1, 0, 0), _quat(0, 0, 1, 0), _quat(0.5, 0.5, 0.5, 0.5)]
 
 
+def _bo_generators():
+    r = 1.0 / math.sqrt(2.0)
+    return _bt_generators() + [_quat(r, r, 0, 0)]
+
+
 GROUPS = {"S1080": (_s1080_generators, 1080), "BI": (_bi_generators, 120),
-          "BT": (_bt_generators, 24)}
+          "BT": (_bt_generators, 24), "BO": (_bo_generators, 48)}
+# SU(4) groups built as Kronecker products of two SU(2) groups: (factors, order).
+PRODUCTS = {"BIxBO": (("BI", "BO"), 2880)}
 
 
 def _key(m: np.ndarray) -> bytes:
     return np.round(np.concatenate([m.real.ravel(), m.imag.ravel()]) * 1e6).astype(np.int64).tobytes()
 
 
-def _snap(x: float, what: str) -> float:
-    """Closed form (a + b*sqrt5)/4 for x, found by bounded integer search."""
-    s5 = math.sqrt(5.0)
+def _snap(x: float, what: str, root: float = 5.0) -> float:
+    """Closed form (a + b*sqrt(root))/4 for x, found by bounded integer search."""
+    sr = math.sqrt(root)
     for b in range(-8, 9):
-        a = round(4 * x - b * s5)
-        if abs(a) <= 24 and abs(x - (a + b * s5) / 4.0) < 1e-7:
-            return (a + b * s5) / 4.0 + 0.0  # +0.0 turns -0.0 into 0.0
+        a = round(4 * x - b * sr)
+        if abs(a) <= 24 and abs(x - (a + b * sr) / 4.0) < 1e-7:
+            return (a + b * sr) / 4.0 + 0.0  # +0.0 turns -0.0 into 0.0
     raise ValueError(f"no closed form for {what} = {x!r}")
 
 
-def _canonical_traces(mats: np.ndarray):
+def _canonical_traces(mats: np.ndarray, root: float = 5.0):
     s3 = math.sqrt(3.0)
     tr = np.trace(mats, axis1=1, axis2=2)
-    retr = np.array([_snap(-t.real, "ReTr") for t in tr])
-    imtr = np.array([s3 * (_snap(-t.imag / s3, "ImTr/sqrt3")) + 0.0 for t in tr])
+    retr = np.array([_snap(-t.real, "ReTr", root) for t in tr])
+    imtr = np.array([s3 * (_snap(-t.imag / s3, "ImTr/sqrt3", root)) + 0.0 for t in tr])
     return retr, imtr
 
 
+def _kronecker_product(name: str) -> GroupTable:
+    """The group {g (x) h} from the Cayley tables of two SU(2) groups A and B.
+
+    (g, h) and (-g, -h) give the same matrix, so an element is the pair with the
+    smaller A index of the two; elements are numbered in (A index, B index)
+    order, which puts the identity (0, 0) first."""
+    (na, nb), order = PRODUCTS[name]
+    A, B = generate(na), generate(nb)
+    neg_a = int(np.flatnonzero(np.isclose(A.retr, 2.0))[0])  # -1 in A: ReTr = -Tr = 2
+    neg_b = int(np.flatnonzero(np.isclose(B.retr, 2.0))[0])
+    negA, negB = A.mult[neg_a], B.mult[neg_b]  # index of -g, -h
+    ii, jj = np.meshgrid(np.arange(A.P), np.arange(B.P), indexing="ij")
+    keep = ii < negA[ii]  # the representative of {(g, h), (-g, -h)}
+    I, J = ii[keep], jj[keep]
+    P = I.size
+    if P != order:
+        raise RuntimeError(f"{name}: {P} elements, expected {order}")
+    canon = np.full((A.P, B.P), -1, np.int64)
+    canon[I, J] = np.arange(P)
+    canon[negA[I], negB[J]] = np.arange(P)
+    mult = canon[A.mult[I[:, None], I[None, :]], B.mult[J[:, None], J[None, :]]].astype(np.int32)
+    # ReTr = -Tr(g) Tr(h) = -(ReTr_A)(ReTr_B): one IEEE product of two snapped values.
+    retr = -(A.retr[I] * B.retr[J]) + 0.0
+    imtr = np.zeros(P)
+    mats = np.einsum("nab,ncd->nacbd", A.mats[I], B.mats[J]).reshape(P, 4, 4)
+    return GroupTable(name, P, retr, imtr, mult, mats)
+
+
 def generate(name: str) -> GroupTable:
+    if name in PRODUCTS:
+        return _kronecker_product(name)
     gens_fn, order = GROUPS[name]
     gens = gens_fn()
     n = gens[0].shape[0]
@@ -152,7 +198,7 @@ def generate(name: str) -> GroupTable:
     for r in range(1, P):  # BFS order: parent row is already filled
         mult[r] = left[via[r]][mult[parent[r]]]
     mats = np.stack(elems)
-    retr, imtr = _canonical_traces(mats)
+    retr, imtr = _canonical_traces(mats, root=2.0 if name == "BO" else 5.0)
     return GroupTable(name, P, retr, imtr, mult, mats)
 
 

@@ -7,9 +7,9 @@ Run in a container where the reference sources exist (REF_DIR, default
 
 It builds oracle/_ref/ (oracle/build_ref.sh) and writes:
 
-* tables_iso.npz -- for each generated table (S1080, BI, BT): an explicit
+* tables_iso.npz -- for each generated table (S1080, BI, BT, BO): an explicit
   trace-preserving isomorphism pi onto the reference's own file
-  (mys1080-v4, myBI, myBT), the SHA-256 of the reference's Cayley table and of
+  (mys1080-v4, myBI, myBT, myBO), the SHA-256 of the reference's Cayley table and of
   ours, and the largest trace difference.  Tests rebuild the reference table
   from ours through pi and compare hashes, so the reference file itself is
   not needed at test time.
@@ -43,7 +43,7 @@ from dym_symanzik_action_gb300.schedule import schedule  # noqa: E402
 from oracle.oracle import OracleGroup, OracleLattice, RefHarness  # noqa: E402
 
 REF_DIR = os.environ.get("REF_DIR", "/root/reference")
-REF_TABLES = {"S1080": "mys1080-v4", "BI": "myBI", "BT": "myBT"}
+REF_TABLES = {"S1080": "mys1080-v4", "BI": "myBI", "BT": "myBT", "BO": "myBO"}
 
 # name: (group, D, Nt, Nx, (beta0, beta1, beta2), start, seed, nhit, pool_all, nsweeps, wl_nx, wl_nt)
 SWEEP_CASES = {

@@ -1,6 +1,8 @@
-"""Group tables: the generated S(1080), BI and BT tables are groups, have
+"""Group tables: the generated S(1080), BI, BT and BO tables are groups, have
 class-constant traces, and are trace-preserving isomorphic to the reference's
-own table files (pinned by tests/golden/tables_iso.npz)."""
+own table files (pinned by tests/golden/tables_iso.npz); the SU(4) table
+BI (x) BO (order 2880) is a group of 4x4 special unitary matrices with
+class-constant traces."""
 import hashlib
 
 import numpy as np
@@ -14,13 +16,13 @@ def sha(a):
     return hashlib.sha256(np.ascontiguousarray(a, np.int32).tobytes()).hexdigest()
 
 
-@pytest.fixture(scope="module", params=["BT", "BI", "S1080"])
+@pytest.fixture(scope="module", params=["BT", "BO", "BI", "S1080", "BIxBO"])
 def tab(request):
     return tables.generate(request.param)
 
 
 def test_order_and_identity(tab):
-    P = {"BT": 24, "BI": 120, "S1080": 1080}[tab.name]
+    P = {"BT": 24, "BO": 48, "BI": 120, "S1080": 1080, "BIxBO": 2880}[tab.name]
     assert tab.P == P
     ar = np.arange(P)
     assert (tab.mult[0] == ar).all() and (tab.mult[:, 0] == ar).all()
@@ -65,6 +67,8 @@ def test_isomorphic_to_reference_table(tab):
     Cayley table from ours through pi reproduces its SHA-256."""
     iso = golden("tables_iso.npz")
     name = tab.name
+    if f"{name}_pi" not in iso.files:
+        pytest.skip(f"the reference ships no table of {name}")
     assert sha(tab.mult) == str(iso[f"{name}_our_sha"])
     pi = iso[f"{name}_pi"].astype(np.int64)
     P = tab.P
@@ -82,6 +86,22 @@ def test_class_statistics():
     nn = s.retr[s.retr > lo].min()
     assert lo == -3.0 and abs(nn + (1 + 5 ** 0.5) / 2) < 1e-15
     assert int(((s.retr > lo) & (s.retr < nn + 1e-6)).sum()) == 72
+
+
+def test_su4_table():
+    t = tables.generate("BIxBO")
+    n = t.mats.shape[1]
+    assert n == 4
+    assert np.abs(np.linalg.det(t.mats) - 1).max() < 1e-12
+    eye = np.eye(4)
+    assert np.abs(t.mats @ np.conj(np.swapaxes(t.mats, 1, 2)) - eye).max() < 1e-12
+    assert t.retr[0] == -4.0 and (t.imtr == 0).all()
+    lo = t.retr.min()
+    nn = t.retr[t.retr > lo].min()
+    assert abs(nn + 1 + 5 ** 0.5) < 1e-15  # -Tr g Tr h with Tr g = golden ratio, h = 1
+    assert int(((t.retr > lo) & (t.retr < nn + 1e-6)).sum()) == 12
+    assert len(set(t.retr)) == 23
+    assert sha(t.mult) == sha(tables.generate("BIxBO").mult)  # deterministic
 
 
 def test_written_file_round_trips(tmp_path):
