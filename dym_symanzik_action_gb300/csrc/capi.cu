@@ -95,32 +95,49 @@ static int build_sub_table(dym_chain* c, const std::vector<uint16_t>& pool) {
   return DYM_OK;
 }
 
-// The mixed-precision kernel applies on top of the sub-table path when element
-// ids fit 11 bits and classes 5 bits of a packed entry, and its shared tables
-// fit the opt-in limit.
+// The mixed-precision kernel applies on top of the sub-table path when the
+// classes fit 5 bits and its shared tables the opt-in limit: with 16-bit
+// packed entries (element in 11 bits) for groups of order <= 2048, with 32-bit
+// entries above.
+static size_t mixed_entry_bytes(const Group& g) { return g.P > kMixedMaxP ? 4 : 2; }
+
 static bool mixed_eligible(const Group& g, uint32_t npool, int device) {
-  if (g.P > kMixedMaxP || g.ncls > kMixedMaxCls || g.ncls < 1) return false;
+  if (g.ncls > kMixedMaxCls || g.ncls < 1) return false;
   int optin = 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) return false;
-  return mixed_smem_bytes(g.P, npool) <= (size_t)optin;
+  return mixed_smem_bytes(g.P, npool, mixed_entry_bytes(g)) <= (size_t)optin;
 }
 
 static int build_mixed_tables(dym_chain* c, const std::vector<uint16_t>& pool) {
   const Group& g = *c->grp->g;
   const uint32_t P = g.P, np = (uint32_t)pool.size();
-  std::vector<uint16_t> psub((size_t)np * P);
-  for (uint32_t k = 0; k < np; ++k)
-    for (uint32_t u = 0; u < P; ++u) {
-      const uint16_t e = g.mult[(size_t)u * P + pool[k]];
-      psub[(size_t)k * P + u] = (uint16_t)(e | (g.cls[e] << 11));
-    }
+  const bool wide = mixed_entry_bytes(g) == 4;
+  if (wide) {
+    std::vector<uint32_t> psub((size_t)np * P);
+    for (uint32_t k = 0; k < np; ++k)
+      for (uint32_t u = 0; u < P; ++u) {
+        const uint32_t e = g.mult[(size_t)u * P + pool[k]];
+        psub[(size_t)k * P + u] = e | ((uint32_t)g.cls[e] << 16);
+      }
+    DYM_CUDA(dmalloc(&c->dev.psub32, psub.size()), "cudaMalloc(psub32)");
+    DYM_CUDA(copy_sync(c->dev.psub32, psub.data(), psub.size() * 4, cudaMemcpyHostToDevice, c->stream),
+             "upload psub32");
+  } else {
+    std::vector<uint16_t> psub((size_t)np * P);
+    for (uint32_t k = 0; k < np; ++k)
+      for (uint32_t u = 0; u < P; ++u) {
+        const uint16_t e = g.mult[(size_t)u * P + pool[k]];
+        psub[(size_t)k * P + u] = (uint16_t)(e | (g.cls[e] << 11));
+      }
+    DYM_CUDA(dmalloc(&c->dev.psub, psub.size()), "cudaMalloc(psub)");
+    DYM_CUDA(copy_sync(c->dev.psub, psub.data(), psub.size() * 2, cudaMemcpyHostToDevice, c->stream), "upload psub");
+  }
+  c->dev.mixed_wide = wide;
   const int S = fix_shift(g, c->p.D);
   std::vector<int32_t> cfix(kMixedMaxCls, 0);
   for (int k = 0; k < g.ncls; ++k) cfix[k] = (int32_t)std::llrint(std::ldexp(g.cls_val[k], S));
-  DYM_CUDA(dmalloc(&c->dev.psub, psub.size()), "cudaMalloc(psub)");
   DYM_CUDA(dmalloc(&c->dev.cls8, (size_t)P), "cudaMalloc(cls8)");
   DYM_CUDA(dmalloc(&c->dev.cfix, (size_t)kMixedMaxCls), "cudaMalloc(cfix)");
-  DYM_CUDA(copy_sync(c->dev.psub, psub.data(), psub.size() * 2, cudaMemcpyHostToDevice, c->stream), "upload psub");
   DYM_CUDA(copy_sync(c->dev.cls8, g.cls.data(), P, cudaMemcpyHostToDevice, c->stream), "upload cls8");
   DYM_CUDA(copy_sync(c->dev.cfix, cfix.data(), kMixedMaxCls * 4, cudaMemcpyHostToDevice, c->stream), "upload cfix");
   // Packed coordinates of every schedule entry (8 bits per axis).
@@ -220,6 +237,7 @@ static void chain_release(dym_chain* c) {
   cudaFree(c->dev.counters);
   cudaFree(c->dev.sub);
   cudaFree(c->dev.psub);
+  cudaFree(c->dev.psub32);
   cudaFree(c->dev.cls8);
   cudaFree(c->dev.cfix);
   cudaFree(c->dev.xyz);
@@ -385,7 +403,7 @@ int dym_chain_create(const dym_group* gh, const dym_chain_params* p, dym_chain**
       if (rc) return rc;
       int optin = 0;
       DYM_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device), "attribute");
-      if (vt_smem_bytes(g.P, d.npool) <= (size_t)optin) {
+      if (!d.mixed_wide && vt_smem_bytes(g.P, d.npool) <= (size_t)optin) {
         rc = build_vt_tables(c.get(), pool);
         if (rc) return rc;
       }
@@ -432,7 +450,10 @@ int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
       cudaError_t e;
       switch (kernel) {
         case DYM_KERNEL_MIXED_VALUES: e = launch_sweep_vt(c->p.D, s.phase_dir[p], a, c->dev.vsub, c->stream); break;
-        case DYM_KERNEL_MIXED: e = launch_sweep_mixed(c->p.D, s.phase_dir[p], a, c->dev.psub, c->stream); break;
+        case DYM_KERNEL_MIXED:
+          e = c->dev.mixed_wide ? launch_sweep_mixed_wide(c->p.D, s.phase_dir[p], a, c->dev.psub32, c->stream)
+                                : launch_sweep_mixed(c->p.D, s.phase_dir[p], a, c->dev.psub, c->stream);
+          break;
         case DYM_KERNEL_SHARED: e = launch_sweep_sub(c->p.D, s.phase_dir[p], a, c->dev.sub, c->stream); break;
         default: e = launch_sweep_direct(c->p.D, s.phase_dir[p], a, c->stream);
       }
@@ -645,6 +666,11 @@ static void batch_release_device(dym_batch* b) {
 }
 
 // Lay out tables, descriptors and per-slot tile lists for the current chains.
+
+// The batched mixed kernel packs 16-bit entries: it takes a chain whose own
+// sweep uses the mixed kernel on a group of order <= 2048.
+static bool batch_mixed_chain(const dym_chain* c) { return c->dev.mixed_ok && !c->dev.mixed_wide; }
+
 static int batch_build(dym_batch* b) {
   batch_release_device(b);
   const size_t nc = b->chains.size();
@@ -652,7 +678,7 @@ static int batch_build(dym_batch* b) {
   b->bg.n = (int)b->groups.size();
   size_t off = 0;
   auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
-  b->mixed = std::all_of(b->chains.begin(), b->chains.end(), [](const dym_chain* c) { return c->dev.mixed_ok; });
+  b->mixed = std::all_of(b->chains.begin(), b->chains.end(), batch_mixed_chain);
   std::vector<int> shift(b->groups.size(), 0);
   for (size_t g = 0; g < b->groups.size(); ++g) {
     const Group& G = *b->groups[g];
@@ -840,7 +866,7 @@ int dym_batch_set_tuning(dym_batch* b, const dym_batch_tuning* t) {
       t->grid_per_sm < 1)
     return fail(DYM_EINVAL, "tuning: tile a multiple of 32, threads 128, 256 or 512, grid_per_sm >= 1");
   if (t->threads == 512 && !b->mixed && !b->chains.empty() &&
-      !std::all_of(b->chains.begin(), b->chains.end(), [](const dym_chain* c) { return c->dev.mixed_ok; }))
+      !std::all_of(b->chains.begin(), b->chains.end(), batch_mixed_chain))
     return fail(DYM_EINVAL, "tuning: 512 threads need the mixed-precision batch kernel");
   if (t->tile != b->tune.tile) b->dirty = true;
   b->tune = *t;
@@ -967,7 +993,7 @@ int dym_batch_autotune(dym_batch* b, int32_t nhit, int32_t nsweeps_per_trial, dy
   float win_ms = 1e30f;
   int rc = DYM_OK;
   const bool all_mixed =
-      std::all_of(b->chains.begin(), b->chains.end(), [](const dym_chain* c) { return c->dev.mixed_ok; });
+      std::all_of(b->chains.begin(), b->chains.end(), batch_mixed_chain);
   for (int threads : {128, 256, 512})
     for (int tile : {128, 256, 512, 1024})
       for (int gps : {1, 2}) {

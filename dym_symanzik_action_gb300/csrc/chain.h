@@ -49,8 +49,11 @@ struct ChainDev {
   unsigned long long* counters = nullptr;
   uint16_t* sub = nullptr;     // sub[k*P + u] = u * pool[k] (shared sub-table kernel)
   bool sub_ok = false;
-  // Mixed-precision kernel: psub[k*P + u] = (u * pool[k]) | class << 11.
+  // Mixed-precision kernel: psub[k*P + u] = (u * pool[k]) | class << 11 for
+  // P <= 2048; otherwise psub32[k*P + u] = (u * pool[k]) | class << 16.
   uint16_t* psub = nullptr;
+  uint32_t* psub32 = nullptr;
+  bool mixed_wide = false;
   uint8_t* cls8 = nullptr;
   int32_t* cfix = nullptr;
   int fix_shift = 0;
@@ -70,17 +73,24 @@ cudaError_t launch_sweep_sub(int D, int dir, const SweepArgs& a, const uint16_t*
 size_t sub_smem_bytes(uint32_t P, uint32_t npool);
 // Launch one colour phase of the mixed-precision shared sub-table sweep.
 cudaError_t launch_sweep_mixed(int D, int dir, const SweepArgs& a, const uint16_t* psub, cudaStream_t s);
-size_t mixed_smem_bytes(uint32_t P, uint32_t npool);
+cudaError_t launch_sweep_mixed_wide(int D, int dir, const SweepArgs& a, const uint32_t* psub, cudaStream_t s);
+size_t mixed_smem_bytes(uint32_t P, uint32_t npool, size_t entry = 2);
 cudaError_t launch_sweep_vt(int D, int dir, const SweepArgs& a, const int16_t* vsub, cudaStream_t s);
 size_t vt_smem_bytes(uint32_t P, uint32_t npool);
 constexpr int kMixedMaxCls = 32;    // classes addressable by the 5 high bits of a psub entry
-constexpr uint32_t kMixedMaxP = 2048;  // element ids in the 11 low bits
+constexpr uint32_t kMixedMaxP = 2048;  // 16-bit packed entries: element ids in the 11 low bits
 constexpr int kMixedMaxExtent = 256;   // coordinates packed 8 bits per axis
 constexpr int kMixedMaxThreads = 512;
 cudaError_t launch_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uint64_t seed, cudaStream_t s);
 cudaError_t launch_fill(uint16_t* links, size_t n, uint16_t v, cudaStream_t s);
 cudaError_t launch_staples(int D, int dir, const SweepArgs& a, const uint32_t* sites, uint32_t n, uint16_t* out,
                            cudaStream_t s);
+// Shared memory of k_sweep_mixed: ReTr (FP64) | class values | inverses | packed
+// sub-table (entries of `entry` bytes; 32-bit entries start on 16 bytes) | classes.
+__host__ __device__ inline size_t mixed_psub_offset(uint32_t P, size_t entry) {
+  const size_t o = (size_t)P * 8 + kMixedMaxCls * 4 + (size_t)P * 2;
+  return entry == 2 ? o : (o + 15) / 16 * 16;
+}
 
 // LLR (interval-restricted sweeps with Robbins-Monro updates): per-chain
 // state in device memory, updated by the commit kernel after every colour

@@ -118,16 +118,19 @@ __global__ void __launch_bounds__(256) k_sweep_sub(SweepArgs a, const uint16_t* 
 }
 
 // Shared memory: ReTr (FP64) | class values (int32 fixed point) | inverses |
-// packed sub-table | element classes.
-template <int D, int DIR>
-__global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_mixed(SweepArgs a, const uint16_t* __restrict__ psub) {
+// packed sub-table (entries of type E, starting at mixed_psub_offset) |
+// element classes.
+template <int D, int DIR, class E>
+__global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_mixed(SweepArgs a, const E* __restrict__ psub) {
   extern __shared__ __align__(16) unsigned char smem[];
   double* s_retr = reinterpret_cast<double*>(smem);
   int32_t* s_cfix = reinterpret_cast<int32_t*>(s_retr + a.P);
   uint16_t* s_inv = reinterpret_cast<uint16_t*>(s_cfix + kMixedMaxCls);
-  uint16_t* s_psub = s_inv + a.P;
+  E* s_psub = reinterpret_cast<E*>(smem + mixed_psub_offset(a.P, sizeof(E)));
   uint8_t* s_cls = reinterpret_cast<uint8_t*>(s_psub + (size_t)a.npool * a.P);
-  stage_sub_tables(a.retr, a.inv, psub, a.P, a.npool, s_retr, s_inv, s_psub);
+  // The staging copies npool * P entries as halfwords.
+  stage_sub_tables(a.retr, a.inv, reinterpret_cast<const uint16_t*>(psub), a.P, a.npool * (uint32_t)(sizeof(E) / 2),
+                   s_retr, s_inv, reinterpret_cast<uint16_t*>(s_psub));
   for (uint32_t t = threadIdx.x; t < a.P; t += blockDim.x) s_cls[t] = a.cls8[t];
   if (threadIdx.x < kMixedMaxCls) s_cfix[threadIdx.x] = a.cfix[threadIdx.x];
   __syncthreads();
@@ -135,8 +138,8 @@ __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_mixed(SweepArgs a
   unsigned hits = 0, accs = 0, rechecks = 0;
   float max_err = 0.0f;
   for (uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x; tid < a.n; tid += gridDim.x * blockDim.x)
-    visit_mixed<D, DIR>(a, a.sites[tid], a.xyz[tid], a.sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs,
-                        rechecks, max_err);
+    visit_mixed<D, DIR, E>(a, a.sites[tid], a.xyz[tid], a.sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs,
+                           rechecks, max_err);
   flush_counters(a.counters, hits, accs, rechecks);
   flush_max_err(a.counters + 3, max_err);
 }
@@ -254,15 +257,15 @@ cudaError_t sub_dispatch(int dir, const SweepArgs& a, const uint16_t* sub, cudaS
   return cudaGetLastError();
 }
 
-template <int D>
-cudaError_t mixed_dispatch(int dir, const SweepArgs& a, const uint16_t* psub, cudaStream_t s) {
-  const size_t smem = mixed_smem_bytes(a.P, a.npool);
-  void (*fn)(SweepArgs, const uint16_t*) = nullptr;
+template <int D, class E>
+cudaError_t mixed_dispatch(int dir, const SweepArgs& a, const E* psub, cudaStream_t s) {
+  const size_t smem = mixed_smem_bytes(a.P, a.npool, sizeof(E));
+  void (*fn)(SweepArgs, const E*) = nullptr;
   switch (dir) {
-    case 0: fn = k_sweep_mixed<D, 0>; break;
-    case 1: fn = k_sweep_mixed<D, 1>; break;
-    case 2: if (D > 2) fn = k_sweep_mixed<D, (D > 2 ? 2 : 0)>; break;
-    case 3: if (D > 3) fn = k_sweep_mixed<D, (D > 3 ? 3 : 0)>; break;
+    case 0: fn = k_sweep_mixed<D, 0, E>; break;
+    case 1: fn = k_sweep_mixed<D, 1, E>; break;
+    case 2: if (D > 2) fn = k_sweep_mixed<D, (D > 2 ? 2 : 0), E>; break;
+    case 3: if (D > 3) fn = k_sweep_mixed<D, (D > 3 ? 3 : 0), E>; break;
   }
   if (!fn) return cudaErrorInvalidValue;
   if (smem > 48 * 1024) {
@@ -329,8 +332,8 @@ size_t sub_smem_bytes(uint32_t P, uint32_t npool) {
   return (size_t)P * 8 + (size_t)P * 2 + (size_t)npool * P * 2 + 16;
 }
 
-size_t mixed_smem_bytes(uint32_t P, uint32_t npool) {
-  return (size_t)P * 8 + kMixedMaxCls * 4 + (size_t)P * 2 + (size_t)npool * P * 2 + (size_t)P + 16;
+size_t mixed_smem_bytes(uint32_t P, uint32_t npool, size_t entry) {
+  return mixed_psub_offset(P, entry) + (size_t)npool * P * entry + (size_t)P + 16;
 }
 
 size_t vt_smem_bytes(uint32_t P, uint32_t npool) {
@@ -343,7 +346,12 @@ cudaError_t launch_sweep_vt(int D, int dir, const SweepArgs& a, const int16_t* v
 }
 
 cudaError_t launch_sweep_mixed(int D, int dir, const SweepArgs& a, const uint16_t* psub, cudaStream_t s) {
-  if (D == 4) return mixed_dispatch<4>(dir, a, psub, s);  // four dimensions only, as launch_sweep_sub
+  if (D == 4) return mixed_dispatch<4, uint16_t>(dir, a, psub, s);  // four dimensions only, as launch_sweep_sub
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_sweep_mixed_wide(int D, int dir, const SweepArgs& a, const uint32_t* psub, cudaStream_t s) {
+  if (D == 4) return mixed_dispatch<4, uint32_t>(dir, a, psub, s);
   return cudaErrorInvalidValue;
 }
 

@@ -92,8 +92,9 @@ __device__ __forceinline__ void visit_sub(const SweepArgs& a, uint32_t i, uint32
 // Mixed-precision visit of link (i, DIR): the decisions of visit_sub, taken
 // without FP64 arithmetic except near the threshold.
 //
-// A packed sub-table entry holds the element (11 low bits) and its ReTr class
-// (5 high bits); the class values are staged as int32 fixed point c * 2^S.  A
+// A packed sub-table entry holds the element and its ReTr class (16-bit
+// entries: 11 + 5 bits, groups of order <= 2048; 32-bit entries: 16 + 16 bits,
+// any order); the class values are staged as int32 fixed point c * 2^S.  A
 // proposal's action change is then dS_fast = (b1 dR + b2 dM) 2^-S with dR, dM
 // exact integer differences of the plaquette and rectangle sums, evaluated in
 // FP32.  a.dmargin bounds |dS_fast - dS_fp64| (class-value rounding, FP32
@@ -131,31 +132,40 @@ __device__ __forceinline__ void mixed_prepare(const SweepArgs& a, uint32_t i, ui
   for (int j = NS; j < NT; ++j) M += (uint32_t)s_cfix[s_cls[u[j]]];
 }
 
+// Packed sub-table entries: the element in the low kBits bits, its class
+// above.  16-bit entries hold ids below 2048; 32-bit entries any uint16 id.
+template <class E>
+struct Packed {
+  static constexpr uint32_t kBits = sizeof(E) == 2 ? 11u : 16u;
+  static constexpr uint32_t kMask = (1u << kBits) - 1u;
+};
+
 // Second half: the nhit hits of link (i, DIR) from the shared tables, starting
 // from mixed_prepare's state; the link is written when it changed.
-template <int D, int DIR>
+template <int D, int DIR, class E = uint16_t>
 __device__ __forceinline__ void mixed_hits(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
-                                           const uint16_t* s_psub, const int32_t* s_cfix, uint32_t* u, uint32_t b,
+                                           const E* s_psub, const int32_t* s_cfix, uint32_t* u, uint32_t b,
                                            uint32_t R, uint32_t M, unsigned& hits, unsigned& accs,
                                            unsigned& rechecks, float& max_err) {
   constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
+  constexpr uint32_t kBits = Packed<E>::kBits, kMask = Packed<E>::kMask;
   const uint32_t b0 = b;
   double oldact = 0.0;
   bool old_ok = false;
   for (int h = 0; h < a.nhit; ++h) {
     const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_METRO);
-    const uint16_t* row = s_psub + dym_pick(r.v[0], a.npool) * a.P;
+    const E* row = s_psub + dym_pick(r.v[0], a.npool) * a.P;
     uint32_t e[NT];
     uint32_t Rn = 0, Mn = 0;
 #pragma unroll
     for (int j = 0; j < NS; ++j) {
       e[j] = row[u[j]];
-      Rn += (uint32_t)s_cfix[e[j] >> 11];
+      Rn += (uint32_t)s_cfix[e[j] >> kBits];
     }
 #pragma unroll
     for (int j = NS; j < NT; ++j) {
       e[j] = row[u[j]];
-      Mn += (uint32_t)s_cfix[e[j] >> 11];
+      Mn += (uint32_t)s_cfix[e[j] >> kBits];
     }
     const float dR = (float)(int32_t)(Rn - R), dM = (float)(int32_t)(Mn - M);
     const float ds = __fmaf_rn(a.b2f, dM, __fmul_rn(a.b1f, dR)) * a.dscale;
@@ -181,9 +191,9 @@ __device__ __forceinline__ void mixed_hits(const SweepArgs& a, uint32_t i, uint3
       }
       double r1n = 0, m1n = 0;
 #pragma unroll
-      for (int j = 0; j < NS; ++j) r1n = DYM_ADD(r1n, s_retr[e[j] & 0x7FFu]);
+      for (int j = 0; j < NS; ++j) r1n = DYM_ADD(r1n, s_retr[e[j] & kMask]);
 #pragma unroll
-      for (int j = NS; j < NT; ++j) m1n = DYM_ADD(m1n, s_retr[e[j] & 0x7FFu]);
+      for (int j = NS; j < NT; ++j) m1n = DYM_ADD(m1n, s_retr[e[j] & kMask]);
       const double newact = dym_action(a.beta0, a.beta1, a.beta2, r1n, m1n);
       acc = dym_accept_fast(oldact, newact, dym_u53(r.v[1], r.v[2]));
       max_err = fmaxf(max_err, fabsf(ds - (float)DYM_SUB(newact, oldact)));
@@ -193,9 +203,9 @@ __device__ __forceinline__ void mixed_hits(const SweepArgs& a, uint32_t i, uint3
     }
     ++hits;
     if (acc) {
-      b = row[b] & 0x7FFu;
+      b = row[b] & kMask;
 #pragma unroll
-      for (int j = 0; j < NT; ++j) u[j] = e[j] & 0x7FFu;
+      for (int j = 0; j < NT; ++j) u[j] = e[j] & kMask;
       R = Rn;
       M = Mn;
       old_ok = exact;
@@ -218,16 +228,16 @@ __device__ __forceinline__ void flush_counters(unsigned long long* ctr, unsigned
 }
 
 
-template <int D, int DIR>
+template <int D, int DIR, class E = uint16_t>
 __device__ __forceinline__ void visit_mixed(const SweepArgs& a, uint32_t i, uint32_t xyz, uint32_t sweep,
-                                            const double* s_retr, const uint16_t* s_inv, const uint16_t* s_psub,
+                                            const double* s_retr, const uint16_t* s_inv, const E* s_psub,
                                             const uint8_t* s_cls, const int32_t* s_cfix, unsigned& hits,
                                             unsigned& accs, unsigned& rechecks, float& max_err) {
   constexpr int NT = 8 * (D - 1);
   uint32_t u[NT];
   uint32_t b, R, M;
   mixed_prepare<D, DIR>(a, i, xyz, s_inv, s_cls, s_cfix, u, b, R, M);
-  mixed_hits<D, DIR>(a, i, sweep, s_retr, s_psub, s_cfix, u, b, R, M, hits, accs, rechecks, max_err);
+  mixed_hits<D, DIR, E>(a, i, sweep, s_retr, s_psub, s_cfix, u, b, R, M, hits, accs, rechecks, max_err);
 }
 
 // Value-table form of the mixed visit.  The shared table holds, for pool

@@ -1,9 +1,11 @@
 """The SU(4) subgroup BI (x) BO of order 2880 -- the order of the reference's
 largest shipped SU(4) table, element ids beyond 11 bits -- through every
 engine path that takes it, bit for bit against the oracle: Metropolis sweeps
-at each precision setting (the mixed kernel packs 11-bit ids, so "mixed" runs
-the FP64 shared-table kernel and reports it), observables, the batched
-ensemble next to SU(2) chains, and LLR on either axis."""
+at each precision setting (the mixed kernel with 32-bit packed sub-table
+entries, the FP64 shared-table kernel, the FP64 direct kernel), observables,
+the batched ensemble next to SU(2) chains (its mixed kernel packs 16-bit
+entries, so this batch runs the FP64 shared-table batch kernel), and LLR on
+either axis."""
 import numpy as np
 import pytest
 
@@ -16,7 +18,7 @@ from test_llr import nplaq, run_oracle
 pytestmark = pytest.mark.gpu
 
 NAME = "BIxBO"
-KERNEL_DIRECT, KERNEL_SHARED = 1, 2
+KERNEL_DIRECT, KERNEL_SHARED, KERNEL_MIXED = 1, 2, 3
 
 
 @pytest.fixture(scope="module")
@@ -32,7 +34,7 @@ def test_group_loads_with_the_shared_table_path(su4):
 
 
 @pytest.mark.parametrize("precision,kernel", [("fp64", KERNEL_DIRECT), ("shared", KERNEL_SHARED),
-                                              ("mixed", KERNEL_SHARED)])
+                                              ("mixed", KERNEL_MIXED)])
 def test_sweeps_and_observables_match_oracle(engine, su4, precision, kernel):
     g, og = su4
     D, Nt, Nx, beta, nhit, seed = 4, 4, 8, (0.0, 2.0, -0.1), 10, 2880
@@ -96,3 +98,29 @@ def test_llr_matches_oracle(engine, su4, case):
     assert (res.hits, res.accepts, res.sweeps) == (r["hits"], r["accepts"], r["sweeps"])
     assert res.S1 == r["S1"] and res.S2 == r["S2"]
     assert (lat.links.ravel() == L.links).all()
+
+
+def test_mixed_kernel_rechecks_and_matches_fp64_at_16x16x16x8(engine, su4):
+    """Hot 16^3 x 8 at beta = (0, 2, -0.1), NHIT 10, 5 sweeps: the mixed kernel
+    (32-bit entries) re-evaluates a small fraction of the hits in FP64, stays
+    within its error bound, and gives the FP64 kernel's configuration; after a
+    cold start (moves rare) it keeps the element-table kernel, the value-table
+    kernel taking only 16-bit entries."""
+    g, _ = su4
+    D, Nt, Nx, beta, nhit = 4, 8, 16, (0.0, 2.0, -0.1), 10
+    res = {}
+    for precision in ("mixed", "fp64"):
+        lat = engine.Lattice(g, D, Nt, Nx, *beta, 4242, start="hot", precision=precision)
+        st = lat.update(5, nhit)
+        res[precision] = (lat.links.ravel(), st)
+    (lm, sm), (lf, sf) = res["mixed"], res["fp64"]
+    assert sm.kernel == KERNEL_MIXED and sf.kernel == KERNEL_DIRECT
+    assert (lm == lf).all() and sm.accepts == sf.accepts
+    assert 0 < sm.rechecks < 1e-3 * sm.hits
+    assert 0.0 <= sm.max_ds_err < 1e-3
+    cold = engine.Lattice(g, D, Nt, Nx, 0.0, 4.0, -0.1, 7, start="cold", precision="mixed")
+    ref = engine.Lattice(g, D, Nt, Nx, 0.0, 4.0, -0.1, 7, start="cold", precision="fp64")
+    for _ in range(2):
+        assert cold.update(1, nhit).kernel == KERNEL_MIXED
+        ref.update(1, nhit)
+        assert (cold.links == ref.links).all()
