@@ -97,9 +97,9 @@ __host__ __device__ inline size_t mixed_psub_offset(uint32_t P, size_t entry) {
 // phase.  Energies are exact: integer class histograms of all plaquettes (h[0])
 // and rectangles (h[1]), one FP64 dot product with the class values.
 constexpr int kLlrMaxCls = 32;
-// The LLR propose kernel runs 256-thread blocks whose warps take 32-link tiles
+// The LLR propose kernel runs 512-thread blocks whose warps take 32-link tiles
 // independently; each warp's class deltas sit at the front of shared memory.
-constexpr int kLlrWarps = 8;
+constexpr int kLlrWarps = 16;
 constexpr int kLlrTile = 32;
 constexpr int kLlrDeltaBytes = kLlrWarps * 2 * kLlrMaxCls * 4;
 constexpr int kLlrMaxPhases = 256;                   // colour phases per sweep with their own drive-in fraction

@@ -382,7 +382,9 @@ __device__ __forceinline__ bool llr_weight_accept(double x, uint32_t r1, uint32_
 // per hit): nhit hits with weight exp(-a dE_w - bg dE_bg), or, in drive-in
 // mode, greedy moves of the link's running energy towards emid.  The link is
 // written in place and its plaquette/rectangle class changes are added to
-// s_delta; returns the value before the visit.
+// s_delta; returns the value before the visit.  The classes of the initial
+// u_j are kept packed, 5 bits each, for the class changes, and the two hit
+// loops are separate so that neither holds the other's state.
 template <int D, int DIR>
 __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
                                               const uint16_t* s_inv, const uint16_t* s_sub, const uint16_t* s_cls,
@@ -390,6 +392,8 @@ __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, ui
                                               const LlrDrive2& d2, bool drive, uint32_t qthr, int* s_delta,
                                               unsigned& hits, unsigned& accs) {
   constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
+  constexpr int NW = (NT + 5) / 6;  // words of six 5-bit classes
+  static_assert(kLlrMaxCls <= 32, "classes are packed in 5 bits");
   SiteGeo<D> geo;
   site_geo<D>(i, a.Nt, a.Nx, geo);
   GlobalTab T{a.mult, s_inv, a.P};
@@ -403,72 +407,98 @@ __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, ui
   const uint32_t b0 = b;
 #pragma unroll
   for (int j = 0; j < NT; ++j) u[j] = T.mul(u[j], b);
-  uint32_t u0[NT];
+  uint32_t c0[NW];
 #pragma unroll
-  for (int j = 0; j < NT; ++j) u0[j] = u[j];
+  for (int w = 0; w < NW; ++w) c0[w] = 0;
+#pragma unroll
+  for (int j = 0; j < NT; ++j) c0[j / 6] |= (uint32_t)s_cls[u[j]] << (5 * (j % 6));
   double r1 = 0, m1 = 0;
 #pragma unroll
   for (int j = 0; j < NS; ++j) r1 = DYM_ADD(r1, s_retr[u[j]]);
 #pragma unroll
   for (int j = NS; j < NT; ++j) m1 = DYM_ADD(m1, s_retr[u[j]]);
-  bool part = true;
-  if (drive) part = dym_hit_random(a.seed, sweep, i, DIR, 0xFFFFFu, DYM_TAG_LLR).v[0] < qthr;
-  double cum = 0, cum2 = 0;
-  for (int h = 0; part && h < a.nhit; ++h) {
-    const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_LLR);
-    const uint16_t* row = s_sub + dym_pick(r.v[0], a.npool) * a.P;
-    uint32_t e[NT];
-    double r1n = 0, m1n = 0;
+  if (drive) {
+    if (dym_hit_random(a.seed, sweep, i, DIR, 0xFFFFFu, DYM_TAG_LLR).v[0] < qthr) {
+      double cum = 0, cum2 = 0;
+      for (int h = 0; h < a.nhit; ++h) {
+        const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_LLR);
+        const uint16_t* row = s_sub + dym_pick(r.v[0], a.npool) * a.P;
+        uint32_t e[NT];
+        double r1n = 0, m1n = 0;
 #pragma unroll
-    for (int j = 0; j < NS; ++j) {
-      e[j] = row[u[j]];
-      r1n = DYM_ADD(r1n, s_retr[e[j]]);
-    }
+        for (int j = 0; j < NS; ++j) {
+          e[j] = row[u[j]];
+          r1n = DYM_ADD(r1n, s_retr[e[j]]);
+        }
 #pragma unroll
-    for (int j = NS; j < NT; ++j) {
-      e[j] = row[u[j]];
-      m1n = DYM_ADD(m1n, s_retr[e[j]]);
-    }
-    const double dS1 = DYM_SUB(r1n, r1), dS2 = DYM_SUB(m1n, m1);
-    const double dEw = axis == 1 ? dS1 : dS2;
-    const double dEbg = axis == 1 ? dS2 : dS1;
-    bool acc;
-    if (drive && d2.dims == 2) {  // closer to the cell centre in normalised distance (llr2d.cpp:206-209)
-      const double c1 = DYM_ADD(E0, cum), c2 = DYM_ADD(d2.E0b, cum2);
-      const double x1 = DYM_MUL(DYM_SUB(c1, emid), d2.ihw0), y1 = DYM_MUL(DYM_SUB(c2, d2.emid2), d2.ihw1);
-      const double x2 = DYM_MUL(DYM_SUB(DYM_ADD(c1, dS1), emid), d2.ihw0);
-      const double y2 = DYM_MUL(DYM_SUB(DYM_ADD(c2, dS2), d2.emid2), d2.ihw1);
-      acc = DYM_ADD(DYM_MUL(x2, x2), DYM_MUL(y2, y2)) < DYM_ADD(DYM_MUL(x1, x1), DYM_MUL(y1, y1));
-    } else if (drive) {
-      const double Ec = DYM_ADD(E0, cum);
-      acc = fabs(DYM_SUB(DYM_ADD(Ec, dEw), emid)) < fabs(DYM_SUB(Ec, emid));
-    } else {
-      acc = llr_weight_accept(DYM_SUB(DYM_MUL(-aa, dEw), DYM_MUL(bg, dEbg)), r.v[1], r.v[2]);
-    }
-    ++hits;
-    if (acc) {
-      b = row[b];
+        for (int j = NS; j < NT; ++j) {
+          e[j] = row[u[j]];
+          m1n = DYM_ADD(m1n, s_retr[e[j]]);
+        }
+        const double dS1 = DYM_SUB(r1n, r1), dS2 = DYM_SUB(m1n, m1);
+        const double dEw = axis == 1 ? dS1 : dS2;
+        bool acc;
+        if (d2.dims == 2) {  // closer to the cell centre in normalised distance (llr2d.cpp:206-209)
+          const double c1 = DYM_ADD(E0, cum), c2 = DYM_ADD(d2.E0b, cum2);
+          const double x1 = DYM_MUL(DYM_SUB(c1, emid), d2.ihw0), y1 = DYM_MUL(DYM_SUB(c2, d2.emid2), d2.ihw1);
+          const double x2 = DYM_MUL(DYM_SUB(DYM_ADD(c1, dS1), emid), d2.ihw0);
+          const double y2 = DYM_MUL(DYM_SUB(DYM_ADD(c2, dS2), d2.emid2), d2.ihw1);
+          acc = DYM_ADD(DYM_MUL(x2, x2), DYM_MUL(y2, y2)) < DYM_ADD(DYM_MUL(x1, x1), DYM_MUL(y1, y1));
+        } else {
+          const double Ec = DYM_ADD(E0, cum);
+          acc = fabs(DYM_SUB(DYM_ADD(Ec, dEw), emid)) < fabs(DYM_SUB(Ec, emid));
+        }
+        ++hits;
+        if (acc) {
+          b = row[b];
 #pragma unroll
-      for (int j = 0; j < NT; ++j) u[j] = e[j];
-      r1 = r1n;
-      m1 = m1n;
-      cum = DYM_ADD(cum, dEw);
-      cum2 = DYM_ADD(cum2, dS2);
-      ++accs;
+          for (int j = 0; j < NT; ++j) u[j] = e[j];
+          r1 = r1n;
+          m1 = m1n;
+          cum = DYM_ADD(cum, dEw);
+          cum2 = DYM_ADD(cum2, dS2);
+          ++accs;
+        }
+      }
+    }
+  } else {
+    for (int h = 0; h < a.nhit; ++h) {
+      const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_LLR);
+      const uint16_t* row = s_sub + dym_pick(r.v[0], a.npool) * a.P;
+      uint32_t e[NT];
+      double r1n = 0, m1n = 0;
+#pragma unroll
+      for (int j = 0; j < NS; ++j) {
+        e[j] = row[u[j]];
+        r1n = DYM_ADD(r1n, s_retr[e[j]]);
+      }
+#pragma unroll
+      for (int j = NS; j < NT; ++j) {
+        e[j] = row[u[j]];
+        m1n = DYM_ADD(m1n, s_retr[e[j]]);
+      }
+      const double dS1 = DYM_SUB(r1n, r1), dS2 = DYM_SUB(m1n, m1);
+      const double dEw = axis == 1 ? dS1 : dS2;
+      const double dEbg = axis == 1 ? dS2 : dS1;
+      ++hits;
+      if (llr_weight_accept(DYM_SUB(DYM_MUL(-aa, dEw), DYM_MUL(bg, dEbg)), r.v[1], r.v[2])) {
+        b = row[b];
+#pragma unroll
+        for (int j = 0; j < NT; ++j) u[j] = e[j];
+        r1 = r1n;
+        m1 = m1n;
+        ++accs;
+      }
     }
   }
   if (b != b0) {
     *own = (uint16_t)b;
     // Class of b s_j equals the class of its conjugate s_j b = u_j.
 #pragma unroll
-    for (int j = 0; j < NS; ++j) {
-      atomicAdd(&s_delta[s_cls[u0[j]]], -1);
-      atomicAdd(&s_delta[s_cls[u[j]]], 1);
-    }
-#pragma unroll
-    for (int j = NS; j < NT; ++j) {
-      atomicAdd(&s_delta[kLlrMaxCls + s_cls[u0[j]]], -1);
-      atomicAdd(&s_delta[kLlrMaxCls + s_cls[u[j]]], 1);
+    for (int j = 0; j < NT; ++j) {
+      const int off = j < NS ? 0 : kLlrMaxCls;
+      atomicAdd(&s_delta[off + ((c0[j / 6] >> (5 * (j % 6))) & 31u)], -1);
+      atomicAdd(&s_delta[off + s_cls[u[j]]], 1);
     }
   }
   return b0;
