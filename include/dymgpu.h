@@ -51,8 +51,9 @@ extern "C" {
                               scaled and tested against -log(u2) in FP32; FP64
                               re-evaluation within a proven bound of the threshold.
                               Decisions identical to DYM_PREC_FP64 (four dimensions,
-                              tables with P <= 2048 and <= 32 ReTr classes; else
-                              as DYM_PREC_SHARED) */
+                              tables with <= 32 ReTr classes whose packed sub-table
+                              fits shared memory: 16-bit entries for P <= 2048,
+                              32-bit above; else as DYM_PREC_SHARED) */
 #define DYM_PREC_SHARED 2  /* FP64 decisions, hit loop served from the shared
                               sub-table (four dimensions, class-constant tables) */
 
