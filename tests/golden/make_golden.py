@@ -55,6 +55,7 @@ SWEEP_CASES = {
     "bt_6666_hot": ("BT", 4, 6, 6, (0.3, 1.0, 0.2), "hot", 3, 5, False, 3, 3, 3),
     "s1080_d3_844_hot": ("S1080", 3, 8, 4, (0.0, 2.5, -0.2), "hot", 13, 10, False, 3, 4, 8),
     "bi_d2_88_hot": ("BI", 2, 8, 8, (0.0, 1.0, 0.5), "hot", 17, 20, False, 3, 8, 8),
+    "su4_bixbo_4448_hot": ("BIxBO", 4, 4, 8, (0.0, 2.0, -0.1), "hot", 2880, 10, False, 3, 4, 4),
 }
 
 
