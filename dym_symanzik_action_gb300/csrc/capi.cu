@@ -160,16 +160,17 @@ static int build_mixed_tables(dym_chain* c, const std::vector<uint16_t>& pool) {
 }
 
 // Value-table kernel tables: int16 fixed-point ReTr of u * g_k and of u, at
-// the largest scale 2^S for which |ReTr| 2^S fits int16.
+// the largest scale 2^S for which |ReTr| 2^S fits int16.  The table is
+// element-major (vsub[u * np + k]) and zero-padded to vt_table_bytes.
 static int build_vt_tables(dym_chain* c, const std::vector<uint16_t>& pool) {
   const Group& g = *c->grp->g;
   const uint32_t P = g.P, np = (uint32_t)pool.size();
   int S = 14;
   while (S > 0 && std::ldexp(std::max(g.max_abs_retr, 1e-3), S) > 32767.0) --S;
-  std::vector<int16_t> vsub((size_t)np * P), val((size_t)P);
+  std::vector<int16_t> vsub(vt_table_bytes(P, np) / 2, 0), val((size_t)P);
   for (uint32_t u = 0; u < P; ++u) val[u] = (int16_t)std::lrint(std::ldexp(g.cls_val[g.cls[u]], S));
-  for (uint32_t k = 0; k < np; ++k)
-    for (uint32_t u = 0; u < P; ++u) vsub[(size_t)k * P + u] = val[g.mult[(size_t)u * P + pool[k]]];
+  for (uint32_t u = 0; u < P; ++u)
+    for (uint32_t k = 0; k < np; ++k) vsub[(size_t)u * np + k] = val[g.mult[(size_t)u * P + pool[k]]];
   DYM_CUDA(dmalloc(&c->dev.vsub, vsub.size()), "cudaMalloc(vsub)");
   DYM_CUDA(dmalloc(&c->dev.val16, (size_t)P), "cudaMalloc(val16)");
   DYM_CUDA(copy_sync(c->dev.vsub, vsub.data(), vsub.size() * 2, cudaMemcpyHostToDevice, c->stream), "upload vsub");

@@ -59,7 +59,7 @@ struct ChainDev {
   int fix_shift = 0;
   bool mixed_ok = false;
   uint32_t* xyz = nullptr;     // packed coordinates of sites[k] (mixed kernel)
-  int16_t* vsub = nullptr;     // value-table kernel: vsub[k*P + u] = ReTr(u * pool[k]) * 2^vt_shift
+  int16_t* vsub = nullptr;     // value-table kernel: vsub[u*npool + k] = ReTr(u * pool[k]) * 2^vt_shift
   int16_t* val16 = nullptr;    // ReTr(u) * 2^vt_shift
   int vt_shift = 0;
   bool vt_ok = false;
@@ -77,6 +77,11 @@ cudaError_t launch_sweep_mixed_wide(int D, int dir, const SweepArgs& a, const ui
 size_t mixed_smem_bytes(uint32_t P, uint32_t npool, size_t entry = 2);
 cudaError_t launch_sweep_vt(int D, int dir, const SweepArgs& a, const int16_t* vsub, cudaStream_t s);
 size_t vt_smem_bytes(uint32_t P, uint32_t npool);
+// Bytes of the value table vsub[u * npool + k], padded with zeros to a
+// multiple of 16 (the unit of its cp.async staging).
+__host__ __device__ inline size_t vt_table_bytes(uint32_t P, uint32_t npool) {
+  return ((size_t)P * npool * 2 + 15) / 16 * 16;
+}
 constexpr int kMixedMaxCls = 32;    // classes addressable by the 5 high bits of a psub entry
 constexpr uint32_t kMixedMaxP = 2048;  // 16-bit packed entries: element ids in the 11 low bits
 constexpr int kMixedMaxExtent = 256;   // coordinates packed 8 bits per axis

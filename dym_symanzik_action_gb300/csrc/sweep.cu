@@ -145,19 +145,30 @@ __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_mixed(SweepArgs a
 }
 
 // Value-table form of k_sweep_mixed (visit.cuh vt_prepare/vt_hits).  Shared
-// memory: ReTr (FP64) | inverses | value table | element values | pool.
+// memory: value table (element-major, padded to 16 bytes) | ReTr (FP64) |
+// inverses | element values | pool.  The value table is copied with cp.async
+// and the small tables with plain loads; none of them is written by the
+// previous colour phase, so the staging runs before the programmatic wait and
+// overlaps the previous launch's tail when launched with PDL.
 template <int D, int DIR>
 __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_vt(SweepArgs a, const int16_t* __restrict__ vsub) {
   extern __shared__ __align__(16) unsigned char smem[];
-  double* s_retr = reinterpret_cast<double*>(smem);
+  const size_t vbytes = vt_table_bytes(a.P, a.npool);
+  int16_t* s_vsub = reinterpret_cast<int16_t*>(smem);
+  double* s_retr = reinterpret_cast<double*>(smem + vbytes);
   uint16_t* s_inv = reinterpret_cast<uint16_t*>(s_retr + a.P);
-  int16_t* s_vsub = reinterpret_cast<int16_t*>(s_inv + a.P);
-  int16_t* s_val = s_vsub + (size_t)a.npool * a.P;
+  int16_t* s_val = reinterpret_cast<int16_t*>(s_inv + a.P);
   uint16_t* s_pool = reinterpret_cast<uint16_t*>(s_val + a.P);
-  stage_sub_tables(a.retr, a.inv, reinterpret_cast<const uint16_t*>(vsub), a.P, a.npool, s_retr, s_inv,
-                   reinterpret_cast<uint16_t*>(s_vsub));
-  for (uint32_t t = threadIdx.x; t < a.P; t += blockDim.x) s_val[t] = a.val16[t];
+  cp_async_stage(s_vsub, vsub, vbytes);
+  for (uint32_t t = threadIdx.x; t < a.P; t += blockDim.x) {
+    s_retr[t] = a.retr[t];
+    s_inv[t] = a.inv[t];
+    s_val[t] = a.val16[t];
+  }
   for (uint32_t t = threadIdx.x; t < a.npool; t += blockDim.x) s_pool[t] = a.pool[t];
+  pdl_launch_dependents();
+  pdl_wait_prior();  // the previous phase's links are final from here on
+  cp_async_wait_all();
   __syncthreads();
   constexpr int NT = 8 * (D - 1);
   unsigned hits = 0, accs = 0, rechecks = 0;
@@ -306,8 +317,20 @@ cudaError_t vt_dispatch(int dir, const SweepArgs& a, const int16_t* vsub, cudaSt
   if (e != cudaSuccess) return e;
   const uint32_t per = (a.n + (uint32_t)sms - 1) / (uint32_t)sms;
   const unsigned threads = std::min<unsigned>(kMixedMaxThreads, std::max<unsigned>(128, (per + 31) / 32 * 32));
-  fn<<<(a.n + threads - 1) / threads, threads, smem, s>>>(a, vsub);
-  return cudaGetLastError();
+  // Programmatic stream serialization: the next phase's blocks may start (and
+  // stage their tables) as this phase's blocks retire; each waits for the
+  // whole previous grid before it reads a link (k_sweep_vt).
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((a.n + threads - 1) / threads);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, fn, a, vsub);
 }
 
 template <int D>
@@ -337,7 +360,7 @@ size_t mixed_smem_bytes(uint32_t P, uint32_t npool, size_t entry) {
 }
 
 size_t vt_smem_bytes(uint32_t P, uint32_t npool) {
-  return (size_t)P * 8 + (size_t)P * 2 + (size_t)npool * P * 2 + (size_t)P * 2 + (size_t)npool * 2 + 16;
+  return vt_table_bytes(P, npool) + (size_t)P * 8 + (size_t)P * 2 + (size_t)P * 2 + (size_t)npool * 2 + 16;
 }
 
 cudaError_t launch_sweep_vt(int D, int dir, const SweepArgs& a, const int16_t* vsub, cudaStream_t s) {

@@ -30,6 +30,29 @@ __device__ __forceinline__ void stage_sub_tables(const double* retr, const uint1
   }
 }
 
+// Asynchronous copy of `bytes` (a multiple of 16; both addresses 16-byte
+// aligned) from global into shared memory in 16-byte cp.async transfers, all
+// in flight at once without passing through registers.  Completes at
+// cp_async_wait_all().
+__device__ __forceinline__ void cp_async_stage(void* sdst, const void* gsrc, size_t bytes) {
+  const uint32_t s0 = (uint32_t)__cvta_generic_to_shared(sdst);
+  const char* g0 = static_cast<const char*>(gsrc);
+  for (uint32_t c = threadIdx.x; c < (uint32_t)(bytes / 16); c += blockDim.x)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s0 + 16u * c), "l"(g0 + 16ull * c) : "memory");
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Programmatic dependent launch: let the next kernel on the stream begin its
+// prologue (table staging, which reads nothing this kernel writes), and wait
+// until the previous kernel has completed and its writes are visible.  Both
+// are no-ops for a kernel launched without the attribute.
+__device__ __forceinline__ void pdl_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait_prior() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // One visit of link (i, DIR): build the staples, then nhit hits with the
 // per-hit products read from the shared sub-table.  With u_j = s_j * b the
 // element u_j * g_k = s_j b g_k is conjugate to bnew s_j = b g_k s_j, so for a
@@ -245,6 +268,10 @@ __device__ __forceinline__ void visit_mixed(const SweepArgs& a, uint32_t i, uint
 // (scale 2^S) rather than the element, so a hit is 24 shared loads and
 // integer adds; the new elements of an accepted (or re-evaluated) proposal,
 // u_j * g_k, come from the L2-resident Cayley table.  Decisions as visit_mixed.
+// The table is element-major, s_vsub[u * npool + k]: the pool products of one
+// element are adjacent, so lanes whose staple elements coincide (ordered
+// lattices) read one or two shared-memory rows instead of one row per pool
+// element picked.
 template <int D, int DIR>
 __device__ __forceinline__ void vt_prepare(const SweepArgs& a, uint32_t i, uint32_t xyz, const uint16_t* s_inv,
                                            const int16_t* s_val, uint32_t* u, uint32_t& b, int32_t& R, int32_t& M) {
@@ -275,18 +302,18 @@ __device__ __forceinline__ void vt_hits(const SweepArgs& a, uint32_t i, uint32_t
   constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
   const uint32_t b0 = b;
   const uint16_t* __restrict__ mult = a.mult;
-  const uint32_t P = a.P;
+  const uint32_t P = a.P, np = a.npool;
   double oldact = 0.0;
   bool old_ok = false;
   for (int h = 0; h < a.nhit; ++h) {
     const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_METRO);
-    const uint32_t k = dym_pick(r.v[0], a.npool);
-    const int16_t* row = s_vsub + k * P;
+    const uint32_t k = dym_pick(r.v[0], np);
+    const int16_t* col = s_vsub + k;
     int32_t Rn = 0, Mn = 0;
 #pragma unroll
-    for (int j = 0; j < NS; ++j) Rn += row[u[j]];
+    for (int j = 0; j < NS; ++j) Rn += col[u[j] * np];
 #pragma unroll
-    for (int j = NS; j < NT; ++j) Mn += row[u[j]];
+    for (int j = NS; j < NT; ++j) Mn += col[u[j] * np];
     const float ds = __fmaf_rn(a.b2f, (float)(Mn - M), __fmul_rn(a.b1f, (float)(Rn - R))) * a.dscale;
     const float u2f = __fmaf_rn((float)r.v[1], 0x1p-32f, (float)(r.v[2] >> 11) * 0x1p-53f);
     const float t = -__logf(u2f);
