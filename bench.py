@@ -56,7 +56,15 @@ def gathers_per_link_hit(nhit: int) -> float:
 # workload, from the ncu --set full captures summarised in
 # profiles/sweep_vt_s1080_32x32x32x8_ncu.md, profiles/sweep_mixed_s1080_32x32x32x8_ncu.md
 # and profiles/sweep_sub_s1080_32x32x32x8_ncu.md (cold cache after ncu's flush).
-DRAM_BYTES_PER_LAUNCH = {"k_sweep_vt": 2834432, "k_sweep_mixed": 2830336, "k_sweep_sub": 2563584}
+DRAM_BYTES_PER_LAUNCH = {"k_sweep_vt": 2833792, "k_sweep_mixed": 2830336, "k_sweep_sub": 2563584}
+# smsp__inst_executed.sum (warp instructions) and lts__t_sectors_srcunit_tex.sum
+# (L2 sectors requested by the SMs) of one sweep launch of this workload, from
+# the same captures.  Both are fixed for the workload: the cold chain accepts
+# no proposal, so every launch runs the same instructions.
+INST_PER_LAUNCH = {"k_sweep_vt": 7403245, "k_sweep_mixed": 9140000, "k_sweep_sub": None}
+L2_SECTORS_PER_LAUNCH = {"k_sweep_vt": 411146, "k_sweep_mixed": 399262, "k_sweep_sub": None}
+# Warp instructions an SM can issue per cycle (four schedulers, one each).
+ISSUE_PER_SM_CYCLE = 4
 
 PRECISION_DTYPE = {"mixed": "u16/i32+f32 (f64 rechecks)", "shared": "u16/f64", "fp64": "u16/f64"}
 PRECISION_TEXT = {
@@ -73,7 +81,7 @@ def kernel_model(kernel: int, P: int, npool: int, nhit: int, links_per_launch: i
         per = -(-links_per_launch // sms)
         threads = min(512, max(128, -(-per // 32) * 32))
         return ("k_sweep_vt", 108, -(-links_per_launch // threads),
-                P * 8 + P * 2 + npool * P * 2 + P * 2 + npool * 2 + 16)
+                -(-(npool * P * 2) // 16) * 16 + P * 8 + P * 2 + P * 2 + npool * 2 + 16)
     if kernel == 3:  # sweep.cu mixed_smem_bytes; 128..512 threads, one block per SM
         per = -(-links_per_launch // sms)
         threads = min(512, max(128, -(-per // 32) * 32))
@@ -348,7 +356,6 @@ def run_ours(args):
     # L2 random-gather peak (roofline denominator), measured live.
     sps = C.c_double()
     check(lib().dym_probe_l2_gather(local, 1080 * 1080 * 2, C.byref(sps)))
-    l2_peak_gbs = sps.value * 32 / 1e9
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -416,8 +423,6 @@ def run_ours(args):
                                                        int(links_per_launch), sms)
     stage_bytes = blocks * block_bytes
     alg_bytes_per_launch = links_per_launch * gathers * 32 + stage_bytes
-    achieved = alg_bytes_per_launch / avg_launch_s / 1e9
-    ref_equiv = hits_per_step / nphase * G_ref * 32 / avg_launch_s / 1e9
     hbm_bytes = links_per_sweep * 2 * 2  # every link read and written once per sweep
     peaks = {}
     try:
@@ -426,6 +431,17 @@ def run_ours(args):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     traffic = DRAM_BYTES_PER_LAUNCH.get(kname)
+    # Issue roofline: the kernel's warp instructions per launch (ncu) over the
+    # live launch time, against SMs x 4 schedulers x the SM clock sampled
+    # during the timed region.
+    sm_hz = (clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0) * 1e6
+    issue_peak = sms * ISSUE_PER_SM_CYCLE * sm_hz
+    inst = INST_PER_LAUNCH.get(kname)
+    issue_achieved = inst / avg_launch_s if inst else None
+    # L2-gather roofline of the reference algorithm: the measured random-gather
+    # sector rate over its 25 + 108/NHIT gathers per link-hit.
+    l2_roof = sps.value / G_ref
+    l2_sectors = L2_SECTORS_PER_LAUNCH.get(kname)
 
     if rank == 0:
         line = {
@@ -436,15 +452,25 @@ def run_ours(args):
             "config": {"workload": WORKLOAD_NAME, "links": links_per_sweep, "nhit": w["nhit"],
                        "colour_phases": nphase, "precision": PRECISION_TEXT[args.precision], "kernel": kname,
                        "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
-            "roofline": {"bound": "l2", "achieved": achieved, "peak": l2_peak_gbs, "unit": "GB/s",
-                         "frac": achieved / l2_peak_gbs, "traffic": traffic,
-                         "peak_source": "measured live: random 2-byte L2 gathers (dym_probe_l2_gather), 32 B/sector",
-                         "algorithmic": (f"{kname}: {gathers} table gathers x 32 B per link visit "
-                                         f"({gathers / w['nhit']:.1f} per link-hit) + {blocks} blocks x "
-                                         f"{block_bytes} B table staging per launch"),
-                         "reference_algorithm_equivalent": {
-                             "gathers_per_link_hit": G_ref, "achieved": ref_equiv, "unit": "GB/s",
-                             "note": "the reference algorithm's gathers at this rate (hits from shared memory here)"},
+            "roofline": {"bound": "issue", "achieved": issue_achieved, "peak": issue_peak, "unit": "warp-inst/s",
+                         "frac": issue_achieved / issue_peak if issue_achieved else None, "traffic": traffic,
+                         "peak_source": (f"{sms} SMs x {ISSUE_PER_SM_CYCLE} warp instructions per cycle x "
+                                         f"{sm_hz / 1e6:.0f} MHz (median SM clock sampled in the timed region)"),
+                         "algorithmic": (f"{kname}: {inst} warp instructions per launch (ncu smsp__inst_executed.sum "
+                                         f"of this workload) / CUDA-event launch time; {links_per_launch:.0f} "
+                                         f"links x {w['nhit']} hits per launch"),
+                         "l2_gather": {
+                             "peak_sectors_per_s": sps.value,
+                             "peak_source": "measured live: random 2-byte L2 gathers (dym_probe_l2_gather)",
+                             "reference_gathers_per_link_hit": G_ref,
+                             "roofline_link_hits_per_s": l2_roof, "frac": value / l2_roof,
+                             "kernel_gathers_per_link_hit": gathers / w["nhit"],
+                             "kernel_alg_bytes_per_launch": alg_bytes_per_launch,
+                             "kernel_l2_sectors_per_launch": l2_sectors,
+                             "kernel_l2_frac": (l2_sectors / avg_launch_s / sps.value) if l2_sectors else None,
+                             "note": ("frac > 1: the hits read shared memory, not L2, and half of the staple "
+                                      "gathers hit L1; kernel_l2_frac is the L2 sector rate the kernel drew "
+                                      "(ncu) against the gather peak")},
                          "hbm": {"achieved": hbm_bytes / (dev_ms * 1e-3 / args.steps) / 1e9, "peak": hbm_peak,
                                  "unit": "GB/s", "note": "compulsory link streaming, 4 B/link/sweep, of measured"}},
             "e2e": {"value": e2e_value, "unit": "link-hits/s", "h2d_bytes_per_step": n * 2,

@@ -45,6 +45,8 @@ __global__ void __launch_bounds__(256) k_sweep_direct(SweepArgs a) {
     s_inv[t] = a.inv[t];
   }
   for (uint32_t t = threadIdx.x; t < a.npool; t += blockDim.x) s_pool[t] = a.pool[t];
+  pdl_launch_dependents();
+  pdl_wait_prior();
   __syncthreads();
 
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -108,6 +110,8 @@ __global__ void __launch_bounds__(256) k_sweep_sub(SweepArgs a, const uint16_t* 
   uint16_t* s_inv = reinterpret_cast<uint16_t*>(s_retr + a.P);
   uint16_t* s_sub = s_inv + a.P;
   stage_sub_tables(a.retr, a.inv, sub, a.P, a.npool, s_retr, s_inv, s_sub);
+  pdl_launch_dependents();
+  pdl_wait_prior();
   __syncthreads();
 
   unsigned hits = 0, accs = 0;
@@ -133,13 +137,27 @@ __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_mixed(SweepArgs a
                    s_retr, s_inv, reinterpret_cast<uint16_t*>(s_psub));
   for (uint32_t t = threadIdx.x; t < a.P; t += blockDim.x) s_cls[t] = a.cls8[t];
   if (threadIdx.x < kMixedMaxCls) s_cfix[threadIdx.x] = a.cfix[threadIdx.x];
+  uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t i_next = 0, xyz_next = 0;  // constant site list: fetched before the wait
+  if (tid < a.n) {
+    i_next = a.sites[tid];
+    xyz_next = a.xyz[tid];
+  }
+  pdl_launch_dependents();
+  pdl_wait_prior();
   __syncthreads();
 
   unsigned hits = 0, accs = 0, rechecks = 0;
   float max_err = 0.0f;
-  for (uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x; tid < a.n; tid += gridDim.x * blockDim.x)
-    visit_mixed<D, DIR, E>(a, a.sites[tid], a.xyz[tid], a.sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs,
-                           rechecks, max_err);
+  for (; tid < a.n; tid += gridDim.x * blockDim.x) {
+    const uint32_t i = i_next, xyz = xyz_next;
+    const uint32_t nt = tid + gridDim.x * blockDim.x;
+    if (nt < a.n) {
+      i_next = a.sites[nt];
+      xyz_next = a.xyz[nt];
+    }
+    visit_mixed<D, DIR, E>(a, i, xyz, a.sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err);
+  }
   flush_counters(a.counters, hits, accs, rechecks);
   flush_max_err(a.counters + 3, max_err);
 }
@@ -166,6 +184,14 @@ __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_vt(SweepArgs a, c
     s_val[t] = a.val16[t];
   }
   for (uint32_t t = threadIdx.x; t < a.npool; t += blockDim.x) s_pool[t] = a.pool[t];
+  // The site list and coordinates are constant: fetch this thread's first
+  // entry before the wait as well.
+  uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t i_next = 0, xyz_next = 0;
+  if (tid < a.n) {
+    i_next = a.sites[tid];
+    xyz_next = a.xyz[tid];
+  }
   pdl_launch_dependents();
   pdl_wait_prior();  // the previous phase's links are final from here on
   cp_async_wait_all();
@@ -173,11 +199,16 @@ __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_vt(SweepArgs a, c
   constexpr int NT = 8 * (D - 1);
   unsigned hits = 0, accs = 0, rechecks = 0;
   float max_err = 0.0f;
-  for (uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x; tid < a.n; tid += gridDim.x * blockDim.x) {
+  for (; tid < a.n; tid += gridDim.x * blockDim.x) {
     uint32_t u[NT], b;
     int32_t R, M;
-    const uint32_t i = a.sites[tid];
-    vt_prepare<D, DIR>(a, i, a.xyz[tid], s_inv, s_val, u, b, R, M);
+    const uint32_t i = i_next, xyz = xyz_next;
+    const uint32_t nt = tid + gridDim.x * blockDim.x;
+    if (nt < a.n) {
+      i_next = a.sites[nt];
+      xyz_next = a.xyz[nt];
+    }
+    vt_prepare<D, DIR>(a, i, xyz, s_inv, s_val, u, b, R, M);
     vt_hits<D, DIR>(a, i, a.sweep, s_retr, s_vsub, s_pool, u, b, R, M, hits, accs, rechecks, max_err);
   }
   flush_counters(a.counters, hits, accs, rechecks);
@@ -220,6 +251,26 @@ __global__ void k_staples(SweepArgs a, const uint32_t* sites, uint32_t n, uint16
   for (int j = 0; j < NR; ++j) out[(size_t)tid * (NS + NR) + NS + j] = (uint16_t)re[j];
 }
 
+// Launch one colour phase with programmatic stream serialization: the next
+// phase's blocks may start, and stage their tables, as this phase's blocks
+// retire; every sweep kernel waits for the whole previous grid (pdl_wait_prior)
+// before it reads a site list entry or a link.
+template <class... K, class... A>
+cudaError_t launch_phase(void (*fn)(K...), unsigned grid, unsigned threads, size_t smem, cudaStream_t s,
+                         A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, fn, args...);
+}
+
 template <int D>
 cudaError_t direct_dispatch(int dir, const SweepArgs& a, cudaStream_t s) {
   const size_t smem = (size_t)a.P * 8 + (size_t)a.P * 2 + (size_t)a.npool * 2 + 16;
@@ -237,8 +288,7 @@ cudaError_t direct_dispatch(int dir, const SweepArgs& a, cudaStream_t s) {
     if (e != cudaSuccess) return e;
   }
   if (grid == 0) return cudaSuccess;
-  fn<<<grid, 256, smem, s>>>(a);
-  return cudaGetLastError();
+  return launch_phase(fn, grid, 256, smem, s, a);
 }
 
 template <int D>
@@ -264,8 +314,7 @@ cudaError_t sub_dispatch(int dir, const SweepArgs& a, const uint16_t* sub, cudaS
   if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem);
   if (e != cudaSuccess) return e;
   const unsigned grid = std::min<unsigned>(need, (unsigned)std::max(1, sms * std::max(per_sm, 1)));
-  fn<<<grid, 256, smem, s>>>(a, sub);
-  return cudaGetLastError();
+  return launch_phase(fn, grid, 256, smem, s, a, sub);
 }
 
 template <int D, class E>
@@ -292,9 +341,7 @@ cudaError_t mixed_dispatch(int dir, const SweepArgs& a, const E* psub, cudaStrea
   if (e != cudaSuccess) return e;
   const uint32_t per = (a.n + (uint32_t)sms - 1) / (uint32_t)sms;
   const unsigned threads = std::min<unsigned>(kMixedMaxThreads, std::max<unsigned>(128, (per + 31) / 32 * 32));
-  const unsigned grid = (a.n + threads - 1) / threads;
-  fn<<<grid, threads, smem, s>>>(a, psub);
-  return cudaGetLastError();
+  return launch_phase(fn, (a.n + threads - 1) / threads, threads, smem, s, a, psub);
 }
 
 template <int D>
@@ -317,20 +364,7 @@ cudaError_t vt_dispatch(int dir, const SweepArgs& a, const int16_t* vsub, cudaSt
   if (e != cudaSuccess) return e;
   const uint32_t per = (a.n + (uint32_t)sms - 1) / (uint32_t)sms;
   const unsigned threads = std::min<unsigned>(kMixedMaxThreads, std::max<unsigned>(128, (per + 31) / 32 * 32));
-  // Programmatic stream serialization: the next phase's blocks may start (and
-  // stage their tables) as this phase's blocks retire; each waits for the
-  // whole previous grid before it reads a link (k_sweep_vt).
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((a.n + threads - 1) / threads);
-  cfg.blockDim = dim3(threads);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, fn, a, vsub);
+  return launch_phase(fn, (a.n + threads - 1) / threads, threads, smem, s, a, vsub);
 }
 
 template <int D>

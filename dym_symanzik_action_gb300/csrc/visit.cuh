@@ -9,27 +9,6 @@
 
 namespace dym {
 
-// Copy ReTr, the inverse table and the sub-table sub[k][u] = u * g_k into
-// shared memory (s_sub must be 4-byte aligned when P is even).
-__device__ __forceinline__ void stage_sub_tables(const double* retr, const uint16_t* inv, const uint16_t* sub,
-                                                 uint32_t P, uint32_t npool, double* s_retr, uint16_t* s_inv,
-                                                 uint16_t* s_sub) {
-  for (uint32_t t = threadIdx.x; t < P; t += blockDim.x) {
-    s_retr[t] = retr[t];
-    s_inv[t] = inv[t];
-  }
-  const uint32_t nsub = npool * P;
-  if ((P & 1u) == 0) {
-    const uint32_t* src = reinterpret_cast<const uint32_t*>(sub);
-    uint32_t* dst = reinterpret_cast<uint32_t*>(s_sub);
-    const uint32_t nw = nsub / 2;
-#pragma unroll 8
-    for (uint32_t t = threadIdx.x; t < nw; t += blockDim.x) dst[t] = src[t];
-  } else {
-    for (uint32_t t = threadIdx.x; t < nsub; t += blockDim.x) s_sub[t] = sub[t];
-  }
-}
-
 // Asynchronous copy of `bytes` (a multiple of 16; both addresses 16-byte
 // aligned) from global into shared memory in 16-byte cp.async transfers, all
 // in flight at once without passing through registers.  Completes at
@@ -43,6 +22,38 @@ __device__ __forceinline__ void cp_async_stage(void* sdst, const void* gsrc, siz
 }
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Copy ReTr, the inverse table and the sub-table sub[k][u] = u * g_k into
+// shared memory (s_sub must be 4-byte aligned when P is even).  When both
+// copies of the sub-table start on 16 bytes its whole 16-byte chunks go by
+// cp.async, so the block's copy costs about one L2 round trip instead of one
+// per eight words a thread moves; the caller's __syncthreads() publishes it.
+__device__ __forceinline__ void stage_sub_tables(const double* retr, const uint16_t* inv, const uint16_t* sub,
+                                                 uint32_t P, uint32_t npool, double* s_retr, uint16_t* s_inv,
+                                                 uint16_t* s_sub) {
+  const uint32_t nsub = npool * P;
+  const bool async = ((reinterpret_cast<uintptr_t>(sub) | (uintptr_t)__cvta_generic_to_shared(s_sub)) & 15u) == 0;
+  if (async) {
+    const uint32_t nb16 = (nsub * 2u) & ~15u;
+    cp_async_stage(s_sub, sub, nb16);
+    for (uint32_t t = nb16 / 2 + threadIdx.x; t < nsub; t += blockDim.x) s_sub[t] = sub[t];
+  }
+  for (uint32_t t = threadIdx.x; t < P; t += blockDim.x) {
+    s_retr[t] = retr[t];
+    s_inv[t] = inv[t];
+  }
+  if (async) {
+    cp_async_wait_all();
+  } else if ((P & 1u) == 0) {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(sub);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(s_sub);
+    const uint32_t nw = nsub / 2;
+#pragma unroll 8
+    for (uint32_t t = threadIdx.x; t < nw; t += blockDim.x) dst[t] = src[t];
+  } else {
+    for (uint32_t t = threadIdx.x; t < nsub; t += blockDim.x) s_sub[t] = sub[t];
+  }
+}
 
 // Programmatic dependent launch: let the next kernel on the stream begin its
 // prologue (table staging, which reads nothing this kernel writes), and wait
