@@ -140,9 +140,10 @@ __device__ __forceinline__ void visit_sub(const SweepArgs& a, uint32_t i, uint32
 // reference's order, dym_accept_fast).  The configurations are therefore those
 // of the FP64 path bit for bit.  The exact action of the current link is
 // rebuilt lazily when a re-evaluation needs it after fast accepts.
-// First half of a mixed-precision visit of link (i, DIR): the staples,
-// u_j = s_j * b and the fixed-point sums R, M of the current link (bound by
-// global-memory latency).
+// First half of a mixed-precision visit of link (i, DIR): u_j = s_j * b
+// (build_u_tree; the shared-table kernels run on associative tables only) and
+// the fixed-point sums R, M of the current link (bound by global-memory
+// latency).
 template <int D, int DIR>
 __device__ __forceinline__ void mixed_prepare(const SweepArgs& a, uint32_t i, uint32_t xyz, const uint16_t* s_inv,
                                               const uint8_t* s_cls, const int32_t* s_cfix, uint32_t* u,
@@ -154,10 +155,8 @@ __device__ __forceinline__ void mixed_prepare(const SweepArgs& a, uint32_t i, ui
   const uint16_t* L = a.links;
   const uint32_t V = a.V;
   auto ld = [L, V](uint32_t s, int d) -> uint32_t { return __ldg(L + (size_t)d * V + s); };
-  build_staples<D, DIR>(i, geo, T, ld, u, u + NS);
   b = a.links[(size_t)DIR * V + i];
-#pragma unroll
-  for (int j = 0; j < NT; ++j) u[j] = T.mul(u[j], b);  // u_j = s_j * b
+  build_u_tree<D, DIR>(i, geo, T, ld, b, u, u + NS);  // u_j = s_j * b
   R = 0;
   M = 0;  // fixed-point sums, modular (differences are exact)
 #pragma unroll
@@ -293,10 +292,8 @@ __device__ __forceinline__ void vt_prepare(const SweepArgs& a, uint32_t i, uint3
   const uint16_t* L = a.links;
   const uint32_t V = a.V;
   auto ld = [L, V](uint32_t s, int d) -> uint32_t { return __ldg(L + (size_t)d * V + s); };
-  build_staples<D, DIR>(i, geo, T, ld, u, u + NS);
   b = a.links[(size_t)DIR * V + i];
-#pragma unroll
-  for (int j = 0; j < NT; ++j) u[j] = T.mul(u[j], b);  // u_j = s_j * b
+  build_u_tree<D, DIR>(i, geo, T, ld, b, u, u + NS);  // u_j = s_j * b
   R = 0;
   M = 0;
 #pragma unroll
