@@ -82,13 +82,10 @@ __device__ __forceinline__ void visit_sub(const SweepArgs& a, uint32_t i, uint32
   const uint32_t V = a.V;
   auto ld = [L, V](uint32_t s, int d) -> uint32_t { return __ldg(L + (size_t)d * V + s); };
   uint32_t u[NT];
-  build_staples<D, DIR>(i, geo, T, ld, u, u + NS);
-
   uint16_t* own = a.links + (size_t)DIR * V + i;
   uint32_t b = *own;
   const uint32_t b0 = b;
-#pragma unroll
-  for (int j = 0; j < NT; ++j) u[j] = T.mul(u[j], b);  // u_j = s_j * b
+  build_u_tree<D, DIR>(i, geo, T, ld, b, u, u + NS);  // u_j = s_j * b (associative tables only)
   double r1 = 0, m1 = 0;
 #pragma unroll
   for (int j = 0; j < NS; ++j) r1 = DYM_ADD(r1, s_retr[u[j]]);
@@ -436,12 +433,10 @@ __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, ui
   const uint32_t V = a.V;
   auto ld = [L, V](uint32_t s, int d) -> uint32_t { return __ldg(L + (size_t)d * V + s); };
   uint32_t u[NT];
-  build_staples<D, DIR>(i, geo, T, ld, u, u + NS);
   uint16_t* own = a.links + (size_t)DIR * V + i;
   uint32_t b = *own;
   const uint32_t b0 = b;
-#pragma unroll
-  for (int j = 0; j < NT; ++j) u[j] = T.mul(u[j], b);
+  build_u_tree<D, DIR>(i, geo, T, ld, b, u, u + NS);  // u_j = s_j * b
   uint32_t c0[NW];
 #pragma unroll
   for (int w = 0; w < NW; ++w) c0[w] = 0;
