@@ -249,6 +249,7 @@ static void chain_release(dym_chain* c) {
   cudaFree(c->d_llr);
   cudaFree(c->d_oldv);
   cudaFree(c->d_stage);
+  cudaFree(c->d_first_bad);
   if (c->h_counters) cudaFreeHost(c->h_counters);
   if (c->h_hist) cudaFreeHost(c->h_hist);
   if (c->ev0) cudaEventDestroy(c->ev0);
@@ -393,7 +394,8 @@ int dym_chain_create(const dym_group* gh, const dym_chain_params* p, dym_chain**
   DYM_CUDA(dmalloc(&d.pool, pool.size()), "cudaMalloc(pool)");
   DYM_CUDA(copy_sync(d.pool, pool.data(), pool.size() * 2, cudaMemcpyHostToDevice, c->stream), "upload pool");
   DYM_CUDA(dmalloc(&d.counters, 5), "cudaMalloc(counters)");
-  DYM_CUDA(cudaHostAlloc((void**)&c->h_counters, 5 * sizeof(unsigned long long), cudaHostAllocDefault),
+  // Pinned words: [0..4] dym_sweep's counters, [5] dym_links_set's check.
+  DYM_CUDA(cudaHostAlloc((void**)&c->h_counters, 6 * sizeof(unsigned long long), cudaHostAllocDefault),
            "cudaHostAlloc");
   if (p->precision != DYM_PREC_FP64 && sub_eligible(g, d.npool, p->device, p->D)) {
     rc = build_sub_table(c.get(), pool);
@@ -556,19 +558,18 @@ int dym_links_set(dym_chain* c, const uint16_t* host_in) {
   const size_t n = (size_t)c->dev.V * c->p.D;
   DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
   if (!c->d_stage) DYM_CUDA(dmalloc(&c->d_stage, n), "cudaMalloc(links stage)");
-  // Upload into the stage while the host checks the ids (a branch-free maximum
-  // that vectorises); the chain's links change only if every id is in range.
+  if (!c->d_first_bad) DYM_CUDA(dmalloc(&c->d_first_bad, 1), "cudaMalloc(links check)");
+  // Upload into the stage; the device finds the first id >= P and copies the
+  // stage into the chain's links only if there is none, so a refused
+  // configuration leaves the chain as it was.
   DYM_CUDA(cudaMemcpyAsync(c->d_stage, host_in, n * 2, cudaMemcpyHostToDevice, c->stream), "upload links");
-  uint16_t mx = 0;
-  for (size_t k = 0; k < n; ++k) mx = host_in[k] > mx ? host_in[k] : mx;
-  if (mx >= P) {
-    size_t k = 0;
-    while (host_in[k] < P) ++k;
-    cudaStreamSynchronize(c->stream);
-    return fail(DYM_EINVAL, "dym_links_set: element id out of range at " + std::to_string(k));
-  }
-  DYM_CUDA(cudaMemcpyAsync(c->dev.links, c->d_stage, n * 2, cudaMemcpyDeviceToDevice, c->stream), "copy links");
+  DYM_CUDA(launch_links_commit(c->dev.links, c->d_stage, n, P, c->d_first_bad, c->stream), "check links");
+  DYM_CUDA(cudaMemcpyAsync(c->h_counters + 5, c->d_first_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                           c->stream),
+           "read links check");
   DYM_CUDA(cudaStreamSynchronize(c->stream), "upload links");
+  if (c->h_counters[5] != ~0ull)
+    return fail(DYM_EINVAL, "dym_links_set: element id out of range at " + std::to_string(c->h_counters[5]));
   return DYM_OK;
 }
 

@@ -88,6 +88,10 @@ constexpr int kMixedMaxExtent = 256;   // coordinates packed 8 bits per axis
 constexpr int kMixedMaxThreads = 512;
 cudaError_t launch_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uint64_t seed, cudaStream_t s);
 cudaError_t launch_fill(uint16_t* links, size_t n, uint16_t v, cudaStream_t s);
+// Check n uploaded ids against P on the device (*first = smallest bad index,
+// or ~0) and copy the stage into the links only if all are in range.
+cudaError_t launch_links_commit(uint16_t* links, const uint16_t* stage, size_t n, uint32_t P,
+                                unsigned long long* first, cudaStream_t s);
 cudaError_t launch_staples(int D, int dir, const SweepArgs& a, const uint32_t* sites, uint32_t n, uint16_t* out,
                            cudaStream_t s);
 // Shared memory of k_sweep_mixed: ReTr (FP64) | class values | inverses | packed
@@ -181,4 +185,5 @@ struct dym_chain {
   uint16_t* d_oldv = nullptr;
   uint64_t llr_phase = 0;  // colour phases run by LLR sweeps (delta-buffer parity)
   uint16_t* d_stage = nullptr;  // dym_links_set: upload buffer, copied into the links once checked
+  unsigned long long* d_first_bad = nullptr;  // dym_links_set: smallest out-of-range index, or ~0
 };

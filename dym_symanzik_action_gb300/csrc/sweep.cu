@@ -229,6 +229,21 @@ __global__ void k_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uint
   }
 }
 
+// dym_links_set on the device: the smallest index whose id is >= P into
+// *first (set to ~0 beforehand), then the stage copied into the links only if
+// there is none.
+__global__ void k_ids_first_bad(const uint16_t* __restrict__ ids, size_t n, uint32_t P, unsigned long long* first) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    if (ids[k] >= P) atomicMin(first, (unsigned long long)k);
+}
+
+__global__ void k_ids_commit(uint16_t* __restrict__ links, const uint16_t* __restrict__ stage, size_t n,
+                             const unsigned long long* first) {
+  if (*first != ~0ull) return;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    links[k] = stage[k];
+}
+
 __global__ void k_fill(uint16_t* p, size_t n, uint16_t v) {
   for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) p[l] = v;
 }
@@ -444,6 +459,16 @@ cudaError_t launch_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uin
   unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 16);
   if (grid == 0) return cudaSuccess;
   k_hot_start<<<grid, 256, 0, s>>>(links, V, D, P, seed);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_links_commit(uint16_t* links, const uint16_t* stage, size_t n, uint32_t P,
+                                unsigned long long* first, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(first, 0xFF, sizeof(unsigned long long), s);
+  if (e != cudaSuccess || n == 0) return e;
+  const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 8);
+  k_ids_first_bad<<<grid, 256, 0, s>>>(stage, n, P, first);
+  k_ids_commit<<<grid, 256, 0, s>>>(links, stage, n, first);
   return cudaGetLastError();
 }
 
