@@ -47,6 +47,8 @@ struct BatchTile {
 // LLR work lists (llr.cu): per-chain descriptors, tiles of one colour-phase
 // slot, and the chains whose phase the slot's commit closes.
 struct LlrState;
+struct LlrLinkRec;
+struct LlrBlockRec;
 struct LlrChainDev {
   uint16_t* links;
   const uint32_t* sites;
@@ -54,7 +56,9 @@ struct LlrChainDev {
   int Nt, Nx;
   uint64_t seed;
   LlrState* st;
-  uint16_t* oldv;
+  LlrLinkRec* rec;    // one per link of the largest phase
+  LlrBlockRec* brec;  // one per block of scan links
+  uint8_t* bref;      // per block: refused by the scan of this slot
   int group;
 };
 struct LlrTile {
@@ -62,6 +66,7 @@ struct LlrTile {
 };
 struct LlrCommit {
   uint32_t chain, last;  // last: this slot holds the chain's last phase of a sweep
+  uint32_t count, dir;   // the phase's links and direction
 };
 void* llr_propose_kernel_for(int D);
 cudaError_t launch_llr_slot(int D, const LlrTile* tiles, uint32_t ntiles, const LlrCommit* commits, uint32_t ncommit,

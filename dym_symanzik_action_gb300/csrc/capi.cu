@@ -247,7 +247,9 @@ static void chain_release(dym_chain* c) {
   cudaFree(c->d_hist);
   cudaFree(c->d_meas_scratch);
   cudaFree(c->d_llr);
-  cudaFree(c->d_oldv);
+  cudaFree(c->d_llr_rec);
+  cudaFree(c->d_llr_blk);
+  cudaFree(c->d_llr_bref);
   cudaFree(c->d_stage);
   cudaFree(c->d_first_bad);
   if (c->h_counters) cudaFreeHost(c->h_counters);

@@ -103,39 +103,56 @@ __host__ __device__ inline size_t mixed_psub_offset(uint32_t P, size_t entry) {
 
 // LLR (interval-restricted sweeps with Robbins-Monro updates): per-chain
 // state in device memory, updated by the commit kernel after every colour
-// phase.  Energies are exact: integer class histograms of all plaquettes (h[0])
-// and rectangles (h[1]), one FP64 dot product with the class values.
+// phase.  Energies are exact 64-bit fixed-point sums of the plaquette (Ef[0])
+// and rectangle (Ef[1]) class values, each value times 2^kLlrFixShift rounded
+// (vf); E holds the same sums as FP64.  The window tests compare fixed-point
+// values: wlo/whi/wmid[0] bound the windowed energy (S1 for axis 1, S2 for
+// axis 2; S1 of a two-dimensional cell), [1] the S2 window of a cell.
 constexpr int kLlrMaxCls = 32;
+constexpr int kLlrFixShift = 32;
 // The LLR propose kernel runs 512-thread blocks whose warps take 32-link tiles
-// independently; each warp's class deltas sit at the front of shared memory.
+// independently.
 constexpr int kLlrWarps = 16;
 constexpr int kLlrTile = 32;
-constexpr int kLlrDeltaBytes = kLlrWarps * 2 * kLlrMaxCls * 4;
-constexpr int kLlrMaxPhases = 256;                   // colour phases per sweep with their own drive-in fraction
 struct LlrState {
   double a, bg, elo, ehi, emid, ewin, w2;
   double E[2];
   double sumE;
-  double v[kLlrMaxCls];
-  long long h[2][kLlrMaxCls];
-  long long d[2][2][kLlrMaxCls];  // [phase parity][plaquette|rectangle][class]
+  long long Ef[2];
+  long long vf[kLlrMaxCls];
+  long long wlo[2], whi[2], wmid[2];
+  double wsc[2];  // 2^-kLlrFixShift / half-width per axis (two-dimensional drive-in)
+  int blk;        // links per block of the scan (dym_llr_block_links)
+  int restore;    // set by the commit: some block of the phase was refused, restore its links
   double a_hist[DYM_LLR_MAX_NRM];
-  int axis, mode, k, m, K, NRM, drive_sweeps, drive_cap, ncls, sweeps;
-  uint32_t phase, sweep;  // colour phases committed (delta parity), Philox sweep counter
-  unsigned long long phase_acc, phase_rej, hits, accepts;
-  // Drive-in: fraction of each colour phase's links that take part, adapted
-  // per phase (the links able to move towards the window differ by class).
-  int nphase;
-  double qp[kLlrMaxPhases];
+  int axis, mode, k, m, K, NRM, drive_sweeps, drive_cap, sweeps;
+  uint32_t phase, sweep;  // colour phases committed, Philox sweep counter
+  unsigned long long phase_acc, phase_rej, hits, accepts;  // phase_acc/rej: links kept/refused by the scan
   // Two-dimensional cells (dims == 2, llr2d.cpp:178-259): S1 in [elo, ehi] and
   // S2 in [elo2, ehi2] (axis is 1); a is a1 and bg is a2, both updated by
   // Robbins-Monro; ihw are the reciprocal half-widths of the normalised
-  // distance to the cell centre used by the drive-in.
+  // distance to the cell centre used by the drive-in hits.
   int dims;
-  int restore;  // set by the commit: the phase's class move was refused, restore its links
   double elo2, ehi2, emid2, ewin2, w2b, sumE2;
   double ihw[2];
   double a2_hist[DYM_LLR_MAX_NRM];
+};
+
+// What the propose kernel leaves for the scan of the commit kernel: per link
+// of the phase (in site-list order) its site, its value before the hits and
+// whether they changed it; per block of LlrState::blk consecutive links the
+// exact fixed-point sums of the links' changes of S1 and S2 and the number of
+// changed links.
+struct LlrLinkRec {
+  uint32_t site;
+  uint16_t old;
+  uint16_t changed;
+};
+
+struct LlrBlockRec {
+  long long s[2];
+  uint32_t nchg;
+  uint32_t pad;
 };
 
 // Drive-in parameters of a two-dimensional cell, as the propose kernel passes
@@ -182,8 +199,9 @@ struct dym_chain {
   size_t h_hist_elems = 0;
   // LLR state (allocated on first use).
   dym::LlrState* d_llr = nullptr;
-  uint16_t* d_oldv = nullptr;
-  uint64_t llr_phase = 0;  // colour phases run by LLR sweeps (delta-buffer parity)
+  dym::LlrLinkRec* d_llr_rec = nullptr;   // per link of the largest colour phase (rounded up to 32)
+  dym::LlrBlockRec* d_llr_blk = nullptr;  // per block of it (as many)
+  uint8_t* d_llr_bref = nullptr;          // per block: refused by the last scan
   uint16_t* d_stage = nullptr;  // dym_links_set: upload buffer, copied into the links once checked
   unsigned long long* d_first_bad = nullptr;  // dym_links_set: smallest out-of-range index, or ~0
 };

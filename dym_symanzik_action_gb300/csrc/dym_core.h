@@ -190,3 +190,26 @@ DYM_HD int dym_accept_fast(double oldact, double newact, double u2) {
   if (d > 38.0 && u2 != 0.0) return 0;
   return dym_exp(-d) > u2;
 }
+
+// ---------------------------------------------------------------------------
+// LLR window scan: links per block.  After a colour class's links have run
+// their hits, the scan keeps or reverts the moves of consecutive blocks of
+// this many links (in site-list order) by the window test on the running
+// energy.  It is the largest power of two up to 32 for which a block's largest
+// possible change of every windowed action -- links x terms a link changes
+// (2(D-1) plaquettes, 6(D-1) rectangles) x the ReTr range -- is at most a
+// quarter of that window's width (half its half-width), and 1 at least; so a
+// block moving away from one wall can never pass the other.
+// dims 2: both actions windowed (half-widths hw, hw2); else axis 1 (S1) or 2.
+// ---------------------------------------------------------------------------
+DYM_HD int dym_llr_block_links(int D, double retr_range, int dims, int axis, double hw, double hw2) {
+  const double t1 = 2.0 * (D - 1) * retr_range, t2 = 6.0 * (D - 1) * retr_range;
+  int s = 32;
+  while (s > 1) {
+    const int ok = dims == 2 ? (s * t1 <= 0.5 * hw && s * t2 <= 0.5 * hw2)
+                             : (s * (axis == 1 ? t1 : t2) <= 0.5 * hw);
+    if (ok) break;
+    s >>= 1;
+  }
+  return s;
+}

@@ -1,31 +1,30 @@
 // Interval-restricted (LLR) Metropolis sweeps with the Robbins-Monro update,
 // on the device, for any number of chains at once.
 //
-// The reference (llr.cpp:178-250) updates links one at a time because the
-// window constraint is on the global energy.  Here a colour class moves at
-// once, in three kernels per colour-phase slot over a work list of chains:
+// The reference (llr.cpp:178-250) updates links one at a time and tests the
+// window on the global energy after every hit.  Here a colour class moves in
+// two kernels per colour-phase slot over a work list of chains:
 //  1. k_llr_propose: every link of the class runs nhit Metropolis hits with
-//     weight exp(-a dE_w - bg dE_bg) (llr.cpp:211) and no window test; links of
-//     one colour share no plaquette or rectangle, so their energy changes add.
-//     Outside the window (drive-in) a hit is kept iff it moves the link's
-//     running energy towards the window centre (llr.cpp:208-209), and only a
-//     deterministic fraction q of the links takes part; after each phase q is
-//     set so that the expected move covers the remaining distance.  Each
-//     link's change of plaquette and rectangle classes is added to the chain's
-//     integer histogram delta.  A warp takes a tile of 32 links, so a short
-//     work list still reaches every SM (the FP64 pipe bounds this kernel).
-//  2. k_llr_commit: one warp per chain forms the energies after the class
-//     move from the histograms plus the delta and keeps the move iff the new
-//     windowed energy lies in [Elo, Ehi] (outside the window: iff it is closer
-//     to the centre); it folds a kept delta into the histograms, adapts q, and
-//     at the end of a sweep advances the drive-in / Robbins-Monro state
-//     machine (a += 12/(W^2 (m+1)) (<E> - Ewin), llr.cpp:244).
-//  3. k_llr_restore: the links of a refused class move get their old values.
-// NHIT identical single-hit Metropolis kernels compose into a reversible
-// kernel, so accepting the class move iff it stays in the window is an exact
-// Metropolis-Hastings step for the window-restricted distribution.  Every
-// chain's state (Philox sweep counter, delta parity, energies) lives in its
-// own LlrState, so a chain gives the same result alone or in any mix.
+//     weight exp(-a dE_w - bg dE_bg) (llr.cpp:211) and no window test; outside
+//     the window (drive-in) a hit is kept iff it moves the link's running
+//     energy towards the window centre (llr.cpp:208-209).  Links of one colour
+//     share no plaquette or rectangle, so each link's energy change is its own:
+//     the kernel records it (exact fixed point) with the link's old value.  A
+//     warp takes a tile of 32 links, so a short work list still reaches every
+//     SM (the FP64 pipe bounds this kernel).
+//  2. k_llr_commit: one warp per chain scans the phase's changed links in
+//     site-list order and keeps link i's move iff the running energy plus its
+//     change stays in the window (outside it: iff it comes closer to the
+//     centre); a refused link gets its old value back.  Then it advances the
+//     drive-in / Robbins-Monro state machine at the end of a sweep
+//     (a += 12/(W^2 (m+1)) (<E> - Ewin), llr.cpp:244).
+// A link's nhit identical single-hit Metropolis kernels compose into a
+// reversible kernel, so keeping its move iff the energy stays in the window is
+// an exact Metropolis-Hastings step for the window-restricted distribution,
+// and the scan is a composition of such steps.  Energies are exact 64-bit
+// fixed-point sums of the class values, so the tracked energy never drifts.
+// Every chain's state (Philox sweep counter, energies) lives in its own
+// LlrState, so a chain gives the same result alone or in any mix.
 #include <cuda_runtime.h>
 
 #include "batch.h"
@@ -38,21 +37,34 @@ namespace dym {
 
 namespace {
 
-// Squared normalised distance of (e1, e2) to a two-dimensional cell's centre
-// (the reference compares hypot() of the same terms, llr2d.cpp:207-209).
-__device__ __forceinline__ double norm_sq(const LlrState* st, double e1, double e2) {
-  const double x = DYM_MUL(DYM_SUB(e1, st->emid), st->ihw[0]);
-  const double y = DYM_MUL(DYM_SUB(e2, st->emid2), st->ihw[1]);
+// Fixed-point window tests of the scan (chain.h LlrState).
+__device__ __forceinline__ bool llr_in(const LlrState* st, long long e1, long long e2) {
+  if (st->dims == 2) return e1 >= st->wlo[0] && e1 <= st->whi[0] && e2 >= st->wlo[1] && e2 <= st->whi[1];
+  const long long e = st->axis == 1 ? e1 : e2;
+  return e >= st->wlo[0] && e <= st->whi[0];
+}
+
+__device__ __forceinline__ double llr_nsq(const LlrState* st, long long e1, long long e2) {
+  const double x = DYM_MUL((double)(e1 - st->wmid[0]), st->wsc[0]);
+  const double y = DYM_MUL((double)(e2 - st->wmid[1]), st->wsc[1]);
   return DYM_ADD(DYM_MUL(x, x), DYM_MUL(y, y));
 }
 
-__device__ __forceinline__ bool in_box(const LlrState* st, double e1, double e2) {
-  return e1 >= st->elo && e1 <= st->ehi && e2 >= st->elo2 && e2 <= st->ehi2;
+__device__ __forceinline__ bool llr_closer(const LlrState* st, long long e1, long long e2, long long p1, long long p2) {
+  if (st->dims == 2) return llr_nsq(st, e1, e2) < llr_nsq(st, p1, p2);
+  const long long e = st->axis == 1 ? e1 : e2, p = st->axis == 1 ? p1 : p2;
+  return llabs(e - st->wmid[0]) < llabs(p - st->wmid[0]);
 }
 
-__device__ __forceinline__ uint32_t q_threshold(double q) {
-  const double t = DYM_MUL(q, 4294967296.0);
-  return t >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)t;
+// Inclusive prefix sum within aligned segments of `seg` lanes (a power of
+// two up to 32; exact: 64-bit integers).
+__device__ __forceinline__ long long seg_prefix(long long x, uint32_t lane, uint32_t seg) {
+#pragma unroll
+  for (uint32_t o = 1; o < 32; o <<= 1) {
+    const long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (o < seg && (lane & (seg - 1)) >= o) x += y;
+  }
+  return x;
 }
 
 template <int D>
@@ -61,8 +73,6 @@ __global__ void __launch_bounds__(kLlrWarps * 32) k_llr_propose(const LlrTile* _
                                                                 BatchGroups groups, int nhit) {
   extern __shared__ __align__(16) unsigned char smem[];
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  int* s_delta = reinterpret_cast<int*>(smem) + warp * 2 * kLlrMaxCls;  // this warp's class deltas
-  for (uint32_t x = lane; x < 2 * kLlrMaxCls; x += 32) s_delta[x] = 0;
   for (int g = 0; g < groups.n; ++g) {
     const BatchGroupDev& G = groups.g[g];
     stage_sub_tables(G.retr, G.inv, G.sub, G.P, G.npool, reinterpret_cast<double*>(smem + G.off_retr),
@@ -99,25 +109,48 @@ __global__ void __launch_bounds__(kLlrWarps * 32) k_llr_propose(const LlrTile* _
     const double aa = st->a, bg = st->bg, emid = st->emid, E0 = st->E[axis - 1];
     const LlrDrive2 d2{st->dims, st->E[1], st->emid2, st->ihw[0], st->ihw[1]};
     const bool drive = (mode == DYM_LLR_DRIVE);
-    const uint32_t qthr = drive ? q_threshold(st->qp[st->phase % (uint32_t)st->nphase]) : 0u;
     const uint32_t sweep = st->sweep;
     unsigned hits = 0, accs = 0;
+    long long de1 = 0, de2 = 0;
+    bool changed = false;
     if (lane < tl.count) {
       const uint32_t i = c.sites[tl.begin + lane];
       uint32_t b0 = 0;
       switch (tl.dir) {
-        case 0: b0 = visit_llr<D, 0>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, axis, aa, bg, E0, emid, d2, drive, qthr,
-                                     s_delta, hits, accs); break;
-        case 1: b0 = visit_llr<D, 1>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, axis, aa, bg, E0, emid, d2, drive, qthr,
-                                     s_delta, hits, accs); break;
-        case 2: if (D > 2) b0 = visit_llr<D, (D > 2 ? 2 : 0)>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, axis, aa,
-                                                               bg, E0, emid, d2, drive, qthr, s_delta, hits, accs);
+        case 0: b0 = visit_llr<D, 0>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, st->vf, axis, aa, bg, E0, emid, d2,
+                                     drive, de1, de2, hits, accs); break;
+        case 1: b0 = visit_llr<D, 1>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, st->vf, axis, aa, bg, E0, emid, d2,
+                                     drive, de1, de2, hits, accs); break;
+        case 2: if (D > 2) b0 = visit_llr<D, (D > 2 ? 2 : 0)>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, st->vf, axis,
+                                                               aa, bg, E0, emid, d2, drive, de1, de2, hits, accs);
           break;
-        case 3: if (D > 3) b0 = visit_llr<D, (D > 3 ? 3 : 0)>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, axis, aa,
-                                                               bg, E0, emid, d2, drive, qthr, s_delta, hits, accs);
+        case 3: if (D > 3) b0 = visit_llr<D, (D > 3 ? 3 : 0)>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, st->vf, axis,
+                                                               aa, bg, E0, emid, d2, drive, de1, de2, hits, accs);
           break;
       }
-      c.oldv[tl.pos + lane] = (uint16_t)b0;
+      changed = c.links[(size_t)tl.dir * c.V + i] != (uint16_t)b0;
+      LlrLinkRec r;
+      r.site = i;
+      r.old = (uint16_t)b0;
+      r.changed = changed;
+      c.rec[tl.pos + lane] = r;
+    }
+    // Block records: tiles start at multiples of 32 and blocks of st->blk
+    // (a power of two up to 32) links never straddle them; lanes past the
+    // phase's end add nothing.
+    {
+      const uint32_t blk = (uint32_t)st->blk;
+      const long long p1 = seg_prefix(de1, lane, blk), p2 = seg_prefix(de2, lane, blk);
+      const uint32_t chg = __ballot_sync(0xffffffffu, changed);
+      if ((lane & (blk - 1)) == blk - 1 && (lane & ~(blk - 1)) < tl.count) {
+        const uint32_t segmask = (blk == 32 ? 0xffffffffu : ((1u << blk) - 1u)) << (lane & ~(blk - 1));
+        LlrBlockRec b;
+        b.s[0] = p1;
+        b.s[1] = p2;
+        b.nchg = __popc(chg & segmask);
+        b.pad = 0;
+        c.brec[(tl.pos + lane) / blk] = b;
+      }
     }
     hits = __reduce_add_sync(0xffffffffu, hits);
     accs = __reduce_add_sync(0xffffffffu, accs);
@@ -125,115 +158,89 @@ __global__ void __launch_bounds__(kLlrWarps * 32) k_llr_propose(const LlrTile* _
       if (hits) atomicAdd(&st->hits, (unsigned long long)hits);
       if (accs) atomicAdd(&st->accepts, (unsigned long long)accs);
     }
-    __syncwarp();  // every lane's shared-memory deltas are in
-    const uint32_t buf = st->phase & 1u;
-    for (uint32_t x = lane; x < 2 * kLlrMaxCls; x += 32) {
-      const int v = s_delta[x];
-      if (v) {
-        atomicAdd(reinterpret_cast<unsigned long long*>(&st->d[buf][x / kLlrMaxCls][x % kLlrMaxCls]),
-                  (unsigned long long)(long long)v);
-        s_delta[x] = 0;
-      }
-    }
-    __syncwarp();
   }
 }
 
-// After the commit: the links of a refused class move get their old values.
-__global__ void k_llr_restore(const LlrTile* __restrict__ tiles, uint32_t ntiles,
-                              const LlrChainDev* __restrict__ chains) {
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t stride = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntiles; t += stride) {
-    const LlrTile tl = tiles[t];
-    const LlrChainDev c = chains[tl.chain];
-    if (!c.st->restore || lane >= tl.count) continue;
-    const uint32_t i = c.sites[tl.begin + lane];
-    uint16_t* own = c.links + (size_t)tl.dir * c.V + i;
-    const uint16_t old = c.oldv[tl.pos + lane];
-    if (*own != old) *own = old;
-  }
-}
-
-// One warp per chain whose phase the slot closes.  The lanes form the class
-// products (h + d) v of both histograms at once; lane 0 sums them in class
-// order, which gives the oracle's class sums bit for bit, decides the class
-// move from them, and runs the chain's state machine.
+// One warp per chain whose phase the slot closes: the scan of the phase's
+// blocks in site-list order, 32 block records per load (the next 32 loading
+// meanwhile).  A block with changed links is kept iff the running energy plus
+// its change stays in the window (in the drive-in: iff it comes closer to the
+// centre); refused blocks are flagged for k_llr_restore.  Lane 0 then
+// advances the chain's state machine.
 __global__ void k_llr_commit(const LlrCommit* __restrict__ commits, uint32_t n,
                              const LlrChainDev* __restrict__ chains) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (idx >= n) return;  // the same for every lane of the warp
   const LlrCommit cm = commits[idx];
-  LlrState* st = chains[cm.chain].st;
+  const LlrChainDev c = chains[cm.chain];
+  LlrState* st = c.st;
   int mode = st->mode;
   if (mode >= DYM_LLR_DONE) {
     if (lane == 0) st->restore = 0;
     return;
   }
-  const uint32_t buf = st->phase & 1u;
-  const int ncls = st->ncls;
-  double p1 = 0, p2 = 0;
-  long long n1 = 0, n2 = 0;
-  if ((int)lane < ncls) {
-    n1 = st->h[0][lane] + st->d[buf][0][lane];
-    n2 = st->h[1][lane] + st->d[buf][1][lane];
-    p1 = DYM_MUL((double)n1, st->v[lane]);
-    p2 = DYM_MUL((double)n2, st->v[lane]);
-  }
-  double En1 = 0, En2 = 0;  // the energies after the class move
-  for (int c = 0; c < ncls; ++c) {
-    En1 = DYM_ADD(En1, __shfl_sync(0xffffffffu, p1, c));
-    En2 = DYM_ADD(En2, __shfl_sync(0xffffffffu, p2, c));
-  }
+  const bool drive = (mode == DYM_LLR_DRIVE);
+  const bool box = st->dims == 2;
   const int w = st->axis - 1;
-  const double Eo1 = st->E[0], Eo2 = st->E[1];
-  const double Enw = w ? En2 : En1, Eow = w ? Eo2 : Eo1;
-  bool ok;
-  if (st->dims == 2) {
-    ok = mode == DYM_LLR_DRIVE ? norm_sq(st, En1, En2) < norm_sq(st, Eo1, Eo2) : in_box(st, En1, En2);
-  } else {
-    ok = mode == DYM_LLR_DRIVE ? fabs(DYM_SUB(Enw, st->emid)) < fabs(DYM_SUB(Eow, st->emid))
-                               : (Enw >= st->elo && Enw <= st->ehi);
-  }
-  if (ok && (int)lane < ncls) {
-    st->h[0][lane] = n1;
-    st->h[1][lane] = n2;
-  }
-  for (uint32_t x = lane; x < (uint32_t)kLlrMaxCls; x += 32) {
-    st->d[buf][0][x] = 0;
-    st->d[buf][1][x] = 0;
+  const long long lo0 = st->wlo[0], hi0 = st->whi[0], mid0 = st->wmid[0];
+  const long long lo1 = st->wlo[1], hi1 = st->whi[1], mid1 = st->wmid[1];
+  const double sc0 = st->wsc[0], sc1 = st->wsc[1];
+  // The scan's tests (llr_in, llr_closer) on register copies of the window.
+  auto in_win = [&](long long e1, long long e2) -> bool {
+    if (box) return e1 >= lo0 && e1 <= hi0 && e2 >= lo1 && e2 <= hi1;
+    const long long e = w ? e2 : e1;
+    return e >= lo0 && e <= hi0;
+  };
+  auto closer = [&](long long e1, long long e2, long long q1, long long q2) -> bool {
+    if (box) {
+      const double x = DYM_MUL((double)(e1 - mid0), sc0), y = DYM_MUL((double)(e2 - mid1), sc1);
+      const double u = DYM_MUL((double)(q1 - mid0), sc0), v = DYM_MUL((double)(q2 - mid1), sc1);
+      return DYM_ADD(DYM_MUL(x, x), DYM_MUL(y, y)) < DYM_ADD(DYM_MUL(u, u), DYM_MUL(v, v));
+    }
+    const long long e = w ? e2 : e1, q = w ? q2 : q1;
+    return llabs(e - mid0) < llabs(q - mid0);
+  };
+  const uint32_t blk = (uint32_t)st->blk, lb = (uint32_t)(__ffs((int)blk) - 1);
+  const uint32_t nblocks = (cm.count + blk - 1) >> lb;
+  long long R1 = st->Ef[0], R2 = st->Ef[1];
+  unsigned kept = 0, refused = 0;
+  LlrBlockRec br{};
+  if (lane < nblocks) br = c.brec[lane];
+  for (uint32_t wave = 0; wave < nblocks; wave += 32) {
+    LlrBlockRec next{};  // the next 32 block records, in flight meanwhile
+    if (wave + 32 + lane < nblocks) next = c.brec[wave + 32 + lane];
+    const uint32_t nj = nblocks - wave < 32 ? nblocks - wave : 32;
+    uint32_t refused_blocks = 0;
+#pragma unroll 8
+    for (uint32_t j = 0; j < 32; ++j) {
+      const uint32_t nch = __shfl_sync(0xffffffffu, br.nchg, j);
+      const long long s1 = __shfl_sync(0xffffffffu, br.s[0], j), s2 = __shfl_sync(0xffffffffu, br.s[1], j);
+      if (j < nj && nch) {  // the same for every lane
+        const long long e1 = R1 + s1, e2 = R2 + s2;
+        if (drive ? closer(e1, e2, R1, R2) : in_win(e1, e2)) {
+          R1 = e1;
+          R2 = e2;
+          kept += nch;
+        } else {
+          refused += nch;
+          refused_blocks |= 1u << j;
+        }
+      }
+    }
+    if (lane < nj) c.bref[wave + lane] = (uint8_t)((refused_blocks >> lane) & 1u);
+    br = next;
   }
   if (lane != 0) return;
-  const double dE = DYM_SUB(Enw, Eow), dE2 = DYM_SUB(En2, Eo2);
-  st->restore = ok ? 0 : 1;
-  if (ok) {
-    st->E[0] = En1;
-    st->E[1] = En2;
-    st->phase_acc++;
-  } else {
-    st->phase_rej++;
-  }
-  const uint32_t pidx = st->phase % (uint32_t)st->nphase;
+  st->restore = refused ? 1 : 0;
+  st->Ef[0] = R1;
+  st->Ef[1] = R2;
+  st->E[0] = DYM_MUL((double)R1, 0x1p-32);
+  st->E[1] = DYM_MUL((double)R2, 0x1p-32);
+  st->phase_acc += kept;
+  st->phase_rej += refused;
   st->phase++;
-  if (mode == DYM_LLR_DRIVE) {
-    // Aim this phase's next expected move at the remaining distance (in a
-    // two-dimensional cell: normalised distance and normalised move).
-    double dist, move;
-    if (st->dims == 2) {
-      dist = sqrt(norm_sq(st, st->E[0], st->E[1]));
-      const double x = DYM_MUL(dE, st->ihw[0]), y = DYM_MUL(dE2, st->ihw[1]);
-      move = sqrt(DYM_ADD(DYM_MUL(x, x), DYM_MUL(y, y)));
-    } else {
-      dist = fabs(DYM_SUB(st->emid, st->E[w]));
-      move = fabs(dE);
-    }
-    const double qo = st->qp[pidx];
-    const double q = move > 0 ? DYM_MUL(qo, dist / move) : DYM_MUL(qo, 2.0);
-    st->qp[pidx] = fmin(1.0, fmax(q, 0x1.0p-32));
-    const bool in = st->dims == 2 ? in_box(st, st->E[0], st->E[1]) : (st->E[w] >= st->elo && st->E[w] <= st->ehi);
-    if (in) mode = DYM_LLR_SETTLE;
-  }
+  if (mode == DYM_LLR_DRIVE && llr_in(st, R1, R2)) mode = DYM_LLR_SETTLE;
   if (cm.last) {
     st->sweeps++;
     st->sweep++;
@@ -268,6 +275,24 @@ __global__ void k_llr_commit(const LlrCommit* __restrict__ commits, uint32_t n,
     }
   }
   st->mode = mode;
+}
+
+// After the commit: the changed links of refused blocks get their old values
+// (a warp per propose tile, so every SM takes part).
+__global__ void k_llr_restore(const LlrTile* __restrict__ tiles, uint32_t ntiles,
+                              const LlrChainDev* __restrict__ chains) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t stride = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntiles; t += stride) {
+    const LlrTile tl = tiles[t];
+    const LlrChainDev c = chains[tl.chain];
+    if (!c.st->restore || lane >= tl.count) continue;
+    const uint32_t pos = tl.pos + lane;
+    const uint32_t lb = (uint32_t)(__ffs(c.st->blk) - 1);
+    if (!c.bref[pos >> lb]) continue;
+    const LlrLinkRec r = c.rec[pos];
+    if (r.changed) c.links[(size_t)tl.dir * c.V + r.site] = r.old;
+  }
 }
 
 }  // namespace

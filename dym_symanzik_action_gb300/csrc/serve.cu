@@ -21,6 +21,10 @@ namespace dym {
 
 namespace {
 
+// A value in the fixed point of the LLR energies (times 2^kLlrFixShift, to
+// the nearest integer).
+long long fix_value(double x) { return std::llrint(std::ldexp(x, kLlrFixShift)); }
+
 double class_sum_host(const long long* h, const std::vector<double>& v, int ncls) {
   double s = 0;
   for (int q = 0; q < ncls; ++q) s = s + (double)h[q] * v[q];
@@ -60,8 +64,6 @@ int check_llr_req(const dym_chain* c, const dym_llr_req* req) {
     return fail(DYM_ENOTSUP, "an S2 window needs every extent >= 3 (1x2 rectangles wrap otherwise)");
   if (c->p.pool != DYM_POOL_NEAREST) return fail(DYM_ENOTSUP, "LLR proposals use the nearest-element pool");
   if (c->p.D != 4) return fail(DYM_ENOTSUP, "LLR runs on four-dimensional lattices");
-  if (c->sched.phase_dir.size() > (size_t)kLlrMaxPhases)
-    return fail(DYM_ENOTSUP, "LLR: the lattice's colour schedule has more than 256 phases");
   return check_llr_group(*c->grp->g);
 }
 
@@ -79,10 +81,14 @@ int llr_init_state(dym_chain* c, const dym_llr_req* req, LlrState* st, const Llr
     DYM_CUDA(dmalloc(&c->d_llr, 1), "cudaMalloc(llr)");
     uint32_t maxlen = 1;
     for (auto l : c->sched.phase_len) maxlen = std::max(maxlen, l);
-    DYM_CUDA(dmalloc(&c->d_oldv, maxlen), "cudaMalloc(llr oldv)");
+    const size_t nrec = (maxlen + 31) / 32 * 32;  // whole 32-link tiles
+    DYM_CUDA(dmalloc(&c->d_llr_rec, nrec), "cudaMalloc(llr link records)");
+    DYM_CUDA(dmalloc(&c->d_llr_blk, nrec), "cudaMalloc(llr block records)");
+    DYM_CUDA(dmalloc(&c->d_llr_bref, nrec), "cudaMalloc(llr block flags)");
   }
   std::memset(st, 0, sizeof(LlrState));
-  int rc = class_histograms(c, st->h);
+  long long h[2][kLlrMaxCls];
+  int rc = class_histograms(c, h);
   if (rc) return rc;
   const double W = 2 * req->hw;
   st->a = req->a0;
@@ -92,19 +98,23 @@ int llr_init_state(dym_chain* c, const dym_llr_req* req, LlrState* st, const Llr
   st->ehi = req->ewin + req->hw;
   st->emid = 0.5 * (st->elo + st->ehi);
   st->w2 = W * W;
-  st->nphase = (int)c->sched.phase_dir.size();
-  for (int p = 0; p < st->nphase; ++p) st->qp[p] = 1.0;
-  st->ncls = g.ncls;
-  for (int q = 0; q < g.ncls; ++q) st->v[q] = g.cls_val[q];
-  st->E[0] = class_sum_host(st->h[0], g.cls_val, g.ncls);
-  st->E[1] = class_sum_host(st->h[1], g.cls_val, g.ncls);
+  // Fixed-point class values, energies and window bounds (LlrState).
+  for (int q = 0; q < g.ncls; ++q) st->vf[q] = fix_value(g.cls_val[q]);
+  for (int t = 0; t < 2; ++t) {
+    st->Ef[t] = 0;
+    for (int q = 0; q < g.ncls; ++q) st->Ef[t] += h[t][q] * st->vf[q];
+    st->E[t] = std::ldexp((double)st->Ef[t], -kLlrFixShift);
+  }
+  st->wlo[0] = fix_value(st->elo);
+  st->whi[0] = fix_value(st->ehi);
+  st->wmid[0] = fix_value(st->emid);
   st->axis = req->axis;
   st->K = req->K;
   st->NRM = req->NRM;
   st->drive_cap = req->drive_cap;
   st->sweep = c->sweep;
-  const double Ew = st->E[req->axis - 1];
-  st->mode = (Ew >= st->elo && Ew <= st->ehi) ? DYM_LLR_RM : DYM_LLR_DRIVE;
+  const long long Ewf = st->Ef[req->axis - 1];
+  st->mode = (Ewf >= st->wlo[0] && Ewf <= st->whi[0]) ? DYM_LLR_RM : DYM_LLR_DRIVE;
   st->dims = 1;
   if (cell) {
     st->dims = 2;
@@ -116,8 +126,19 @@ int llr_init_state(dym_chain* c, const dym_llr_req* req, LlrState* st, const Llr
     st->w2b = (2 * cell->hw2) * (2 * cell->hw2);
     st->ihw[0] = 1.0 / req->hw;
     st->ihw[1] = 1.0 / cell->hw2;
-    const bool in = st->E[0] >= st->elo && st->E[0] <= st->ehi && st->E[1] >= st->elo2 && st->E[1] <= st->ehi2;
+    st->wlo[1] = fix_value(st->elo2);
+    st->whi[1] = fix_value(st->ehi2);
+    st->wmid[1] = fix_value(st->emid2);
+    st->wsc[0] = std::ldexp(st->ihw[0], -kLlrFixShift);
+    st->wsc[1] = std::ldexp(st->ihw[1], -kLlrFixShift);
+    const bool in = st->Ef[0] >= st->wlo[0] && st->Ef[0] <= st->whi[0] && st->Ef[1] >= st->wlo[1] &&
+                    st->Ef[1] <= st->whi[1];
     st->mode = in ? DYM_LLR_RM : DYM_LLR_DRIVE;
+  }
+  {
+    const auto mm = std::minmax_element(g.retr.begin(), g.retr.end());
+    st->blk = dym_llr_block_links(c->p.D, *mm.second - *mm.first, st->dims, st->axis, req->hw,
+                                  cell ? cell->hw2 : 0.0);
   }
   if (req->NRM == 0 && st->mode == DYM_LLR_RM) st->mode = DYM_LLR_DONE;
   if (st->mode == DYM_LLR_DRIVE && req->drive_cap == 0) st->mode = DYM_LLR_UNREACHED;
@@ -178,7 +199,7 @@ struct LlrWork {
     groups.push_back(g);
     // layout
     auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
-    size_t off = kLlrDeltaBytes;
+    size_t off = 0;
     bg.n = (int)groups.size();
     for (size_t k = 0; k < groups.size(); ++k) {
       const Group& G = *groups[k];
@@ -226,7 +247,9 @@ struct LlrWork {
       d.Nx = c->p.Nx;
       d.seed = c->p.seed;
       d.st = c->d_llr;
-      d.oldv = c->d_oldv;
+      d.rec = c->d_llr_rec;
+      d.brec = c->d_llr_blk;
+      d.bref = c->d_llr_bref;
       d.group = (int)(std::find(groups.begin(), groups.end(), c->grp->g) - groups.begin());
       maxph = std::max(maxph, c->sched.phase_dir.size());
     }
@@ -246,7 +269,8 @@ struct LlrWork {
         for (uint32_t j = 0; j < s.phase_len[k]; j += T)
           tiles.push_back(LlrTile{(uint32_t)i, s.phase_off[k] + j, std::min(T, s.phase_len[k] - j),
                                   (uint32_t)s.phase_dir[k], j});
-        commits.push_back(LlrCommit{(uint32_t)i, k + 1 == s.phase_dir.size() ? 1u : 0u});
+        commits.push_back(LlrCommit{(uint32_t)i, k + 1 == s.phase_dir.size() ? 1u : 0u, s.phase_len[k],
+                                    (uint32_t)s.phase_dir[k]});
       }
       tile_cnt[k] = (uint32_t)tiles.size() - tile_off[k];
       commit_cnt[k] = (uint32_t)commits.size() - commit_off[k];
@@ -436,8 +460,10 @@ namespace {
 uint64_t chain_bytes(int D, int Nt, int Nx, uint32_t P) {
   uint64_t V = (uint64_t)Nt;
   for (int d = 1; d < D; ++d) V *= (uint64_t)Nx;
-  // links + site lists + oldv + LLR state + measurement histograms and pinned copies
-  return V * D * 2 + V * D * 4 + V * 2 + sizeof(LlrState) + 2 * 3ull * P * 8;
+  // links + site lists + link and block records of a phase (at most V links) +
+  // LLR state + measurement histograms and pinned copies
+  return V * D * 2 + V * D * 4 + (V + 31) / 32 * 32 * (sizeof(LlrLinkRec) + sizeof(LlrBlockRec) + 1) +
+         sizeof(LlrState) + 2 * 3ull * P * 8;
 }
 
 int server_admit(dym_server* s) {

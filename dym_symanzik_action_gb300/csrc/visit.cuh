@@ -413,16 +413,17 @@ __device__ __forceinline__ bool llr_weight_accept(double x, uint32_t r1, uint32_
 // One LLR visit of link (i, DIR) with the shared sub-table (llr.cpp:186-216
 // per hit): nhit hits with weight exp(-a dE_w - bg dE_bg), or, in drive-in
 // mode, greedy moves of the link's running energy towards emid.  The link is
-// written in place and its plaquette/rectangle class changes are added to
-// s_delta; returns the value before the visit.  The classes of the initial
-// u_j are kept packed, 5 bits each, for the class changes, and the two hit
-// loops are separate so that neither holds the other's state.
+// written in place; returns its value before the visit, and in de1, de2 the
+// exact fixed-point change of S1 and S2 (vf: class values times
+// 2^kLlrFixShift), which the scan of the commit kernel tests against the
+// window.  The classes of the initial u_j are kept packed, 5 bits each, and
+// the two hit loops are separate so that neither holds the other's state.
 template <int D, int DIR>
 __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
                                               const uint16_t* s_inv, const uint16_t* s_sub, const uint16_t* s_cls,
-                                              int axis, double aa, double bg, double E0, double emid,
-                                              const LlrDrive2& d2, bool drive, uint32_t qthr, int* s_delta,
-                                              unsigned& hits, unsigned& accs) {
+                                              const long long* __restrict__ vf, int axis, double aa, double bg,
+                                              double E0, double emid, const LlrDrive2& d2, bool drive,
+                                              long long& de1, long long& de2, unsigned& hits, unsigned& accs) {
   constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
   constexpr int NW = (NT + 5) / 6;  // words of six 5-bit classes
   static_assert(kLlrMaxCls <= 32, "classes are packed in 5 bits");
@@ -448,47 +449,45 @@ __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, ui
 #pragma unroll
   for (int j = NS; j < NT; ++j) m1 = DYM_ADD(m1, s_retr[u[j]]);
   if (drive) {
-    if (dym_hit_random(a.seed, sweep, i, DIR, 0xFFFFFu, DYM_TAG_LLR).v[0] < qthr) {
-      double cum = 0, cum2 = 0;
-      for (int h = 0; h < a.nhit; ++h) {
-        const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_LLR);
-        const uint16_t* row = s_sub + dym_pick(r.v[0], a.npool) * a.P;
-        uint32_t e[NT];
-        double r1n = 0, m1n = 0;
+    double cum = 0, cum2 = 0;
+    for (int h = 0; h < a.nhit; ++h) {
+      const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_LLR);
+      const uint16_t* row = s_sub + dym_pick(r.v[0], a.npool) * a.P;
+      uint32_t e[NT];
+      double r1n = 0, m1n = 0;
 #pragma unroll
-        for (int j = 0; j < NS; ++j) {
-          e[j] = row[u[j]];
-          r1n = DYM_ADD(r1n, s_retr[e[j]]);
-        }
+      for (int j = 0; j < NS; ++j) {
+        e[j] = row[u[j]];
+        r1n = DYM_ADD(r1n, s_retr[e[j]]);
+      }
 #pragma unroll
-        for (int j = NS; j < NT; ++j) {
-          e[j] = row[u[j]];
-          m1n = DYM_ADD(m1n, s_retr[e[j]]);
-        }
-        const double dS1 = DYM_SUB(r1n, r1), dS2 = DYM_SUB(m1n, m1);
-        const double dEw = axis == 1 ? dS1 : dS2;
-        bool acc;
-        if (d2.dims == 2) {  // closer to the cell centre in normalised distance (llr2d.cpp:206-209)
-          const double c1 = DYM_ADD(E0, cum), c2 = DYM_ADD(d2.E0b, cum2);
-          const double x1 = DYM_MUL(DYM_SUB(c1, emid), d2.ihw0), y1 = DYM_MUL(DYM_SUB(c2, d2.emid2), d2.ihw1);
-          const double x2 = DYM_MUL(DYM_SUB(DYM_ADD(c1, dS1), emid), d2.ihw0);
-          const double y2 = DYM_MUL(DYM_SUB(DYM_ADD(c2, dS2), d2.emid2), d2.ihw1);
-          acc = DYM_ADD(DYM_MUL(x2, x2), DYM_MUL(y2, y2)) < DYM_ADD(DYM_MUL(x1, x1), DYM_MUL(y1, y1));
-        } else {
-          const double Ec = DYM_ADD(E0, cum);
-          acc = fabs(DYM_SUB(DYM_ADD(Ec, dEw), emid)) < fabs(DYM_SUB(Ec, emid));
-        }
-        ++hits;
-        if (acc) {
-          b = row[b];
+      for (int j = NS; j < NT; ++j) {
+        e[j] = row[u[j]];
+        m1n = DYM_ADD(m1n, s_retr[e[j]]);
+      }
+      const double dS1 = DYM_SUB(r1n, r1), dS2 = DYM_SUB(m1n, m1);
+      const double dEw = axis == 1 ? dS1 : dS2;
+      bool acc;
+      if (d2.dims == 2) {  // closer to the cell centre in normalised distance (llr2d.cpp:206-209)
+        const double c1 = DYM_ADD(E0, cum), c2 = DYM_ADD(d2.E0b, cum2);
+        const double x1 = DYM_MUL(DYM_SUB(c1, emid), d2.ihw0), y1 = DYM_MUL(DYM_SUB(c2, d2.emid2), d2.ihw1);
+        const double x2 = DYM_MUL(DYM_SUB(DYM_ADD(c1, dS1), emid), d2.ihw0);
+        const double y2 = DYM_MUL(DYM_SUB(DYM_ADD(c2, dS2), d2.emid2), d2.ihw1);
+        acc = DYM_ADD(DYM_MUL(x2, x2), DYM_MUL(y2, y2)) < DYM_ADD(DYM_MUL(x1, x1), DYM_MUL(y1, y1));
+      } else {
+        const double Ec = DYM_ADD(E0, cum);
+        acc = fabs(DYM_SUB(DYM_ADD(Ec, dEw), emid)) < fabs(DYM_SUB(Ec, emid));
+      }
+      ++hits;
+      if (acc) {
+        b = row[b];
 #pragma unroll
-          for (int j = 0; j < NT; ++j) u[j] = e[j];
-          r1 = r1n;
-          m1 = m1n;
-          cum = DYM_ADD(cum, dEw);
-          cum2 = DYM_ADD(cum2, dS2);
-          ++accs;
-        }
+        for (int j = 0; j < NT; ++j) u[j] = e[j];
+        r1 = r1n;
+        m1 = m1n;
+        cum = DYM_ADD(cum, dEw);
+        cum2 = DYM_ADD(cum2, dS2);
+        ++accs;
       }
     }
   } else {
@@ -521,14 +520,16 @@ __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, ui
       }
     }
   }
+  de1 = 0;
+  de2 = 0;
   if (b != b0) {
     *own = (uint16_t)b;
     // Class of b s_j equals the class of its conjugate s_j b = u_j.
 #pragma unroll
     for (int j = 0; j < NT; ++j) {
-      const int off = j < NS ? 0 : kLlrMaxCls;
-      atomicAdd(&s_delta[off + ((c0[j / 6] >> (5 * (j % 6))) & 31u)], -1);
-      atomicAdd(&s_delta[off + s_cls[u[j]]], 1);
+      const long long dv = __ldg(vf + s_cls[u[j]]) - __ldg(vf + ((c0[j / 6] >> (5 * (j % 6))) & 31u));
+      if (j < NS) de1 += dv;
+      else de2 += dv;
     }
   }
   return b0;

@@ -261,12 +261,12 @@ typedef struct {
 
 typedef struct {
   double a;            /* final a_n */
-  double S1, S2;       /* energies at the end (exact class sums) */
+  double S1, S2;       /* energies at the end (exact 2^-32 fixed-point class sums) */
   int32_t status;      /* DYM_LLR_DONE or DYM_LLR_UNREACHED */
   int32_t drive_sweeps;
   int32_t sweeps;      /* sweeps run by this call */
   uint64_t hits, accepts;
-  uint64_t phase_accepts, phase_rejects;  /* colour-class moves kept / reverted by the window */
+  uint64_t phase_accepts, phase_rejects;  /* changed links kept / reverted by the window scan */
 } dym_llr_result;
 
 /* Exact S1 = sum over plaquettes of ReTr and S2 = sum over 1x2 rectangles of
@@ -279,10 +279,12 @@ int dym_llr_energy(dym_chain* c, double* S1, double* S2);
  * iterations of K constrained sweeps, a += 12/(W^2 (m+1)) (<E> - ewin)
  * (rm_solve, llr.cpp:234-250).  Sweeps are colour-parallel: every link of a
  * colour class does nhit Metropolis hits of weight exp(-a dE_w - bg dE_bg)
- * (llr.cpp:208-212) and the class move is kept iff the new windowed energy
- * lies in the window, else reverted (outside the window: kept iff it moves the
- * energy towards the centre).  a_hist (may be NULL) receives a after each of
- * the NRM iterations. */
+ * (llr.cpp:208-212), then the class's changed links are scanned in site-list
+ * order and a link's move is kept iff the running windowed energy stays in
+ * the window, else reverted (outside the window: kept iff it moves the energy
+ * towards the centre) -- the reference's per-hit window test at the
+ * granularity of one link's hits.  a_hist (may be NULL) receives a after each
+ * of the NRM iterations. */
 int dym_llr_run(dym_chain* c, const dym_llr_req* req, dym_llr_result* out, double* a_hist);
 
 /* Two-dimensional LLR cell (replaces update_constrained2d, seed_cell and

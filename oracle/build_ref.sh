@@ -10,6 +10,8 @@
 #                       flags of the reference Makefile (-O3 -g -pg -fopenmp)
 #   _ref/dym-mod-metro-nhit10   the same with NHIT 10 instead of 20: the source
 #                       is streamed through sed into the compiler (no copy)
+#   _ref/llr            the unmodified LLR window-ladder executable (llr.cpp),
+#                       reference Makefile flags
 set -e
 REF_DIR=${REF_DIR:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -41,4 +43,6 @@ $CXX -O3 -g -pg -fopenmp -std=c++11 -w -I"$REF_DIR" "$REF_DIR/dym-mod-metro.cpp"
 sed 's/^#define NHIT[ \t]*20/#define NHIT 10/' "$REF_DIR/dym-mod-metro.cpp" | \
   $CXX -O3 -g -pg -fopenmp -std=c++11 -w -I"$REF_DIR" -x c++ - -x none \
   "$OUT/lattice.o" "$OUT/group.o" "$OUT/timer.o" -lm -o "$OUT/dym-mod-metro-nhit10"
+$CXX -O3 -g -pg -fopenmp -std=c++11 -w -I"$REF_DIR" "$REF_DIR/llr.cpp" \
+  "$OUT/lattice.o" "$OUT/group.o" "$OUT/timer.o" -lm -o "$OUT/llr"
 echo "built $OUT"

@@ -454,12 +454,23 @@ void or_measure(const or_lattice* L, int wl_nx, int wl_nt, double* out, uint64_t
 /* -------------------------------------------------------------------- LLR */
 /* Restatement of the engine's colour-parallel LLR (test oracle), following
  * llr.cpp:178-250 of the reference for the per-hit rule, the drive-in rule
- * and the Robbins-Monro step, with the class-level window test of the engine
- * (a colour class's move is kept iff the new windowed energy is in the
- * window; outside the window iff it is closer to the centre).  Energies are
- * exact integer class histograms of plaquettes and rectangles. */
+ * and the Robbins-Monro step.  The reference tests the window after every
+ * hit, one link at a time.  The engine lets every link of a colour class run
+ * its hits at once (the links of a class share no plaquette or rectangle) and
+ * then scans the class in site-list order in blocks of dym_llr_block_links
+ * links: a block's moves are kept iff the running energy plus their change
+ * stays in the window (outside the window: iff it comes closer to the
+ * centre), else its links get their old values back.  Each step of the scan
+ * leaves the window-restricted distribution invariant, as the reference's
+ * per-hit test does, and a block's change is at most a quarter of the window
+ * width, so a block can always move away from a wall.  Energies
+ * are exact 64-bit fixed-point sums of the plaquette and rectangle class
+ * values (each value times 2^32, rounded): a kept link adds its exact integer
+ * change, so the tracked energy never drifts from the configuration's, and
+ * the FP64 energy the Robbins-Monro step averages is that sum times 2^-32. */
 
 #define OR_MAXCLS 32
+#define OR_FIX_S 32
 
 /* ReTr value classes: elements sorted by ReTr, a new class whenever a value
  * exceeds the first value of the current class by more than 1e-9; the class
@@ -490,16 +501,43 @@ static int or_classes(const or_group* g, int* cls, double* val) {
   return n;
 }
 
-static double or_class_sum(const long long* h, const long long* d, const double* v, int n) {
-  double s = 0;
-  for (int c = 0; c < n; ++c) s = s + (double)(h[c] + (d ? d[c] : 0)) * v[c];
+static long long or_class_fix(const long long* h, const long long* vf, int n) {
+  long long s = 0;
+  for (int c = 0; c < n; ++c) s += h[c] * vf[c];
   return s;
 }
 
+static long long or_fix(double x) { return llrint(ldexp(x, OR_FIX_S)); }
+
 enum { OR_DRIVE = 0, OR_SETTLE = 1, OR_RM = 2, OR_DONE = 3, OR_UNREACHED = 4 };
 
+/* The window tests of the scan on fixed-point energies (e1, e2): in the
+ * window (box), and closer to the centre than (p1, p2). */
+typedef struct {
+  int dims, w;
+  long long lo[2], hi[2], mid[2];
+  double sc[2]; /* 2^-32 / half-width per axis (two-dimensional drive-in) */
+} or_win;
+
+static int or_in(const or_win* W, long long e1, long long e2) {
+  if (W->dims == 2) return e1 >= W->lo[0] && e1 <= W->hi[0] && e2 >= W->lo[1] && e2 <= W->hi[1];
+  const long long e = W->w == 0 ? e1 : e2;
+  return e >= W->lo[0] && e <= W->hi[0];
+}
+
+static double or_nsq(const or_win* W, long long e1, long long e2) {
+  const double x = (double)(e1 - W->mid[0]) * W->sc[0], y = (double)(e2 - W->mid[1]) * W->sc[1];
+  return x * x + y * y;
+}
+
+static int or_closer(const or_win* W, long long e1, long long e2, long long p1, long long p2) {
+  if (W->dims == 2) return or_nsq(W, e1, e2) < or_nsq(W, p1, p2);
+  const long long e = W->w == 0 ? e1 : e2, p = W->w == 0 ? p1 : p2;
+  return llabs(e - W->mid[0]) < llabs(p - W->mid[0]);
+}
+
 /* out[0..3] = a, S1, S2, mode; iout[0..5] = drive_sweeps, sweeps, hits,
- * accepts, phase_accepts, phase_rejects; a_hist[NRM]. */
+ * accepts, links kept by the scan, links refused; a_hist[NRM]. */
 /* dims == 2: a two-dimensional cell (llr2d.cpp:178-259), axis 1, S2 window
  * [ewin2 - hw2, ewin2 + hw2], bg is a2 and is Robbins-Monro updated too, a2_hist
  * receives it; drive-in compares squared normalised distances to the centre. */
@@ -511,9 +549,11 @@ static int llr_impl(or_lattice* L, const int* phase_dir, const uint32_t* phase_l
   const unsigned D = L->D, V = L->V;
   int* cls = (int*)malloc(sizeof(int) * g->P);
   double v[OR_MAXCLS];
+  long long vf[OR_MAXCLS];
   const int ncls = or_classes(g, cls, v);
   if (ncls < 0) { free(cls); return -6; }
-  long long h[2][OR_MAXCLS] = {{0}}, d[2][OR_MAXCLS];
+  for (int c = 0; c < ncls; ++c) vf[c] = or_fix(v[c]);
+  long long h[2][OR_MAXCLS] = {{0}};
   for (unsigned i = 0; i < V; ++i) {
     for (unsigned d1 = 0; d1 < D; ++d1)
       for (unsigned d2 = d1 + 1; d2 < D; ++d2) h[0][cls[plaq_elem(L, i, d1, d2)]]++;
@@ -521,38 +561,47 @@ static int llr_impl(or_lattice* L, const int* phase_dir, const uint32_t* phase_l
       for (unsigned d2 = 0; d2 < D; ++d2)
         if (d1 != d2) h[1][cls[wilson_elem(L, i, d1, d2, 2, 1)]]++;
   }
-  double E[2] = {or_class_sum(h[0], NULL, v, ncls), or_class_sum(h[1], NULL, v, ncls)};
+  long long Ef[2] = {or_class_fix(h[0], vf, ncls), or_class_fix(h[1], vf, ncls)};
+  double E[2] = {ldexp((double)Ef[0], -OR_FIX_S), ldexp((double)Ef[1], -OR_FIX_S)};
   const double W = 2 * hw, elo = ewin - hw, ehi = ewin + hw;
   const double emid = 0.5 * (elo + ehi), w2 = W * W;
   const double elo2 = ewin2 - hw2, ehi2 = ewin2 + hw2, emid2 = 0.5 * (elo2 + ehi2), w2b = (2 * hw2) * (2 * hw2);
   const double ihw0 = dims == 2 ? 1.0 / hw : 0, ihw1 = dims == 2 ? 1.0 / hw2 : 0;
-#define OR_NSQ(e1, e2) ((((e1) - emid) * ihw0) * (((e1) - emid) * ihw0) + (((e2) - emid2) * ihw1) * (((e2) - emid2) * ihw1))
-#define OR_INBOX(e1, e2) ((e1) >= elo && (e1) <= ehi && (e2) >= elo2 && (e2) <= ehi2)
+  or_win win;
+  win.dims = dims;
+  win.w = axis - 1;
+  win.lo[0] = or_fix(elo); win.hi[0] = or_fix(ehi); win.mid[0] = or_fix(emid);
+  win.lo[1] = or_fix(elo2); win.hi[1] = or_fix(ehi2); win.mid[1] = or_fix(emid2);
+  win.sc[0] = ldexp(ihw0, -OR_FIX_S); win.sc[1] = ldexp(ihw1, -OR_FIX_S);
   const int w = axis - 1;
   double a = a0, sumE = 0, sumE2 = 0;
-  double* qv = (double*)malloc(sizeof(double) * (size_t)(nphase > 0 ? nphase : 1));
-  for (int p = 0; p < nphase; ++p) qv[p] = 1.0;  /* drive-in fraction per colour phase */
-  int mode = (E[w] >= elo && E[w] <= ehi) ? OR_RM : OR_DRIVE;
-  if (dims == 2) mode = OR_INBOX(E[0], E[1]) ? OR_RM : OR_DRIVE;
+  int mode = or_in(&win, Ef[0], Ef[1]) ? OR_RM : OR_DRIVE;
   if (NRM == 0 && mode == OR_RM) mode = OR_DONE;
   if (mode == OR_DRIVE && drive_cap == 0) mode = OR_UNREACHED;
   int k = 0, m = 0, drive_sweeps = 0;
   long long hits = 0, accs = 0, pacc = 0, prej = 0;
   const long max_sweeps = (long)drive_cap + (long)K * NRM + 2;
   long sweeps = 0;
-  const int ns = 2 * ((int)D - 1), nr = 6 * ((int)D - 1);
-  uint32_t* chg_site = (uint32_t*)malloc(sizeof(uint32_t) * V);
-  int* chg_old = (int*)malloc(sizeof(int) * V);
+  const int ns = 2 * ((int)D - 1), nr = 6 * ((int)D - 1), nt = ns + nr;
+  double rmin = g->ReTr[0], rmax = g->ReTr[0];
+  for (unsigned e = 1; e < g->P; ++e) {
+    if (g->ReTr[e] < rmin) rmin = g->ReTr[e];
+    if (g->ReTr[e] > rmax) rmax = g->ReTr[e];
+  }
+  const int blk = dym_llr_block_links((int)D, rmax - rmin, dims, axis, hw, hw2);
+  /* Changed links of one phase: position in the phase, site, old value,
+   * fixed-point energy changes. */
+  uint32_t* rp = (uint32_t*)malloc(sizeof(uint32_t) * V);
+  uint32_t* rs = (uint32_t*)malloc(sizeof(uint32_t) * V);
+  int* rb0 = (int*)malloc(sizeof(int) * V);
+  long long* rde = (long long*)malloc(sizeof(long long) * 2 * V);
   while (mode < OR_DONE && sweeps < max_sweeps) {
     const uint32_t sweep = first_sweep + (uint32_t)sweeps;
     size_t off = 0;
     for (int p = 0; p < nphase && mode < OR_DONE; ++p) {
       const unsigned dir = (unsigned)phase_dir[p];
-      memset(d, 0, sizeof d);
       int nchg = 0;
       const int drive = (mode == OR_DRIVE);
-      const double t = qv[p] * 4294967296.0;
-      const uint32_t qthr = drive ? (t >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)t) : 0u;
       for (uint32_t kk = 0; kk < phase_len[p]; ++kk) {
         const unsigned i = sites[off + kk];
         int st[2 * 7], re[6 * 7];
@@ -562,13 +611,8 @@ static int llr_impl(or_lattice* L, const int* phase_dir, const uint32_t* phase_l
         double r1 = 0, m1 = 0;
         for (int j = 0; j < ns; ++j) r1 += g->ReTr[g->mult[b][st[j]]];
         for (int j = 0; j < nr; ++j) m1 += g->ReTr[g->mult[b][re[j]]];
-        int part = 1;
-        if (drive) {
-          dym_u32x4 r = dym_hit_random(seed, sweep, i, dir, 0xFFFFFu, DYM_TAG_LLR);
-          part = r.v[0] < qthr;
-        }
         double cum = 0, cum2 = 0;
-        for (int hh = 0; part && hh < nhit; ++hh) {
+        for (int hh = 0; hh < nhit; ++hh) {
           dym_u32x4 r = dym_hit_random(seed, sweep, i, dir, (uint32_t)hh, DYM_TAG_LLR);
           const double u1 = (double)r.v[0] * 0x1p-32;
           const int bnew = g->mult[b][g->pool[(size_t)(g->npool * u1)]];
@@ -594,38 +638,46 @@ static int llr_impl(or_lattice* L, const int* phase_dir, const uint32_t* phase_l
         }
         if (b != b0) {
           L->a[i * D + dir] = b;
-          chg_site[nchg] = i;
-          chg_old[nchg++] = b0;
-          for (int j = 0; j < ns; ++j) { d[0][cls[g->mult[b0][st[j]]]]--; d[0][cls[g->mult[b][st[j]]]]++; }
-          for (int j = 0; j < nr; ++j) { d[1][cls[g->mult[b0][re[j]]]]--; d[1][cls[g->mult[b][re[j]]]]++; }
+          long long de1 = 0, de2 = 0;
+          for (int j = 0; j < nt; ++j) {
+            const int s = j < ns ? st[j] : re[j - ns];
+            const long long dv = vf[cls[g->mult[b][s]]] - vf[cls[g->mult[b0][s]]];
+            if (j < ns) de1 += dv;
+            else de2 += dv;
+          }
+          rp[nchg] = kk;
+          rs[nchg] = i;
+          rb0[nchg] = b0;
+          rde[2 * nchg] = de1;
+          rde[2 * nchg + 1] = de2;
+          ++nchg;
         }
       }
       off += phase_len[p];
-      const double En = or_class_sum(h[w], d[w], v, ncls);
-      const double En2 = or_class_sum(h[1], d[1], v, ncls);
-      int ok = (mode == OR_DRIVE) ? (fabs(En - emid) < fabs(E[w] - emid)) : (En >= elo && En <= ehi);
-      if (dims == 2) ok = (mode == OR_DRIVE) ? (OR_NSQ(En, En2) < OR_NSQ(E[0], E[1])) : OR_INBOX(En, En2);
-      const double dE = En - E[w], dE2 = En2 - E[1];
-      if (ok) {
-        for (int c = 0; c < ncls; ++c) { h[0][c] += d[0][c]; h[1][c] += d[1][c]; }
-        E[0] = or_class_sum(h[0], NULL, v, ncls);
-        E[1] = or_class_sum(h[1], NULL, v, ncls);
-        ++pacc;
-      } else {
-        for (int c2 = 0; c2 < nchg; ++c2) L->a[chg_site[c2] * D + dir] = chg_old[c2];
-        ++prej;
-      }
-      if (mode == OR_DRIVE) {
-        double dist = fabs(emid - E[w]), move = fabs(dE);
-        if (dims == 2) {
-          dist = sqrt(OR_NSQ(E[0], E[1]));
-          const double x = dE * ihw0, y = dE2 * ihw1;
-          move = sqrt(x * x + y * y);
+      /* The scan, block by block in site-list order. */
+      long long R1 = Ef[0], R2 = Ef[1];
+      for (int c2 = 0; c2 < nchg;) {
+        const uint32_t b = rp[c2] / (uint32_t)blk;
+        int e2 = c2;
+        long long s1 = 0, s2 = 0;
+        while (e2 < nchg && rp[e2] / (uint32_t)blk == b) { s1 += rde[2 * e2]; s2 += rde[2 * e2 + 1]; ++e2; }
+        const long long n1 = R1 + s1, n2 = R2 + s2;
+        const int keep = drive ? or_closer(&win, n1, n2, R1, R2) : or_in(&win, n1, n2);
+        if (keep) {
+          R1 = n1;
+          R2 = n2;
+          pacc += e2 - c2;
+        } else {
+          for (int x = c2; x < e2; ++x) L->a[rs[x] * D + dir] = rb0[x];
+          prej += e2 - c2;
         }
-        const double qq = move > 0 ? qv[p] * (dist / move) : qv[p] * 2.0;
-        qv[p] = fmin(1.0, fmax(qq, 0x1.0p-32));
-        if (dims == 2 ? OR_INBOX(E[0], E[1]) : (E[w] >= elo && E[w] <= ehi)) mode = OR_SETTLE;
+        c2 = e2;
       }
+      Ef[0] = R1;
+      Ef[1] = R2;
+      E[0] = ldexp((double)Ef[0], -OR_FIX_S);
+      E[1] = ldexp((double)Ef[1], -OR_FIX_S);
+      if (mode == OR_DRIVE && or_in(&win, Ef[0], Ef[1])) mode = OR_SETTLE;
       if (p == nphase - 1) {
         if (mode == OR_DRIVE) {
           if (++drive_sweeps >= drive_cap) mode = OR_UNREACHED;
@@ -655,11 +707,9 @@ static int llr_impl(or_lattice* L, const int* phase_dir, const uint32_t* phase_l
   }
   out[0] = a; out[1] = E[0]; out[2] = E[1]; out[3] = mode;
   iout[0] = drive_sweeps; iout[1] = sweeps; iout[2] = hits; iout[3] = accs; iout[4] = pacc; iout[5] = prej;
-  free(cls); free(chg_site); free(chg_old); free(qv);
+  free(cls); free(rp); free(rs); free(rb0); free(rde);
   if (dims == 2) out[4] = bg;
   return 0;
-#undef OR_NSQ
-#undef OR_INBOX
 }
 
 int or_llr_run(or_lattice* L, const int* phase_dir, const uint32_t* phase_len, const uint32_t* sites, int nphase,

@@ -22,6 +22,12 @@ It builds oracle/_ref/ (oracle/build_ref.sh) and writes:
 * chains_1sigma.npz -- GMES/RMES series of the unmodified reference
   executable (its own table, NHIT 20, one thread) at the 4^4 couplings
   (0, 1.5, 0.1) for several seeds: the oracle for the 1-sigma comparison.
+* llr_ref.npz -- the ANE table (window centre, mean a_n, sd, samples) of the
+  unmodified reference llr executable (its own S(1080) table, one thread) on a
+  four-window ladder of a 4^3x2 lattice with R = 6 repeats of the hot-down and
+  cold-up passes: the statistical oracle for the device LLR.
+
+    python tests/golden/make_golden.py --only llr     # one fixture only
 """
 from __future__ import annotations
 
@@ -244,14 +250,52 @@ def make_chains():
     np.savez_compressed(os.path.join(HERE, "chains_1sigma.npz"), **out)
 
 
+# The LLR ladder of llr_ref.npz, in the reference llr's argument order
+# (group D Nt Nx axis bg Etop Ebot step hw a0 seed K NRM R).  With
+# NPLAQ = 768: window centres -0.6..-1.2 NPLAQ in steps of 0.2 NPLAQ, width
+# 0.0225 NPLAQ (0.5% of the S(1080) plaquette-energy range).
+LLR_LADDER = dict(D=4, Nt=2, Nx=4, axis=1, bg=0.0, Etop=-460.8, Ebot=-921.6, step=153.6, hw=8.64, a0=1.5,
+                  seed=20261203, K=50, NRM=80, R=6)
+
+
+def make_llr():
+    exe = os.path.join(ROOT, "oracle", "_ref", "llr")
+    table = os.path.join(REF_DIR, "groups", "mys1080-v4")
+    L = LLR_LADDER
+    args = [L[k] for k in ("D", "Nt", "Nx", "axis", "bg", "Etop", "Ebot", "step", "hw", "a0", "seed", "K", "NRM",
+                           "R")]
+    with tempfile.TemporaryDirectory() as td:  # the -pg build writes gmon.out into its cwd
+        r = subprocess.run([exe, table, *map(str, args)], cwd=td, env=dict(os.environ, OMP_NUM_THREADS="1"),
+                           stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, check=True)
+    rows = [l.split()[1:] for l in r.stdout.splitlines() if l.startswith("ANE:")]
+    if any(len(x) != 4 for x in rows):
+        raise RuntimeError("reference llr left a window unreached:\n" + r.stdout)
+    ane = np.array(rows, float)
+    print(r.stdout)
+    np.savez_compressed(os.path.join(HERE, "llr_ref.npz"), ewin=ane[:, 0], mean=ane[:, 1], sd=ane[:, 2],
+                        nrep=ane[:, 3].astype(np.int64),
+                        args=np.array(" ".join(f"{k}={v}" for k, v in LLR_LADDER.items())),
+                        table=np.array("mys1080-v4"))
+
+
 def main():
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", choices=["iso", "staples", "sweeps", "chains", "llr"])
+    only = ap.parse_args().only
     subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True,
                    env=dict(os.environ, REF_DIR=REF_DIR), stdout=subprocess.DEVNULL)
     with tempfile.TemporaryDirectory() as tabdir:
-        make_iso(tabdir)
-        make_staples(tabdir)
-        make_sweeps(tabdir)
-    make_chains()
+        if only in (None, "iso"):
+            make_iso(tabdir)
+        if only in (None, "staples"):
+            make_staples(tabdir)
+        if only in (None, "sweeps"):
+            make_sweeps(tabdir)
+    if only in (None, "chains"):
+        make_chains()
+    if only in (None, "llr"):
+        make_llr()
 
 
 if __name__ == "__main__":

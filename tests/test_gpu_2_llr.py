@@ -24,8 +24,11 @@ def test_gpu_llr_matches_oracle(engine, case):
     assert (res.phase_accepts, res.phase_rejects) == (r["phase_accepts"], r["phase_rejects"])
     assert res.S1 == r["S1"] and res.S2 == r["S2"]
     assert (lat.links.ravel() == L.links).all()
+    # The tracked energies are fixed-point class sums (class values rounded to
+    # 2^-32): within half a unit per term of the FP64 recount.
     s1, s2 = lat.llr_energy()
-    assert s1 == res.S1 and s2 == res.S2
+    n1 = nplaq(D, Nt, Nx)
+    assert abs(s1 - res.S1) <= n1 * 2.0 ** -33 and abs(s2 - res.S2) <= 2 * n1 * 2.0 ** -33
 
 
 CASES_2D = [

@@ -71,3 +71,25 @@ def test_dym_llr_matches_oracle_ladder(engine):
     got = [l for l in lines if l.startswith("ANE:")]
     assert got == want
     assert sum(reached) > 0
+
+
+def test_dym_llr_matches_unmodified_reference():
+    """The a_n ladder of dym-llr against the unmodified reference llr
+    executable (tests/golden/llr_ref.npz: its own S(1080) table, R = 6 repeats
+    of both passes, K = 50, NRM = 80) on a 4^3x2 lattice whose 32-link colour
+    classes move the energy by about the window width: every window's mean a_n
+    within 4 combined standard errors of the reference's."""
+    ref = np.load(os.path.join(os.path.dirname(__file__), "golden", "llr_ref.npz"))
+    kv = dict(x.split("=") for x in str(ref["args"]).split())
+    keys = ("D", "Nt", "Nx", "axis", "bg", "Etop", "Ebot", "step", "hw", "a0", "seed", "K", "NRM", "R")
+    args = [tables.ensure_table("S1080"), *[kv[k] for k in keys]]
+    out = subprocess.run([build.LLR_CLI, *args], capture_output=True, text=True, timeout=900)
+    assert out.returncode == 0, out.stderr
+    rows = [l.split()[1:] for l in out.stdout.splitlines() if l.startswith("ANE:")]
+    assert len(rows) == len(ref["ewin"]) and all(len(r) == 4 for r in rows), out.stdout
+    got = np.array(rows, float)
+    np.testing.assert_allclose(got[:, 0], ref["ewin"], atol=1e-9)
+    assert (got[:, 3] == ref["nrep"]).all()
+    se = np.sqrt(got[:, 2] ** 2 / got[:, 3] + ref["sd"] ** 2 / ref["nrep"])
+    z = (got[:, 1] - ref["mean"]) / se
+    assert np.all(np.abs(z) < 4), (got[:, 1], ref["mean"], z)

@@ -1,8 +1,8 @@
 """LLR (interval-restricted sweeps + Robbins-Monro, llr.cpp:178-250).
 
-CPU: the oracle's colour-parallel LLR tracks the energies exactly (its class
-histogram sums equal the reference's plaquette/rectangle loops), drives into
-the window, and is deterministic.
+CPU: the oracle's colour-parallel LLR tracks the energies exactly (its
+fixed-point class sums equal the reference's plaquette/rectangle loops to
+1e-9), drives into the window, and is deterministic.
 GPU: dym_llr_run reproduces the oracle bit for bit -- every a_n, the final
 energies, the configuration and all counters."""
 import numpy as np
