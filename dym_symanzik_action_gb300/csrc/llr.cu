@@ -3,28 +3,32 @@
 //
 // The reference (llr.cpp:178-250) updates links one at a time and tests the
 // window on the global energy after every hit.  Here a colour class moves in
-// two kernels per colour-phase slot over a work list of chains:
+// three kernels per colour-phase slot over a work list of chains:
 //  1. k_llr_propose: every link of the class runs nhit Metropolis hits with
 //     weight exp(-a dE_w - bg dE_bg) (llr.cpp:211) and no window test; outside
 //     the window (drive-in) a hit is kept iff it moves the link's running
 //     energy towards the window centre (llr.cpp:208-209).  Links of one colour
 //     share no plaquette or rectangle, so each link's energy change is its own:
-//     the kernel records it (exact fixed point) with the link's old value.  A
-//     warp takes a tile of 32 links, so a short work list still reaches every
-//     SM (the FP64 pipe bounds this kernel).
-//  2. k_llr_commit: one warp per chain scans the phase's changed links in
-//     site-list order and keeps link i's move iff the running energy plus its
-//     change stays in the window (outside it: iff it comes closer to the
-//     centre); a refused link gets its old value back.  Then it advances the
-//     drive-in / Robbins-Monro state machine at the end of a sweep
-//     (a += 12/(W^2 (m+1)) (<E> - Ewin), llr.cpp:244).
+//     the kernel records each link's old value and, per block of st->blk
+//     consecutive links, the exact fixed-point sum of their changes.  A warp
+//     takes a tile of 32 links, so a short work list still reaches every SM
+//     (the FP64 pipe bounds this kernel).
+//  2. k_llr_commit: one warp per chain scans the phase's blocks in site-list
+//     order and keeps a block's moves iff the running energy plus their change
+//     stays in the window (outside it: iff it comes closer to the centre),
+//     then advances the drive-in / Robbins-Monro state machine at the end of
+//     a sweep (a += 12/(W^2 (m+1)) (<E> - Ewin), llr.cpp:244).
+//  3. k_llr_restore: the changed links of refused blocks get their old values.
 // A link's nhit identical single-hit Metropolis kernels compose into a
-// reversible kernel, so keeping its move iff the energy stays in the window is
-// an exact Metropolis-Hastings step for the window-restricted distribution,
-// and the scan is a composition of such steps.  Energies are exact 64-bit
-// fixed-point sums of the class values, so the tracked energy never drifts.
-// Every chain's state (Philox sweep counter, energies) lives in its own
-// LlrState, so a chain gives the same result alone or in any mix.
+// reversible kernel, so keeping a block's moves iff the energy stays in the
+// window is an exact Metropolis-Hastings step for the window-restricted
+// distribution, and the scan is a composition of such steps.  A block's
+// largest possible change is a quarter of the window width
+// (dym_llr_block_links), so a block can always move away from a wall; on
+// narrow windows a block is one link.  Energies are exact 64-bit fixed-point
+// sums of the class values, so the tracked energy never drifts.  Every
+// chain's state (Philox sweep counter, energies) lives in its own LlrState,
+// so a chain gives the same result alone or in any mix.
 #include <cuda_runtime.h>
 
 #include "batch.h"
