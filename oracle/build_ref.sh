@@ -12,6 +12,8 @@
 #                       is streamed through sed into the compiler (no copy)
 #   _ref/llr            the unmodified LLR window-ladder executable (llr.cpp),
 #                       reference Makefile flags
+#   _ref/llr2d          the unmodified two-dimensional LLR executable
+#                       (llr2d.cpp), reference Makefile flags
 set -e
 REF_DIR=${REF_DIR:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -45,4 +47,6 @@ sed 's/^#define NHIT[ \t]*20/#define NHIT 10/' "$REF_DIR/dym-mod-metro.cpp" | \
   "$OUT/lattice.o" "$OUT/group.o" "$OUT/timer.o" -lm -o "$OUT/dym-mod-metro-nhit10"
 $CXX -O3 -g -pg -fopenmp -std=c++11 -w -I"$REF_DIR" "$REF_DIR/llr.cpp" \
   "$OUT/lattice.o" "$OUT/group.o" "$OUT/timer.o" -lm -o "$OUT/llr"
+$CXX -O3 -g -pg -fopenmp -std=c++11 -w -I"$REF_DIR" "$REF_DIR/llr2d.cpp" \
+  "$OUT/lattice.o" "$OUT/group.o" "$OUT/timer.o" -lm -o "$OUT/llr2d"
 echo "built $OUT"

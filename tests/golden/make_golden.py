@@ -27,6 +27,12 @@ It builds oracle/_ref/ (oracle/build_ref.sh) and writes:
   four-window ladder of a 4^3x2 lattice with R = 6 repeats of the hot-down and
   cold-up passes: the statistical oracle for the device LLR.
 
+* llr2d_ref.npz -- the ANE2 table (cell centres, mean a1 and a2, sds, samples)
+  of the unmodified reference llr2d executable (full mode, its own S(1080)
+  table, one thread) on three cells of a 4^4 lattice along the S2 ridge that
+  one-dimensional windows at beta2 = 0 hold, with R = 4 repeats of its cold
+  and hot passes.
+
     python tests/golden/make_golden.py --only llr     # one fixture only
 """
 from __future__ import annotations
@@ -278,10 +284,41 @@ def make_llr():
                         table=np.array("mys1080-v4"))
 
 
+# The two-dimensional cells of llr2d_ref.npz, in the reference llr2d's argument
+# order (group D Nt Nx E1top E1bot step1 hw1 c0 c1 c2 step2 hw2 nperp a0 seed
+# K NRM R).  4^4 lattice (NPLAQ 1536, NRECT 3072); cells E1 = -0.6, -0.8, -1.0
+# NPLAQ, half-widths 0.0225/2 of NPLAQ and NRECT; the ridge E2(E1) is the
+# quadratic through the mean S2 of the one-dimensional S1 windows at these
+# centres (beta2 = 0), so each cell lies inside the configurations' support.
+LLR2D_GRID = dict(D=4, Nt=4, Nx=4, E1top=-921.6, E1bot=-1536.0, step1=307.2, hw1=17.28, c0=80.333, c1=0.143764,
+                  c2=-0.000374147, step2=69.12, hw2=34.56, nperp=0, a0=1.0, seed=11, K=40, NRM=70, R=4)
+
+
+def make_llr2d():
+    exe = os.path.join(ROOT, "oracle", "_ref", "llr2d")
+    table = os.path.join(REF_DIR, "groups", "mys1080-v4")
+    G = LLR2D_GRID
+    args = [G[k] for k in ("D", "Nt", "Nx", "E1top", "E1bot", "step1", "hw1", "c0", "c1", "c2", "step2", "hw2",
+                           "nperp", "a0", "seed", "K", "NRM", "R")]
+    with tempfile.TemporaryDirectory() as td:  # the -pg build writes gmon.out into its cwd
+        r = subprocess.run([exe, table, *map(str, args)], cwd=td, env=dict(os.environ, OMP_NUM_THREADS="1"),
+                           stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, check=True)
+    rows = [l.split()[1:] for l in r.stdout.splitlines() if l.startswith("ANE2:")]
+    n1 = int((G["E1top"] - G["E1bot"]) / G["step1"] + 0.5) + 1
+    if len(rows) != n1 * (2 * G["nperp"] + 1):
+        raise RuntimeError("reference llr2d left a cell unreached:\n" + r.stdout)
+    ane = np.array(rows, float)
+    print(r.stdout)
+    np.savez_compressed(os.path.join(HERE, "llr2d_ref.npz"), e1=ane[:, 0], e2=ane[:, 1], a1=ane[:, 2], a2=ane[:, 3],
+                        sd1=ane[:, 4], sd2=ane[:, 5], nrep=ane[:, 6].astype(np.int64),
+                        args=np.array(" ".join(f"{k}={v}" for k, v in LLR2D_GRID.items())),
+                        table=np.array("mys1080-v4"))
+
+
 def main():
     import argparse
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["iso", "staples", "sweeps", "chains", "llr"])
+    ap.add_argument("--only", choices=["iso", "staples", "sweeps", "chains", "llr", "llr2d"])
     only = ap.parse_args().only
     subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True,
                    env=dict(os.environ, REF_DIR=REF_DIR), stdout=subprocess.DEVNULL)
@@ -296,6 +333,8 @@ def main():
         make_chains()
     if only in (None, "llr"):
         make_llr()
+    if only in (None, "llr2d"):
+        make_llr2d()
 
 
 if __name__ == "__main__":

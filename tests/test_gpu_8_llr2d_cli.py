@@ -176,3 +176,28 @@ def test_seed_and_solve_modes_match_oracle(engine, tmp_path):
         if r["status"] == "done":
             exp.append("ANE2: %9.2f %9.2f %10.6f %10.6f %9.5f %9.5f %d" % (E1, E2, r["a1"], r["a2"], 0.0, 0.0, 1))
     assert got == exp
+
+
+def test_dym_llr2d_matches_unmodified_reference():
+    """Full mode of dym-llr2d against the unmodified reference llr2d executable
+    (tests/golden/llr2d_ref.npz: its own S(1080) table, R = 4 repeats of the
+    cold and hot ridge passes, K = 40, NRM = 70) on three cells of a 4^4
+    lattice along the S2 ridge: every cell's mean a1 and a2 within 4 combined
+    standard errors of the reference's."""
+    ref = np.load(os.path.join(os.path.dirname(__file__), "golden", "llr2d_ref.npz"))
+    kv = dict(x.split("=") for x in str(ref["args"]).split())
+    keys = ("D", "Nt", "Nx", "E1top", "E1bot", "step1", "hw1", "c0", "c1", "c2", "step2", "hw2", "nperp", "a0",
+            "seed", "K", "NRM", "R")
+    out = subprocess.run([build.LLR2D_CLI, tables.ensure_table("S1080"), *[kv[k] for k in keys]],
+                         capture_output=True, text=True, timeout=900)
+    assert out.returncode == 0, out.stderr
+    rows = [l.split()[1:] for l in out.stdout.splitlines() if l.startswith("ANE2:")]
+    assert len(rows) == len(ref["e1"]), out.stdout
+    got = np.array(rows, float)
+    np.testing.assert_allclose(got[:, 0], ref["e1"], atol=1e-9)
+    np.testing.assert_allclose(got[:, 1], ref["e2"], atol=0.006)
+    assert (got[:, 6] == ref["nrep"]).all()
+    for col, sdc, name in ((2, 4, "a1"), (3, 5, "a2")):
+        se = np.sqrt(got[:, sdc] ** 2 / got[:, 6] + ref["sd" + name[1]] ** 2 / ref["nrep"])
+        z = (got[:, col] - ref[name]) / se
+        assert np.all(np.abs(z) < 4), (name, got[:, col], ref[name], z)
