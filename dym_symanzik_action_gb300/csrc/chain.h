@@ -155,11 +155,14 @@ struct LlrBlockRec {
   uint32_t pad;
 };
 
-// Drive-in parameters of a two-dimensional cell, as the propose kernel passes
-// them to visit_llr.
-struct LlrDrive2 {
-  int dims;
-  double E0b, emid2, ihw0, ihw1;
+// Drive-in parameters as the propose kernel passes them to visit_llr: the
+// phase-start fixed-point energies, the window centre (the windowed axis's in
+// index 0; a cell's S2 centre in index 1) and, for a two-dimensional cell,
+// 2^-kLlrFixShift over each half-width.
+struct LlrDrive {
+  int dims, axis;
+  long long E[2], mid[2];
+  double sc[2];
 };
 
 // Observables.

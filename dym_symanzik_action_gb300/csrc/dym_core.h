@@ -213,3 +213,18 @@ DYM_HD int dym_llr_block_links(int D, double retr_range, int dims, int axis, dou
   }
   return s;
 }
+
+// ---------------------------------------------------------------------------
+// Fixed-point scale 2^S of ReTr class values for exact integer sums of a
+// link's staple terms: the largest S <= 24 for which the difference of two
+// sums of 6(D-1) terms, each at most amax 2^S + 1/2 in magnitude (amax the
+// largest |ReTr|), stays inside int32.
+// ---------------------------------------------------------------------------
+DYM_HD int dym_fix_shift(double amax, int D) {
+  const double NR = 6.0 * (D - 1);
+  const double a = amax > 1e-3 ? amax : 1e-3;
+  const double lim = (2147483647.0 - 2.0 * NR) / (2.0 * NR * a);
+  int S = 24;
+  while (S > 0 && ldexp(1.0, S) > lim) --S;
+  return S;
+}

@@ -77,13 +77,22 @@ __global__ void __launch_bounds__(kLlrWarps * 32) k_llr_propose(const LlrTile* _
                                                                 BatchGroups groups, int nhit) {
   extern __shared__ __align__(16) unsigned char smem[];
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  for (int g = 0; g < groups.n; ++g) {
+  for (int g = 0; g < groups.n; ++g) {  // sub-table by cp.async (16-byte aligned on both sides)
     const BatchGroupDev& G = groups.g[g];
-    stage_sub_tables(G.retr, G.inv, G.sub, G.P, G.npool, reinterpret_cast<double*>(smem + G.off_retr),
-                     reinterpret_cast<uint16_t*>(smem + G.off_inv), reinterpret_cast<uint16_t*>(smem + G.off_sub));
+    const uint32_t nsub = G.npool * G.P, nb16 = (nsub * 2u) & ~15u;
+    uint16_t* s_sub = reinterpret_cast<uint16_t*>(smem + G.off_sub);
+    cp_async_stage(s_sub, G.sub, nb16);
+    for (uint32_t t = nb16 / 2 + threadIdx.x; t < nsub; t += blockDim.x) s_sub[t] = G.sub[t];
+    int32_t* s_ev = reinterpret_cast<int32_t*>(smem + G.off_ev);
+    uint16_t* s_inv = reinterpret_cast<uint16_t*>(smem + G.off_inv);
     uint16_t* s_cls = reinterpret_cast<uint16_t*>(smem + G.off_cls);
-    for (uint32_t t = threadIdx.x; t < G.P; t += blockDim.x) s_cls[t] = G.cls16[t];
+    for (uint32_t t = threadIdx.x; t < G.P; t += blockDim.x) {
+      s_ev[t] = G.ev[t];
+      s_inv[t] = G.inv[t];
+      s_cls[t] = G.cls16[t];
+    }
   }
+  cp_async_wait_all();
   __syncthreads();
   // Tile t goes to warp t / gridDim.x of block t % gridDim.x: a short list
   // spreads over the SMs (one warp each) before any SM takes a second tile.
@@ -105,14 +114,24 @@ __global__ void __launch_bounds__(kLlrWarps * 32) k_llr_propose(const LlrTile* _
     a.npool = G.npool;
     a.seed = c.seed;
     a.nhit = nhit;
-    const double* s_retr = reinterpret_cast<const double*>(smem + G.off_retr);
+    const int32_t* s_ev = reinterpret_cast<const int32_t*>(smem + G.off_ev);
     const uint16_t* s_inv = reinterpret_cast<const uint16_t*>(smem + G.off_inv);
     const uint16_t* s_sub = reinterpret_cast<const uint16_t*>(smem + G.off_sub);
     const uint16_t* s_cls = reinterpret_cast<const uint16_t*>(smem + G.off_cls);
     const int axis = st->axis;
-    const double aa = st->a, bg = st->bg, emid = st->emid, E0 = st->E[axis - 1];
-    const LlrDrive2 d2{st->dims, st->E[1], st->emid2, st->ihw[0], st->ihw[1]};
+    const double aa = st->a, bg = st->bg;
     const bool drive = (mode == DYM_LLR_DRIVE);
+    LlrDrive dr;
+    dr.dims = st->dims;
+    dr.axis = axis;
+    if (drive) {
+      dr.E[0] = st->Ef[0];
+      dr.E[1] = st->Ef[1];
+      dr.mid[0] = st->wmid[0];
+      dr.mid[1] = st->wmid[1];
+      dr.sc[0] = st->wsc[0];
+      dr.sc[1] = st->wsc[1];
+    }
     const uint32_t sweep = st->sweep;
     unsigned hits = 0, accs = 0;
     long long de1 = 0, de2 = 0;
@@ -121,15 +140,15 @@ __global__ void __launch_bounds__(kLlrWarps * 32) k_llr_propose(const LlrTile* _
       const uint32_t i = c.sites[tl.begin + lane];
       uint32_t b0 = 0;
       switch (tl.dir) {
-        case 0: b0 = visit_llr<D, 0>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, st->vf, axis, aa, bg, E0, emid, d2,
+        case 0: b0 = visit_llr<D, 0>(a, i, sweep, s_ev, G.evshift, s_inv, s_sub, s_cls, st->vf, axis, aa, bg, dr,
                                      drive, de1, de2, hits, accs); break;
-        case 1: b0 = visit_llr<D, 1>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, st->vf, axis, aa, bg, E0, emid, d2,
+        case 1: b0 = visit_llr<D, 1>(a, i, sweep, s_ev, G.evshift, s_inv, s_sub, s_cls, st->vf, axis, aa, bg, dr,
                                      drive, de1, de2, hits, accs); break;
-        case 2: if (D > 2) b0 = visit_llr<D, (D > 2 ? 2 : 0)>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, st->vf, axis,
-                                                               aa, bg, E0, emid, d2, drive, de1, de2, hits, accs);
+        case 2: if (D > 2) b0 = visit_llr<D, (D > 2 ? 2 : 0)>(a, i, sweep, s_ev, G.evshift, s_inv, s_sub, s_cls,
+                                                               st->vf, axis, aa, bg, dr, drive, de1, de2, hits, accs);
           break;
-        case 3: if (D > 3) b0 = visit_llr<D, (D > 3 ? 3 : 0)>(a, i, sweep, s_retr, s_inv, s_sub, s_cls, st->vf, axis,
-                                                               aa, bg, E0, emid, d2, drive, de1, de2, hits, accs);
+        case 3: if (D > 3) b0 = visit_llr<D, (D > 3 ? 3 : 0)>(a, i, sweep, s_ev, G.evshift, s_inv, s_sub, s_cls,
+                                                               st->vf, axis, aa, bg, dr, drive, de1, de2, hits, accs);
           break;
       }
       changed = c.links[(size_t)tl.dir * c.V + i] != (uint16_t)b0;

@@ -157,6 +157,7 @@ struct LlrWork {
   std::vector<Group*> groups;
   std::vector<uint16_t*> d_sub;
   std::vector<uint16_t*> d_cls16;
+  std::vector<int32_t*> d_ev;
   BatchGroups bg{};
   size_t smem = 0;
   LlrChainDev* d_chains = nullptr;
@@ -181,6 +182,8 @@ struct LlrWork {
     release_lists();
     for (auto p : d_sub) cudaFree(p);
     d_sub.clear();
+    for (auto p : d_ev) cudaFree(p);
+    d_ev.clear();
     groups.clear();
   }
 
@@ -196,6 +199,15 @@ struct LlrWork {
     DYM_CUDA(dmalloc(&d, sub.size()), "cudaMalloc(llr sub)");
     DYM_CUDA(copy_sync(d, sub.data(), sub.size() * 2, cudaMemcpyHostToDevice, stream), "upload llr sub");
     d_sub.push_back(d);
+    // Fixed-point ReTr of every element's class (the hits' exact sums); LLR
+    // runs on four-dimensional lattices only.
+    std::vector<int32_t> ev(g->P);
+    const int S = fix_shift(*g, 4);
+    for (uint32_t e = 0; e < g->P; ++e) ev[e] = (int32_t)std::llrint(std::ldexp(g->cls_val[g->cls[e]], S));
+    int32_t* dv = nullptr;
+    DYM_CUDA(dmalloc(&dv, ev.size()), "cudaMalloc(llr values)");
+    DYM_CUDA(copy_sync(dv, ev.data(), ev.size() * 4, cudaMemcpyHostToDevice, stream), "upload llr values");
+    d_ev.push_back(dv);
     groups.push_back(g);
     // layout
     auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
@@ -209,10 +221,13 @@ struct LlrWork {
       b.retr = (const double*)G.d_retr;
       b.sub = d_sub[k];
       b.cls16 = (const uint16_t*)G.d_cls16;
+      b.ev = d_ev[k];
+      b.evshift = fix_shift(G, 4);
       b.P = G.P;
       b.npool = (uint32_t)G.pool_nearest.size();
-      b.off_retr = (uint32_t)off;
-      off = up16(off + (size_t)G.P * 8);
+      b.off_retr = 0;
+      b.off_ev = (uint32_t)off;
+      off = up16(off + (size_t)G.P * 4);
       b.off_inv = (uint32_t)off;
       off = up16(off + (size_t)G.P * 2);
       b.off_cls = (uint32_t)off;

@@ -34,14 +34,7 @@ inline cudaError_t copy_sync(void* dst, const void* src, size_t bytes, cudaMemcp
 // Fixed-point scale 2^S of the class values for the mixed-precision kernels:
 // the largest S <= 24 for which a difference of two sums of NR = 6(D-1)
 // rectangle terms, each at most |c| 2^S + 1/2, stays inside int32.
-inline int fix_shift(const Group& g, int D) {
-  const double NR = 6.0 * (D - 1);
-  const double amax = std::max(g.max_abs_retr, 1e-3);
-  const double lim = (2147483647.0 - 2.0 * NR) / (2.0 * NR * amax);
-  int S = 24;
-  while (S > 0 && std::ldexp(1.0, S) > lim) --S;
-  return S;
-}
+inline int fix_shift(const Group& g, int D) { return dym_fix_shift(g.max_abs_retr, D); }
 
 // Rounding error of one fixed-point class value: half a unit plus the spread
 // of ReTr inside a class.

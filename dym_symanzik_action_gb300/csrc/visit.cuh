@@ -410,20 +410,37 @@ __device__ __forceinline__ bool llr_weight_accept(double x, uint32_t r1, uint32_
   return dym_exp(x) > dym_u53(r1, r2);
 }
 
+// Closer to the window centre (fixed-point energies; a two-dimensional cell
+// compares squared normalised distances) -- the drive-in test of the hits and
+// of the commit's scan.
+__device__ __forceinline__ double llr_drive_nsq(const LlrDrive& d, long long e1, long long e2) {
+  const double x = DYM_MUL((double)(e1 - d.mid[0]), d.sc[0]), y = DYM_MUL((double)(e2 - d.mid[1]), d.sc[1]);
+  return DYM_ADD(DYM_MUL(x, x), DYM_MUL(y, y));
+}
+
+__device__ __forceinline__ bool llr_drive_closer(const LlrDrive& d, long long e1, long long e2, long long q1,
+                                                 long long q2) {
+  if (d.dims == 2) return llr_drive_nsq(d, e1, e2) < llr_drive_nsq(d, q1, q2);
+  const long long e = d.axis == 1 ? e1 : e2, q = d.axis == 1 ? q1 : q2;
+  return llabs(e - d.mid[0]) < llabs(q - d.mid[0]);
+}
+
 // One LLR visit of link (i, DIR) with the shared sub-table (llr.cpp:186-216
 // per hit): nhit hits with weight exp(-a dE_w - bg dE_bg), or, in drive-in
-// mode, greedy moves of the link's running energy towards emid.  The link is
-// written in place; returns its value before the visit, and in de1, de2 the
-// exact fixed-point change of S1 and S2 (vf: class values times
-// 2^kLlrFixShift), which the scan of the commit kernel tests against the
-// window.  The classes of the initial u_j are kept packed, 5 bits each, and
-// the two hit loops are separate so that neither holds the other's state.
+// mode, greedy moves of the link's running energy towards the centre.  A
+// hit's dS1, dS2 are exact integer sums of its terms' class values at scale
+// 2^evshift (s_ev: per element); the weight's exponent is formed from them in
+// FP64.  The link is written in place; returns its value before the visit, and
+// in de1, de2 the exact change of S1 and S2 at scale 2^kLlrFixShift (vf: class
+// values), which the commit's scan tests against the window.  The classes of
+// the initial u_j are kept packed, 5 bits each, and the two hit loops are
+// separate so that neither holds the other's state.
 template <int D, int DIR>
-__device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
-                                              const uint16_t* s_inv, const uint16_t* s_sub, const uint16_t* s_cls,
-                                              const long long* __restrict__ vf, int axis, double aa, double bg,
-                                              double E0, double emid, const LlrDrive2& d2, bool drive,
-                                              long long& de1, long long& de2, unsigned& hits, unsigned& accs) {
+__device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, uint32_t sweep, const int32_t* s_ev,
+                                              int evshift, const uint16_t* s_inv, const uint16_t* s_sub,
+                                              const uint16_t* s_cls, const long long* __restrict__ vf, int axis,
+                                              double aa, double bg, const LlrDrive& dr, bool drive, long long& de1,
+                                              long long& de2, unsigned& hits, unsigned& accs) {
   constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
   constexpr int NW = (NT + 5) / 6;  // words of six 5-bit classes
   static_assert(kLlrMaxCls <= 32, "classes are packed in 5 bits");
@@ -443,70 +460,60 @@ __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, ui
   for (int w = 0; w < NW; ++w) c0[w] = 0;
 #pragma unroll
   for (int j = 0; j < NT; ++j) c0[j / 6] |= (uint32_t)s_cls[u[j]] << (5 * (j % 6));
-  double r1 = 0, m1 = 0;
+  int32_t R = 0, M = 0;  // exact sums (the differences below fit int32: dym_fix_shift)
 #pragma unroll
-  for (int j = 0; j < NS; ++j) r1 = DYM_ADD(r1, s_retr[u[j]]);
+  for (int j = 0; j < NS; ++j) R += s_ev[u[j]];
 #pragma unroll
-  for (int j = NS; j < NT; ++j) m1 = DYM_ADD(m1, s_retr[u[j]]);
+  for (int j = NS; j < NT; ++j) M += s_ev[u[j]];
   if (drive) {
-    double cum = 0, cum2 = 0;
+    const int up = kLlrFixShift - evshift;
+    long long cum1 = 0, cum2 = 0;  // the link's kept moves, scale 2^kLlrFixShift
     for (int h = 0; h < a.nhit; ++h) {
       const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_LLR);
       const uint16_t* row = s_sub + dym_pick(r.v[0], a.npool) * a.P;
       uint32_t e[NT];
-      double r1n = 0, m1n = 0;
+      int32_t Rn = 0, Mn = 0;
 #pragma unroll
       for (int j = 0; j < NS; ++j) {
         e[j] = row[u[j]];
-        r1n = DYM_ADD(r1n, s_retr[e[j]]);
+        Rn += s_ev[e[j]];
       }
 #pragma unroll
       for (int j = NS; j < NT; ++j) {
         e[j] = row[u[j]];
-        m1n = DYM_ADD(m1n, s_retr[e[j]]);
+        Mn += s_ev[e[j]];
       }
-      const double dS1 = DYM_SUB(r1n, r1), dS2 = DYM_SUB(m1n, m1);
-      const double dEw = axis == 1 ? dS1 : dS2;
-      bool acc;
-      if (d2.dims == 2) {  // closer to the cell centre in normalised distance (llr2d.cpp:206-209)
-        const double c1 = DYM_ADD(E0, cum), c2 = DYM_ADD(d2.E0b, cum2);
-        const double x1 = DYM_MUL(DYM_SUB(c1, emid), d2.ihw0), y1 = DYM_MUL(DYM_SUB(c2, d2.emid2), d2.ihw1);
-        const double x2 = DYM_MUL(DYM_SUB(DYM_ADD(c1, dS1), emid), d2.ihw0);
-        const double y2 = DYM_MUL(DYM_SUB(DYM_ADD(c2, dS2), d2.emid2), d2.ihw1);
-        acc = DYM_ADD(DYM_MUL(x2, x2), DYM_MUL(y2, y2)) < DYM_ADD(DYM_MUL(x1, x1), DYM_MUL(y1, y1));
-      } else {
-        const double Ec = DYM_ADD(E0, cum);
-        acc = fabs(DYM_SUB(DYM_ADD(Ec, dEw), emid)) < fabs(DYM_SUB(Ec, emid));
-      }
+      const long long n1 = cum1 + (long long)(Rn - R) * (1ll << up), n2 = cum2 + (long long)(Mn - M) * (1ll << up);
       ++hits;
-      if (acc) {
+      if (llr_drive_closer(dr, dr.E[0] + n1, dr.E[1] + n2, dr.E[0] + cum1, dr.E[1] + cum2)) {
         b = row[b];
 #pragma unroll
         for (int j = 0; j < NT; ++j) u[j] = e[j];
-        r1 = r1n;
-        m1 = m1n;
-        cum = DYM_ADD(cum, dEw);
-        cum2 = DYM_ADD(cum2, dS2);
+        R = Rn;
+        M = Mn;
+        cum1 = n1;
+        cum2 = n2;
         ++accs;
       }
     }
   } else {
+    const double scale = ldexp(1.0, -evshift);
     for (int h = 0; h < a.nhit; ++h) {
       const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_LLR);
       const uint16_t* row = s_sub + dym_pick(r.v[0], a.npool) * a.P;
       uint32_t e[NT];
-      double r1n = 0, m1n = 0;
+      int32_t Rn = 0, Mn = 0;
 #pragma unroll
       for (int j = 0; j < NS; ++j) {
         e[j] = row[u[j]];
-        r1n = DYM_ADD(r1n, s_retr[e[j]]);
+        Rn += s_ev[e[j]];
       }
 #pragma unroll
       for (int j = NS; j < NT; ++j) {
         e[j] = row[u[j]];
-        m1n = DYM_ADD(m1n, s_retr[e[j]]);
+        Mn += s_ev[e[j]];
       }
-      const double dS1 = DYM_SUB(r1n, r1), dS2 = DYM_SUB(m1n, m1);
+      const double dS1 = DYM_MUL((double)(Rn - R), scale), dS2 = DYM_MUL((double)(Mn - M), scale);
       const double dEw = axis == 1 ? dS1 : dS2;
       const double dEbg = axis == 1 ? dS2 : dS1;
       ++hits;
@@ -514,8 +521,8 @@ __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, ui
         b = row[b];
 #pragma unroll
         for (int j = 0; j < NT; ++j) u[j] = e[j];
-        r1 = r1n;
-        m1 = m1n;
+        R = Rn;
+        M = Mn;
         ++accs;
       }
     }

@@ -456,7 +456,9 @@ void or_measure(const or_lattice* L, int wl_nx, int wl_nt, double* out, uint64_t
  * llr.cpp:178-250 of the reference for the per-hit rule, the drive-in rule
  * and the Robbins-Monro step.  The reference tests the window after every
  * hit, one link at a time.  The engine lets every link of a colour class run
- * its hits at once (the links of a class share no plaquette or rectangle) and
+ * its hits at once (the links of a class share no plaquette or rectangle;
+ * each hit weighs the exact integer sums of its terms' class values at scale
+ * 2^dym_fix_shift, drive-in hits compare fixed-point energies) and
  * then scans the class in site-list order in blocks of dym_llr_block_links
  * links: a block's moves are kept iff the running energy plus their change
  * stays in the window (outside the window: iff it comes closer to the
@@ -589,6 +591,12 @@ static int llr_impl(or_lattice* L, const int* phase_dir, const uint32_t* phase_l
     if (g->ReTr[e] > rmax) rmax = g->ReTr[e];
   }
   const int blk = dym_llr_block_links((int)D, rmax - rmin, dims, axis, hw, hw2);
+  /* The hits compare exact integer sums of class values at the scale 2^S of
+   * the mixed-precision sweep (dym_fix_shift); vS per class. */
+  const int S = dym_fix_shift(fabs(rmax) > fabs(rmin) ? fabs(rmax) : fabs(rmin), (int)D);
+  const int up = OR_FIX_S - S;
+  long long vS[OR_MAXCLS];
+  for (int c = 0; c < ncls; ++c) vS[c] = llrint(ldexp(v[c], S));
   /* Changed links of one phase: position in the phase, site, old value,
    * fixed-point energy changes. */
   uint32_t* rp = (uint32_t*)malloc(sizeof(uint32_t) * V);
@@ -608,33 +616,31 @@ static int llr_impl(or_lattice* L, const int* phase_dir, const uint32_t* phase_l
         or_staples(L, i, dir, st, re);
         const int b0 = L->a[i * D + dir];
         int b = b0;
-        double r1 = 0, m1 = 0;
-        for (int j = 0; j < ns; ++j) r1 += g->ReTr[g->mult[b][st[j]]];
-        for (int j = 0; j < nr; ++j) m1 += g->ReTr[g->mult[b][re[j]]];
-        double cum = 0, cum2 = 0;
+        long long R = 0, M = 0;
+        for (int j = 0; j < ns; ++j) R += vS[cls[g->mult[b][st[j]]]];
+        for (int j = 0; j < nr; ++j) M += vS[cls[g->mult[b][re[j]]]];
+        long long cum1 = 0, cum2 = 0; /* drive-in: the link's moves so far, scale 2^32 */
         for (int hh = 0; hh < nhit; ++hh) {
           dym_u32x4 r = dym_hit_random(seed, sweep, i, dir, (uint32_t)hh, DYM_TAG_LLR);
           const double u1 = (double)r.v[0] * 0x1p-32;
           const int bnew = g->mult[b][g->pool[(size_t)(g->npool * u1)]];
-          double r1n = 0, m1n = 0;
-          for (int j = 0; j < ns; ++j) r1n += g->ReTr[g->mult[bnew][st[j]]];
-          for (int j = 0; j < nr; ++j) m1n += g->ReTr[g->mult[bnew][re[j]]];
-          const double dS1 = r1n - r1, dS2 = m1n - m1;
-          const double dEw = axis == 1 ? dS1 : dS2, dEbg = axis == 1 ? dS2 : dS1;
+          long long Rn = 0, Mn = 0;
+          for (int j = 0; j < ns; ++j) Rn += vS[cls[g->mult[bnew][st[j]]]];
+          for (int j = 0; j < nr; ++j) Mn += vS[cls[g->mult[bnew][re[j]]]];
+          const long long d1 = Rn - R, d2 = Mn - M;
           int acc;
-          if (drive && dims == 2) {
-            const double c1 = E[0] + cum, c2 = E[1] + cum2;
-            const double x1 = (c1 - emid) * ihw0, y1 = (c2 - emid2) * ihw1;
-            const double x2 = ((c1 + dS1) - emid) * ihw0, y2 = ((c2 + dS2) - emid2) * ihw1;
-            acc = (x2 * x2 + y2 * y2) < (x1 * x1 + y1 * y1);
-          } else if (drive) {
-            const double Ec = E[w] + cum;
-            acc = fabs(Ec + dEw - emid) < fabs(Ec - emid);
+          long long n1 = 0, n2 = 0;
+          if (drive) {
+            n1 = cum1 + d1 * (1ll << up);
+            n2 = cum2 + d2 * (1ll << up);
+            acc = or_closer(&win, Ef[0] + n1, Ef[1] + n2, Ef[0] + cum1, Ef[1] + cum2);
           } else {
+            const double dS1 = ldexp((double)d1, -S), dS2 = ldexp((double)d2, -S);
+            const double dEw = axis == 1 ? dS1 : dS2, dEbg = axis == 1 ? dS2 : dS1;
             acc = dym_weight_accept(-a * dEw - bg * dEbg, dym_u53(r.v[1], r.v[2]));
           }
           ++hits;
-          if (acc) { b = bnew; r1 = r1n; m1 = m1n; cum = cum + dEw; cum2 = cum2 + dS2; ++accs; }
+          if (acc) { b = bnew; R = Rn; M = Mn; cum1 = n1; cum2 = n2; ++accs; }
         }
         if (b != b0) {
           L->a[i * D + dir] = b;
