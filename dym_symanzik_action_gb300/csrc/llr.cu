@@ -235,6 +235,19 @@ __global__ void k_llr_commit(const LlrCommit* __restrict__ commits, uint32_t n,
     if (wave + 32 + lane < nblocks) next = c.brec[wave + 32 + lane];
     const uint32_t nj = nblocks - wave < 32 ? nblocks - wave : 32;
     uint32_t refused_blocks = 0;
+    if (!drive) {
+      // All 32 kept when every running energy, every block kept, stays in the
+      // window (then the serial walk keeps each one in turn).
+      const long long p1 = seg_prefix(br.s[0], lane, 32), p2 = seg_prefix(br.s[1], lane, 32);
+      if (__all_sync(0xffffffffu, br.nchg == 0 || in_win(R1 + p1, R2 + p2))) {
+        kept += __reduce_add_sync(0xffffffffu, br.nchg);
+        R1 += __shfl_sync(0xffffffffu, p1, 31);
+        R2 += __shfl_sync(0xffffffffu, p2, 31);
+        if (lane < nj) c.bref[wave + lane] = 0;
+        br = next;
+        continue;
+      }
+    }
 #pragma unroll 8
     for (uint32_t j = 0; j < 32; ++j) {
       const uint32_t nch = __shfl_sync(0xffffffffu, br.nchg, j);
