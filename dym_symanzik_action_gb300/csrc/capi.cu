@@ -545,11 +545,22 @@ int dym_measure(dym_chain* c, const dym_meas_opts* opts, dym_obs* out, double* w
   return DYM_OK;
 }
 
+// The device address of page-locked host memory (allocated or registered with
+// CUDA, hence mapped for the device), or nullptr for any other pointer.
+static void* mapped_host(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // clear the error of an unknown pointer
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int dym_links_get(dym_chain* c, uint16_t* host_out) {
   if (!c || !host_out) return fail(DYM_EINVAL, "dym_links_get: null argument");
   DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
-  DYM_CUDA(cudaMemcpyAsync(host_out, c->dev.links, (size_t)c->dev.V * c->p.D * 2, cudaMemcpyDeviceToHost, c->stream),
-           "download links");
+  const size_t n = (size_t)c->dev.V * c->p.D;
+  DYM_CUDA(cudaMemcpyAsync(host_out, c->dev.links, n * 2, cudaMemcpyDeviceToHost, c->stream), "download links");
   DYM_CUDA(cudaStreamSynchronize(c->stream), "download links");
   return DYM_OK;
 }
@@ -564,8 +575,14 @@ int dym_links_set(dym_chain* c, const uint16_t* host_in) {
   // Upload into the stage; the device finds the first id >= P and copies the
   // stage into the chain's links only if there is none, so a refused
   // configuration leaves the chain as it was.
-  DYM_CUDA(cudaMemcpyAsync(c->d_stage, host_in, n * 2, cudaMemcpyHostToDevice, c->stream), "upload links");
-  DYM_CUDA(launch_links_commit(c->dev.links, c->d_stage, n, P, c->d_first_bad, c->stream), "check links");
+  if (const void* mh = mapped_host(host_in)) {  // page-locked: read by the checking kernel itself
+    DYM_CUDA(launch_links_from_host(c->dev.links, c->d_stage, static_cast<const uint16_t*>(mh), n, P,
+                                    c->d_first_bad, c->stream),
+             "check links");
+  } else {
+    DYM_CUDA(cudaMemcpyAsync(c->d_stage, host_in, n * 2, cudaMemcpyHostToDevice, c->stream), "upload links");
+    DYM_CUDA(launch_links_commit(c->dev.links, c->d_stage, n, P, c->d_first_bad, c->stream), "check links");
+  }
   DYM_CUDA(cudaMemcpyAsync(c->h_counters + 5, c->d_first_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                            c->stream),
            "read links check");

@@ -92,6 +92,10 @@ cudaError_t launch_fill(uint16_t* links, size_t n, uint16_t v, cudaStream_t s);
 // or ~0) and copy the stage into the links only if all are in range.
 cudaError_t launch_links_commit(uint16_t* links, const uint16_t* stage, size_t n, uint32_t P,
                                 unsigned long long* first, cudaStream_t s);
+// The same reading the ids from page-locked host memory through its device
+// mapping (no copy-engine transfer).
+cudaError_t launch_links_from_host(uint16_t* links, uint16_t* stage, const uint16_t* host_mapped, size_t n,
+                                   uint32_t P, unsigned long long* first, cudaStream_t s);
 cudaError_t launch_staples(int D, int dir, const SweepArgs& a, const uint32_t* sites, uint32_t n, uint16_t* out,
                            cudaStream_t s);
 // Shared memory of k_sweep_mixed: ReTr (FP64) | class values | inverses | packed

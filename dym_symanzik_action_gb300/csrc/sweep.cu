@@ -237,6 +237,32 @@ __global__ void k_ids_first_bad(const uint16_t* __restrict__ ids, size_t n, uint
     if (ids[k] >= P) atomicMin(first, (unsigned long long)k);
 }
 
+// The same check reading the ids straight from page-locked host memory (the
+// caller's buffer, through its device mapping) and writing them to the stage:
+// one pass over the host link instead of a copy-engine transfer and a pass.
+// Host reads are 16 bytes wide (eight ids) when the host buffer starts on 16
+// bytes; `nv` is the number of such groups (0 otherwise), the ids after them
+// go one by one.
+__global__ void k_ids_from_host(uint16_t* __restrict__ stage, const uint16_t* __restrict__ host, size_t n, size_t nv,
+                                uint32_t P, unsigned long long* first) {
+  const size_t t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x, dt = (size_t)gridDim.x * blockDim.x;
+  for (size_t q = t0; q < nv; q += dt) {
+    const uint4 w = reinterpret_cast<const uint4*>(host)[q];
+    reinterpret_cast<uint4*>(stage)[q] = w;
+    const uint32_t x[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+    for (int h = 0; h < 8; ++h) {
+      const uint32_t v = (x[h >> 1] >> (16 * (h & 1))) & 0xFFFFu;
+      if (v >= P) atomicMin(first, (unsigned long long)(8 * q + h));
+    }
+  }
+  for (size_t k = 8 * nv + t0; k < n; k += dt) {
+    const uint16_t v = host[k];
+    stage[k] = v;
+    if (v >= P) atomicMin(first, (unsigned long long)k);
+  }
+}
+
 __global__ void k_ids_commit(uint16_t* __restrict__ links, const uint16_t* __restrict__ stage, size_t n,
                              const unsigned long long* first) {
   if (*first != ~0ull) return;
@@ -468,6 +494,17 @@ cudaError_t launch_links_commit(uint16_t* links, const uint16_t* stage, size_t n
   if (e != cudaSuccess || n == 0) return e;
   const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 8);
   k_ids_first_bad<<<grid, 256, 0, s>>>(stage, n, P, first);
+  k_ids_commit<<<grid, 256, 0, s>>>(links, stage, n, first);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_links_from_host(uint16_t* links, uint16_t* stage, const uint16_t* host_mapped, size_t n,
+                                   uint32_t P, unsigned long long* first, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(first, 0xFF, sizeof(unsigned long long), s);
+  if (e != cudaSuccess || n == 0) return e;
+  const size_t nv = (reinterpret_cast<uintptr_t>(host_mapped) & 15u) ? 0 : n / 8;
+  const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 8);
+  k_ids_from_host<<<grid, 256, 0, s>>>(stage, host_mapped, n, nv, P, first);
   k_ids_commit<<<grid, 256, 0, s>>>(links, stage, n, first);
   return cudaGetLastError();
 }

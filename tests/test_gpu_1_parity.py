@@ -183,3 +183,29 @@ def test_links_set_rejects_out_of_range_ids(engine):
     good = np.roll(before.ravel(), 5)
     lat.links = good
     assert (lat.links.ravel() == good).all()
+
+
+def test_links_transfer_page_locked(engine):
+    """A page-locked host buffer is read by the checking kernel itself: the
+    same refusal (first bad index, chain unchanged) and the same round trip as
+    a pageable buffer."""
+    import ctypes as C
+    import torch
+    from dym_symanzik_action_gb300._lib import DymError, check, lib, ptr
+    lat = engine.Lattice(group(engine, "BT"), 4, 4, 4, 0.0, 1.0, 0.0, 3, start="hot")
+    before = lat.links.copy().ravel()
+    n = before.size
+    hin = torch.empty(n, dtype=torch.uint16, pin_memory=True).numpy()
+    hout = torch.empty(n, dtype=torch.uint16, pin_memory=True).numpy()
+    hin[:] = before
+    hin[321] = lat.group.P
+    hin[400] = 0xFFFF
+    with pytest.raises(DymError, match="at 321$"):
+        check(lib().dym_links_set(lat._h, ptr(hin, C.c_uint16)))
+    check(lib().dym_links_get(lat._h, ptr(hout, C.c_uint16)))
+    assert (hout == before).all()
+    hin[:] = np.roll(before, 7)
+    check(lib().dym_links_set(lat._h, ptr(hin, C.c_uint16)))
+    hout[:] = 0
+    check(lib().dym_links_get(lat._h, ptr(hout, C.c_uint16)))
+    assert (hout == np.roll(before, 7)).all() and (lat.links.ravel() == hout).all()
