@@ -410,6 +410,41 @@ __device__ __forceinline__ bool llr_weight_accept(double x, uint32_t r1, uint32_
   return dym_exp(x) > dym_u53(r1, r2);
 }
 
+// Weights of an LLR hit: exponent -a dE_w - bg dE_bg with dE = d 2^-S for the
+// exact integer sums d (d_w of the windowed action, d_bg of the other).
+struct LlrWeight {
+  double naa, bg, scale;  // -a, bg, 2^-S
+  float naf, bgf, sf;     // the same in FP32
+};
+
+// dym_weight_accept(x, u2), x = -a dE_w - bg dE_bg formed in FP64 as the
+// oracle does, decided in FP32 for all but the hits near a threshold.
+// xf = (-a_f d_w - bg_f d_bg) 2^-S from FP32 copies of a, bg and d: each
+// conversion and product is within 2^-24 relative and the difference adds one
+// rounding, so |xf - x| <= 2^-22 T + 2^-52 T with T = (|p| + |q|) 2^-S, and
+// B = 2^-20 T bounds it twice over.  xf - B >= 0 implies x >= 0 (accept).
+// When B <= 2^-12 and xf lies in [-38 + B, -B], x is in [-38, 0) and
+// exp(xf) is within a factor exp(2^-14) of exp(x); with __expf's documented
+// error (at most 46 ulp there) and u2f within 2^-22 of u2 the FP32 test of
+// llr_weight_accept (band 2^-10) decides.  Every other hit forms x in FP64
+// and runs llr_weight_accept.  The decision is dym_weight_accept's, bit for
+// bit.
+__device__ __forceinline__ bool llr_fix_accept(int32_t dw, int32_t dbg, const LlrWeight& wt, uint32_t r1,
+                                               uint32_t r2) {
+  const float p = __fmul_rn(wt.naf, (float)dw), q = __fmul_rn(wt.bgf, (float)dbg);
+  const float xf = __fmul_rn(__fsub_rn(p, q), wt.sf);
+  const float B = __fmul_rn(__fadd_rn(fabsf(p), fabsf(q)), __fmul_rn(wt.sf, 0x1p-20f));
+  if (__fsub_rn(xf, B) >= 0.0f) return true;
+  if (B <= 0x1p-12f && __fadd_rn(xf, B) < 0.0f && __fsub_rn(xf, B) >= -38.0f) {
+    const float ef = __expf(xf);
+    const float u2f = __fmaf_rn((float)r1, 0x1p-32f, (float)(r2 >> 11) * 0x1p-53f);
+    if (ef > __fmul_rn(u2f, 1.0f + 0x1p-10f)) return true;
+    if (ef < __fmul_rn(u2f, 1.0f - 0x1p-10f)) return false;
+  }
+  const double dEw = DYM_MUL((double)dw, wt.scale), dEbg = DYM_MUL((double)dbg, wt.scale);
+  return llr_weight_accept(DYM_SUB(DYM_MUL(wt.naa, dEw), DYM_MUL(wt.bg, dEbg)), r1, r2);
+}
+
 // Closer to the window centre (fixed-point energies; a two-dimensional cell
 // compares squared normalised distances) -- the drive-in test of the hits and
 // of the commit's scan.
@@ -429,8 +464,8 @@ __device__ __forceinline__ bool llr_drive_closer(const LlrDrive& d, long long e1
 // per hit): nhit hits with weight exp(-a dE_w - bg dE_bg), or, in drive-in
 // mode, greedy moves of the link's running energy towards the centre.  A
 // hit's dS1, dS2 are exact integer sums of its terms' class values at scale
-// 2^evshift (s_ev: per element); the weight's exponent is formed from them in
-// FP64.  The link is written in place; returns its value before the visit, and
+// 2^evshift (s_ev: per element); the weight's exponent is formed from them
+// (llr_fix_accept: in FP32, in FP64 near a threshold).  The link is written in place; returns its value before the visit, and
 // in de1, de2 the exact change of S1 and S2 at scale 2^kLlrFixShift (vf: class
 // values), which the commit's scan tests against the window.  The classes of
 // the initial u_j are kept packed, 5 bits each, and the two hit loops are
@@ -497,7 +532,13 @@ __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, ui
       }
     }
   } else {
-    const double scale = ldexp(1.0, -evshift);
+    LlrWeight wt;
+    wt.naa = -aa;
+    wt.bg = bg;
+    wt.scale = ldexp(1.0, -evshift);
+    wt.naf = __double2float_rn(-aa);
+    wt.bgf = __double2float_rn(bg);
+    wt.sf = ldexpf(1.0f, -evshift);
     for (int h = 0; h < a.nhit; ++h) {
       const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_LLR);
       const uint16_t* row = s_sub + dym_pick(r.v[0], a.npool) * a.P;
@@ -513,11 +554,9 @@ __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, ui
         e[j] = row[u[j]];
         Mn += s_ev[e[j]];
       }
-      const double dS1 = DYM_MUL((double)(Rn - R), scale), dS2 = DYM_MUL((double)(Mn - M), scale);
-      const double dEw = axis == 1 ? dS1 : dS2;
-      const double dEbg = axis == 1 ? dS2 : dS1;
+      const int32_t d1 = Rn - R, d2 = Mn - M;
       ++hits;
-      if (llr_weight_accept(DYM_SUB(DYM_MUL(-aa, dEw), DYM_MUL(bg, dEbg)), r.v[1], r.v[2])) {
+      if (llr_fix_accept(axis == 1 ? d1 : d2, axis == 1 ? d2 : d1, wt, r.v[1], r.v[2])) {
         b = row[b];
 #pragma unroll
         for (int j = 0; j < NT; ++j) u[j] = e[j];
