@@ -47,11 +47,12 @@ def gathers_per_link_hit(nhit: int) -> float:
     return 25.0 + 108.0 / nhit
 
 
-# L2 work per link visit in 4D.  Shared-table kernels (mixed, shared): 84
-# staple products + 24 u_j = s_j * b products, each a random 2-byte gather (one
-# 32-byte sector) from the L2-resident Cayley table; the hits run from shared
-# memory.  Direct kernel (fp64): the same 108 plus 25 per hit.  Per launch
-# every block also stages its shared tables from L2.
+# L2 work per link visit in 4D, in random 2-byte gathers (one 32-byte sector
+# each) from the L2-resident Cayley table.  Mixed-precision kernels (mixed,
+# value table): the 87 products of the u_j = s_j * b tree (staples.cuh
+# build_u_tree); the hits run from shared memory.  FP64 shared-table kernel:
+# 84 staple products + 24 u_j products.  Direct kernel (fp64): those 108 plus
+# 25 per hit.  Per launch every block also stages its shared tables from L2.
 # dram__bytes_read.sum + dram__bytes_write.sum of one sweep launch of this
 # workload, from the ncu --set full captures summarised in
 # profiles/sweep_vt_s1080_32x32x32x8_ncu.md, profiles/sweep_mixed_s1080_32x32x32x8_ncu.md
@@ -80,12 +81,12 @@ def kernel_model(kernel: int, P: int, npool: int, nhit: int, links_per_launch: i
     if kernel == 4:  # value table (sweep.cu vt_smem_bytes); accepted moves add 25 gathers each
         per = -(-links_per_launch // sms)
         threads = min(512, max(128, -(-per // 32) * 32))
-        return ("k_sweep_vt", 108, -(-links_per_launch // threads),
+        return ("k_sweep_vt", 87, -(-links_per_launch // threads),
                 -(-(npool * P * 2) // 16) * 16 + P * 8 + P * 2 + P * 2 + npool * 2 + 16)
     if kernel == 3:  # sweep.cu mixed_smem_bytes; 128..512 threads, one block per SM
         per = -(-links_per_launch // sms)
         threads = min(512, max(128, -(-per // 32) * 32))
-        return ("k_sweep_mixed", 108, -(-links_per_launch // threads),
+        return ("k_sweep_mixed", 87, -(-links_per_launch // threads),
                 P * 8 + 32 * 4 + P * 2 + npool * P * 2 + P + 16)
     if kernel == 2:  # sweep.cu sub_smem_bytes; one wave of 256-thread blocks
         return ("k_sweep_sub", 108, min(sms, -(-links_per_launch // 256)), P * 8 + P * 2 + npool * P * 2 + 16)
