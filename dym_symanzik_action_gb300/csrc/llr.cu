@@ -31,6 +31,8 @@
 // so a chain gives the same result alone or in any mix.
 #include <cuda_runtime.h>
 
+#include <climits>
+
 #include "batch.h"
 #include "chain.h"
 #include "dym_core.h"
@@ -248,19 +250,39 @@ __global__ void k_llr_commit(const LlrCommit* __restrict__ commits, uint32_t n,
         continue;
       }
     }
+    if (!drive) {
+      // In the window: the same walk without branches (the keep bit selects).
+      const long long lo2 = box ? lo1 : LLONG_MIN, hi2 = box ? hi1 : LLONG_MAX;
+      const long long loA = (box || !w) ? lo0 : LLONG_MIN, hiA = (box || !w) ? hi0 : LLONG_MAX;
+      const long long loB = box ? lo2 : (w ? lo0 : LLONG_MIN), hiB = box ? hi2 : (w ? hi0 : LLONG_MAX);
 #pragma unroll 8
-    for (uint32_t j = 0; j < 32; ++j) {
-      const uint32_t nch = __shfl_sync(0xffffffffu, br.nchg, j);
-      const long long s1 = __shfl_sync(0xffffffffu, br.s[0], j), s2 = __shfl_sync(0xffffffffu, br.s[1], j);
-      if (j < nj && nch) {  // the same for every lane
+      for (uint32_t j = 0; j < 32; ++j) {
+        const uint32_t nch = j < nj ? __shfl_sync(0xffffffffu, br.nchg, j) : 0u;
+        const long long s1 = __shfl_sync(0xffffffffu, br.s[0], j), s2 = __shfl_sync(0xffffffffu, br.s[1], j);
         const long long e1 = R1 + s1, e2 = R2 + s2;
-        if (drive ? closer(e1, e2, R1, R2) : in_win(e1, e2)) {
-          R1 = e1;
-          R2 = e2;
-          kept += nch;
-        } else {
-          refused += nch;
-          refused_blocks |= 1u << j;
+        const bool ok = e1 >= loA && e1 <= hiA && e2 >= loB && e2 <= hiB;
+        const bool keep = nch != 0u && ok, drop = nch != 0u && !ok;
+        R1 = keep ? e1 : R1;
+        R2 = keep ? e2 : R2;
+        kept += keep ? nch : 0u;
+        refused += drop ? nch : 0u;
+        refused_blocks |= drop ? (1u << j) : 0u;
+      }
+    } else {
+#pragma unroll 8
+      for (uint32_t j = 0; j < 32; ++j) {
+        const uint32_t nch = __shfl_sync(0xffffffffu, br.nchg, j);
+        const long long s1 = __shfl_sync(0xffffffffu, br.s[0], j), s2 = __shfl_sync(0xffffffffu, br.s[1], j);
+        if (j < nj && nch) {  // the same for every lane
+          const long long e1 = R1 + s1, e2 = R2 + s2;
+          if (closer(e1, e2, R1, R2)) {
+            R1 = e1;
+            R2 = e2;
+            kept += nch;
+          } else {
+            refused += nch;
+            refused_blocks |= 1u << j;
+          }
         }
       }
     }
