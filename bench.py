@@ -254,7 +254,7 @@ def ensemble_bench(dym, device: int, sweeps: int = 5, nhit: int = 10) -> dict:
 
 
 def serving_bench(dym, device: int, n_requests: int, nhit: int = 20, step_sweeps: int = 5,
-                  max_chains: int = 256, max_links: int = 0) -> dict:
+                  max_chains: int = 512, max_links: int = 0) -> dict:
     """Config 5: LLR windows arriving as a Poisson stream (200/s) on S(1080)
     lattices Nx in {6,8,12,16}, Nt in {2,4}, beta2 in {0,-0.1}; each request one
     window of 0.5% of the plaquette-energy range, 20 Robbins-Monro iterations of
@@ -291,8 +291,9 @@ def serving_bench(dym, device: int, n_requests: int, nhit: int = 20, step_sweeps
     hits = srv.status()["link_hits"]
     srv.close()
     L = np.array(list(lat.values()))
-    return {"workload": f"first {len(reqs)} of 2000 LLR window requests, Poisson 200/s, S(1080), Nx in {{6,8,12,16}}, "
-                        f"Nt in {{2,4}}, 20 RM x 50 sweeps, {nhit} hits/link",
+    which = "all 2000" if len(reqs) == 2000 else f"first {len(reqs)} of 2000"
+    return {"workload": f"{which} LLR window requests, Poisson 200/s, S(1080), Nx in {{6,8,12,16}}, "
+                        f"Nt in {{2,4}}, 20 RM x 50 sweeps, {nhit} hits/link, at most {max_chains} resident",
             "requests": len(reqs), "wall_s": wall, "link_hits_per_s": hits / wall,
             "latency_p50_s": float(np.percentile(L, 50)), "latency_p99_s": float(np.percentile(L, 99)),
             "unreached": sum(1 for v in status.values() if v != "done"), "max_resident_chains": max_chains,
@@ -505,7 +506,7 @@ def main():
                     help="single-chain kernel: mixed (default), shared (FP64 shared-table), fp64 (direct)")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched 256-chain ensemble")
     ap.add_argument("--no-mixed-scan", action="store_true", help="skip the 48^3x12 mixed-vs-FP64 scan")
-    ap.add_argument("--serve-requests", type=int, default=60,
+    ap.add_argument("--serve-requests", type=int, default=2000,
                     help="requests of the served LLR stream to run (2000 = the whole stream; 0 = skip)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
