@@ -24,11 +24,13 @@ struct BatchGroupDev {
   const double* retr;
   const uint16_t* sub;  // sub[k][u] = u * pool[k]
   const uint16_t* cls16;  // ReTr class of each element (LLR only)
-  const int32_t* ev;      // LLR: ReTr of each element's class times 2^evshift, rounded (dym_fix_shift)
+  const int32_t* ev;      // LLR: each class's ReTr times 2^evshift, rounded (dym_fix_shift); kLlrMaxCls
   int evshift;
+  int wide;               // LLR: sub holds 32-bit entries element | class << 16 (P > 2048), else 16-bit
+                          // element | class << 11
   uint32_t P, npool;
   uint32_t off_retr, off_inv, off_sub, off_cls;  // byte offsets of the staged copies in shared memory
-  uint32_t off_ev;                               // LLR: staged ev (off_retr is unused there)
+  uint32_t off_ev;                               // LLR: staged class values (off_retr is unused there)
   // Mixed-precision kernel: sub holds packed entries (element | class << 11),
   // cls8 the class of each element, cfix the fixed-point class values.
   const uint8_t* cls8;

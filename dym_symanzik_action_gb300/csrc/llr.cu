@@ -79,17 +79,17 @@ __global__ void __launch_bounds__(kLlrWarps * 32) k_llr_propose(const LlrTile* _
                                                                 BatchGroups groups, int nhit) {
   extern __shared__ __align__(16) unsigned char smem[];
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  for (int g = 0; g < groups.n; ++g) {  // sub-table by cp.async (16-byte aligned on both sides)
+  for (int g = 0; g < groups.n; ++g) {  // packed sub-table by cp.async (16-byte aligned on both sides)
     const BatchGroupDev& G = groups.g[g];
-    const uint32_t nsub = G.npool * G.P, nb16 = (nsub * 2u) & ~15u;
+    const uint32_t nsub = G.npool * G.P * (G.wide ? 2u : 1u), nb16 = (nsub * 2u) & ~15u;  // halfwords
     uint16_t* s_sub = reinterpret_cast<uint16_t*>(smem + G.off_sub);
     cp_async_stage(s_sub, G.sub, nb16);
     for (uint32_t t = nb16 / 2 + threadIdx.x; t < nsub; t += blockDim.x) s_sub[t] = G.sub[t];
-    int32_t* s_ev = reinterpret_cast<int32_t*>(smem + G.off_ev);
+    int32_t* s_cv = reinterpret_cast<int32_t*>(smem + G.off_ev);
+    if (threadIdx.x < kLlrMaxCls) s_cv[threadIdx.x] = G.ev[threadIdx.x];
     uint16_t* s_inv = reinterpret_cast<uint16_t*>(smem + G.off_inv);
     uint16_t* s_cls = reinterpret_cast<uint16_t*>(smem + G.off_cls);
     for (uint32_t t = threadIdx.x; t < G.P; t += blockDim.x) {
-      s_ev[t] = G.ev[t];
       s_inv[t] = G.inv[t];
       s_cls[t] = G.cls16[t];
     }
@@ -116,9 +116,9 @@ __global__ void __launch_bounds__(kLlrWarps * 32) k_llr_propose(const LlrTile* _
     a.npool = G.npool;
     a.seed = c.seed;
     a.nhit = nhit;
-    const int32_t* s_ev = reinterpret_cast<const int32_t*>(smem + G.off_ev);
+    const int32_t* s_cv = reinterpret_cast<const int32_t*>(smem + G.off_ev);
     const uint16_t* s_inv = reinterpret_cast<const uint16_t*>(smem + G.off_inv);
-    const uint16_t* s_sub = reinterpret_cast<const uint16_t*>(smem + G.off_sub);
+    const unsigned char* s_sub = smem + G.off_sub;
     const uint16_t* s_cls = reinterpret_cast<const uint16_t*>(smem + G.off_cls);
     const int axis = st->axis;
     const double aa = st->a, bg = st->bg;
@@ -141,18 +141,21 @@ __global__ void __launch_bounds__(kLlrWarps * 32) k_llr_propose(const LlrTile* _
     if (lane < tl.count) {
       const uint32_t i = c.sites[tl.begin + lane];
       uint32_t b0 = 0;
+      // The packed entries' width is the group's (uniform across the warp).
+#define DYM_LLR_VISIT(DD, E)                                                                                   \
+  visit_llr<D, DD, E>(a, i, sweep, s_cv, G.evshift, s_inv, reinterpret_cast<const E*>(s_sub), s_cls, st->vf, \
+                      axis, aa, bg, dr, drive, de1, de2, hits, accs)
       switch (tl.dir) {
-        case 0: b0 = visit_llr<D, 0>(a, i, sweep, s_ev, G.evshift, s_inv, s_sub, s_cls, st->vf, axis, aa, bg, dr,
-                                     drive, de1, de2, hits, accs); break;
-        case 1: b0 = visit_llr<D, 1>(a, i, sweep, s_ev, G.evshift, s_inv, s_sub, s_cls, st->vf, axis, aa, bg, dr,
-                                     drive, de1, de2, hits, accs); break;
-        case 2: if (D > 2) b0 = visit_llr<D, (D > 2 ? 2 : 0)>(a, i, sweep, s_ev, G.evshift, s_inv, s_sub, s_cls,
-                                                               st->vf, axis, aa, bg, dr, drive, de1, de2, hits, accs);
+        case 0: b0 = G.wide ? DYM_LLR_VISIT(0, uint32_t) : DYM_LLR_VISIT(0, uint16_t); break;
+        case 1: b0 = G.wide ? DYM_LLR_VISIT(1, uint32_t) : DYM_LLR_VISIT(1, uint16_t); break;
+        case 2:
+          if (D > 2) b0 = G.wide ? DYM_LLR_VISIT((D > 2 ? 2 : 0), uint32_t) : DYM_LLR_VISIT((D > 2 ? 2 : 0), uint16_t);
           break;
-        case 3: if (D > 3) b0 = visit_llr<D, (D > 3 ? 3 : 0)>(a, i, sweep, s_ev, G.evshift, s_inv, s_sub, s_cls,
-                                                               st->vf, axis, aa, bg, dr, drive, de1, de2, hits, accs);
+        case 3:
+          if (D > 3) b0 = G.wide ? DYM_LLR_VISIT((D > 3 ? 3 : 0), uint32_t) : DYM_LLR_VISIT((D > 3 ? 3 : 0), uint16_t);
           break;
       }
+#undef DYM_LLR_VISIT
       changed = c.links[(size_t)tl.dir * c.V + i] != (uint16_t)b0;
       LlrLinkRec r;
       r.site = i;

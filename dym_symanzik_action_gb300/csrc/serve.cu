@@ -191,19 +191,31 @@ struct LlrWork {
   int add_group(Group* g) {
     if (std::find(groups.begin(), groups.end(), g) != groups.end()) return DYM_OK;
     if ((int)groups.size() == kBatchMaxGroups) return fail(DYM_ENOTSUP, "at most 4 groups");
+    // Packed sub-table sub[k][u] = e | class(e) << 11 with e = u * pool[k]
+    // (32-bit entries, class << 16, for groups of order above 2048) and the
+    // fixed-point value of every class (the hits' exact sums; LLR runs on
+    // four-dimensional lattices only).
     const auto& pool = g->pool_nearest;
-    std::vector<uint16_t> sub(pool.size() * (size_t)g->P);
+    const bool wide = g->P > kMixedMaxP;
+    const size_t nent = pool.size() * (size_t)g->P;
+    std::vector<uint16_t> sub(nent * (wide ? 2 : 1));
     for (size_t k = 0; k < pool.size(); ++k)
-      for (uint32_t u = 0; u < g->P; ++u) sub[k * g->P + u] = g->mult[(size_t)u * g->P + pool[k]];
+      for (uint32_t u = 0; u < g->P; ++u) {
+        const uint32_t e = g->mult[(size_t)u * g->P + pool[k]];
+        if (wide) {
+          const uint32_t w = e | ((uint32_t)g->cls[e] << 16);
+          std::memcpy(&sub[2 * (k * g->P + u)], &w, 4);
+        } else {
+          sub[k * g->P + u] = (uint16_t)(e | ((uint32_t)g->cls[e] << 11));
+        }
+      }
     uint16_t* d = nullptr;
     DYM_CUDA(dmalloc(&d, sub.size()), "cudaMalloc(llr sub)");
     DYM_CUDA(copy_sync(d, sub.data(), sub.size() * 2, cudaMemcpyHostToDevice, stream), "upload llr sub");
     d_sub.push_back(d);
-    // Fixed-point ReTr of every element's class (the hits' exact sums); LLR
-    // runs on four-dimensional lattices only.
-    std::vector<int32_t> ev(g->P);
+    std::vector<int32_t> ev(kLlrMaxCls, 0);
     const int S = fix_shift(*g, 4);
-    for (uint32_t e = 0; e < g->P; ++e) ev[e] = (int32_t)std::llrint(std::ldexp(g->cls_val[g->cls[e]], S));
+    for (int c = 0; c < g->ncls; ++c) ev[c] = (int32_t)std::llrint(std::ldexp(g->cls_val[c], S));
     int32_t* dv = nullptr;
     DYM_CUDA(dmalloc(&dv, ev.size()), "cudaMalloc(llr values)");
     DYM_CUDA(copy_sync(dv, ev.data(), ev.size() * 4, cudaMemcpyHostToDevice, stream), "upload llr values");
@@ -223,17 +235,18 @@ struct LlrWork {
       b.cls16 = (const uint16_t*)G.d_cls16;
       b.ev = d_ev[k];
       b.evshift = fix_shift(G, 4);
+      b.wide = G.P > kMixedMaxP ? 1 : 0;
       b.P = G.P;
       b.npool = (uint32_t)G.pool_nearest.size();
       b.off_retr = 0;
       b.off_ev = (uint32_t)off;
-      off = up16(off + (size_t)G.P * 4);
+      off = up16(off + (size_t)kLlrMaxCls * 4);
       b.off_inv = (uint32_t)off;
       off = up16(off + (size_t)G.P * 2);
       b.off_cls = (uint32_t)off;
       off = up16(off + (size_t)G.P * 2);
       b.off_sub = (uint32_t)off;
-      off = up16(off + (size_t)b.npool * G.P * 2);
+      off = up16(off + (size_t)b.npool * G.P * (b.wide ? 4 : 2));
     }
     smem = off;
     int optin = 0;

@@ -462,21 +462,24 @@ __device__ __forceinline__ bool llr_drive_closer(const LlrDrive& d, long long e1
 
 // One LLR visit of link (i, DIR) with the shared sub-table (llr.cpp:186-216
 // per hit): nhit hits with weight exp(-a dE_w - bg dE_bg), or, in drive-in
-// mode, greedy moves of the link's running energy towards the centre.  A
-// hit's dS1, dS2 are exact integer sums of its terms' class values at scale
-// 2^evshift (s_ev: per element); the weight's exponent is formed from them
+// mode, greedy moves of the link's running energy towards the centre.  The
+// sub-table's entries pack element and class (Packed<E>), so a term's value
+// is one read of the class-value table s_cv (one word per bank: no bank
+// conflicts); a hit's dS1, dS2 are exact integer sums of its terms' class
+// values at scale 2^evshift, and the weight's exponent is formed from them
 // (llr_fix_accept: in FP32, in FP64 near a threshold).  The link is written in place; returns its value before the visit, and
 // in de1, de2 the exact change of S1 and S2 at scale 2^kLlrFixShift (vf: class
 // values), which the commit's scan tests against the window.  The classes of
 // the initial u_j are kept packed, 5 bits each, and the two hit loops are
 // separate so that neither holds the other's state.
-template <int D, int DIR>
-__device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, uint32_t sweep, const int32_t* s_ev,
-                                              int evshift, const uint16_t* s_inv, const uint16_t* s_sub,
+template <int D, int DIR, class E>
+__device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, uint32_t sweep, const int32_t* s_cv,
+                                              int evshift, const uint16_t* s_inv, const E* s_psub,
                                               const uint16_t* s_cls, const long long* __restrict__ vf, int axis,
                                               double aa, double bg, const LlrDrive& dr, bool drive, long long& de1,
                                               long long& de2, unsigned& hits, unsigned& accs) {
   constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
+  constexpr uint32_t kBits = Packed<E>::kBits, kMask = Packed<E>::kMask;
   constexpr int NW = (NT + 5) / 6;  // words of six 5-bit classes
   static_assert(kLlrMaxCls <= 32, "classes are packed in 5 bits");
   SiteGeo<D> geo;
@@ -493,37 +496,38 @@ __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, ui
   uint32_t c0[NW];
 #pragma unroll
   for (int w = 0; w < NW; ++w) c0[w] = 0;
-#pragma unroll
-  for (int j = 0; j < NT; ++j) c0[j / 6] |= (uint32_t)s_cls[u[j]] << (5 * (j % 6));
   int32_t R = 0, M = 0;  // exact sums (the differences below fit int32: dym_fix_shift)
 #pragma unroll
-  for (int j = 0; j < NS; ++j) R += s_ev[u[j]];
-#pragma unroll
-  for (int j = NS; j < NT; ++j) M += s_ev[u[j]];
+  for (int j = 0; j < NT; ++j) {
+    const uint32_t cj = s_cls[u[j]];
+    c0[j / 6] |= cj << (5 * (j % 6));
+    if (j < NS) R += s_cv[cj];
+    else M += s_cv[cj];
+  }
   if (drive) {
     const int up = kLlrFixShift - evshift;
     long long cum1 = 0, cum2 = 0;  // the link's kept moves, scale 2^kLlrFixShift
     for (int h = 0; h < a.nhit; ++h) {
       const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_LLR);
-      const uint16_t* row = s_sub + dym_pick(r.v[0], a.npool) * a.P;
+      const E* row = s_psub + dym_pick(r.v[0], a.npool) * a.P;
       uint32_t e[NT];
       int32_t Rn = 0, Mn = 0;
 #pragma unroll
       for (int j = 0; j < NS; ++j) {
         e[j] = row[u[j]];
-        Rn += s_ev[e[j]];
+        Rn += s_cv[e[j] >> kBits];
       }
 #pragma unroll
       for (int j = NS; j < NT; ++j) {
         e[j] = row[u[j]];
-        Mn += s_ev[e[j]];
+        Mn += s_cv[e[j] >> kBits];
       }
       const long long n1 = cum1 + (long long)(Rn - R) * (1ll << up), n2 = cum2 + (long long)(Mn - M) * (1ll << up);
       ++hits;
       if (llr_drive_closer(dr, dr.E[0] + n1, dr.E[1] + n2, dr.E[0] + cum1, dr.E[1] + cum2)) {
-        b = row[b];
+        b = row[b] & kMask;
 #pragma unroll
-        for (int j = 0; j < NT; ++j) u[j] = e[j];
+        for (int j = 0; j < NT; ++j) u[j] = e[j] & kMask;
         R = Rn;
         M = Mn;
         cum1 = n1;
@@ -541,25 +545,25 @@ __device__ __forceinline__ uint32_t visit_llr(const SweepArgs& a, uint32_t i, ui
     wt.sf = ldexpf(1.0f, -evshift);
     for (int h = 0; h < a.nhit; ++h) {
       const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_LLR);
-      const uint16_t* row = s_sub + dym_pick(r.v[0], a.npool) * a.P;
+      const E* row = s_psub + dym_pick(r.v[0], a.npool) * a.P;
       uint32_t e[NT];
       int32_t Rn = 0, Mn = 0;
 #pragma unroll
       for (int j = 0; j < NS; ++j) {
         e[j] = row[u[j]];
-        Rn += s_ev[e[j]];
+        Rn += s_cv[e[j] >> kBits];
       }
 #pragma unroll
       for (int j = NS; j < NT; ++j) {
         e[j] = row[u[j]];
-        Mn += s_ev[e[j]];
+        Mn += s_cv[e[j] >> kBits];
       }
       const int32_t d1 = Rn - R, d2 = Mn - M;
       ++hits;
       if (llr_fix_accept(axis == 1 ? d1 : d2, axis == 1 ? d2 : d1, wt, r.v[1], r.v[2])) {
-        b = row[b];
+        b = row[b] & kMask;
 #pragma unroll
-        for (int j = 0; j < NT; ++j) u[j] = e[j];
+        for (int j = 0; j < NT; ++j) u[j] = e[j] & kMask;
         R = Rn;
         M = Mn;
         ++accs;
