@@ -94,6 +94,11 @@ __global__ void __launch_bounds__(kLlrWarps * 32) k_llr_propose(const LlrTile* _
       s_cls[t] = G.cls16[t];
     }
   }
+  // The tables are constant: they were staged while the previous kernel of the
+  // stream (the last slot's restore) ran; its links and chain states are read
+  // from here on.
+  pdl_launch_dependents();
+  pdl_wait_prior();
   cp_async_wait_all();
   __syncthreads();
   // Tile t goes to warp t / gridDim.x of block t % gridDim.x: a short list
@@ -200,8 +205,10 @@ __global__ void k_llr_commit(const LlrCommit* __restrict__ commits, uint32_t n,
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (idx >= n) return;  // the same for every lane of the warp
-  const LlrCommit cm = commits[idx];
+  const LlrCommit cm = commits[idx];  // constant: read before the propose kernel has finished
   const LlrChainDev c = chains[cm.chain];
+  pdl_launch_dependents();
+  pdl_wait_prior();
   LlrState* st = c.st;
   int mode = st->mode;
   if (mode >= DYM_LLR_DONE) {
@@ -344,6 +351,8 @@ __global__ void k_llr_restore(const LlrTile* __restrict__ tiles, uint32_t ntiles
                               const LlrChainDev* __restrict__ chains) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t stride = (gridDim.x * blockDim.x) >> 5;
+  pdl_launch_dependents();
+  pdl_wait_prior();  // the commit's flags and states
   for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntiles; t += stride) {
     const LlrTile tl = tiles[t];
     const LlrChainDev c = chains[tl.chain];
@@ -356,6 +365,27 @@ __global__ void k_llr_restore(const LlrTile* __restrict__ tiles, uint32_t ntiles
   }
 }
 
+// Launch, with programmatic stream serialization when `pdl`: each of a slot's
+// kernels may then start its constant prologue (the propose kernel: table
+// staging) while the previous kernel drains, and waits for it (pdl_wait_prior)
+// before it reads links or chain states.  Without the attribute the waits are
+// no-ops and the stream orders the kernels.
+template <class... K, class... A>
+cudaError_t launch_pdl(bool pdl, void (*fn)(K...), unsigned grid, unsigned threads, size_t smem, cudaStream_t s,
+                       A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, fn, args...);
+}
+
 }  // namespace
 
 void* llr_propose_kernel_for(int D) { return D == 4 ? (void*)k_llr_propose<4> : nullptr; }
@@ -364,13 +394,20 @@ cudaError_t launch_llr_slot(int D, const LlrTile* tiles, uint32_t ntiles, const 
                             const LlrChainDev* chains, const BatchGroups& groups, int nhit, unsigned grid,
                             size_t smem, cudaStream_t s) {
   if (D != 4) return cudaErrorInvalidValue;  // four dimensions only (see launch_sweep_sub)
+  // Overlap the launches only when a slot is short (at most one tile per warp
+  // of the propose grid): then the gaps between its three kernels are a large
+  // part of it; on a loaded work list the early propose blocks cost more than
+  // they hide (measured on the served stream).
+  const bool pdl = ntiles <= (size_t)grid * kLlrWarps;
+  cudaError_t e = cudaSuccess;
   if (ntiles) {
     const unsigned g = grid < ntiles ? grid : ntiles;
-    k_llr_propose<4><<<g, kLlrWarps * 32, smem, s>>>(tiles, ntiles, chains, groups, nhit);
+    e = launch_pdl(pdl, k_llr_propose<4>, g, kLlrWarps * 32, smem, s, tiles, ntiles, chains, groups, nhit);
   }
-  if (ncommit) k_llr_commit<<<(ncommit + 3) / 4, 128, 0, s>>>(commits, ncommit, chains);
-  if (ntiles) k_llr_restore<<<(ntiles + 7) / 8, 256, 0, s>>>(tiles, ntiles, chains);
-  return cudaGetLastError();
+  if (e == cudaSuccess && ncommit)
+    e = launch_pdl(pdl, k_llr_commit, (ncommit + 3) / 4, 128, 0, s, commits, ncommit, chains);
+  if (e == cudaSuccess && ntiles) e = launch_pdl(pdl, k_llr_restore, (ntiles + 7) / 8, 256, 0, s, tiles, ntiles, chains);
+  return e;
 }
 
 }  // namespace dym
