@@ -24,8 +24,11 @@ It builds oracle/_ref/ (oracle/build_ref.sh) and writes:
   (0, 1.5, 0.1) for several seeds: the oracle for the 1-sigma comparison.
 * llr_ref.npz -- the ANE table (window centre, mean a_n, sd, samples) of the
   unmodified reference llr executable (its own S(1080) table, one thread) on a
-  four-window ladder of a 4^3x2 lattice with R = 6 repeats of the hot-down and
-  cold-up passes: the statistical oracle for the device LLR.
+  four-window ladder of S1 (plaquette) windows on a 4^3x2 lattice with R = 6
+  repeats of the hot-down and cold-up passes: the statistical oracle for the
+  device LLR.
+* llr_ref_s2.npz -- the same for two S2 (rectangle) windows on a 4^4 lattice
+  (axis 2; every extent >= 3 so that no 1x2 rectangle wraps), R = 4.
 
 * llr2d_ref.npz -- the ANE2 table (cell centres, mean a1 and a2, sds, samples)
   of the unmodified reference llr2d executable (full mode, its own S(1080)
@@ -262,12 +265,15 @@ def make_chains():
 # 0.0225 NPLAQ (0.5% of the S(1080) plaquette-energy range).
 LLR_LADDER = dict(D=4, Nt=2, Nx=4, axis=1, bg=0.0, Etop=-460.8, Ebot=-921.6, step=153.6, hw=8.64, a0=1.5,
                   seed=20261203, K=50, NRM=80, R=6)
+# S2 windows (NRECT 3072 on 4^4): centres -0.15 and -0.30 NRECT, width 0.0225 NRECT, beta1 = 0; a0 near the
+# solution, so that Robbins-Monro converges within NRM on these wide windows.
+LLR_LADDER_S2 = dict(D=4, Nt=4, Nx=4, axis=2, bg=0.0, Etop=-460.8, Ebot=-921.6, step=460.8, hw=34.56, a0=0.5,
+                     seed=20261203, K=50, NRM=80, R=4)
 
 
-def make_llr():
+def make_llr(L=LLR_LADDER, name="llr_ref.npz"):
     exe = os.path.join(ROOT, "oracle", "_ref", "llr")
     table = os.path.join(REF_DIR, "groups", "mys1080-v4")
-    L = LLR_LADDER
     args = [L[k] for k in ("D", "Nt", "Nx", "axis", "bg", "Etop", "Ebot", "step", "hw", "a0", "seed", "K", "NRM",
                            "R")]
     with tempfile.TemporaryDirectory() as td:  # the -pg build writes gmon.out into its cwd
@@ -278,9 +284,9 @@ def make_llr():
         raise RuntimeError("reference llr left a window unreached:\n" + r.stdout)
     ane = np.array(rows, float)
     print(r.stdout)
-    np.savez_compressed(os.path.join(HERE, "llr_ref.npz"), ewin=ane[:, 0], mean=ane[:, 1], sd=ane[:, 2],
+    np.savez_compressed(os.path.join(HERE, name), ewin=ane[:, 0], mean=ane[:, 1], sd=ane[:, 2],
                         nrep=ane[:, 3].astype(np.int64),
-                        args=np.array(" ".join(f"{k}={v}" for k, v in LLR_LADDER.items())),
+                        args=np.array(" ".join(f"{k}={v}" for k, v in L.items())),
                         table=np.array("mys1080-v4"))
 
 
@@ -318,7 +324,7 @@ def make_llr2d():
 def main():
     import argparse
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["iso", "staples", "sweeps", "chains", "llr", "llr2d"])
+    ap.add_argument("--only", choices=["iso", "staples", "sweeps", "chains", "llr", "llr_s2", "llr2d"])
     only = ap.parse_args().only
     subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True,
                    env=dict(os.environ, REF_DIR=REF_DIR), stdout=subprocess.DEVNULL)
@@ -333,6 +339,8 @@ def main():
         make_chains()
     if only in (None, "llr"):
         make_llr()
+    if only in (None, "llr_s2"):
+        make_llr(LLR_LADDER_S2, "llr_ref_s2.npz")
     if only in (None, "llr2d"):
         make_llr2d()
 

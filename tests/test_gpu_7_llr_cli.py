@@ -73,13 +73,15 @@ def test_dym_llr_matches_oracle_ladder(engine):
     assert sum(reached) > 0
 
 
-def test_dym_llr_matches_unmodified_reference():
+@pytest.mark.parametrize("fixture", ["llr_ref.npz", "llr_ref_s2.npz"])
+def test_dym_llr_matches_unmodified_reference(fixture):
     """The a_n ladder of dym-llr against the unmodified reference llr
-    executable (tests/golden/llr_ref.npz: its own S(1080) table, R = 6 repeats
-    of both passes, K = 50, NRM = 80) on a 4^3x2 lattice whose 32-link colour
-    classes move the energy by about the window width: every window's mean a_n
-    within 4 combined standard errors of the reference's."""
-    ref = np.load(os.path.join(os.path.dirname(__file__), "golden", "llr_ref.npz"))
+    executable (its own S(1080) table, K = 50, NRM = 80): llr_ref.npz, S1
+    windows on a 4^3x2 lattice whose 32-link colour classes move the energy by
+    about the window width (R = 6); llr_ref_s2.npz, S2 (rectangle) windows on
+    4^4 (R = 4).  Every window's mean a_n within 4 combined standard errors of
+    the reference's."""
+    ref = np.load(os.path.join(os.path.dirname(__file__), "golden", fixture))
     kv = dict(x.split("=") for x in str(ref["args"]).split())
     keys = ("D", "Nt", "Nx", "axis", "bg", "Etop", "Ebot", "step", "hw", "a0", "seed", "K", "NRM", "R")
     args = [tables.ensure_table("S1080"), *[kv[k] for k in keys]]
