@@ -382,7 +382,10 @@ cudaError_t mixed_dispatch(int dir, const SweepArgs& a, const E* psub, cudaStrea
   if (e != cudaSuccess) return e;
   const uint32_t per = (a.n + (uint32_t)sms - 1) / (uint32_t)sms;
   const unsigned threads = std::min<unsigned>(kMixedMaxThreads, std::max<unsigned>(128, (per + 31) / 32 * 32));
-  return launch_phase(fn, (a.n + threads - 1) / threads, threads, smem, s, a, psub);
+  // One wave: a phase larger than the SMs' blocks is walked by each block in
+  // turn (the kernel's grid-stride loop), so each SM stages its tables once.
+  const unsigned grid = std::min<unsigned>((a.n + threads - 1) / threads, (unsigned)sms);
+  return launch_phase(fn, grid, threads, smem, s, a, psub);
 }
 
 template <int D>
@@ -405,7 +408,8 @@ cudaError_t vt_dispatch(int dir, const SweepArgs& a, const int16_t* vsub, cudaSt
   if (e != cudaSuccess) return e;
   const uint32_t per = (a.n + (uint32_t)sms - 1) / (uint32_t)sms;
   const unsigned threads = std::min<unsigned>(kMixedMaxThreads, std::max<unsigned>(128, (per + 31) / 32 * 32));
-  return launch_phase(fn, (a.n + threads - 1) / threads, threads, smem, s, a, vsub);
+  const unsigned grid = std::min<unsigned>((a.n + threads - 1) / threads, (unsigned)sms);  // one wave, as above
+  return launch_phase(fn, grid, threads, smem, s, a, vsub);
 }
 
 template <int D>
