@@ -299,7 +299,7 @@ def serving_bench(dym, device: int, n_requests: int, nhit: int = 20, step_sweeps
             "requests": len(reqs), "wall_s": wall, "link_hits_per_s": hits / wall,
             "latency_p50_s": float(np.percentile(L, 50)), "latency_p99_s": float(np.percentile(L, 99)),
             "unreached": sum(1 for v in status.values() if v != "done"), "max_resident_chains": max_chains,
-            "max_resident_links": max_links}
+            "max_resident_links": max_links or None}  # 0 = no cap
 
 
 def mixed_precision_scan(dym, device: int, sweeps: int = 300, nhit: int = 10) -> dict:
