@@ -122,6 +122,7 @@ PROTOTYPES = {
     "dym_chain_create": (C.c_int, [_P, C.POINTER(ChainParams), C.POINTER(_P)]),
     "dym_chain_free": (C.c_int, [_P]),
     "dym_chain_set_beta": (C.c_int, [_P, C.c_double, C.c_double, C.c_double]),
+    "dym_chain_set_l2_window": (C.c_int, [_P, C.c_int32]),
     "dym_sweep": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(Stats)]),
     "dym_measure": (C.c_int, [_P, C.POINTER(MeasOpts), C.POINTER(Obs), _f64p]),
     "dym_measure_noalloc": (C.c_int, [_P, C.POINTER(MeasOpts), C.POINTER(Obs), _f64p]),

@@ -5,7 +5,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 
 #include "batch.h"
@@ -228,6 +230,42 @@ static SweepArgs sweep_args(dym_chain* c, int kernel = DYM_KERNEL_MIXED) {
   return a;
 }
 
+// Persisting-L2 set-aside shared by the chains that pin their group's table
+// (dym_chain_set_l2_window): per device, how many windows are open and the
+// set-aside in force before the first was opened, restored when the last
+// closes.
+struct L2SetAside {
+  int users = 0;
+  size_t prev = 0;
+};
+static std::mutex g_l2_mu;
+static std::map<int, L2SetAside> g_l2;
+
+static int l2_acquire(int device, size_t bytes, size_t* granted) {
+  std::lock_guard<std::mutex> lock(g_l2_mu);
+  L2SetAside& s = g_l2[device];
+  if (s.users == 0) DYM_CUDA(cudaDeviceGetLimit(&s.prev, cudaLimitPersistingL2CacheSize), "cudaDeviceGetLimit");
+  size_t cur = 0;
+  DYM_CUDA(cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize), "cudaDeviceGetLimit");
+  if (cur < bytes) {
+    DYM_CUDA(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, bytes), "cudaDeviceSetLimit(persisting L2)");
+    DYM_CUDA(cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize), "cudaDeviceGetLimit");
+  }
+  ++s.users;
+  *granted = cur;
+  return DYM_OK;
+}
+
+static void l2_release(int device) {
+  std::lock_guard<std::mutex> lock(g_l2_mu);
+  auto it = g_l2.find(device);
+  if (it == g_l2.end() || it->second.users == 0) return;
+  if (--it->second.users == 0) {
+    cudaCtxResetPersistingL2Cache();
+    cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, it->second.prev);
+  }
+}
+
 static void chain_release(dym_chain* c) {
   if (!c) return;
   cudaSetDevice(c->p.device);
@@ -257,6 +295,7 @@ static void chain_release(dym_chain* c) {
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
+  if (c->l2_window) l2_release(c->p.device);
   delete c;
 }
 
@@ -425,6 +464,43 @@ int dym_chain_create(const dym_group* gh, const dym_chain_params* p, dym_chain**
 
 int dym_chain_free(dym_chain* c) {
   chain_release(c);
+  return DYM_OK;
+}
+
+int dym_chain_set_l2_window(dym_chain* c, int32_t on) {
+  if (!c) return fail(DYM_EINVAL, "dym_chain_set_l2_window: null chain");
+  DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+  if ((on != 0) == c->l2_window) return DYM_OK;
+  cudaStreamAttrValue v{};
+  if (on) {
+    int max_set_aside = 0, max_window = 0;
+    DYM_CUDA(cudaDeviceGetAttribute(&max_set_aside, cudaDevAttrMaxPersistingL2CacheSize, c->p.device), "attribute");
+    DYM_CUDA(cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, c->p.device), "attribute");
+    if (max_set_aside <= 0 || max_window <= 0) return fail(DYM_ENOTSUP, "device has no persisting L2");
+    const Group& g = *c->grp->g;
+    const size_t table = (size_t)g.P * g.P * sizeof(uint16_t);
+    const size_t window = std::min(table, (size_t)max_window);
+    size_t granted = 0;
+    int rc = l2_acquire(c->p.device, std::min(window, (size_t)max_set_aside), &granted);
+    if (rc) return rc;
+    v.accessPolicyWindow.base_ptr = g.d_mult;
+    v.accessPolicyWindow.num_bytes = window;
+    v.accessPolicyWindow.hitRatio = (float)std::min(1.0, (double)granted / (double)window);
+    v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    const cudaError_t e = cudaStreamSetAttribute(c->stream, cudaStreamAttributeAccessPolicyWindow, &v);
+    if (e != cudaSuccess) {
+      l2_release(c->p.device);
+      return cuda_fail(e, "cudaStreamSetAttribute(access policy window)");
+    }
+    c->l2_window = true;
+  } else {
+    v.accessPolicyWindow.num_bytes = 0;  // no window
+    DYM_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    DYM_CUDA(cudaStreamSetAttribute(c->stream, cudaStreamAttributeAccessPolicyWindow, &v), "cudaStreamSetAttribute");
+    c->l2_window = false;
+    l2_release(c->p.device);
+  }
   return DYM_OK;
 }
 

@@ -211,4 +211,5 @@ struct dym_chain {
   uint8_t* d_llr_bref = nullptr;          // per block: refused by the last scan
   uint16_t* d_stage = nullptr;  // dym_links_set: upload buffer, copied into the links once checked
   unsigned long long* d_first_bad = nullptr;  // dym_links_set: smallest out-of-range index, or ~0
+  bool l2_window = false;  // dym_chain_set_l2_window: the stream pins the Cayley table in L2
 };

@@ -192,6 +192,11 @@ class Lattice:
         check(lib().dym_chain_set_beta(self._h, beta0, beta1, beta2))
         self.beta = (beta0, beta1, beta2)
 
+    def set_l2_window(self, on: bool = True) -> None:
+        """Pin the group's Cayley table in L2 for this chain's kernels (an
+        access-policy window on the chain's stream); opt-in, results unchanged."""
+        check(lib().dym_chain_set_l2_window(self._h, 1 if on else 0))
+
     def update(self, nsweeps: int = 1, nhit: int = 20) -> SweepStats:
         """nsweeps calls of the reference's update() (dym-mod-metro.cpp:146-197)."""
         st = _lib.Stats()

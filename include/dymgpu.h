@@ -111,6 +111,18 @@ int dym_chain_free(dym_chain* c);
 /* Change the couplings of an existing chain (beta scans). */
 int dym_chain_set_beta(dym_chain* c, double beta0, double beta1, double beta2);
 
+/* Pin the group's Cayley table in L2 for this chain's kernels (on != 0), or
+ * stop (on == 0).  Sets an access-policy window over the table on the chain's
+ * stream (hits persisting, misses streaming) and raises the device's
+ * persisting-L2 set-aside to the window size while any chain of the process
+ * holds a window; the previous set-aside is restored when the last one stops
+ * or is freed.  Opt-in: a table of a few MB already stays L2-resident on its
+ * own, so this matters only when a large lattice streams through L2 beside
+ * it.  Configurations do not depend on it.  DYM_ENOTSUP when the device has
+ * no persisting L2.  (No reference counterpart: group.c keeps the table in
+ * host memory.) */
+int dym_chain_set_l2_window(dym_chain* c, int32_t on);
+
 typedef struct {
   uint64_t hits;        /* Metropolis hits (reference `hit`) */
   uint64_t accepts;     /* accepted hits (reference `acc`) */

@@ -209,3 +209,28 @@ def test_links_transfer_page_locked(engine):
     hout[:] = 0
     check(lib().dym_links_get(lat._h, ptr(hout, C.c_uint16)))
     assert (hout == np.roll(before, 7)).all() and (lat.links.ravel() == hout).all()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_l2_window_leaves_configurations_unchanged(engine, precision):
+    """Pinning the Cayley table in L2 (an access-policy window on the chain's
+    stream) changes where the table lives, not what the sweep computes: the
+    same chain with and without the window, switched on and off between
+    calls, gives the same links and counters after every call."""
+    g = group(engine, "S1080")
+    plain = engine.Lattice(g, 4, 4, 8, 0.0, 2.0, -0.1, 11, start="hot", precision=precision)
+    pinned = engine.Lattice(g, 4, 4, 8, 0.0, 2.0, -0.1, 11, start="hot", precision=precision)
+    pinned.set_l2_window(True)
+    pinned.set_l2_window(True)  # idempotent
+    for on in (True, False, True):
+        pinned.set_l2_window(on)
+        a = plain.update(2, 10)
+        b = pinned.update(2, 10)
+        assert (a.hits, a.accepts) == (b.hits, b.accepts)
+        assert (plain.links == pinned.links).all()
+    pinned.close()  # releases the window and the set-aside
+    again = engine.Lattice(g, 4, 4, 8, 0.0, 2.0, -0.1, 11, start="hot", precision=precision)
+    again.set_l2_window(True)
+    again.set_l2_window(False)
+    again.close()
+    plain.close()
