@@ -34,7 +34,8 @@ extern "C" {
 #define DYM_ENOMEM -4     /* host or device allocation failed */
 #define DYM_ECUDA -5      /* CUDA runtime error (no device, launch failure) */
 #define DYM_ENOTSUP -6    /* combination not supported (e.g. D out of range) */
-#define DYM_ETIMEDOUT -7  /* bounded device wait expired */
+#define DYM_ETIMEDOUT -7  /* reserved for a bounded device wait that expired; no kernel of this
+                                  library waits on another, so no entry point returns it */
 #define DYM_ERANGE -8     /* size limit exceeded (group order > DYM_PMAX, ...) */
 
 /* Largest group order accepted; same limit as the reference's PMAX (group.h:4). */
