@@ -117,9 +117,10 @@ int dym_chain_set_beta(dym_chain* c, double beta0, double beta1, double beta2);
  * stream (hits persisting, misses streaming) and raises the device's
  * persisting-L2 set-aside to the window size while any chain of the process
  * holds a window; the previous set-aside is restored when the last one stops
- * or is freed.  Opt-in: a table of a few MB already stays L2-resident on its
- * own, so this matters only when a large lattice streams through L2 beside
- * it.  Configurations do not depend on it.  DYM_ENOTSUP when the device has
+ * or is freed.  Opt-in: no gain was measured with it, even beside a lattice
+ * (96^3 x 24, 170 MB of links) larger than L2, where the table, gathered on
+ * every staple, stayed resident without it.  Configurations do not depend
+ * on it.  DYM_ENOTSUP when the device has
  * no persisting L2.  (No reference counterpart: group.c keeps the table in
  * host memory.) */
 int dym_chain_set_l2_window(dym_chain* c, int32_t on);
