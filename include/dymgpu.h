@@ -118,9 +118,8 @@ int dym_chain_set_beta(dym_chain* c, double beta0, double beta1, double beta2);
  * persisting-L2 set-aside to the window size while any chain of the process
  * holds a window; the previous set-aside is restored when the last one stops
  * or is freed.  Opt-in: no gain was measured with it, even beside a lattice
- * (96^3 x 24, 170 MB of links) larger than L2, where the table, gathered on
- * every staple, stayed resident without it.  Configurations do not depend
- * on it.  DYM_ENOTSUP when the device has
+ * (96^3 x 24, 170 MB of links) larger than L2: sweeps took the same time
+ * with and without the window.  Configurations do not depend on it.  DYM_ENOTSUP when the device has
  * no persisting L2.  (No reference counterpart: group.c keeps the table in
  * host memory.) */
 int dym_chain_set_l2_window(dym_chain* c, int32_t on);
