@@ -6,6 +6,6 @@ CUDA kernels for sm_103a behind the C ABI of include/dymgpu.h
 host interface.
 """
 from ._lib import DymError  # noqa: F401
-from .metro import Group, Lattice, Measurement, SweepStats, load_group  # noqa: F401
+from .metro import Group, Lattice, Measurement, SweepStats, checkpoint_info, load_group  # noqa: F401
 
-__all__ = ["DymError", "Group", "Lattice", "Measurement", "SweepStats", "load_group"]
+__all__ = ["DymError", "Group", "Lattice", "Measurement", "SweepStats", "checkpoint_info", "load_group"]

@@ -38,6 +38,12 @@ class ChainParams(C.Structure):
                 ("pool", C.c_int32), ("precision", C.c_int32), ("device", C.c_int32)]
 
 
+class CheckpointInfo(C.Structure):
+    _fields_ = [("D", C.c_int32), ("Nt", C.c_int32), ("Nx", C.c_int32), ("order", C.c_uint32), ("pool", C.c_int32),
+                ("table_hash", C.c_uint64), ("seed", C.c_uint64), ("sweep", C.c_uint32), ("beta0", C.c_double),
+                ("beta1", C.c_double), ("beta2", C.c_double)]
+
+
 class Stats(C.Structure):
     _fields_ = [("hits", C.c_uint64), ("accepts", C.c_uint64), ("rechecks", C.c_uint64),
                 ("max_ds_err", C.c_double), ("sweep", C.c_uint32), ("launches", C.c_uint32),
@@ -123,6 +129,10 @@ PROTOTYPES = {
     "dym_chain_free": (C.c_int, [_P]),
     "dym_chain_set_beta": (C.c_int, [_P, C.c_double, C.c_double, C.c_double]),
     "dym_chain_set_l2_window": (C.c_int, [_P, C.c_int32]),
+    "dym_chain_checkpoint_save": (C.c_int, [_P, C.c_char_p]),
+    "dym_chain_checkpoint_load": (C.c_int, [_P, C.c_char_p]),
+    "dym_checkpoint_read_info": (C.c_int, [C.c_char_p, C.POINTER(CheckpointInfo)]),
+    "dym_group_table_hash": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "dym_sweep": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(Stats)]),
     "dym_measure": (C.c_int, [_P, C.POINTER(MeasOpts), C.POINTER(Obs), _f64p]),
     "dym_measure_noalloc": (C.c_int, [_P, C.POINTER(MeasOpts), C.POINTER(Obs), _f64p]),

@@ -35,7 +35,7 @@ BOUNDS = os.environ.get("DYM_BOUNDS_CHECK") == "1"
 if BOUNDS:
     OBJDIR = os.path.join(PKG, "_build_bounds")
 CU_SOURCES = ["sweep.cu", "measure.cu", "capi.cu", "probe.cu", "llr.cu", "batch.cu", "serve.cu", "noalloc.cu"]
-CXX_SOURCES = ["group.cpp", "schedule.cpp"]
+CXX_SOURCES = ["group.cpp", "schedule.cpp", "checkpoint.cpp"]
 
 
 def _nvcc() -> str:

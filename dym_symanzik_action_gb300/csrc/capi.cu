@@ -668,6 +668,64 @@ int dym_links_set(dym_chain* c, const uint16_t* host_in) {
   return DYM_OK;
 }
 
+static dym_checkpoint_info chain_checkpoint_info(const dym_chain* c) {
+  dym_checkpoint_info h{};
+  h.D = c->p.D;
+  h.Nt = c->p.Nt;
+  h.Nx = c->p.Nx;
+  h.order = c->grp->g->P;
+  h.pool = c->p.pool;
+  h.table_hash = table_hash(*c->grp->g);
+  h.seed = c->p.seed;
+  h.sweep = c->sweep;
+  h.beta0 = c->p.beta0;
+  h.beta1 = c->p.beta1;
+  h.beta2 = c->p.beta2;
+  return h;
+}
+
+int dym_chain_checkpoint_save(dym_chain* c, const char* path) {
+  if (!c || !path) return fail(DYM_EINVAL, "dym_chain_checkpoint_save: null argument");
+  std::vector<uint16_t> links((size_t)c->dev.V * c->p.D);
+  int rc = dym_links_get(c, links.data());
+  if (rc) return rc;
+  return checkpoint_write(path, chain_checkpoint_info(c), links.data());
+}
+
+int dym_chain_checkpoint_load(dym_chain* c, const char* path) {
+  if (!c || !path) return fail(DYM_EINVAL, "dym_chain_checkpoint_load: null argument");
+  dym_checkpoint_info h{};
+  std::vector<uint16_t> links;
+  int rc = checkpoint_read(path, &h, &links);
+  if (rc) return rc;
+  const dym_checkpoint_info me = chain_checkpoint_info(c);
+  if (h.D != me.D || h.Nt != me.Nt || h.Nx != me.Nx)
+    return fail(DYM_EINVAL, "dym_chain_checkpoint_load: the checkpoint is of a " + std::to_string(h.D) + "D " +
+                                std::to_string(h.Nt) + "x" + std::to_string(h.Nx) + " lattice");
+  if (h.order != me.order || h.table_hash != me.table_hash)
+    return fail(DYM_EINVAL, "dym_chain_checkpoint_load: the checkpoint is of another group table");
+  if (h.pool != me.pool) return fail(DYM_EINVAL, "dym_chain_checkpoint_load: the checkpoint uses another proposal pool");
+  rc = dym_links_set(c, links.data());  // ids checked; a refused file leaves the chain as it was
+  if (rc) return rc;
+  c->p.seed = h.seed;
+  c->sweep = h.sweep;
+  c->p.beta0 = h.beta0;
+  c->p.beta1 = h.beta1;
+  c->p.beta2 = h.beta2;
+  return DYM_OK;
+}
+
+int dym_checkpoint_read_info(const char* path, dym_checkpoint_info* out) {
+  if (!path || !out) return fail(DYM_EINVAL, "dym_checkpoint_read_info: null argument");
+  return checkpoint_read(path, out, nullptr);
+}
+
+int dym_group_table_hash(const dym_group* g, uint64_t* out) {
+  if (!g || !out) return fail(DYM_EINVAL, "dym_group_table_hash: null argument");
+  *out = table_hash(*g->g);
+  return DYM_OK;
+}
+
 int dym_chain_get_schedule(const dym_chain* c, uint32_t* V, int32_t* nphase, int32_t* phase_dir,
                            uint32_t* phase_len, uint32_t* sites) {
   if (!c) return fail(DYM_EINVAL, "dym_chain_get_schedule: null chain");

@@ -53,6 +53,12 @@ int group_load(const char* path, Group** out);
 int group_to_device(Group* g);
 void group_free(Group* g);
 
+// Chain checkpoint files (checkpoint.cpp): FNV-1a 64 of the Cayley table, and
+// the file's writer and validating reader (links may be null: header only).
+uint64_t table_hash(const Group& g);
+int checkpoint_write(const char* path, const dym_checkpoint_info& h, const uint16_t* links);
+int checkpoint_read(const char* path, dym_checkpoint_info* h, std::vector<uint16_t>* links);
+
 // --------------------------------------------------------------- schedule --
 // Race-free update order.  A link (x, d) update reads same-direction links at
 // x +- e_a, x +- 2 e_a (a != d), x +- e_d and x +- e_d +- e_a (from the staple

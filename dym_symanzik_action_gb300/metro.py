@@ -74,6 +74,13 @@ class Group:
         """Proposal pool nearest the identity (dym-mod-metro.cpp:239-245)."""
         return self._load_tables()[4]
 
+    @property
+    def table_hash(self) -> int:
+        """FNV-1a 64 of the Cayley table, as checkpoints record it."""
+        h = C.c_uint64()
+        check(lib().dym_group_table_hash(self._h, C.byref(h)))
+        return h.value
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             lib().dym_group_free(self._h)
@@ -88,6 +95,13 @@ class Group:
 
 def load_group(path: str) -> Group:
     return Group(path)
+
+
+def checkpoint_info(path: str) -> dict:
+    """Header of a chain checkpoint file (dym_checkpoint_read_info; host only)."""
+    h = _lib.CheckpointInfo()
+    check(lib().dym_checkpoint_read_info(str(path).encode(), C.byref(h)))
+    return {k: getattr(h, k) for k, _ in h._fields_}
 
 
 @dataclass
@@ -196,6 +210,19 @@ class Lattice:
         """Pin the group's Cayley table in L2 for this chain's kernels (an
         access-policy window on the chain's stream); opt-in, results unchanged."""
         check(lib().dym_chain_set_l2_window(self._h, 1 if on else 0))
+
+    def save_checkpoint(self, path: str) -> None:
+        """Links, seed, sweeps done and couplings to `path`; a chain loaded
+        from it continues bit for bit (dym_chain_checkpoint_save)."""
+        check(lib().dym_chain_checkpoint_save(self._h, str(path).encode()))
+
+    def load_checkpoint(self, path: str) -> None:
+        """Resume from a checkpoint of a chain with the same shape, pool and
+        group table (dym_chain_checkpoint_load)."""
+        check(lib().dym_chain_checkpoint_load(self._h, str(path).encode()))
+        info = checkpoint_info(path)
+        self.seed = info["seed"]
+        self.beta = (info["beta0"], info["beta1"], info["beta2"])
 
     def update(self, nsweeps: int = 1, nhit: int = 20) -> SweepStats:
         """nsweeps calls of the reference's update() (dym-mod-metro.cpp:146-197)."""

@@ -124,6 +124,39 @@ int dym_chain_set_beta(dym_chain* c, double beta0, double beta1, double beta2);
  * host memory.) */
 int dym_chain_set_l2_window(dym_chain* c, int32_t on);
 
+/* Checkpoint / resume (no reference counterpart for dym-mod-metro, which
+ * keeps no state between runs; llr2d.cpp:262-271 saves raw int32 links).  A
+ * checkpoint holds the links and everything else that, with the group table,
+ * fixes the rest of the run: shape, proposal pool, seed, sweeps done and
+ * couplings.  Hits draw from Philox keyed by (seed, sweep, link, hit), so a
+ * chain loaded from a checkpoint continues bit for bit as the chain that
+ * wrote it, in any precision mode.  File layout: csrc/checkpoint.cpp. */
+typedef struct {
+  int32_t D, Nt, Nx;
+  uint32_t order;        /* P of the group whose ids the links hold */
+  int32_t pool;          /* DYM_POOL_* */
+  uint64_t table_hash;   /* FNV-1a 64 of the Cayley table, row-major uint16 little-endian */
+  uint64_t seed;
+  uint32_t sweep;        /* sweeps done: the key component of the next sweep */
+  double beta0, beta1, beta2;
+} dym_checkpoint_info;
+
+/* Write the chain's checkpoint to `path` (through `path`.tmp, renamed over
+ * it, so an interrupted save keeps the previous file).  DYM_EIO on a file
+ * error. */
+int dym_chain_checkpoint_save(dym_chain* c, const char* path);
+/* Load a checkpoint into a chain of the same shape, pool and group table
+ * (else DYM_EINVAL, chain unchanged): links (ids checked on the device as
+ * dym_links_set), seed, sweeps done and couplings.  DYM_EFORMAT for a file
+ * that is not a valid checkpoint (magic, version, size, link checksum),
+ * DYM_EIO when it cannot be read. */
+int dym_chain_checkpoint_load(dym_chain* c, const char* path);
+/* Header of a checkpoint file (validated as by the load; host only, no
+ * device needed). */
+int dym_checkpoint_read_info(const char* path, dym_checkpoint_info* out);
+/* FNV-1a 64 of the group's Cayley table, as stored in checkpoints. */
+int dym_group_table_hash(const dym_group* g, uint64_t* out);
+
 typedef struct {
   uint64_t hits;        /* Metropolis hits (reference `hit`) */
   uint64_t accepts;     /* accepted hits (reference `acc`) */

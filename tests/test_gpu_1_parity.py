@@ -234,3 +234,52 @@ def test_l2_window_leaves_configurations_unchanged(engine, precision):
     again.set_l2_window(False)
     again.close()
     plain.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_checkpoint_resume_is_bit_exact(engine, tmp_path, precision):
+    """A chain saved after 3 sweeps and loaded into a fresh chain (created
+    with another seed, couplings, start and precision mode) continues exactly
+    as the chain that ran 6 sweeps without stopping: the checkpoint carries
+    the seed and the sweep counter that key the Philox stream, and the
+    couplings.  Refused loads (another lattice, ids out of range) leave the
+    chain as it was."""
+    from dym_symanzik_action_gb300._lib import DymError
+    from test_checkpoint import write_checkpoint
+    g = group(engine, "S1080")
+    whole = engine.Lattice(g, 4, 4, 8, 0.0, 2.0, -0.1, 21, start="hot", precision=precision)
+    whole.update(3, 10)
+    b = whole.update(3, 10)
+    first = engine.Lattice(g, 4, 4, 8, 0.0, 2.0, -0.1, 21, start="hot", precision=precision)
+    first.update(3, 10)
+    p = tmp_path / "c.ckpt"
+    first.save_checkpoint(p)
+    saved = first.links.copy()
+    first.close()
+    info = engine.checkpoint_info(p)
+    assert (info["sweep"], info["seed"], info["beta1"], info["beta2"]) == (3, 21, 2.0, -0.1)
+    assert info["table_hash"] == g.table_hash
+    other = "shared" if precision == "fp64" else "fp64"
+    resumed = engine.Lattice(g, 4, 4, 8, 1.0, 0.5, 0.0, 999, start="cold", precision=other)
+    resumed.load_checkpoint(p)
+    assert (resumed.links == saved).all() and resumed.seed == 21 and resumed.beta == (0.0, 2.0, -0.1)
+    r = resumed.update(3, 10)
+    assert (resumed.links == whole.links).all()
+    assert (r.hits, r.accepts, r.sweep) == (b.hits, b.accepts, b.sweep) == (b.hits, b.accepts, 6)
+
+    before = resumed.links.copy()
+    small = engine.Lattice(g, 4, 4, 6, 0.0, 2.0, -0.1, 21, start="hot")
+    with pytest.raises(DymError) as e:
+        small.load_checkpoint(p)
+    assert e.value.code == -1
+    small.close()
+    bad = saved.ravel().copy()
+    bad[1234] = g.P
+    q = tmp_path / "bad.ckpt"
+    write_checkpoint(q, 4, 4, 8, g.P, 0, g.table_hash, 5, 77, (0.0, 1.0, 0.0), bad)
+    with pytest.raises(DymError, match="at 1234$"):
+        resumed.load_checkpoint(q)
+    assert (resumed.links == before).all()
+    assert resumed.update(1, 10).sweep == 7  # counter untouched by the refused load
+    resumed.close()
+    whole.close()
