@@ -12,6 +12,9 @@
 //   DYM_WLOOP_MAX=KxL         Wilson grid 1..K by 1..L (default the full Nx x Nt grid)
 //   DYM_DEVICE=n              CUDA device
 //   DYM_PERF=1                add PERF lines (link-hits/s and sweeps/s per block)
+//   DYM_CHECKPOINT=path       resume from `path` when it exists (links, seed, sweeps done;
+//                             the command line's couplings then apply, so a checkpoint of
+//                             a neighbouring beta is a warm start) and write it at the end
 // There is no CPU fallback: without a working GPU the program exits non-zero.
 #include <stdio.h>
 #include <stdlib.h>
@@ -126,6 +129,17 @@ int main(int argc, char* argv[]) {
   printf("Initializing nearest neighbours [%d:%d]... \n", Nt, Nx);
   dym_chain* c = nullptr;
   if (dym_chain_create(g, &p, &c) != DYM_OK) return die("cannot create chain");
+  const char* ckpt = getenv("DYM_CHECKPOINT");
+  if (ckpt && *ckpt) {
+    dym_checkpoint_info ci;
+    if (FILE* f = fopen(ckpt, "rb")) {
+      fclose(f);
+      if (dym_checkpoint_read_info(ckpt, &ci) != DYM_OK || dym_chain_checkpoint_load(c, ckpt) != DYM_OK ||
+          dym_chain_set_beta(c, beta0, beta1, beta2) != DYM_OK)
+        return die("cannot resume from DYM_CHECKPOINT");
+      fprintf(stderr, "dym-mod-metro: resumed from %s after %u sweeps\n", ckpt, ci.sweep);
+    }
+  }
   printf("init done\n");
   fflush(stdout);
 
@@ -167,6 +181,7 @@ int main(int argc, char* argv[]) {
     printf("ACC: %f\n", ((double)acc) / hit);
     tm.stop();
   }
+  if (ckpt && *ckpt && dym_chain_checkpoint_save(c, ckpt) != DYM_OK) return die("cannot write DYM_CHECKPOINT");
   dym_chain_free(c);
   dym_group_free(g);
   return 0;

@@ -87,3 +87,32 @@ def test_cli_cold_start_and_wilson_restriction(engine):
     gm = [l for l in r.stdout.splitlines() if l.startswith("GMES:")]
     assert "START: cold" in r.stdout and "RUN(K,N,Ntherm,NHIT): 1 2 0 10" in r.stdout
     assert len(gm) == 2 and len(gm[0].split()) == 1 + 4 + 4
+
+
+def test_cli_checkpoint_resume(engine, tmp_path):
+    """DYM_CHECKPOINT: a run of 2 measurement blocks, resumed for 2 more (no
+    thermalisation), prints the GMES and RMES lines of one run of 4 blocks.
+    ACC is each run's own running ratio, as in the reference."""
+    from dym_symanzik_action_gb300.build import CLI
+    path = tables.ensure_table("S1080")
+    args = [CLI, path, "4", "4", "4", "0", "1.5", "0.1", "7", "2"]
+
+    def run(extra, env=None):
+        r = subprocess.run(args + extra, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=120,
+                           env=env)
+        assert r.returncode == 0, r.stderr
+        return r
+
+    def tagged(r, tag):
+        return [l for l in r.stdout.splitlines() if l.startswith(tag)]
+
+    straight = run(["4", "3"])
+    ck = tmp_path / "chain.ckpt"
+    env = dict(os.environ, DYM_CHECKPOINT=str(ck))
+    first = run(["2", "3"], env)
+    assert ck.exists() and "resumed" not in first.stderr
+    second = run(["2", "0"], env)
+    assert "resumed from" in second.stderr and "after 7 sweeps" in second.stderr
+    for tag in ("GMES:", "RMES:"):
+        assert tagged(first, tag) + tagged(second, tag) == tagged(straight, tag)
+    assert engine.checkpoint_info(ck)["sweep"] == 11
