@@ -513,6 +513,7 @@ int dym_chain_set_beta(dym_chain* c, double beta0, double beta1, double beta2) {
 }
 
 int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
+  NvtxRange nvtx("dym_sweep");
   if (!c) return fail(DYM_EINVAL, "dym_sweep: null chain");
   if (nsweeps < 0 || nhit < 0 || nhit > (1 << 20)) return fail(DYM_EINVAL, "dym_sweep: bad nsweeps or nhit");
   DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
@@ -570,6 +571,7 @@ int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
 }
 
 int dym_measure(dym_chain* c, const dym_meas_opts* opts, dym_obs* out, double* wloop) {
+  NvtxRange nvtx("dym_measure");
   if (!c || !out) return fail(DYM_EINVAL, "dym_measure: null argument");
   DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
   const Group& g = *c->grp->g;
@@ -1044,6 +1046,7 @@ int dym_batch_get_tuning(const dym_batch* b, dym_batch_tuning* t) {
 }
 
 int dym_batch_sweep(dym_batch* b, int32_t nsweeps, int32_t nhit, dym_stats* total) {
+  NvtxRange nvtx("dym_batch_sweep");
   if (!b) return fail(DYM_EINVAL, "dym_batch_sweep: null batch");
   if (nsweeps < 0 || nhit < 0 || nhit > (1 << 20)) return fail(DYM_EINVAL, "dym_batch_sweep: bad nsweeps or nhit");
   DYM_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
@@ -1129,6 +1132,7 @@ int dym_batch_chain_counters(const dym_batch* b, int32_t idx, uint64_t* hits, ui
 }
 
 int dym_batch_autotune(dym_batch* b, int32_t nhit, int32_t nsweeps_per_trial, dym_batch_tuning* best) {
+  NvtxRange nvtx("dym_batch_autotune");
   if (!b || nsweeps_per_trial < 1) return fail(DYM_EINVAL, "dym_batch_autotune: bad argument");
   if (b->chains.empty()) return fail(DYM_EINVAL, "empty batch");
   DYM_CUDA(cudaSetDevice(b->device), "cudaSetDevice");

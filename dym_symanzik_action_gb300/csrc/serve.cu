@@ -394,6 +394,7 @@ int llr_run_state(dym_chain* c, LlrState* st, int nhit, long max_sweeps) {
 extern "C" {
 
 int dym_llr_run(dym_chain* c, const dym_llr_req* req, dym_llr_result* out, double* a_hist) {
+  NvtxRange nvtx("dym_llr_run");
   if (!c || !req || !out) return fail(DYM_EINVAL, "dym_llr_run: null argument");
   int rc = check_llr_req(c, req);
   if (rc) return rc;
@@ -418,6 +419,7 @@ int dym_llr_run(dym_chain* c, const dym_llr_req* req, dym_llr_result* out, doubl
 }
 
 int dym_llr2d_run(dym_chain* c, const dym_llr2d_req* req, dym_llr2d_result* out, double* a_hist) {
+  NvtxRange nvtx("dym_llr2d_run");
   if (!c || !req || !out) return fail(DYM_EINVAL, "dym_llr2d_run: null argument");
   dym_llr_req q{};
   q.axis = 1;
@@ -638,6 +640,7 @@ int dym_server_submit(dym_server* s, const dym_llr_request* r) {
 }
 
 int dym_server_step(dym_server* s, int32_t nsweeps) {
+  NvtxRange nvtx("dym_server_step");
   if (!s || nsweeps < 0) return fail(DYM_EINVAL, "dym_server_step: bad argument");
   DYM_CUDA(cudaSetDevice(s->p.device), "cudaSetDevice");
   int rc = server_admit(s);

@@ -1,6 +1,7 @@
 // Internal helpers shared by the host translation units.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -10,6 +11,15 @@
 #include "engine.h"
 
 namespace dym {
+
+// NVTX range over an entry point, for timeline profilers (header-only NVTX 3:
+// a no-op unless a tool injects itself).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 inline int cuda_fail(cudaError_t e, const char* what) {
   return fail(DYM_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
