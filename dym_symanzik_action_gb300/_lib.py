@@ -108,7 +108,7 @@ class LlrResponse(C.Structure):
                 ("hits", C.c_uint64), ("accepts", C.c_uint64), ("a_hist", C.c_double * SERVE_MAX_NRM)]
 
 
-LLR_STATUS = {0: "drive", 1: "settle", 2: "rm", 3: "done", 4: "unreached"}
+LLR_STATUS = {0: "drive", 1: "settle", 2: "rm", 3: "done", 4: "unreached", 5: "cancelled", 6: "rejected"}
 
 _P = C.c_void_p
 _u16p = C.POINTER(C.c_uint16)
@@ -153,6 +153,7 @@ PROTOTYPES = {
     "dym_batch_free": (C.c_int, [_P]),
     "dym_server_create": (C.c_int, [_P, C.POINTER(ServerParams), C.POINTER(_P)]),
     "dym_server_submit": (C.c_int, [_P, C.POINTER(LlrRequest)]),
+    "dym_server_cancel": (C.c_int, [_P, C.c_uint64]),
     "dym_server_step": (C.c_int, [_P, C.c_int32]),
     "dym_server_poll": (C.c_int, [_P, C.POINTER(LlrResponse), C.c_int32, _i32p]),
     "dym_server_status": (C.c_int, [_P, _i32p, _i32p, _u64p, _u64p]),

@@ -496,6 +496,47 @@ uint64_t chain_bytes(int D, int Nt, int Nx, uint32_t P) {
          sizeof(LlrState) + 2 * 3ull * P * 8;
 }
 
+dym_llr_response rejected(const dym_llr_request& r) {
+  dym_llr_response resp{};
+  resp.id = r.id;
+  resp.status = DYM_LLR_REJECTED;
+  resp.NRM = r.NRM;
+  return resp;
+}
+
+// Response of resident chain i from its device state, with `status` (its own
+// mode when finished, DYM_LLR_CANCELLED when withdrawn); the chain goes to the
+// spare pool and its budget is returned.  The caller rebuilds the work list.
+int retire_one(dym_server* s, size_t i, int status) {
+  dym_server::Active& a = s->active[i];
+  LlrState st;
+  DYM_CUDA(copy_sync(&st, a.chain->d_llr, sizeof(LlrState), cudaMemcpyDeviceToHost, s->work.stream), "read llr state");
+  dym_llr_response resp{};
+  resp.id = a.req.id;
+  resp.a = st.a;
+  resp.S1 = st.E[0];
+  resp.S2 = st.E[1];
+  resp.status = status;
+  resp.sweeps = st.sweeps;
+  resp.drive_sweeps = st.drive_sweeps;
+  resp.NRM = a.req.NRM;
+  resp.hits = st.hits;
+  resp.accepts = st.accepts;
+  for (int m = 0; m < a.req.NRM && m < DYM_SERVE_MAX_NRM; ++m) resp.a_hist[m] = st.a_hist[m];
+  s->done.push_back(resp);
+  s->link_hits += st.hits;
+  s->hbm_used -= a.bytes;
+  s->links_used -= a.links;
+  s->spare[std::make_tuple(a.req.D, a.req.Nt, a.req.Nx)].push_back(a.chain);
+  return DYM_OK;
+}
+
+void rebuild_work(dym_server* s) {
+  s->work.chains.clear();
+  for (auto& a : s->active) s->work.chains.push_back(a.chain);
+  s->work.dirty = true;
+}
+
 int server_admit(dym_server* s) {
   const Group& g = *s->grp->g;
   while (!s->queue.empty() && (int)s->active.size() < s->p.max_chains) {
@@ -513,7 +554,10 @@ int server_admit(dym_server* s) {
       c = it->second.back();
       it->second.pop_back();
       int rc = chain_reset(c, r.seed, r.start);
-      if (rc) return rc;
+      if (rc) {
+        dym_chain_free(c);
+        return rc;
+      }
     } else {
       dym_chain_params cp{};
       cp.D = r.D;
@@ -525,7 +569,16 @@ int server_admit(dym_server* s) {
       cp.precision = DYM_PREC_FP64;
       cp.device = s->p.device;
       int rc = dym_chain_create(s->grp, &cp, &c);
-      if (rc) return rc;
+      if (rc && !s->active.empty()) {
+        // Device memory may free up as resident chains retire: keep the
+        // request at the head of the queue and admit nothing more this step.
+        s->queue.push_front(r);
+        break;
+      }
+      if (rc) {
+        s->done.push_back(rejected(r));
+        continue;
+      }
     }
     dym_llr_req q{};
     q.axis = r.axis;
@@ -540,9 +593,10 @@ int server_admit(dym_server* s) {
     LlrState st;
     int rc = check_llr_req(c, &q);
     if (!rc) rc = llr_init_state(c, &q, &st);
-    if (rc) {
+    if (rc) {  // an invalid window or parameter set: answered, not fatal to the others
       dym_chain_free(c);
-      return rc;
+      s->done.push_back(rejected(r));
+      continue;
     }
     s->active.push_back(dym_server::Active{r, c, bytes, links});
     s->hbm_used += bytes;
@@ -570,32 +624,13 @@ int server_retire(dym_server* s) {
       keep.push_back(a);
       continue;
     }
-    LlrState st;
-    DYM_CUDA(copy_sync(&st, a.chain->d_llr, sizeof(LlrState), cudaMemcpyDeviceToHost, s->work.stream), "read llr state");
-    dym_llr_response resp{};
-    resp.id = a.req.id;
-    resp.a = st.a;
-    resp.S1 = st.E[0];
-    resp.S2 = st.E[1];
-    resp.status = st.mode;
-    resp.sweeps = st.sweeps;
-    resp.drive_sweeps = st.drive_sweeps;
-    resp.NRM = a.req.NRM;
-    resp.hits = st.hits;
-    resp.accepts = st.accepts;
-    for (int m = 0; m < a.req.NRM && m < DYM_SERVE_MAX_NRM; ++m) resp.a_hist[m] = st.a_hist[m];
-    s->done.push_back(resp);
-    s->link_hits += st.hits;
-    s->hbm_used -= a.bytes;
-    s->links_used -= a.links;
-    s->spare[std::make_tuple(a.req.D, a.req.Nt, a.req.Nx)].push_back(a.chain);
+    int rc = retire_one(s, i, s->h_modes[i]);
+    if (rc) return rc;
     changed = true;
   }
   if (changed) {
     s->active.swap(keep);
-    s->work.chains.clear();
-    for (auto& a : s->active) s->work.chains.push_back(a.chain);
-    s->work.dirty = true;
+    rebuild_work(s);
   }
   return DYM_OK;
 }
@@ -634,9 +669,36 @@ int dym_server_submit(dym_server* s, const dym_llr_request* r) {
   if (r->NRM < 0 || r->NRM > DYM_SERVE_MAX_NRM) return fail(DYM_EINVAL, "request NRM out of range");
   if (r->D != 4 || r->Nt < 1 || r->Nx < 1) return fail(DYM_EINVAL, "bad lattice shape (LLR runs on D = 4)");
   if (!s->active.empty() && r->D != s->work.D) return fail(DYM_ENOTSUP, "all requests of a server share D");
+  const uint64_t bytes = chain_bytes(r->D, r->Nt, r->Nx, s->grp->g->P);
+  if (bytes > s->p.hbm_budget)
+    return fail(DYM_ERANGE, "dym_server_submit: the request's chain needs " + std::to_string(bytes) +
+                                " bytes, more than the server's budget of " + std::to_string(s->p.hbm_budget));
   if (s->work.D == 0) s->work.D = r->D;
   s->queue.push_back(*r);
   return DYM_OK;
+}
+
+int dym_server_cancel(dym_server* s, uint64_t id) {
+  if (!s) return fail(DYM_EINVAL, "dym_server_cancel: null server");
+  for (auto q = s->queue.begin(); q != s->queue.end(); ++q)
+    if (q->id == id) {
+      dym_llr_response resp = rejected(*q);
+      resp.status = DYM_LLR_CANCELLED;
+      s->done.push_back(resp);
+      s->queue.erase(q);
+      return DYM_OK;
+    }
+  for (size_t i = 0; i < s->active.size(); ++i)
+    if (s->active[i].req.id == id) {
+      DYM_CUDA(cudaSetDevice(s->p.device), "cudaSetDevice");
+      DYM_CUDA(cudaStreamSynchronize(s->work.stream), "cudaStreamSynchronize");
+      int rc = retire_one(s, i, DYM_LLR_CANCELLED);
+      if (rc) return rc;
+      s->active.erase(s->active.begin() + (std::ptrdiff_t)i);
+      rebuild_work(s);
+      return DYM_OK;
+    }
+  return fail(DYM_EINVAL, "dym_server_cancel: no queued or resident request " + std::to_string(id));
 }
 
 int dym_server_step(dym_server* s, int32_t nsweeps) {

@@ -47,6 +47,11 @@ class Server:
                             ewin=ewin, hw=hw, a0=a0, K=K, NRM=NRM, drive_cap=drive_cap)
         check(lib().dym_server_submit(self._h, C.byref(r)))
 
+    def cancel(self, rid: int) -> None:
+        """Withdraw a queued or resident request; its "cancelled" response is
+        returned by the next poll."""
+        check(lib().dym_server_cancel(self._h, rid))
+
     def step(self, nsweeps: int = 1) -> None:
         check(lib().dym_server_step(self._h, nsweeps))
 

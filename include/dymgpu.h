@@ -291,6 +291,9 @@ int dym_batch_free(dym_batch* b);
 #define DYM_LLR_RM 2         /* Robbins-Monro iterations */
 #define DYM_LLR_DONE 3       /* all NRM iterations done */
 #define DYM_LLR_UNREACHED 4  /* drive-in cap reached outside the window */
+#define DYM_LLR_CANCELLED 5  /* server only: withdrawn by dym_server_cancel */
+#define DYM_LLR_REJECTED 6   /* server only: the request's window or parameters are invalid, or its
+                                chain could not be created with no other chain resident */
 
 typedef struct {
   int32_t axis;      /* 1: window on S1 (plaquettes), background bg on S2; 2: the reverse (llr.cpp:42-43, 286) */
@@ -397,14 +400,22 @@ typedef struct {
 typedef struct {
   uint64_t id;
   double a, S1, S2;
-  int32_t status;       /* DYM_LLR_DONE or DYM_LLR_UNREACHED */
+  int32_t status;       /* DYM_LLR_DONE, DYM_LLR_UNREACHED, DYM_LLR_CANCELLED or DYM_LLR_REJECTED */
   int32_t sweeps, drive_sweeps, NRM;
   uint64_t hits, accepts;
   double a_hist[DYM_SERVE_MAX_NRM];
 } dym_llr_response;
 
 int dym_server_create(const dym_group* g, const dym_server_params* p, dym_server** out);
+/* Queue a request.  DYM_ERANGE when its chain alone needs more device memory
+ * than the server's budget; DYM_EINVAL for a malformed shape or NRM.  Every
+ * accepted request gets exactly one response. */
 int dym_server_submit(dym_server* s, const dym_llr_request* r);
+/* Withdraw a queued or resident request: its response (status
+ * DYM_LLR_CANCELLED, with the state reached so far for a resident one) is
+ * queued for dym_server_poll at once and its chain and budget are freed.
+ * DYM_EINVAL when no queued or resident request has this id. */
+int dym_server_cancel(dym_server* s, uint64_t id);
 int dym_server_step(dym_server* s, int32_t nsweeps);
 /* Up to `max` finished responses (in completion order); *n receives the count. */
 int dym_server_poll(dym_server* s, dym_llr_response* out, int32_t max, int32_t* n);

@@ -54,3 +54,64 @@ def test_served_results_equal_alone(engine):
             a = alone[rid]
             assert r.status == a.status and r.sweeps == a.sweeps and r.hits == a.hits
             assert (r.a_hist == a.a_hist).all() and r.S1 == a.S1 and r.S2 == a.S2
+
+
+def test_server_cancel_reject_and_budget(engine):
+    """Every accepted request gets exactly one response.  A request whose
+    chain alone exceeds the device-memory budget is refused at submit
+    (DYM_ERANGE); a request with an invalid window is answered "rejected"
+    without failing the step or the other requests; a queued or a resident
+    request can be withdrawn ("cancelled", the resident one with the sweeps it
+    ran), freeing its slot; the rest finish as they would alone."""
+    from dym_symanzik_action_gb300._lib import DymError
+    g = engine.load_group(tables.ensure_table("S1080"))
+    s = Server(g, max_chains=2, hbm_budget=64 << 20, nhit=NHIT)
+    with pytest.raises(DymError) as e:
+        s.submit(99, 16, 48, *window(16, 48, -1.0), a0=2.0, seed=1, K=K, NRM=NRM, drive_cap=CAP)  # ~100 MB
+    assert e.value.code == -8
+    for rid, Nt, Nx, cen, start, bg in REQS[:4]:
+        ewin, hw = window(Nt, Nx, cen)
+        s.submit(rid, Nt, Nx, ewin, hw if rid != 1 else 0.0, a0=2.0, seed=1000 + rid, start=start, bg=bg, K=K,
+                 NRM=NRM, drive_cap=CAP)
+    s.cancel(3)  # still queued
+    got = {r.id: r for r in s.poll()}
+    assert set(got) == {3} and got[3].status == "cancelled" and got[3].hits == 0
+    s.step(2)  # admits 0 and 2 (1 is rejected on admission)
+    got = {r.id: r for r in s.poll()}
+    assert set(got) == {1} and got[1].status == "rejected"
+    assert s.status()["active"] == 2
+    s.cancel(2)  # resident
+    got = {r.id: r for r in s.poll()}
+    assert set(got) == {2} and got[2].status == "cancelled" and got[2].hits > 0
+    st = s.status()
+    assert st["active"] == 1 and st["queued"] == 0
+    with pytest.raises(DymError) as e:
+        s.cancel(2)
+    assert e.value.code == -1
+    for _ in range(10000):
+        s.step(2)
+        got.update({r.id: r for r in s.poll()})
+        if 0 in got:
+            break
+    assert got[0].status in ("done", "unreached")
+    alone, _ = run_server_subset(engine, [REQS[0]])
+    assert got[0].a == alone[0].a and got[0].hits == alone[0].hits and (got[0].a_hist == alone[0].a_hist).all()
+    assert s.status()["active"] == 0
+    s.close()
+
+
+def run_server_subset(engine, reqs):
+    g = engine.load_group(tables.ensure_table("S1080"))
+    s = Server(g, max_chains=1, nhit=NHIT)
+    for rid, Nt, Nx, cen, start, bg in reqs:
+        ewin, hw = window(Nt, Nx, cen)
+        s.submit(rid, Nt, Nx, ewin, hw, a0=2.0, seed=1000 + rid, start=start, bg=bg, K=K, NRM=NRM, drive_cap=CAP)
+    out = {}
+    for _ in range(10000):
+        s.step(2)
+        out.update({r.id: r for r in s.poll()})
+        if len(out) == len(reqs):
+            break
+    st = s.status()
+    s.close()
+    return out, st
