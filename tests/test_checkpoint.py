@@ -82,3 +82,33 @@ def test_malformed_checkpoints_are_refused(engine, bt, tmp_path, case):
     with pytest.raises(DymError) as e:
         engine.checkpoint_info(p)
     assert e.value.code == (-2 if case == "missing" else -3), str(e.value)
+
+
+def test_mutated_checkpoints_never_crash_the_reader(engine, bt, tmp_path):
+    """Random truncations and byte flips of a valid file either still parse
+    (a flip in the seed, couplings or sweep count changes only those fields)
+    or are refused with DYM_EFORMAT; the reader never crashes or reads past
+    the file."""
+    from dym_symanzik_action_gb300._lib import DymError
+    D, Nt, Nx = 4, 2, 2
+    n = D * Nt * Nx ** (D - 1)
+    good = tmp_path / "good"
+    write_checkpoint(good, D, Nt, Nx, bt.P, 0, bt.table_hash, 9, 1, (0.0, 1.0, 0.0), np.arange(n) % bt.P)
+    raw = good.read_bytes()
+    rng = np.random.default_rng(17)
+    p = tmp_path / "m"
+    refused = 0
+    for k in range(300):
+        b = bytearray(raw)
+        if k % 3 == 0:
+            b = b[: int(rng.integers(0, len(raw)))]
+        else:
+            for _ in range(int(rng.integers(1, 4))):
+                b[int(rng.integers(0, len(b)))] ^= int(rng.integers(1, 256))
+        p.write_bytes(bytes(b))
+        try:
+            engine.checkpoint_info(p)
+        except DymError as e:
+            assert e.code == -3, str(e)
+            refused += 1
+    assert refused >= 100
