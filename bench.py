@@ -16,8 +16,11 @@ every step starts with the lattice and table out of L2.  `e2e` times the same
 sweep through the C ABI with the configuration copied in from and out to
 pinned host memory every step.
 
---impl reference times the reference algorithm on the host cores (the oracle
-port, all threads) on the same workload; one step is one sweep.
+--impl reference times the unmodified reference executable (dym-mod-metro
+built from the staged sources with its Makefile's flags and NHIT 10, all host
+cores) on the same workload and its own mys1080-v4 table: W untimed sweeps
+(its Ntherm), then the K steps as one block timed by its TM_END update line.
+The engine is not loaded on that arm.
 Under torchrun (N > 1) every rank runs its own replica of the chain
 (replicas only: a single chain is not sharded); value = total link-hits / the
 slowest rank's time.
@@ -155,15 +158,54 @@ def dist_env():
     return world, rank, local
 
 
-def cpu_oracle_run(nsweeps: int, nthreads: int):
-    """Reference algorithm on the host (oracle port): returns (link-hits, seconds)."""
-    from dym_symanzik_action_gb300 import tables
-    from dym_symanzik_action_gb300.schedule import schedule
-    from oracle.oracle import OracleGroup, OracleLattice
+def reference_table_path():
+    """The reference's own S(1080) table file (mys1080-v4) from the staged
+    reference (baseline/_ref, or $REF_DIR), or None."""
+    from oracle.oracle import ref_dir
+    r = ref_dir()
+    return os.path.join(r, "groups", "mys1080-v4") if r else None
+
+
+def ensure_reference_build():
+    """The unmodified reference executables in oracle/_ref/, built for this
+    machine from the staged sources by oracle/build_ref.sh if missing."""
+    from oracle import oracle
+    exe = os.path.join(oracle.REF_BIN, "dym-mod-metro-nhit10")
+    if not os.path.exists(exe):
+        ref = oracle.ref_dir()
+        if ref is None:
+            raise FileNotFoundError("reference sources not staged (oracle/stage_ref.sh) and REF_DIR unset")
+        subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True,
+                       env=dict(os.environ, REF_DIR=ref), stdout=subprocess.DEVNULL)
+    return exe
+
+
+def reference_binary_run(nsweeps: int, ntherm: int, threads: int):
+    """The unmodified reference (dym-mod-metro.cpp built with its Makefile's
+    flags, NHIT 10) on the workload: cold 32^3 x 8 chain on its own
+    mys1080-v4, beta = (0, 3.0, -0.15), Ntherm untimed sweeps, then one block
+    of nsweeps sweeps timed by its own timer (TM_END update,
+    dym-mod-metro.cpp:273-278), then its one measurement (untimed).  Returns
+    (link-hits, seconds)."""
+    from oracle.oracle import run_reference_metro
     w = WORKLOAD
-    og = OracleGroup(tables.ensure_table(w["group"]))
-    L = OracleLattice(og, w["D"], w["Nt"], w["Nx"])
-    sched = schedule(w["D"], w["Nt"], w["Nx"])
+    _, blocks = run_reference_metro(reference_table_path(), w["D"], w["Nt"], w["Nx"], w["beta"], w["seed"],
+                                    K=nsweeps, N=1, Ntherm=ntherm, start=w["start"], nhit10=True, threads=threads)
+    if len(blocks) != 1:
+        raise RuntimeError(f"reference printed {len(blocks)} TM_END update lines, expected 1")
+    V = w["Nt"] * w["Nx"] ** (w["D"] - 1)
+    return V * w["D"] * w["nhit"] * nsweeps, blocks[0]
+
+
+def cpu_oracle_run(nsweeps: int, nthreads: int):
+    """The oracle port of the reference algorithm on the same workload and the
+    reference's own table file, colour phases from oracle.colour_schedule
+    (the engine is not loaded): returns (link-hits, seconds)."""
+    from oracle.oracle import OracleGroup, OracleLattice, colour_schedule
+    w = WORKLOAD
+    og = OracleGroup(reference_table_path())
+    L = OracleLattice(og, w["D"], w["Nt"], w["Nx"])  # cold start: every link the identity
+    sched = colour_schedule(w["D"], w["Nt"], w["Nx"])
     L.sweep(sched, w["beta"], w["seed"], 0, 1, w["nhit"], nthreads=nthreads)  # warm-up sweep
     t0 = time.perf_counter()
     L.sweep(sched, w["beta"], w["seed"], 1, nsweeps, w["nhit"], nthreads=nthreads)
@@ -172,36 +214,74 @@ def cpu_oracle_run(nsweeps: int, nthreads: int):
 
 
 def cpu_baseline(budget_s: float = 15.0):
+    """The reference's own OpenMP build timed on this host's cores (all of
+    them), with the oracle port beside it as a second, labelled figure."""
     from oracle import oracle
     oracle.build()
     n = os.cpu_count() or 1
-    hits1, dt1 = cpu_oracle_run(1, n)
-    ns = max(1, min(200, int(budget_s / max(dt1, 1e-3))))
-    hits, dt = cpu_oracle_run(ns, n)
-    return {"value": hits / dt, "unit": "link-hits/s", "cores": n, "kind": "port",
-            "sample": f"{ns} sweeps of the 32^3x8 cold chain ({hits:.3e} link-hits, {dt:.1f} s) with the oracle "
-                      f"port of the reference algorithm (reference data layout, OpenMP, {n} threads)"}
+    out = {}
+    try:
+        ensure_reference_build()
+        hits1, dt1 = reference_binary_run(2, 0, n)
+        ns = max(2, min(200, int(budget_s / max(dt1 / 2, 1e-3))))
+        hits, dt = reference_binary_run(ns, 1, n)
+        out = {"value": hits / dt, "unit": "link-hits/s", "cores": n, "kind": "reference",
+               "sample": f"unmodified reference dym-mod-metro (its Makefile flags, NHIT 10, OMP_NUM_THREADS={n}) "
+                         f"on its own mys1080-v4: 1 untimed sweep, then {ns} sweeps of the cold 32^3x8 chain timed "
+                         f"by its TM_END update line ({hits:.3e} link-hits, {dt:.2f} s)"}
+    except Exception as e:  # reported, not hidden: the line then carries the port only
+        out = {"reference_error": f"{type(e).__name__}: {e}"[:300]}
+    try:
+        h1, d1 = cpu_oracle_run(1, n)
+        nsp = max(1, min(200, int(budget_s / max(d1, 1e-3))))
+        hp, dp = cpu_oracle_run(nsp, n)
+        port = {"value": hp / dp, "unit": "link-hits/s", "cores": n, "kind": "port",
+                "sample": f"{nsp} sweeps of the same chain by the oracle restatement of the reference algorithm "
+                          f"(reference data layout, OpenMP over a colour phase, {n} threads)"}
+    except Exception as e:
+        port = {"error": f"{type(e).__name__}: {e}"[:300]}
+    if "value" not in out:
+        out.update({k: port.get(k) for k in ("value", "unit", "cores", "kind", "sample")})
+    out["port"] = port
+    return out
 
 
 def run_reference(args):
+    """--impl reference: the unmodified reference executable on this host's
+    cores (rank 0 only): W untimed sweeps, then the K timed steps as one
+    block of its own update timer."""
     world, rank, _ = dist_env()
     if rank != 0:
         return
-    from oracle import oracle
-    oracle.build()
     n = os.cpu_count() or 1
-    cpu_oracle_run(max(args.warmup, 0), n) if args.warmup else None
-    hits, dt = cpu_oracle_run(args.steps, n)
+    try:
+        from oracle import oracle
+        oracle.build()
+        ensure_reference_build()
+        hits, dt = reference_binary_run(args.steps, args.warmup, n)
+    except Exception as e:
+        print(json.dumps({"impl": "reference", "unavailable": f"{type(e).__name__}: {e}"[:300]}), flush=True)
+        return
     v = hits / dt
     line = {"impl": "reference", "metric": "link-hits/s", "value": v, "unit": "link-hits/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": WORKLOAD_NAME, "l2": "n/a (CPU)"},
-            "cpu_baseline": {"value": v, "unit": "link-hits/s", "cores": n, "kind": "port",
-                             "sample": f"{args.steps} sweeps of the full workload, oracle port of the reference "
-                                       f"algorithm, OpenMP {n} threads"},
+            "data": "synthetic", "config": bench_config(args.gpus),
+            "cpu_baseline": {"value": v, "unit": "link-hits/s", "cores": n, "kind": "reference",
+                             "sample": f"unmodified reference dym-mod-metro (Makefile flags, NHIT 10, "
+                                       f"OMP_NUM_THREADS={n}) on its own mys1080-v4: {args.warmup} untimed sweeps "
+                                       f"(its Ntherm), then {args.steps} sweeps timed by its TM_END update line"},
             "e2e": {"value": v, "unit": "link-hits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def bench_config(world: int) -> dict:
+    """The workload keys shared by both arms' lines."""
+    w = WORKLOAD
+    V = w["Nt"] * w["Nx"] ** (w["D"] - 1)
+    return {"workload": WORKLOAD_NAME, "links": V * w["D"], "nhit": w["nhit"], "sweeps_per_step": 1,
+            "l2": "GPU arm: a 256 MB buffer written between steps (L2 flushed); CPU arm: the reference's own "
+                  "update timer", "parallelism": f"replicas x{world}"}
 
 
 def ensemble_bench(dym, device: int, sweeps: int = 5, nhit: int = 10) -> dict:
@@ -453,9 +533,9 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": PRECISION_DTYPE[args.precision],
             "data": "synthetic",
-            "config": {"workload": WORKLOAD_NAME, "links": links_per_sweep, "nhit": w["nhit"],
-                       "colour_phases": nphase, "precision": PRECISION_TEXT[args.precision], "kernel": kname,
-                       "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
+            "config": bench_config(world),
+            "method": {"colour_phases": nphase, "precision": PRECISION_TEXT[args.precision], "kernel": kname,
+                       "table": "generated S(1080) (trace-isomorphic to the reference's mys1080-v4)"},
             "roofline": {"bound": "issue", "achieved": issue_achieved, "peak": issue_peak, "unit": "warp-inst/s",
                          "frac": issue_achieved / issue_peak if issue_achieved else None, "traffic": traffic,
                          "peak_source": (f"{sms} SMs x {ISSUE_PER_SM_CYCLE} warp instructions per cycle x "

@@ -70,16 +70,22 @@ void group_free(Group* g) {
   delete g;
 }
 
-// Whether the shared sub-table kernel applies: the table is associative,
-// ReTr is one double per conjugacy class (so ReTr[u_j g] == ReTr[bnew s_j]
-// bit for bit), the sub-table fits the shared-memory opt-in, and D = 4.
-// The D = 2 and D = 3 instantiations of the shared-table kernels faulted on
-// the GPU (illegal address / invalid address space) while their source runs
+// Whether the shared-table kernels apply at all: D = 4 and an associative
+// table whose ReTr classes (values equal to 1e-9) are unions of conjugacy
+// classes, so that ReTr[u_j g] and ReTr[bnew s_j] fall in one class.  The
+// D = 2 and D = 3 instantiations of the shared-table kernels faulted on the
+// GPU (illegal address / invalid address space) while their source runs
 // bit-exact under AddressSanitizer in a host emulation; no cause was found,
 // so they are not built and those lattices use the FP64 direct kernel.
+static bool shared_structure_ok(const Group& g, int D) { return D == 4 && g.assoc_ok && g.cls_conj_invariant; }
+
+// The FP64 shared sub-table kernel sums ReTr of the conjugates u_j g_k, which
+// equal the reference's terms bit for bit only when ReTr is one double per
+// class (true of generated tables, not of the reference's shipped files,
+// whose traces carry ~1e-16 of rounding noise); its tables must also fit the
+// shared-memory opt-in.
 static bool sub_eligible(const Group& g, uint32_t npool, int device, int D) {
-  if (D != 4) return false;
-  if (!g.assoc_ok || !g.cls_conj_invariant || !g.cls_exact) return false;
+  if (!shared_structure_ok(g, D) || !g.cls_exact) return false;
   int optin = 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) return false;
   return sub_smem_bytes(g.P, npool) <= (size_t)optin;
@@ -103,8 +109,12 @@ static int build_sub_table(dym_chain* c, const std::vector<uint16_t>& pool) {
 // entries above.
 static size_t mixed_entry_bytes(const Group& g) { return g.P > kMixedMaxP ? 4 : 2; }
 
-static bool mixed_eligible(const Group& g, uint32_t npool, int device) {
-  if (g.ncls > kMixedMaxCls || g.ncls < 1) return false;
+// The mixed kernels take their fast decisions from class values with the
+// class spread inside the error bound and re-evaluate the rest on the
+// reference's own elements (visit.cuh exact_actions), so they need no
+// class-exact table.
+static bool mixed_eligible(const Group& g, uint32_t npool, int device, int D) {
+  if (!shared_structure_ok(g, D) || g.ncls > kMixedMaxCls || g.ncls < 1) return false;
   int optin = 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) return false;
   return mixed_smem_bytes(g.P, npool, mixed_entry_bytes(g)) <= (size_t)optin;
@@ -356,7 +366,7 @@ int dym_group_get_info(const dym_group* gh, dym_group_info* out) {
   out->fast_path = 0;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0)
-    out->fast_path = sub_eligible(g, (uint32_t)g.pool_nearest.size(), dev, 4) ? 1 : 0;
+    out->fast_path = mixed_eligible(g, (uint32_t)g.pool_nearest.size(), dev, 4) ? 1 : 0;
   else
     cudaGetLastError();
   out->class_spread = g.cls_spread;
@@ -438,11 +448,13 @@ int dym_chain_create(const dym_group* gh, const dym_chain_params* p, dym_chain**
   // Pinned words: [0..4] dym_sweep's counters, [5] dym_links_set's check.
   DYM_CUDA(cudaHostAlloc((void**)&c->h_counters, 6 * sizeof(unsigned long long), cudaHostAllocDefault),
            "cudaHostAlloc");
-  if (p->precision != DYM_PREC_FP64 && sub_eligible(g, d.npool, p->device, p->D)) {
-    rc = build_sub_table(c.get(), pool);
-    if (rc) return rc;
-    if (p->precision == DYM_PREC_MIXED && mixed_eligible(g, d.npool, p->device) && p->Nt <= kMixedMaxExtent &&
-        p->Nx <= kMixedMaxExtent) {
+  if (p->precision != DYM_PREC_FP64 && shared_structure_ok(g, p->D)) {
+    if (sub_eligible(g, d.npool, p->device, p->D)) {
+      rc = build_sub_table(c.get(), pool);
+      if (rc) return rc;
+    }
+    if (p->precision == DYM_PREC_MIXED && mixed_eligible(g, d.npool, p->device, p->D) &&
+        p->Nt <= kMixedMaxExtent && p->Nx <= kMixedMaxExtent) {
       rc = build_mixed_tables(c.get(), pool);
       if (rc) return rc;
       int optin = 0;
@@ -836,6 +848,9 @@ static int batch_build(dym_batch* b) {
   size_t off = 0;
   auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
   b->mixed = std::all_of(b->chains.begin(), b->chains.end(), batch_mixed_chain);
+  if (!b->mixed && !std::all_of(b->chains.begin(), b->chains.end(), [](const dym_chain* c) { return c->dev.sub_ok; }))
+    return fail(DYM_ENOTSUP, "a batch with FP64 shared-table chains cannot hold a chain whose table's ReTr is not "
+                             "one double per class (create every chain with the mixed precision)");
   std::vector<int> shift(b->groups.size(), 0);
   for (size_t g = 0; g < b->groups.size(); ++g) {
     const Group& G = *b->groups[g];
@@ -988,7 +1003,7 @@ int dym_batch_add(dym_batch* b, dym_chain* c) {
   if (!b || !c) return fail(DYM_EINVAL, "dym_batch_add: null argument");
   if (c->p.device != b->device) return fail(DYM_EINVAL, "chain and batch are on different devices");
   if (!b->chains.empty() && c->p.D != b->D) return fail(DYM_EINVAL, "all chains of a batch must have the same D");
-  if (!c->dev.sub_ok || c->p.D != 4)
+  if (!(c->dev.sub_ok || batch_mixed_chain(c)) || c->p.D != 4)
     return fail(DYM_ENOTSUP, "batch chains need D = 4 and the shared-table path (nearest pool, mixed)");
   if (std::find(b->chains.begin(), b->chains.end(), c) != b->chains.end())
     return fail(DYM_EINVAL, "chain already in the batch");

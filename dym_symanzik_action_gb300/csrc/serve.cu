@@ -50,8 +50,12 @@ int class_histograms(dym_chain* c, long long h[2][kLlrMaxCls]) {
 }
 
 int check_llr_group(const Group& g) {
-  if (g.ncls > kLlrMaxCls || !g.cls_conj_invariant || !g.cls_exact || !g.assoc_ok)
-    return fail(DYM_ENOTSUP, "LLR needs a group table whose ReTr is one double per class (at most 32 classes)");
+  // The LLR's energies are exact sums of class values (one value per class,
+  // that of its lowest-numbered element), so a table whose ReTr varies inside
+  // a class by rounding noise is taken as its class values.
+  if (g.ncls > kLlrMaxCls || !g.cls_conj_invariant || !g.assoc_ok)
+    return fail(DYM_ENOTSUP, "LLR needs an associative group table whose ReTr classes are conjugation-invariant "
+                             "(at most 32 classes)");
   return DYM_OK;
 }
 

@@ -16,10 +16,15 @@
 //    advances u_j <- u_j * g_k from the same entries.  108 L2 gathers per
 //    link visit remain (staples and u_j).
 //
-//  * k_sweep_mixed  -- k_sweep_sub's decisions with exact integer sums of
+//  * k_sweep_mixed  -- the same decisions with exact integer sums of
 //    fixed-point class values and an FP32 threshold test; FP64 only for the
-//    hits within a proven bound of the threshold (visit_mixed), so the
-//    configurations are the FP64 path's bit for bit.
+//    hits within a proven bound of the threshold (visit_mixed), re-evaluated
+//    on the reference's own elements b s_j, so the configurations are the
+//    FP64 path's bit for bit on any table (also one whose ReTr carries
+//    rounding noise inside a class, as the reference's shipped files do).
+//
+//  * k_sweep_vt     -- k_sweep_mixed with the shared table holding fixed-point
+//    values instead of elements (fastest while accepted moves are rare).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -209,7 +214,7 @@ __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_vt(SweepArgs a, c
       xyz_next = a.xyz[nt];
     }
     vt_prepare<D, DIR>(a, i, xyz, s_inv, s_val, u, b, R, M);
-    vt_hits<D, DIR>(a, i, a.sweep, s_retr, s_vsub, s_pool, u, b, R, M, hits, accs, rechecks, max_err);
+    vt_hits<D, DIR>(a, i, a.sweep, s_retr, s_inv, s_vsub, s_pool, u, b, R, M, hits, accs, rechecks, max_err);
   }
   flush_counters(a.counters, hits, accs, rechecks);
   flush_max_err(a.counters + 3, max_err);

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <string>
 
 #include "dym_core.h"
@@ -51,8 +52,12 @@ inline int fix_shift(const Group& g, int D) { return dym_fix_shift(g.max_abs_ret
 inline double fix_q(const Group& g, int S) { return std::ldexp(1.0, -(S + 1)) + g.cls_spread; }
 
 // dym_mixed_margin for a Metropolis sweep at couplings (b0, b1, b2), rounded up
-// to FP32.
+// to FP32.  With DYM_RECHECK_ALL=1 in the environment (a validation mode, read
+// when a sweep or batch is set up) the bound is infinite, so every hit of the
+// mixed kernels takes the FP64 re-evaluation path.
 inline float mixed_margin(const Group& g, int D, int S, double b0, double b1, double b2) {
+  const char* all = std::getenv("DYM_RECHECK_ALL");
+  if (all && all[0] == '1') return INFINITY;
   const double m = dym_mixed_margin(b0, b1, 2.0 * (D - 1), b2, 6.0 * (D - 1), fix_q(g, S), g.max_abs_retr);
   return std::nextafter((float)m, INFINITY);
 }

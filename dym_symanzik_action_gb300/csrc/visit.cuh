@@ -64,6 +64,40 @@ __device__ __forceinline__ void pdl_launch_dependents() {
 }
 __device__ __forceinline__ void pdl_wait_prior() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
+// The reference's FP64 actions of the current link value b and of a proposal
+// bnew (dym-mod-metro.cpp:166-181): beta0 + beta1 r1 + beta2 m1 with r1, m1 the
+// sums of ReTr[b s_j] (ReTr[bnew s_j]) over the plaquette and rectangle staples
+// in the reference's order.  The staples are recovered from the kernels'
+// u_j = s_j b as s_j = u_j b^-1, so the summed elements are the reference's
+// own and the sums its bits on any table -- also one whose ReTr differs inside
+// a conjugacy class in the last bits (the reference's shipped files), where
+// the conjugate u_j g used by the fast path would not do.  Three table
+// gathers per term; only hits within the error bound of their threshold come
+// here.  need_old false leaves oldact as it is.
+template <int D>
+__device__ __forceinline__ void exact_actions(const SweepArgs& a, const uint16_t* s_inv, const double* s_retr,
+                                              const uint32_t* u, uint32_t b, uint32_t bnew, bool need_old,
+                                              double& oldact, double& newact) {
+  constexpr int NS = 2 * (D - 1), NT = 8 * (D - 1);
+  const uint16_t* __restrict__ mult = a.mult;
+  const uint32_t P = a.P, bi = s_inv[b];
+  double r1 = 0, m1 = 0, r1n = 0, m1n = 0;
+#pragma unroll
+  for (int j = 0; j < NT; ++j) {
+    const uint32_t sj = __ldg(mult + u[j] * P + bi);
+    const double vn = s_retr[__ldg(mult + bnew * P + sj)];
+    if (j < NS) r1n = DYM_ADD(r1n, vn);
+    else m1n = DYM_ADD(m1n, vn);
+    if (need_old) {
+      const double vo = s_retr[__ldg(mult + b * P + sj)];
+      if (j < NS) r1 = DYM_ADD(r1, vo);
+      else m1 = DYM_ADD(m1, vo);
+    }
+  }
+  if (need_old) oldact = dym_action(a.beta0, a.beta1, a.beta2, r1, m1);
+  newact = dym_action(a.beta0, a.beta1, a.beta2, r1n, m1n);
+}
+
 // One visit of link (i, DIR): build the staples, then nhit hits with the
 // per-hit products read from the shared sub-table.  With u_j = s_j * b the
 // element u_j * g_k = s_j b g_k is conjugate to bnew s_j = b g_k s_j, so for a
@@ -133,10 +167,12 @@ __device__ __forceinline__ void visit_sub(const SweepArgs& a, uint32_t i, uint32
 // computed in FP32 with a bound of 2^-19 + 2^-20 t.  The reference accepts iff
 // dS <= 0 or exp(-dS) > u2, i.e. iff dS < t (dym_exp is within an ulp of exp),
 // so dS_fast < t - band accepts, dS_fast > t + band rejects, and only the hits
-// in between are re-evaluated exactly as visit_sub does (FP64 sums in the
-// reference's order, dym_accept_fast).  The configurations are therefore those
-// of the FP64 path bit for bit.  The exact action of the current link is
-// rebuilt lazily when a re-evaluation needs it after fast accepts.
+// in between are re-evaluated exactly (exact_actions: FP64 sums over the
+// reference's own elements b s_j in its order, dym_accept_fast).  The
+// configurations are therefore those of the FP64 path bit for bit, on tables
+// whose ReTr is class-constant only up to a spread (the spread is part of
+// a.dmargin).  The exact action of the current link is rebuilt lazily when a
+// re-evaluation needs it after fast accepts.
 // First half of a mixed-precision visit of link (i, DIR): u_j = s_j * b
 // (build_u_tree; the shared-table kernels run on associative tables only) and
 // the fixed-point sums R, M of the current link (bound by global-memory
@@ -174,7 +210,8 @@ struct Packed {
 // from mixed_prepare's state; the link is written when it changed.
 template <int D, int DIR, class E = uint16_t>
 __device__ __forceinline__ void mixed_hits(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
-                                           const E* s_psub, const int32_t* s_cfix, uint32_t* u, uint32_t b,
+                                           const uint16_t* s_inv, const E* s_psub, const int32_t* s_cfix,
+                                           uint32_t* u, uint32_t b,
                                            uint32_t R, uint32_t M, unsigned& hits, unsigned& accs,
                                            unsigned& rechecks, float& max_err) {
   constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
@@ -210,21 +247,9 @@ __device__ __forceinline__ void mixed_hits(const SweepArgs& a, uint32_t i, uint3
     } else if (ds > t + band) {
       acc = false;
     } else {  // too close to call (also u2 == 0, where t - band is NaN)
-      if (!old_ok) {
-        double r1 = 0, m1 = 0;
-#pragma unroll
-        for (int j = 0; j < NS; ++j) r1 = DYM_ADD(r1, s_retr[u[j]]);
-#pragma unroll
-        for (int j = NS; j < NT; ++j) m1 = DYM_ADD(m1, s_retr[u[j]]);
-        oldact = dym_action(a.beta0, a.beta1, a.beta2, r1, m1);
-        old_ok = true;
-      }
-      double r1n = 0, m1n = 0;
-#pragma unroll
-      for (int j = 0; j < NS; ++j) r1n = DYM_ADD(r1n, s_retr[e[j] & kMask]);
-#pragma unroll
-      for (int j = NS; j < NT; ++j) m1n = DYM_ADD(m1n, s_retr[e[j] & kMask]);
-      const double newact = dym_action(a.beta0, a.beta1, a.beta2, r1n, m1n);
+      double newact;
+      exact_actions<D>(a, s_inv, s_retr, u, b, row[b] & kMask, !old_ok, oldact, newact);
+      old_ok = true;
       acc = dym_accept_fast(oldact, newact, dym_u53(r.v[1], r.v[2]));
       max_err = fmaxf(max_err, fabsf(ds - (float)DYM_SUB(newact, oldact)));
       ++rechecks;
@@ -267,7 +292,7 @@ __device__ __forceinline__ void visit_mixed(const SweepArgs& a, uint32_t i, uint
   uint32_t u[NT];
   uint32_t b, R, M;
   mixed_prepare<D, DIR>(a, i, xyz, s_inv, s_cls, s_cfix, u, b, R, M);
-  mixed_hits<D, DIR, E>(a, i, sweep, s_retr, s_psub, s_cfix, u, b, R, M, hits, accs, rechecks, max_err);
+  mixed_hits<D, DIR, E>(a, i, sweep, s_retr, s_inv, s_psub, s_cfix, u, b, R, M, hits, accs, rechecks, max_err);
 }
 
 // Value-table form of the mixed visit.  The shared table holds, for pool
@@ -301,7 +326,8 @@ __device__ __forceinline__ void vt_prepare(const SweepArgs& a, uint32_t i, uint3
 
 template <int D, int DIR>
 __device__ __forceinline__ void vt_hits(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
-                                        const int16_t* s_vsub, const uint16_t* s_pool, uint32_t* u, uint32_t b,
+                                        const uint16_t* s_inv, const int16_t* s_vsub, const uint16_t* s_pool,
+                                        uint32_t* u, uint32_t b,
                                         int32_t R, int32_t M, unsigned& hits, unsigned& accs, unsigned& rechecks,
                                         float& max_err) {
   constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
@@ -336,21 +362,9 @@ __device__ __forceinline__ void vt_hits(const SweepArgs& a, uint32_t i, uint32_t
 #pragma unroll
       for (int j = 0; j < NT; ++j) e[j] = __ldg(mult + u[j] * P + g);
       have_e = true;
-      if (!old_ok) {
-        double r1 = 0, m1 = 0;
-#pragma unroll
-        for (int j = 0; j < NS; ++j) r1 = DYM_ADD(r1, s_retr[u[j]]);
-#pragma unroll
-        for (int j = NS; j < NT; ++j) m1 = DYM_ADD(m1, s_retr[u[j]]);
-        oldact = dym_action(a.beta0, a.beta1, a.beta2, r1, m1);
-        old_ok = true;
-      }
-      double r1n = 0, m1n = 0;
-#pragma unroll
-      for (int j = 0; j < NS; ++j) r1n = DYM_ADD(r1n, s_retr[e[j]]);
-#pragma unroll
-      for (int j = NS; j < NT; ++j) m1n = DYM_ADD(m1n, s_retr[e[j]]);
-      const double newact = dym_action(a.beta0, a.beta1, a.beta2, r1n, m1n);
+      double newact;
+      exact_actions<D>(a, s_inv, s_retr, u, b, __ldg(mult + b * P + g), !old_ok, oldact, newact);
+      old_ok = true;
       acc = dym_accept_fast(oldact, newact, dym_u53(r.v[1], r.v[2]));
       max_err = fmaxf(max_err, fabsf(ds - (float)DYM_SUB(newact, oldact)));
       ++rechecks;

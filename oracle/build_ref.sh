@@ -1,7 +1,8 @@
 #!/bin/sh
 # Builds the reference-derived checkers into oracle/_ref/ (git-ignored), from
-# the reference's sources where they lie (REF_DIR, default /root/reference);
-# nothing is copied.  Test infrastructure only.
+# the reference's sources where they lie: REF_DIR, or else baseline/_ref (the
+# unmodified files oracle/stage_ref.sh placed there); nothing is copied.  Test
+# infrastructure and the reference arm of bench.py only.
 #
 #   _ref/libdymref.so   the reference's group.c, lattice.c and dym-mod-metro.cpp
 #                       (main renamed) + oracle/ref_harness.cpp, no OpenMP so
@@ -15,8 +16,8 @@
 #   _ref/llr2d          the unmodified two-dimensional LLR executable
 #                       (llr2d.cpp), reference Makefile flags
 set -e
-REF_DIR=${REF_DIR:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+REF_DIR=${REF_DIR:-$HERE/../baseline/_ref}
 OUT="$HERE/_ref"
 CORE="$HERE/../dym_symanzik_action_gb300/csrc"
 CC=${CC:-gcc}

@@ -7,7 +7,9 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import re
 import subprocess
+import tempfile
 
 import numpy as np
 
@@ -16,6 +18,18 @@ SRC = os.path.join(HERE, "dym_oracle.c")
 OUT = os.path.join(HERE, "_build", "liboracle.so")
 CORE = os.path.join(os.path.dirname(HERE), "dym_symanzik_action_gb300", "csrc", "dym_core.h")
 REF_LIB = os.path.join(HERE, "_ref", "libdymref.so")
+REF_BIN = os.path.join(HERE, "_ref")
+STAGED_REF = os.path.join(os.path.dirname(HERE), "baseline", "_ref")
+
+
+def ref_dir():
+    """The reference sources to build the checkers from: $REF_DIR, or else
+    baseline/_ref (filled by oracle/stage_ref.sh); None when neither holds
+    dym-mod-metro.cpp."""
+    for cand in (os.environ.get("REF_DIR"), STAGED_REF):
+        if cand and os.path.isfile(os.path.join(cand, "dym-mod-metro.cpp")):
+            return cand
+    return None
 
 
 def build() -> str:
@@ -203,6 +217,111 @@ class OracleLattice:
         hist = np.zeros((3 + max(wl_nx, 0) * max(wl_nt, 0)) * self.group.P, np.uint64) if want_hist else None
         lib().or_measure(self.h, wl_nx, wl_nt, _p(out, C.c_double), _p(hist, C.c_uint64))
         return (out, hist) if want_hist else out
+
+
+def _conflict_offsets(D: int, d: int):
+    """Same-direction links read by the update of link (x, d) (the staple index
+    sets of dym-mod-metro.cpp:63-142): +-e_d, +-e_a, +-2e_a, +-e_d +-e_a."""
+    out = []
+    for s in (-1, 1):
+        v = [0] * D
+        v[d] = s
+        out.append(v)
+    for a in range(D):
+        if a == d:
+            continue
+        for s in (-2, -1, 1, 2):
+            v = [0] * D
+            v[a] = s
+            out.append(v)
+        for sd in (-1, 1):
+            for sa in (-1, 1):
+                v = [0] * D
+                v[d], v[a] = sd, sa
+                out.append(v)
+    return out
+
+
+def colour_schedule(D: int, Nt: int, Nx: int):
+    """The race-free colour-phase schedule, restated in plain Python for the
+    CPU legs that must not load the engine: per direction the linear colouring
+    colour = (sum_b w_b x_b) mod m with the smallest m <= 24 and the first
+    periodic weights (axis 0 fastest) for which every conflicting offset that
+    names another site changes the colour, else a greedy colouring in site
+    order; phases are the non-empty colour classes in colour order, sites
+    ascending.  Returns (phase_dir int32, phase_len uint32, sites uint32)."""
+    ext = [Nt] + [Nx] * (D - 1)
+    V = int(np.prod(ext))
+    idx = np.arange(V)
+    coords = []
+    rem = idx.copy()
+    for b in range(D):
+        coords.append(rem % ext[b])
+        rem //= ext[b]
+    coords = np.stack(coords, 1)
+    strides = np.cumprod([1] + ext[:-1])
+    pd, pl, sites = [], [], []
+    for d in range(D):
+        offs = _conflict_offsets(D, d)
+        need = [v for v in offs if any(v[b] % ext[b] for b in range(D))]
+        colour, ncol = None, 0
+        for m in range(2, 25):
+            cand = [[w for w in range(m) if (ext[b] * w) % m == 0] for b in range(D)]
+            found = None
+            for wi in np.ndindex(*[len(c) for c in reversed(cand)]):
+                w = [cand[b][wi[D - 1 - b]] for b in range(D)]
+                if all(sum(w[b] * v[b] for b in range(D)) % m for v in need):
+                    found = w
+                    break
+            if found is not None:
+                colour, ncol = (coords @ np.array(found)) % m, m
+                break
+        if colour is None:
+            colour = -np.ones(V, np.int64)
+            for i in range(V):
+                used = set()
+                for v in offs:
+                    j = int((((coords[i] + v) % ext) * strides).sum())
+                    if j != i and colour[j] >= 0:
+                        used.add(int(colour[j]))
+                c = 0
+                while c in used:
+                    c += 1
+                colour[i] = c
+            ncol = int(colour.max()) + 1
+        for c in range(ncol):
+            lst = idx[colour == c]
+            if len(lst):
+                pd.append(d)
+                pl.append(len(lst))
+                sites.append(lst)
+    return (np.array(pd, np.int32), np.array(pl, np.uint32), np.concatenate(sites).astype(np.uint32))
+
+
+# TM_END line of the reference's timer (timer.cpp:19-26) around the K
+# update() calls of one measurement block (dym-mod-metro.cpp:273-278).
+_TM_UPDATE = re.compile(r"^TM_END:\s+update\s.*done in\s+([0-9.eE+-]+)\s+sec", re.M)
+
+
+def run_reference_metro(table: str, D: int, Nt: int, Nx: int, beta, seed: int, K: int, N: int, Ntherm: int,
+                        start: str = "hot", nhit10: bool = True, threads: int | None = None, timeout: float = 1800):
+    """Run the unmodified reference executable (oracle/_ref/dym-mod-metro, or
+    its NHIT = 10 build) and return (stdout, [seconds of every TM_END update
+    block]).  It runs in a scratch directory (the -pg build writes gmon.out
+    into its working directory) with OMP_NUM_THREADS = threads (all host cores
+    by default)."""
+    exe = os.path.join(REF_BIN, "dym-mod-metro-nhit10" if nhit10 else "dym-mod-metro")
+    if not os.path.exists(exe):
+        raise FileNotFoundError(exe)
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads or os.cpu_count() or 1))
+    args = [exe, table, str(D), str(Nt), str(Nx), *(repr(float(b)) for b in beta), str(seed), str(K), str(N),
+            str(Ntherm), start]
+    with tempfile.TemporaryDirectory() as td:
+        r = subprocess.run(args, cwd=td, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
+                           timeout=timeout)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference dym-mod-metro failed ({r.returncode}):\n{r.stdout[-2000:]}")
+    return r.stdout, [float(x) for x in _TM_UPDATE.findall(r.stdout)]
 
 
 class RefHarness:

@@ -1,7 +1,7 @@
 """Generate the golden fixtures under tests/golden/ from the reference itself.
 
-Run in a container where the reference sources exist (REF_DIR, default
-/root/reference):
+Run where the reference sources exist: REF_DIR, or else baseline/_ref (the
+unmodified files oracle/stage_ref.sh places there):
 
     python tests/golden/make_golden.py
 
@@ -17,6 +17,9 @@ It builds oracle/_ref/ (oracle/build_ref.sh) and writes:
   observables, from the reference's get_staples/get_rect_loops/plaquette/
   wilson/getpoly (compiled from its sources) driven by the Philox colour-phase
   hit loop, for several groups, shapes, couplings and proposal pools.
+* ref_tables.npz -- the reference's own mys1080-v4 and myBI traces, and
+  configurations after every sweep on those files (reference staples, Philox
+  hit loop): the pin for the fast kernels on tables with trace noise.
 * staples.npz -- every staple of every link of a random S(1080) 4^4 field, by
   the reference's get_staples and get_rect_loops.
 * chains_1sigma.npz -- GMES/RMES series of the unmodified reference
@@ -55,9 +58,11 @@ sys.path.insert(0, ROOT)
 
 from dym_symanzik_action_gb300 import tables  # noqa: E402
 from dym_symanzik_action_gb300.schedule import schedule  # noqa: E402
-from oracle.oracle import OracleGroup, OracleLattice, RefHarness  # noqa: E402
+from oracle.oracle import OracleGroup, OracleLattice, RefHarness, ref_dir  # noqa: E402
 
-REF_DIR = os.environ.get("REF_DIR", "/root/reference")
+REF_DIR = ref_dir()
+if REF_DIR is None:
+    sys.exit("make_golden.py: set REF_DIR to a reference checkout, or stage one with oracle/stage_ref.sh")
 REF_TABLES = {"S1080": "mys1080-v4", "BI": "myBI", "BT": "myBT", "BO": "myBO"}
 
 # name: (group, D, Nt, Nx, (beta0, beta1, beta2), start, seed, nhit, pool_all, nsweeps, wl_nx, wl_nt)
@@ -230,6 +235,51 @@ def make_staples(tabdir):
     print("staples: 4^4 S1080, 1024 links x 24 staples")
 
 
+# Cases run on the reference's own table files (traces with ~1e-16 of noise
+# inside a class), in the reference's element numbering:
+# name: (file, D, Nt, Nx, (beta0, beta1, beta2), start, seed, nhit, nsweeps)
+REF_TABLE_CASES = {
+    "mys1080_4444_hot": ("mys1080-v4", 4, 4, 4, (0.0, 1.5, 0.1), "hot", 20261203, 10, 4),
+    "mys1080_4448_hot_b25": ("mys1080-v4", 4, 8, 4, (0.0, 2.5, -0.1), "hot", 31, 10, 3),
+    "mys1080_4444_cold_b3": ("mys1080-v4", 4, 4, 4, (0.0, 3.0, -0.15), "cold", 11, 10, 3),
+    "mybi_4444_hot": ("myBI", 4, 4, 4, (0.0, 2.0, 0.0), "hot", 5, 20, 3),
+}
+
+
+def make_reftables():
+    """ref_tables.npz: the ReTr/ImTr rows of the reference's mys1080-v4 and
+    myBI (its numbering; with tables_iso.npz's pi and the generated Cayley
+    table they rebuild the reference file's content exactly), and
+    configurations/counts after every sweep of REF_TABLE_CASES by the
+    reference's own staples on those files."""
+    ref = RefHarness()
+    out = {}
+    for mine, name in (("S1080", "mys1080-v4"), ("BI", "myBI")):
+        P, rer, imr, rm = load_text_table(os.path.join(REF_DIR, "groups", name))
+        out[f"{mine}_retr"] = rer
+        out[f"{mine}_imtr"] = imr
+    for case, (fname, D, Nt, Nx, beta, start, seed, nhit, nsw) in REF_TABLE_CASES.items():
+        path = os.path.join(REF_DIR, "groups", fname)
+        og = OracleGroup(path)
+        ol = OracleLattice(og, D, Nt, Nx)
+        if start == "hot":
+            ol.hot_start(seed)
+        sched = schedule(D, Nt, Nx)
+        ref.init(path, D, Nt, Nx)
+        ref.set_links(ol.links)
+        links = [ref.get_links()]
+        counts = []
+        for k in range(nsw):
+            counts.append(ref.sweep(sched, beta, seed, k, 1, nhit, False))
+            links.append(ref.get_links())
+        out[case + "_links"] = np.stack(links)
+        out[case + "_counts"] = np.array(counts, np.uint64)
+        acc = np.array(counts)[:, 1].sum() / max(np.array(counts)[:, 0].sum(), 1)
+        print(f"{case}: {nsw} sweeps on the reference's {fname}, acceptance {acc:.3f}")
+    out["cases"] = np.array(repr(REF_TABLE_CASES))
+    np.savez_compressed(os.path.join(HERE, "ref_tables.npz"), **out)
+
+
 def parse_log(text):
     gmes = [list(map(float, l.split()[1:])) for l in text.splitlines() if l.startswith("GMES:")]
     rmes = [list(map(float, l.split()[1:])) for l in text.splitlines() if l.startswith("RMES:")]
@@ -324,7 +374,8 @@ def make_llr2d():
 def main():
     import argparse
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["iso", "staples", "sweeps", "chains", "llr", "llr_s2", "llr2d"])
+    ap.add_argument("--only", choices=["iso", "staples", "sweeps", "reftables", "chains", "llr", "llr_s2",
+                                       "llr2d"])
     only = ap.parse_args().only
     subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True,
                    env=dict(os.environ, REF_DIR=REF_DIR), stdout=subprocess.DEVNULL)
@@ -335,6 +386,8 @@ def main():
             make_staples(tabdir)
         if only in (None, "sweeps"):
             make_sweeps(tabdir)
+    if only in (None, "reftables"):
+        make_reftables()
     if only in (None, "chains"):
         make_chains()
     if only in (None, "llr"):

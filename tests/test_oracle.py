@@ -92,3 +92,24 @@ def test_oracle_threads_deterministic():
         L.sweep(sched, (0, 1.5, 0.1), 5, 0, 2, 10, nthreads=nt)
         out.append(L.links)
     assert (out[0] == out[1]).all()
+
+
+@pytest.mark.parametrize("name", list(__import__("conftest").ref_table_cases().keys()))
+def test_oracle_on_reference_files(name, ref_table):
+    """The oracle on the reference's own table files (ReTr with rounding noise
+    inside a class), rebuilt from the fixtures, reproduces the reference's
+    staples and hit loop run on the files themselves."""
+    from conftest import ref_table_cases
+    from dym_symanzik_action_gb300.schedule import schedule
+    fname, D, Nt, Nx, beta, start, seed, nhit, nsw = ref_table_cases()[name]
+    gold = golden("ref_tables.npz")
+    og = OracleGroup(ref_table(fname))
+    L = OracleLattice(og, D, Nt, Nx)
+    if start == "hot":
+        L.hot_start(seed)
+    assert (L.links == gold[name + "_links"][0]).all()
+    sched = schedule(D, Nt, Nx)
+    for s in range(nsw):
+        h, a = L.sweep(sched, beta, seed, s, 1, nhit, False, nthreads=2)
+        assert (h, a) == tuple(int(x) for x in gold[name + "_counts"][s])
+        assert (L.links == gold[name + "_links"][s + 1]).all(), f"sweep {s}"

@@ -61,3 +61,14 @@ def test_reference_parity_checkerboard_races(bt):
             sites.append(s)
     bad = L.conflicts((np.array(pd, np.int32), np.array(pl, np.uint32), np.concatenate(sites)))
     assert bad > 0
+
+
+@pytest.mark.parametrize("shape", [(4, 4, 4), (4, 2, 4), (4, 6, 6), (3, 8, 4), (2, 8, 8), (4, 5, 5), (4, 3, 4),
+                                   (4, 2, 12), (4, 6, 8), (4, 4, 6), (4, 8, 16)])
+def test_plain_python_schedule_equals_library(shape):
+    """The CPU legs of bench.py build their colour phases without the engine
+    (oracle.colour_schedule); they must be the library's phases exactly."""
+    from oracle.oracle import colour_schedule
+    a, b = colour_schedule(*shape), schedule(*shape)
+    for x, y in zip(a, b):
+        assert x.dtype == y.dtype and x.shape == y.shape and (x == y).all()
