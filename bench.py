@@ -382,6 +382,45 @@ def serving_bench(dym, device: int, n_requests: int, nhit: int = 20, step_sweeps
             "max_resident_links": max_links or None}  # 0 = no cap
 
 
+def chain_rate(dym, group, start: str, device: int, steps: int, warmup: int, flush, beta=None, Nt=None, Nx=None):
+    """Device link-hits/s of one chain of the workload's shape (or Nt x Nx^3)
+    on `group`, each step one sweep after an L2 flush, as the headline."""
+    import torch
+    w = WORKLOAD
+    Nt, Nx = Nt or w["Nt"], Nx or w["Nx"]
+    lat = dym.Lattice(group, w["D"], Nt, Nx, *(beta or w["beta"]), w["seed"], start=start, precision="mixed",
+                      device=device)
+    for _ in range(warmup):
+        lat.update(1, w["nhit"])
+    ms, hits, acc, kernels = 0.0, 0, 0, set()
+    for k in range(steps):
+        flush.fill_(k & 0xFF)
+        torch.cuda.synchronize()
+        st = lat.update(1, w["nhit"])
+        ms += st.device_ms
+        hits += st.hits
+        acc += st.accepts
+        kernels.add(int(st.kernel))
+    lat.close()
+    names = {2: "k_sweep_sub", 3: "k_sweep_mixed", 4: "k_sweep_vt", 1: "k_sweep_direct"}
+    return {"link_hits_per_s": hits / (ms * 1e-3), "ms_per_sweep": ms / steps, "acceptance": acc / hits,
+            "kernels": sorted(names.get(k, str(k)) for k in kernels), "sweeps_timed": steps}
+
+
+def reference_table_bench(dym, device: int, steps: int, warmup: int, flush) -> dict:
+    """The headline workload on the reference's own mys1080-v4 file (ReTr with
+    rounding noise inside a class), beside the same on the generated table."""
+    path = reference_table_path()
+    if path is None:
+        return {"unavailable": "reference not staged (oracle/stage_ref.sh)"}
+    g = dym.load_group(path)
+    out = {"table": "the reference's groups/mys1080-v4", "fast_path": bool(g.fast_path),
+           "classes_exact": bool(g.classes_exact), "class_spread": g.class_spread}
+    out.update(chain_rate(dym, g, "cold", device, steps, warmup, flush))
+    g.close()
+    return out
+
+
 def mixed_precision_scan(dym, device: int, sweeps: int = 300, nhit: int = 10) -> dict:
     """S(1080) 48^3 x 12 (5,308,416 links), hot start, beta1 in {2.0, 2.5, 3.0},
     beta2 = -0.1: the mixed kernel against the all-FP64 shared-table kernel from
@@ -564,6 +603,11 @@ def run_ours(args):
             "clocks": clocks,
             "wall_s_timed_region": t_wall,
         }
+        # A moving (hot-start) chain of the same shape and couplings, beside the
+        # frozen cold one, and the headline on the reference's own table file.
+        line["moving_chain"] = dict(workload="single chain S(1080) 32^3x8 HOT, beta=(0,3.0,-0.15), 10 hits/link",
+                                    **chain_rate(dym, g, "hot", local, args.steps, args.warmup, flush))
+        line["reference_table"] = reference_table_bench(dym, local, args.steps, args.warmup, flush)
         if not args.no_ensemble:
             line["batched"] = ensemble_bench(dym, local)
         if args.serve_requests > 0:
