@@ -192,6 +192,14 @@ static int build_vt_tables(dym_chain* c, const std::vector<uint16_t>& pool) {
   return DYM_OK;
 }
 
+// Hits per group whose draws the mixed kernels compute ahead (1, 2, 5 or
+// 10; DYM_HIT_UNROLL overrides the default).
+static int hit_unroll_setting() {
+  const char* e = std::getenv("DYM_HIT_UNROLL");
+  const int v = e ? std::atoi(e) : kDefaultHitUnroll;
+  return v >= 10 ? 10 : v >= 5 ? 5 : v >= 2 ? 2 : 1;
+}
+
 // The kernel dym_sweep runs for this call (DYM_KERNEL_*).  Both mixed kernels
 // take the same decisions; the value-table one is faster while accepted moves
 // are rare, since each accepted move fetches its 25 new elements from L2.
@@ -533,6 +541,7 @@ int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
   const int kernel = sweep_kernel(c);
   SweepArgs a = sweep_args(c, kernel);
   a.nhit = nhit;
+  a.hit_unroll = hit_unroll_setting();
   const Schedule& s = c->sched;
   DYM_CUDA(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
   for (int k = 0; k < nsweeps; ++k) {

@@ -37,6 +37,7 @@ struct SweepArgs {
   float b1f, b2f, dscale, dmargin;
   const uint32_t* xyz;  // coordinates of sites[k], 8 bits per axis (already offset)
   const int16_t* val16;  // value-table kernel: fixed-point ReTr of every element
+  int hit_unroll;        // mixed kernels: hits per group of draws computed ahead (1, 2, 5 or 10)
 };
 
 struct ChainDev {
@@ -86,6 +87,7 @@ constexpr int kMixedMaxCls = 32;    // classes addressable by the 5 high bits of
 constexpr uint32_t kMixedMaxP = 2048;  // 16-bit packed entries: element ids in the 11 low bits
 constexpr int kMixedMaxExtent = 256;   // coordinates packed 8 bits per axis
 constexpr int kMixedMaxThreads = 512;
+constexpr int kDefaultHitUnroll = 1;
 cudaError_t launch_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uint64_t seed, cudaStream_t s);
 cudaError_t launch_fill(uint16_t* links, size_t n, uint16_t v, cudaStream_t s);
 // Check n uploaded ids against P on the device (*first = smallest bad index,

@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(256) k_sweep_sub(SweepArgs a, const uint16_t* 
 // Shared memory: ReTr (FP64) | class values (int32 fixed point) | inverses |
 // packed sub-table (entries of type E, starting at mixed_psub_offset) |
 // element classes.
-template <int D, int DIR, class E>
+template <int D, int DIR, class E, int HU>
 __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_mixed(SweepArgs a, const E* __restrict__ psub) {
   extern __shared__ __align__(16) unsigned char smem[];
   double* s_retr = reinterpret_cast<double*>(smem);
@@ -161,7 +161,8 @@ __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_mixed(SweepArgs a
       i_next = a.sites[nt];
       xyz_next = a.xyz[nt];
     }
-    visit_mixed<D, DIR, E>(a, i, xyz, a.sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err);
+    visit_mixed<D, DIR, E, HU>(a, i, xyz, a.sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks,
+                               max_err);
   }
   flush_counters(a.counters, hits, accs, rechecks);
   flush_max_err(a.counters + 3, max_err);
@@ -173,7 +174,7 @@ __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_mixed(SweepArgs a
 // and the small tables with plain loads; none of them is written by the
 // previous colour phase, so the staging runs before the programmatic wait and
 // overlaps the previous launch's tail when launched with PDL.
-template <int D, int DIR>
+template <int D, int DIR, int HU>
 __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_vt(SweepArgs a, const int16_t* __restrict__ vsub) {
   extern __shared__ __align__(16) unsigned char smem[];
   const size_t vbytes = vt_table_bytes(a.P, a.npool);
@@ -214,7 +215,7 @@ __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_vt(SweepArgs a, c
       xyz_next = a.xyz[nt];
     }
     vt_prepare<D, DIR>(a, i, xyz, s_inv, s_val, u, b, R, M);
-    vt_hits<D, DIR>(a, i, a.sweep, s_retr, s_inv, s_vsub, s_pool, u, b, R, M, hits, accs, rechecks, max_err);
+    vt_hits<D, DIR, HU>(a, i, a.sweep, s_retr, s_inv, s_vsub, s_pool, u, b, R, M, hits, accs, rechecks, max_err);
   }
   flush_counters(a.counters, hits, accs, rechecks);
   flush_max_err(a.counters + 3, max_err);
@@ -317,6 +318,10 @@ cudaError_t launch_phase(void (*fn)(K...), unsigned grid, unsigned threads, size
   return cudaLaunchKernelEx(&cfg, fn, args...);
 }
 
+// Hit-unroll factors the mixed kernels are built for (hits whose draws are
+// computed ahead as a group, visit.cuh HitDraws): 1, 2, 5, 10.
+int hit_unroll_index(int hu) { return hu >= 10 ? 3 : hu >= 5 ? 2 : hu >= 2 ? 1 : 0; }
+
 template <int D>
 cudaError_t direct_dispatch(int dir, const SweepArgs& a, cudaStream_t s) {
   const size_t smem = (size_t)a.P * 8 + (size_t)a.P * 2 + (size_t)a.npool * 2 + 16;
@@ -367,11 +372,14 @@ template <int D, class E>
 cudaError_t mixed_dispatch(int dir, const SweepArgs& a, const E* psub, cudaStream_t s) {
   const size_t smem = mixed_smem_bytes(a.P, a.npool, sizeof(E));
   void (*fn)(SweepArgs, const E*) = nullptr;
-  switch (dir) {
-    case 0: fn = k_sweep_mixed<D, 0, E>; break;
-    case 1: fn = k_sweep_mixed<D, 1, E>; break;
-    case 2: if (D > 2) fn = k_sweep_mixed<D, (D > 2 ? 2 : 0), E>; break;
-    case 3: if (D > 3) fn = k_sweep_mixed<D, (D > 3 ? 3 : 0), E>; break;
+  switch (hit_unroll_index(a.hit_unroll) * 4 + dir) {
+#define DYM_MIXED_CASE(q, hu, d) \
+    case 4 * q + d: if (D > d) fn = k_sweep_mixed<D, (D > d ? d : 0), E, hu>; break;
+#define DYM_MIXED_HU(q, hu) DYM_MIXED_CASE(q, hu, 0) DYM_MIXED_CASE(q, hu, 1) DYM_MIXED_CASE(q, hu, 2) \
+    DYM_MIXED_CASE(q, hu, 3)
+    DYM_MIXED_HU(0, 1) DYM_MIXED_HU(1, 2) DYM_MIXED_HU(2, 5) DYM_MIXED_HU(3, 10)
+#undef DYM_MIXED_HU
+#undef DYM_MIXED_CASE
   }
   if (!fn) return cudaErrorInvalidValue;
   if (smem > 48 * 1024) {
@@ -397,11 +405,13 @@ template <int D>
 cudaError_t vt_dispatch(int dir, const SweepArgs& a, const int16_t* vsub, cudaStream_t s) {
   const size_t smem = vt_smem_bytes(a.P, a.npool);
   void (*fn)(SweepArgs, const int16_t*) = nullptr;
-  switch (dir) {
-    case 0: fn = k_sweep_vt<D, 0>; break;
-    case 1: fn = k_sweep_vt<D, 1>; break;
-    case 2: if (D > 2) fn = k_sweep_vt<D, (D > 2 ? 2 : 0)>; break;
-    case 3: if (D > 3) fn = k_sweep_vt<D, (D > 3 ? 3 : 0)>; break;
+  switch (hit_unroll_index(a.hit_unroll) * 4 + dir) {
+#define DYM_VT_CASE(q, hu, d) \
+    case 4 * q + d: if (D > d) fn = k_sweep_vt<D, (D > d ? d : 0), hu>; break;
+#define DYM_VT_HU(q, hu) DYM_VT_CASE(q, hu, 0) DYM_VT_CASE(q, hu, 1) DYM_VT_CASE(q, hu, 2) DYM_VT_CASE(q, hu, 3)
+    DYM_VT_HU(0, 1) DYM_VT_HU(1, 2) DYM_VT_HU(2, 5) DYM_VT_HU(3, 10)
+#undef DYM_VT_HU
+#undef DYM_VT_CASE
   }
   if (!fn) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -198,6 +198,29 @@ __device__ __forceinline__ void mixed_prepare(const SweepArgs& a, uint32_t i, ui
   for (int j = NS; j < NT; ++j) M += (uint32_t)s_cfix[s_cls[u[j]]];
 }
 
+// Draws of the HU consecutive hits h0 .. h0+HU-1 of link (i, dir): the pool
+// index k = floor(npool u1) and t = -log(u2) in FP32, the threshold of the
+// fast decision (u2 rebuilt from its two Philox words to within a relative
+// 2^-22).  A hit's draws depend on nothing an earlier hit changes, so a group
+// of hits computes its draws first: the Philox rounds of the group are
+// independent of one another and of the hits' shared-memory loads, and
+// interleave with them.  The draws of hits past nhit in the last group are
+// computed and not used.  A hit that needs the exact u2 (re-evaluation)
+// draws its Philox words again.
+template <int HU>
+struct HitDraws {
+  uint32_t k[HU];
+  float t[HU];
+  __device__ __forceinline__ void fill(const SweepArgs& a, uint32_t sweep, uint32_t i, uint32_t dir, int h0) {
+#pragma unroll
+    for (int q = 0; q < HU; ++q) {
+      const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, dir, (uint32_t)(h0 + q), DYM_TAG_METRO);
+      k[q] = dym_pick(r.v[0], a.npool);
+      t[q] = -__logf(__fmaf_rn((float)r.v[1], 0x1p-32f, (float)(r.v[2] >> 11) * 0x1p-53f));
+    }
+  }
+};
+
 // Packed sub-table entries: the element in the low kBits bits, its class
 // above.  16-bit entries hold ids below 2048; 32-bit entries any uint16 id.
 template <class E>
@@ -207,8 +230,9 @@ struct Packed {
 };
 
 // Second half: the nhit hits of link (i, DIR) from the shared tables, starting
-// from mixed_prepare's state; the link is written when it changed.
-template <int D, int DIR, class E = uint16_t>
+// from mixed_prepare's state, in groups of HU hits whose draws are computed
+// ahead (HitDraws); the link is written when it changed.
+template <int D, int DIR, class E = uint16_t, int HU = 1>
 __device__ __forceinline__ void mixed_hits(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
                                            const uint16_t* s_inv, const E* s_psub, const int32_t* s_cfix,
                                            uint32_t* u, uint32_t b,
@@ -219,52 +243,56 @@ __device__ __forceinline__ void mixed_hits(const SweepArgs& a, uint32_t i, uint3
   const uint32_t b0 = b;
   double oldact = 0.0;
   bool old_ok = false;
-  for (int h = 0; h < a.nhit; ++h) {
-    const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_METRO);
-    const E* row = s_psub + dym_pick(r.v[0], a.npool) * a.P;
-    uint32_t e[NT];
-    uint32_t Rn = 0, Mn = 0;
+  for (int h0 = 0; h0 < a.nhit; h0 += HU) {
+    HitDraws<HU> dr;
+    dr.fill(a, sweep, i, DIR, h0);
 #pragma unroll
-    for (int j = 0; j < NS; ++j) {
-      e[j] = row[u[j]];
-      Rn += (uint32_t)s_cfix[e[j] >> kBits];
-    }
+    for (int q = 0; q < HU; ++q) {
+      if (HU > 1 && h0 + q >= a.nhit) break;
+      const E* row = s_psub + dr.k[q] * a.P;
+      uint32_t e[NT];
+      uint32_t Rn = 0, Mn = 0;
 #pragma unroll
-    for (int j = NS; j < NT; ++j) {
-      e[j] = row[u[j]];
-      Mn += (uint32_t)s_cfix[e[j] >> kBits];
-    }
-    const float dR = (float)(int32_t)(Rn - R), dM = (float)(int32_t)(Mn - M);
-    const float ds = __fmaf_rn(a.b2f, dM, __fmul_rn(a.b1f, dR)) * a.dscale;
-    // u2 = (r1 * 2^21 + (r2 >> 11)) * 2^-53 to within a relative 2^-22.
-    const float u2f = __fmaf_rn((float)r.v[1], 0x1p-32f, (float)(r.v[2] >> 11) * 0x1p-53f);
-    const float t = -__logf(u2f);
-    const float band = a.dmargin + __fmaf_rn(t, 0x1p-20f, 0x1p-19f);
-    bool acc;
-    bool exact = false;
-    if (ds < t - band) {
-      acc = true;
-    } else if (ds > t + band) {
-      acc = false;
-    } else {  // too close to call (also u2 == 0, where t - band is NaN)
-      double newact;
-      exact_actions<D>(a, s_inv, s_retr, u, b, row[b] & kMask, !old_ok, oldact, newact);
-      old_ok = true;
-      acc = dym_accept_fast(oldact, newact, dym_u53(r.v[1], r.v[2]));
-      max_err = fmaxf(max_err, fabsf(ds - (float)DYM_SUB(newact, oldact)));
-      ++rechecks;
-      exact = true;
-      if (acc) oldact = newact;
-    }
-    ++hits;
-    if (acc) {
-      b = row[b] & kMask;
+      for (int j = 0; j < NS; ++j) {
+        e[j] = row[u[j]];
+        Rn += (uint32_t)s_cfix[e[j] >> kBits];
+      }
 #pragma unroll
-      for (int j = 0; j < NT; ++j) u[j] = e[j] & kMask;
-      R = Rn;
-      M = Mn;
-      old_ok = exact;
-      ++accs;
+      for (int j = NS; j < NT; ++j) {
+        e[j] = row[u[j]];
+        Mn += (uint32_t)s_cfix[e[j] >> kBits];
+      }
+      const float dR = (float)(int32_t)(Rn - R), dM = (float)(int32_t)(Mn - M);
+      const float ds = __fmaf_rn(a.b2f, dM, __fmul_rn(a.b1f, dR)) * a.dscale;
+      const float t = dr.t[q];
+      const float band = a.dmargin + __fmaf_rn(t, 0x1p-20f, 0x1p-19f);
+      bool acc;
+      bool exact = false;
+      if (ds < t - band) {
+        acc = true;
+      } else if (ds > t + band) {
+        acc = false;
+      } else {  // too close to call (also u2 == 0, where t - band is NaN)
+        const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)(h0 + q), DYM_TAG_METRO);
+        double newact;
+        exact_actions<D>(a, s_inv, s_retr, u, b, row[b] & kMask, !old_ok, oldact, newact);
+        old_ok = true;
+        acc = dym_accept_fast(oldact, newact, dym_u53(r.v[1], r.v[2]));
+        max_err = fmaxf(max_err, fabsf(ds - (float)DYM_SUB(newact, oldact)));
+        ++rechecks;
+        exact = true;
+        if (acc) oldact = newact;
+      }
+      ++hits;
+      if (acc) {
+        b = row[b] & kMask;
+#pragma unroll
+        for (int j = 0; j < NT; ++j) u[j] = e[j] & kMask;
+        R = Rn;
+        M = Mn;
+        old_ok = exact;
+        ++accs;
+      }
     }
   }
   if (b != b0) a.links[(size_t)DIR * a.V + i] = (uint16_t)b;
@@ -283,7 +311,7 @@ __device__ __forceinline__ void flush_counters(unsigned long long* ctr, unsigned
 }
 
 
-template <int D, int DIR, class E = uint16_t>
+template <int D, int DIR, class E = uint16_t, int HU = 1>
 __device__ __forceinline__ void visit_mixed(const SweepArgs& a, uint32_t i, uint32_t xyz, uint32_t sweep,
                                             const double* s_retr, const uint16_t* s_inv, const E* s_psub,
                                             const uint8_t* s_cls, const int32_t* s_cfix, unsigned& hits,
@@ -292,7 +320,7 @@ __device__ __forceinline__ void visit_mixed(const SweepArgs& a, uint32_t i, uint
   uint32_t u[NT];
   uint32_t b, R, M;
   mixed_prepare<D, DIR>(a, i, xyz, s_inv, s_cls, s_cfix, u, b, R, M);
-  mixed_hits<D, DIR, E>(a, i, sweep, s_retr, s_inv, s_psub, s_cfix, u, b, R, M, hits, accs, rechecks, max_err);
+  mixed_hits<D, DIR, E, HU>(a, i, sweep, s_retr, s_inv, s_psub, s_cfix, u, b, R, M, hits, accs, rechecks, max_err);
 }
 
 // Value-table form of the mixed visit.  The shared table holds, for pool
@@ -324,68 +352,72 @@ __device__ __forceinline__ void vt_prepare(const SweepArgs& a, uint32_t i, uint3
   for (int j = NS; j < NT; ++j) M += s_val[u[j]];
 }
 
-template <int D, int DIR>
+template <int D, int DIR, int HU = 1>
 __device__ __forceinline__ void vt_hits(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
                                         const uint16_t* s_inv, const int16_t* s_vsub, const uint16_t* s_pool,
-                                        uint32_t* u, uint32_t b,
-                                        int32_t R, int32_t M, unsigned& hits, unsigned& accs, unsigned& rechecks,
-                                        float& max_err) {
+                                        uint32_t* u, uint32_t b, int32_t R, int32_t M, unsigned& hits,
+                                        unsigned& accs, unsigned& rechecks, float& max_err) {
   constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
   const uint32_t b0 = b;
   const uint16_t* __restrict__ mult = a.mult;
   const uint32_t P = a.P, np = a.npool;
   double oldact = 0.0;
   bool old_ok = false;
-  for (int h = 0; h < a.nhit; ++h) {
-    const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_METRO);
-    const uint32_t k = dym_pick(r.v[0], np);
-    const int16_t* col = s_vsub + k;
-    int32_t Rn = 0, Mn = 0;
+  for (int h0 = 0; h0 < a.nhit; h0 += HU) {
+    HitDraws<HU> dr;
+    dr.fill(a, sweep, i, DIR, h0);
 #pragma unroll
-    for (int j = 0; j < NS; ++j) Rn += col[u[j] * np];
+    for (int q = 0; q < HU; ++q) {
+      if (HU > 1 && h0 + q >= a.nhit) break;
+      const uint32_t k = dr.k[q];
+      const int16_t* col = s_vsub + k;
+      int32_t Rn = 0, Mn = 0;
 #pragma unroll
-    for (int j = NS; j < NT; ++j) Mn += col[u[j] * np];
-    const float ds = __fmaf_rn(a.b2f, (float)(Mn - M), __fmul_rn(a.b1f, (float)(Rn - R))) * a.dscale;
-    const float u2f = __fmaf_rn((float)r.v[1], 0x1p-32f, (float)(r.v[2] >> 11) * 0x1p-53f);
-    const float t = -__logf(u2f);
-    const float band = a.dmargin + __fmaf_rn(t, 0x1p-20f, 0x1p-19f);
-    bool acc;
-    bool exact = false;
-    uint32_t e[NT];
-    bool have_e = false;
-    if (ds < t - band) {
-      acc = true;
-    } else if (ds > t + band) {
-      acc = false;
-    } else {
-      const uint32_t g = s_pool[k];
+      for (int j = 0; j < NS; ++j) Rn += col[u[j] * np];
 #pragma unroll
-      for (int j = 0; j < NT; ++j) e[j] = __ldg(mult + u[j] * P + g);
-      have_e = true;
-      double newact;
-      exact_actions<D>(a, s_inv, s_retr, u, b, __ldg(mult + b * P + g), !old_ok, oldact, newact);
-      old_ok = true;
-      acc = dym_accept_fast(oldact, newact, dym_u53(r.v[1], r.v[2]));
-      max_err = fmaxf(max_err, fabsf(ds - (float)DYM_SUB(newact, oldact)));
-      ++rechecks;
-      exact = true;
-      if (acc) oldact = newact;
-    }
-    ++hits;
-    if (acc) {
-      const uint32_t g = s_pool[k];
-      b = __ldg(mult + b * P + g);
-      if (have_e) {
-#pragma unroll
-        for (int j = 0; j < NT; ++j) u[j] = e[j];
+      for (int j = NS; j < NT; ++j) Mn += col[u[j] * np];
+      const float ds = __fmaf_rn(a.b2f, (float)(Mn - M), __fmul_rn(a.b1f, (float)(Rn - R))) * a.dscale;
+      const float t = dr.t[q];
+      const float band = a.dmargin + __fmaf_rn(t, 0x1p-20f, 0x1p-19f);
+      bool acc;
+      bool exact = false;
+      uint32_t e[NT];
+      bool have_e = false;
+      if (ds < t - band) {
+        acc = true;
+      } else if (ds > t + band) {
+        acc = false;
       } else {
+        const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)(h0 + q), DYM_TAG_METRO);
+        const uint32_t g = s_pool[k];
 #pragma unroll
-        for (int j = 0; j < NT; ++j) u[j] = __ldg(mult + u[j] * P + g);
+        for (int j = 0; j < NT; ++j) e[j] = __ldg(mult + u[j] * P + g);
+        have_e = true;
+        double newact;
+        exact_actions<D>(a, s_inv, s_retr, u, b, __ldg(mult + b * P + g), !old_ok, oldact, newact);
+        old_ok = true;
+        acc = dym_accept_fast(oldact, newact, dym_u53(r.v[1], r.v[2]));
+        max_err = fmaxf(max_err, fabsf(ds - (float)DYM_SUB(newact, oldact)));
+        ++rechecks;
+        exact = true;
+        if (acc) oldact = newact;
       }
-      R = Rn;
-      M = Mn;
-      old_ok = exact;
-      ++accs;
+      ++hits;
+      if (acc) {
+        const uint32_t g = s_pool[k];
+        b = __ldg(mult + b * P + g);
+        if (have_e) {
+#pragma unroll
+          for (int j = 0; j < NT; ++j) u[j] = e[j];
+        } else {
+#pragma unroll
+          for (int j = 0; j < NT; ++j) u[j] = __ldg(mult + u[j] * P + g);
+        }
+        R = Rn;
+        M = Mn;
+        old_ok = exact;
+        ++accs;
+      }
     }
   }
   if (b != b0) a.links[(size_t)DIR * a.V + i] = (uint16_t)b;
