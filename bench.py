@@ -23,7 +23,10 @@ cores) on the same workload and its own mys1080-v4 table: W untimed sweeps
 The engine is not loaded on that arm.
 Under torchrun (N > 1) every rank runs its own replica of the chain
 (replicas only: a single chain is not sharded); value = total link-hits / the
-slowest rank's time.
+slowest rank's time.  The forms that do shard -- the 256-chain ensemble and
+the served LLR stream -- then also run sharded by work over the ranks
+(shard.run_sharded: one Batch / one Server per GPU, per-chain results
+gathered to rank 0, no collective on the data path): the `sharded` block.
 """
 from __future__ import annotations
 
@@ -342,44 +345,76 @@ def serving_bench(dym, device: int, n_requests: int, nhit: int = 20, step_sweeps
     window of 0.5% of the plaquette-energy range, 20 Robbins-Monro iterations of
     50 sweeps.  Requests are submitted when their arrival time has passed (wall
     clock), the server admits them by resident-chain count and device memory,
-    and latency is completion minus arrival."""
+    and latency is completion minus arrival (serve.serve_stream)."""
     import numpy as np
     from dym_symanzik_action_gb300 import tables
-    from dym_symanzik_action_gb300.serve import Server
+    from dym_symanzik_action_gb300.serve import Server, serve_stream
     from dym_symanzik_action_gb300.workloads import llr_requests
     reqs = llr_requests(n=2000)[:n_requests]
     g = dym.load_group(tables.ensure_table("S1080"))
     srv = Server(g, max_chains=max_chains, hbm_budget=8 << 30, nhit=nhit, device=device, max_links=max_links)
-    lat = {}
-    status = {}
-    i = 0
-    t0 = time.perf_counter()
-    while len(lat) < len(reqs):
-        now = time.perf_counter() - t0
-        while i < len(reqs) and reqs[i].arrival <= now:
-            r = reqs[i]
-            srv.submit(r.rid, r.Nt, r.Nx, r.ewin, r.hw, r.a0, r.seed, start=r.start, axis=1, bg=r.bg, K=r.K,
-                       NRM=r.NRM, drive_cap=2000)
-            i += 1
-        st = srv.status()
-        if st["active"] or st["queued"]:
-            srv.step(step_sweeps)
-        elif i < len(reqs):
-            time.sleep(max(0.0, reqs[i].arrival - (time.perf_counter() - t0)))
-        for resp in srv.poll():
-            lat[resp.id] = time.perf_counter() - t0 - reqs[resp.id].arrival
-            status[resp.id] = resp.status
-    wall = time.perf_counter() - t0
+    res, wall = serve_stream(srv, reqs, step_sweeps)
     hits = srv.status()["link_hits"]
     srv.close()
-    L = np.array(list(lat.values()))
+    L = np.array([v[3] for v in res.values()])
     which = "all 2000" if len(reqs) == 2000 else f"first {len(reqs)} of 2000"
     return {"workload": f"{which} LLR window requests, Poisson 200/s, S(1080), Nx in {{6,8,12,16}}, "
                         f"Nt in {{2,4}}, 20 RM x 50 sweeps, {nhit} hits/link, at most {max_chains} resident",
             "requests": len(reqs), "wall_s": wall, "link_hits_per_s": hits / wall,
             "latency_p50_s": float(np.percentile(L, 50)), "latency_p99_s": float(np.percentile(L, 99)),
-            "unreached": sum(1 for v in status.values() if v != "done"), "max_resident_chains": max_chains,
+            "unreached": sum(1 for v in res.values() if v[0] != "done"), "max_resident_chains": max_chains,
             "max_resident_links": max_links or None}  # 0 = no cap
+
+
+def sharded_bench(local: int, rank: int, world: int, n_requests: int, sweeps: int = 5, nhit: int = 10) -> dict:
+    """The forms that shard (configs 3 and 5): every rank runs its share of the
+    256-chain ensemble as one Batch and its share of the request stream
+    through one Server (shard.run_sharded; partition by work, no data-path
+    collective), results gathered to rank 0.  Value = all ranks' link-hits /
+    the slowest rank's wall time (total work fixed: strong scaling)."""
+    import numpy as np
+    import torch.distributed as dist
+    from dym_symanzik_action_gb300 import ensemble, shard
+    from dym_symanzik_action_gb300.workloads import ensemble as ens_specs
+    from dym_symanzik_action_gb300.workloads import llr_requests
+
+    def all_timings(t):
+        parts = [None] * world
+        if world > 1:
+            dist.all_gather_object(parts, t)
+        else:
+            parts = [t]
+        return parts
+
+    out = {}
+    specs = ens_specs()
+    work = shard.chain_work([s.links for s in specs], sweeps)
+    t = {}
+    merged = shard.run_sharded(work, ensemble.batch_compute(specs, sweeps, nhit, local, timing=t), rank, world)
+    ts = all_timings(t)
+    if rank == 0:
+        wall = max(x["wall_s"] for x in ts)
+        hits = sum(x.get("hits", 0) for x in ts)
+        out["ensemble"] = {"workload": "256 chains (config 3), 5 sweeps, 10 hits/link, sharded by work",
+                           "ranks": world, "chains_per_rank": [x["chains"] for x in ts],
+                           "links_per_rank": [x["links"] for x in ts], "chains_gathered": len(merged),
+                           "link_hits_per_s": hits / wall, "slowest_rank_wall_s": wall, "scaling": "strong"}
+    if n_requests > 0:
+        reqs = llr_requests(n=2000)[:n_requests]
+        rwork = [float(r.nplaq * r.K * r.NRM) for r in reqs]
+        t = {}
+        merged = shard.run_sharded(rwork, ensemble.stream_compute(reqs, local, timing=t), rank, world)
+        ts = all_timings(t)
+        if rank == 0:
+            wall = max(x["wall_s"] for x in ts)
+            L = np.array([v[3] for v in merged.values()])
+            out["serving"] = {"workload": f"first {len(reqs)} requests of the config-5 stream, sharded by work",
+                              "ranks": world, "requests_per_rank": [x["requests"] for x in ts],
+                              "link_hits_per_s": sum(x["link_hits"] for x in ts) / wall,
+                              "latency_p50_s": float(np.percentile(L, 50)),
+                              "latency_p99_s": float(np.percentile(L, 99)),
+                              "unreached": sum(1 for v in merged.values() if v[0] != "done"), "scaling": "strong"}
+    return out
 
 
 def chain_rate(dym, group, start: str, device: int, steps: int, warmup: int, flush, beta=None, Nt=None, Nx=None):
@@ -603,8 +638,10 @@ def run_ours(args):
             "clocks": clocks,
             "wall_s_timed_region": t_wall,
         }
-        # A moving (hot-start) chain of the same shape and couplings, beside the
-        # frozen cold one, and the headline on the reference's own table file.
+    if rank == 0 and world == 1:
+        # Single-GPU extras.  A moving (hot-start) chain of the same shape and
+        # couplings, beside the frozen cold one, and the headline on the
+        # reference's own table file.
         line["moving_chain"] = dict(workload="single chain S(1080) 32^3x8 HOT, beta=(0,3.0,-0.15), 10 hits/link",
                                     **chain_rate(dym, g, "hot", local, args.steps, args.warmup, flush))
         line["reference_table"] = reference_table_bench(dym, local, args.steps, args.warmup, flush)
@@ -614,8 +651,14 @@ def run_ours(args):
             line["serving"] = serving_bench(dym, local, args.serve_requests)
         if not args.no_mixed_scan:
             line["mixed_precision"] = mixed_precision_scan(dym, local)
-        if world == 1 and not args.no_cpu_baseline:
+        if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline()
+    if world > 1:
+        # every rank takes part: each runs its share of configs 3 and 5
+        sh = sharded_bench(local, rank, world, min(args.serve_requests, 400))
+        if rank == 0:
+            line["sharded"] = sh
+    if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

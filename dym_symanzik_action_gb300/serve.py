@@ -80,3 +80,33 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def serve_stream(srv: Server, requests, step_sweeps: int = 5, drive_cap: int = 2000):
+    """Serve `requests` (workloads.LlrRequest, sorted by arrival) on `srv` as
+    they arrive: a request is submitted once its arrival time (seconds after
+    the call starts) has passed, the server steps while anything is resident
+    or queued, and finished responses are collected.  Returns
+    ({request id: [status, a, sweeps, latency in s]}, wall seconds)."""
+    import time
+    reqs = sorted(requests, key=lambda r: r.arrival)
+    arrival = {r.rid: r.arrival for r in reqs}
+    out = {}
+    i = 0
+    t0 = time.perf_counter()
+    while len(out) < len(reqs):
+        now = time.perf_counter() - t0
+        while i < len(reqs) and reqs[i].arrival <= now:
+            r = reqs[i]
+            srv.submit(r.rid, r.Nt, r.Nx, r.ewin, r.hw, r.a0, r.seed, start=r.start, axis=1, bg=r.bg, K=r.K,
+                       NRM=r.NRM, drive_cap=drive_cap)
+            i += 1
+        st = srv.status()
+        if st["active"] or st["queued"]:
+            srv.step(step_sweeps)
+        elif i < len(reqs):
+            time.sleep(max(0.0, reqs[i].arrival - (time.perf_counter() - t0)))
+        for resp in srv.poll():
+            out[resp.id] = [resp.status, float(resp.a), int(resp.sweeps),
+                            time.perf_counter() - t0 - arrival[resp.id]]
+    return out, time.perf_counter() - t0

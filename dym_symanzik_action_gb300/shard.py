@@ -12,11 +12,14 @@ is the same split with one process per GPU.
   the largest single chain.
 * gather(): rank 0 receives every rank's {chain index: result} (torch.distributed
   all_gather_object on the default process group: gloo on CPU, nccl on GPUs).
+* run_sharded(): the driver -- this rank's share by partition(), run by the
+  caller's compute (one Batch or one Server on the rank's GPU: ensemble.py;
+  the oracle in the CPU tests), gathered to rank 0.
 """
 from __future__ import annotations
 
 import heapq
-from typing import Any, Dict, List, Sequence
+from typing import Any, Callable, Dict, List, Sequence
 
 
 def partition(work: Sequence[float], world: int) -> List[List[int]]:
@@ -58,3 +61,13 @@ def gather(results: Dict[int, Any], rank: int, world: int) -> Dict[int, Any] | N
                 raise ValueError(f"chain {k} ran on two ranks")
             merged[k] = v
     return merged
+
+
+def run_sharded(work: Sequence[float], compute: Callable[[List[int]], Dict[int, Any]], rank: int,
+                world: int) -> Dict[int, Any] | None:
+    """Run this rank's share of the items (partition() by `work`) through
+    compute(indices) -> {index: result} and merge every rank's results on
+    rank 0 (None on the other ranks).  Nothing crosses ranks but that final
+    gather: the chains or requests of one share never meet another's."""
+    mine = partition(work, world)[rank]
+    return gather(compute(mine), rank, world)

@@ -1,7 +1,9 @@
 """Ensemble sharding over ranks, on CPU: the partition covers every chain once
-and is balanced, and two gloo ranks that each sweep their share (with the
-oracle, one small chain at a time) and gather the results to rank 0 give
-exactly the per-chain results of a single process running all chains."""
+and is balanced, and two gloo ranks that each run their share through
+shard.run_sharded (the driver bench.py runs on GPUs, here with the oracle as
+the per-rank compute, one small chain at a time) and gather the results to
+rank 0 give exactly the per-chain results of a single process running all
+chains."""
 import hashlib
 import json
 import os
@@ -46,8 +48,8 @@ def _rank_main(rank, world, port, out_path):
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
         work = shard.chain_work([4 * c[1] * c[2] ** 3 for c in CHAINS], SWEEPS)
-        mine = shard.partition(work, world)[rank]
-        merged = shard.gather({k: run_chain(k) for k in mine}, rank, world)
+        # the same driver bench.py runs on GPUs, with the oracle as the per-rank compute
+        merged = shard.run_sharded(work, lambda idx: {k: run_chain(k) for k in idx}, rank, world)
         if rank == 0:
             with open(out_path, "w") as f:
                 json.dump({str(k): v for k, v in merged.items()}, f)
