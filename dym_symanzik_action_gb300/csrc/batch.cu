@@ -27,7 +27,7 @@ namespace {
 
 template <int D>
 __global__ void __launch_bounds__(256) k_batch_sub(const BatchTile* __restrict__ tiles, uint32_t ntiles,
-                                                   const BatchChainDev* __restrict__ chains, BatchGroups groups,
+                                                   const BatchChainDev* __restrict__ chains, const __grid_constant__ BatchGroups groups,
                                                    const uint32_t* __restrict__ sweeps, int nhit) {
   extern __shared__ __align__(16) unsigned char smem[];
   for (int g = 0; g < groups.n; ++g) {
@@ -39,6 +39,7 @@ __global__ void __launch_bounds__(256) k_batch_sub(const BatchTile* __restrict__
   for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const BatchTile tl = tiles[t];
     const BatchChainDev c = chains[tl.chain];
+    if ((unsigned)c.group >= (unsigned)groups.n) continue;  // checked on the host as well
     const BatchGroupDev& G = groups.g[c.group];
     SweepArgs a{};
     a.links = c.links;
@@ -76,7 +77,7 @@ __global__ void __launch_bounds__(256) k_batch_sub(const BatchTile* __restrict__
 // fixed-point class values.
 template <int D>
 __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_batch_mixed(const BatchTile* __restrict__ tiles, uint32_t ntiles,
-                                                     const BatchChainDev* __restrict__ chains, BatchGroups groups,
+                                                     const BatchChainDev* __restrict__ chains, const __grid_constant__ BatchGroups groups,
                                                      const uint32_t* __restrict__ sweeps, int nhit) {
   extern __shared__ __align__(16) unsigned char smem[];
   for (int g = 0; g < groups.n; ++g) {
@@ -91,6 +92,7 @@ __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_batch_mixed(const Batch
   for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const BatchTile tl = tiles[t];
     const BatchChainDev c = chains[tl.chain];
+    if ((unsigned)c.group >= (unsigned)groups.n) continue;  // checked on the host as well
     const BatchGroupDev& G = groups.g[c.group];
     SweepArgs a{};
     a.links = c.links;

@@ -923,6 +923,7 @@ static int batch_build(dym_batch* b) {
     d.Nt = c->p.Nt;
     d.Nx = c->p.Nx;
     d.group = (int)(std::find(b->groups.begin(), b->groups.end(), c->grp->g) - b->groups.begin());
+    if (d.group < 0 || d.group >= b->bg.n) return fail(DYM_ENOTSUP, "internal: chain's group missing from the batch");
     d.beta0 = c->p.beta0;
     d.beta1 = c->p.beta1;
     d.beta2 = c->p.beta2;

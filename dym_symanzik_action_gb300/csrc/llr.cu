@@ -76,7 +76,7 @@ __device__ __forceinline__ long long seg_prefix(long long x, uint32_t lane, uint
 template <int D>
 __global__ void __launch_bounds__(kLlrWarps * 32) k_llr_propose(const LlrTile* __restrict__ tiles, uint32_t ntiles,
                                                                 const LlrChainDev* __restrict__ chains,
-                                                                BatchGroups groups, int nhit) {
+                                                                const __grid_constant__ BatchGroups groups, int nhit) {
   extern __shared__ __align__(16) unsigned char smem[];
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   for (int g = 0; g < groups.n; ++g) {  // packed sub-table by cp.async (16-byte aligned on both sides)
@@ -110,6 +110,7 @@ __global__ void __launch_bounds__(kLlrWarps * 32) k_llr_propose(const LlrTile* _
     LlrState* st = c.st;
     const int mode = st->mode;
     if (mode >= DYM_LLR_DONE) continue;  // the same for every lane of the warp
+    if ((unsigned)c.group >= (unsigned)groups.n) continue;  // checked on the host as well
     const BatchGroupDev& G = groups.g[c.group];
     SweepArgs a{};
     a.links = c.links;

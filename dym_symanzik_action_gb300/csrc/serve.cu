@@ -283,6 +283,8 @@ struct LlrWork {
       d.brec = c->d_llr_blk;
       d.bref = c->d_llr_bref;
       d.group = (int)(std::find(groups.begin(), groups.end(), c->grp->g) - groups.begin());
+      if (d.group < 0 || d.group >= (int)groups.size() || d.group >= kBatchMaxGroups)
+        return fail(DYM_ENOTSUP, "internal: chain's group missing from the work list's group table");
       maxph = std::max(maxph, c->sched.phase_dir.size());
     }
     std::vector<LlrTile> tiles;
