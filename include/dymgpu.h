@@ -209,7 +209,11 @@ int dym_measure(dym_chain* c, const dym_meas_opts* opts, dym_obs* out, double* w
  * library's device code, walks Wilson loops link by link instead of building
  * lattice-sized line-product tables, takes the dot products on the device and
  * copies only the results, into *out and wloop.  Results are identical to
- * dym_measure's.
+ * dym_measure's, bit for bit (the same exact histograms, and the same
+ * correctly rounded multiplies, adds and division in the same order).
+ * Cost: a walked (k+1) x (l+1) loop takes 2(k+l+2) table products against
+ * dym_measure's 3 (line products), so a Wilson grid costs about (k+l)/1.5
+ * times dym_measure's Wilson-loop work (8x8 grid: up to ~11x).
  * Limits: (3 + wl_nx*wl_nt) * P <= DYM_NOALLOC_HIST_BINS and
  * wl_nx*wl_nt <= DYM_NOALLOC_MAX_LOOPS (S(1080): up to 118 loops, e.g. the 8x8
  * grid); larger requests return DYM_ERANGE before any device work.
@@ -217,9 +221,11 @@ int dym_measure(dym_chain* c, const dym_meas_opts* opts, dym_obs* out, double* w
  * the bins it uses (they must start at zero), so calls whose device work
  * overlaps -- from several host threads, or on chains of one device -- race
  * and must be serialised by the caller.  The first call on each device looks
- * up the array's device address (which may load the library's device code);
- * make that first call before any stream capture begins.  On success nothing
- * is allocated, host or device; an error records its message as every call. */
+ * up the array's device address (which may load the library's device code).
+ * The call synchronises the chain's stream and copies into pageable host
+ * memory, so it must not be made while any stream of the device is being
+ * captured into a CUDA graph.  On success nothing is allocated, host or
+ * device; an error records its message as every call. */
 #define DYM_NOALLOC_HIST_BINS 131072
 #define DYM_NOALLOC_MAX_LOOPS 1024
 int dym_measure_noalloc(dym_chain* c, const dym_meas_opts* opts, dym_obs* out, double* wloop);

@@ -309,16 +309,69 @@ def make_chains():
     np.savez_compressed(os.path.join(HERE, "chains_1sigma.npz"), **out)
 
 
+def _ref_chain(job):
+    """One run of the unmodified reference (NHIT 10 build) in a scratch
+    directory; returns (seed, GMES rows, RMES rows, final ACC)."""
+    table, D, Nt, Nx, beta, seed, K, N, Ntherm, threads = job
+    from oracle.oracle import run_reference_metro
+    out, _ = run_reference_metro(table, D, Nt, Nx, beta, seed, K, N, Ntherm, start="hot", nhit10=True,
+                                 threads=threads, timeout=7200)
+    g, rm, acc = parse_log(out)
+    return seed, g, rm, acc[-1]
+
+
+# The BASELINE workloads as statistical fixtures: config 1 as stated (4^4 hot,
+# beta = (0, 1.5, 0.1), NHIT 10, Ntherm 100, K 10, N 100, the reference's
+# nearest-element pool), and the config-2 lattice (32^3 x 8) with Polyakov
+# loop and the 8 x 8 Wilson grid, from a hot start at the config-1 couplings
+# (at config 2's own couplings a cold chain is frozen and a hot one relaxes
+# for far longer than a fixture run), Ntherm 30, K 5, N 4.
+CHAINS_CONFIG1 = dict(D=4, Nt=4, Nx=4, beta=(0.0, 1.5, 0.1), K=10, N=100, Ntherm=100, seeds=list(range(3001, 3025)),
+                      threads=1)
+CHAINS_CONFIG2 = dict(D=4, Nt=8, Nx=32, beta=(0.0, 1.5, 0.1), K=5, N=4, Ntherm=30, seeds=list(range(4001, 4013)),
+                      threads=os.cpu_count() or 1, wl=8)
+
+
+def make_chains_baseline():
+    """chains_config1.npz and chains_config2.npz: per-run GMES/RMES of the
+    unmodified reference (its Makefile flags, NHIT 10, its own mys1080-v4):
+    config 1 one thread per run (runs in parallel), the config-2 lattice with
+    all cores per run.  Stored per run: the measurement series of ReP, ImP,
+    plaq, rect and the Wilson grid (config 2: its first 8 x 8)."""
+    from concurrent.futures import ProcessPoolExecutor
+    table = os.path.join(REF_DIR, "groups", "mys1080-v4")
+    for name, C in (("chains_config1.npz", CHAINS_CONFIG1), ("chains_config2.npz", CHAINS_CONFIG2)):
+        jobs = [(table, C["D"], C["Nt"], C["Nx"], C["beta"], s, C["K"], C["N"], C["Ntherm"], C["threads"])
+                for s in C["seeds"]]
+        workers = max(1, (os.cpu_count() or 1) // C["threads"])
+        with ProcessPoolExecutor(workers) as ex:
+            res = list(ex.map(_ref_chain, jobs))
+        out = {}
+        for seed, g, rm, acc in res:
+            wl = C.get("wl")
+            grid = g[:, 4:].reshape(len(g), C["Nx"], C["Nt"])
+            if wl:
+                grid = grid[:, :wl, :wl]
+            out[f"series_{seed}"] = np.concatenate([g[:, 1:4], rm[:, 2:3], grid.reshape(len(g), -1)], 1)
+            out[f"acc_{seed}"] = np.array(acc)
+            print(f"{name} seed {seed}: {len(g)} measurements, <plaq> {g[:, 3].mean():.5f}, acceptance {acc:.3f}")
+        out["columns"] = np.array("ReP ImP plaq rect W[k][l] (k spatial outer, l temporal inner)")
+        out["params"] = np.array(repr({k: v for k, v in C.items() if k != "threads"}) +
+                                 " table=mys1080-v4 NHIT=10 start=hot pool=nearest")
+        out["seeds"] = np.array(C["seeds"])
+        np.savez_compressed(os.path.join(HERE, name), **out)
+
+
 # The LLR ladder of llr_ref.npz, in the reference llr's argument order
 # (group D Nt Nx axis bg Etop Ebot step hw a0 seed K NRM R).  With
 # NPLAQ = 768: window centres -0.6..-1.2 NPLAQ in steps of 0.2 NPLAQ, width
 # 0.0225 NPLAQ (0.5% of the S(1080) plaquette-energy range).
 LLR_LADDER = dict(D=4, Nt=2, Nx=4, axis=1, bg=0.0, Etop=-460.8, Ebot=-921.6, step=153.6, hw=8.64, a0=1.5,
-                  seed=20261203, K=50, NRM=80, R=6)
+                  seed=20261203, K=50, NRM=80, R=20)
 # S2 windows (NRECT 3072 on 4^4): centres -0.15 and -0.30 NRECT, width 0.0225 NRECT, beta1 = 0; a0 near the
 # solution, so that Robbins-Monro converges within NRM on these wide windows.
 LLR_LADDER_S2 = dict(D=4, Nt=4, Nx=4, axis=2, bg=0.0, Etop=-460.8, Ebot=-921.6, step=460.8, hw=34.56, a0=0.5,
-                     seed=20261203, K=50, NRM=80, R=4)
+                     seed=20261203, K=50, NRM=80, R=20)
 
 
 def make_llr(L=LLR_LADDER, name="llr_ref.npz"):
@@ -347,7 +400,7 @@ def make_llr(L=LLR_LADDER, name="llr_ref.npz"):
 # quadratic through the mean S2 of the one-dimensional S1 windows at these
 # centres (beta2 = 0), so each cell lies inside the configurations' support.
 LLR2D_GRID = dict(D=4, Nt=4, Nx=4, E1top=-921.6, E1bot=-1536.0, step1=307.2, hw1=17.28, c0=80.333, c1=0.143764,
-                  c2=-0.000374147, step2=69.12, hw2=34.56, nperp=0, a0=1.0, seed=11, K=40, NRM=70, R=4)
+                  c2=-0.000374147, step2=69.12, hw2=34.56, nperp=0, a0=1.0, seed=11, K=40, NRM=70, R=20)
 
 
 def make_llr2d():
@@ -374,8 +427,8 @@ def make_llr2d():
 def main():
     import argparse
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["iso", "staples", "sweeps", "reftables", "chains", "llr", "llr_s2",
-                                       "llr2d"])
+    ap.add_argument("--only", choices=["iso", "staples", "sweeps", "reftables", "chains", "chains_baseline", "llr",
+                                       "llr_s2", "llr2d"])
     only = ap.parse_args().only
     subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True,
                    env=dict(os.environ, REF_DIR=REF_DIR), stdout=subprocess.DEVNULL)
@@ -390,6 +443,8 @@ def main():
         make_reftables()
     if only in (None, "chains"):
         make_chains()
+    if only in (None, "chains_baseline"):
+        make_chains_baseline()
     if only in (None, "llr"):
         make_llr()
     if only in (None, "llr_s2"):

@@ -2,12 +2,13 @@
 both called through the C ABI.
 
 Both count every loop in exact integer histograms and then take the same FP64
-dot products in the same order, so the observables are expected to be
-identical; the tolerance below only guards against a last-bit difference in
-the final division.  Two calls in a row check that the shared scratch is
-cleared between calls; a sweep between calls checks that it follows the
-configuration.  This file is collected last so that it also runs after the
-other GPU tests have used the device."""
+dot products (correctly rounded multiplies and adds, then one division) in
+the same order, so the observables must be identical, bit for bit.  Two
+calls in a row check that the shared scratch is cleared between calls; a
+sweep between calls checks that it follows the configuration.  On a fresh
+chain whose first measurement is the no-allocation call, the device's free
+memory is unchanged across the calls.  This file is collected last so that
+it also runs after the other GPU tests have used the device."""
 import ctypes as C
 
 import numpy as np
@@ -17,8 +18,6 @@ from dym_symanzik_action_gb300 import _lib, tables
 from dym_symanzik_action_gb300._lib import check, lib, ptr
 
 pytestmark = pytest.mark.gpu
-
-TOL = 1e-12  # absolute, on observables of magnitude <= 3
 
 CASES = {
     # group, D, Nt, Nx, betas, start, seed, (wl_nx, wl_nt)
@@ -44,8 +43,8 @@ def measure_via(fn_name, lat, wl_nx, wl_nt):
 def assert_same(a, b):
     (ha, ga, wa), (hb, gb, wb) = a, b
     assert ga == gb
-    np.testing.assert_allclose(ha, hb, rtol=0, atol=TOL)
-    np.testing.assert_allclose(wa, wb, rtol=0, atol=TOL)
+    np.testing.assert_array_equal(ha, hb)
+    np.testing.assert_array_equal(wa, wb)
 
 
 @pytest.mark.parametrize("name", list(CASES))
@@ -83,3 +82,26 @@ def test_noalloc_rejects_oversize(engine, grid):
     h, gr, _ = measure_via("dym_measure_noalloc", lat, 2, 2)
     assert gr == (2, 2) and np.isfinite(h).all()
     lat.close()
+
+
+def test_noalloc_allocates_nothing_on_a_fresh_chain(engine):
+    """The first measurement of a new chain through dym_measure_noalloc: the
+    device's free memory (cudaMemGetInfo) is the same before and after two
+    calls, and the results equal dym_measure's taken afterwards."""
+    torch = pytest.importorskip("torch")
+    g = engine.load_group(tables.ensure_table("S1080"))
+    warm = engine.Lattice(g, 4, 4, 4, 0.0, 1.5, 0.1, 21)
+    measure_via("dym_measure_noalloc", warm, 2, 2)  # the device's array is looked up (device code loaded)
+    lat = engine.Lattice(g, 4, 4, 8, 0.0, 1.5, 0.1, 22, start="hot")
+    lat.update(2, 10)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info(0)[0]
+    first = measure_via("dym_measure_noalloc", lat, 4, 4)
+    second = measure_via("dym_measure_noalloc", lat, 4, 4)
+    free1 = torch.cuda.mem_get_info(0)[0]
+    assert free1 == free0, (free0, free1)
+    ref = measure_via("dym_measure", lat, 4, 4)  # allocates the chain's histogram buffers now
+    assert_same(first, ref)
+    assert_same(second, ref)
+    lat.close()
+    warm.close()
