@@ -200,11 +200,18 @@ static int hit_unroll_setting() {
   return v >= 10 ? 10 : v >= 5 ? 5 : v >= 2 ? 2 : 1;
 }
 
+// Largest acceptance of a chain's previous call for which its next call runs
+// the value-table kernel (DYM_VT_MAX_ACCEPT overrides the default).
+static double vt_max_accept() {
+  const char* e = std::getenv("DYM_VT_MAX_ACCEPT");
+  return e ? std::atof(e) : kDefaultVtMaxAccept;
+}
+
 // The kernel dym_sweep runs for this call (DYM_KERNEL_*).  Both mixed kernels
 // take the same decisions; the value-table one is faster while accepted moves
 // are rare, since each accepted move fetches its 25 new elements from L2.
 static int sweep_kernel(const dym_chain* c) {
-  if (c->dev.vt_ok && c->dev.last_acc < 0.01) return DYM_KERNEL_MIXED_VALUES;
+  if (c->dev.vt_ok && c->dev.last_acc < vt_max_accept()) return DYM_KERNEL_MIXED_VALUES;
   if (c->dev.mixed_ok) return DYM_KERNEL_MIXED;
   if (c->dev.sub_ok) return DYM_KERNEL_SHARED;
   return DYM_KERNEL_DIRECT;

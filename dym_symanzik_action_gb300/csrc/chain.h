@@ -88,6 +88,7 @@ constexpr uint32_t kMixedMaxP = 2048;  // 16-bit packed entries: element ids in 
 constexpr int kMixedMaxExtent = 256;   // coordinates packed 8 bits per axis
 constexpr int kMixedMaxThreads = 512;
 constexpr int kDefaultHitUnroll = 1;
+constexpr double kDefaultVtMaxAccept = 0.01;
 cudaError_t launch_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uint64_t seed, cudaStream_t s);
 cudaError_t launch_fill(uint16_t* links, size_t n, uint16_t v, cudaStream_t s);
 // Check n uploaded ids against P on the device (*first = smallest bad index,

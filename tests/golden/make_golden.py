@@ -323,16 +323,20 @@ def _ref_chain(job):
 # The BASELINE workloads as statistical fixtures: config 1 as stated (4^4 hot,
 # beta = (0, 1.5, 0.1), NHIT 10, Ntherm 100, K 10, N 100, the reference's
 # nearest-element pool), and the config-2 lattice (32^3 x 8) with Polyakov
-# loop and the 8 x 8 Wilson grid, from a hot start at the config-1 couplings
-# (at config 2's own couplings a cold chain is frozen and a hot one relaxes
-# for far longer than a fixture run), Ntherm 30, K 5, N 4.
+# loop and the 8 x 8 Wilson grid, from a hot start in the disordered phase,
+# beta = (0, 1.0, 0.1), where the plaquette settles within a few sweeps (at
+# config 2's own couplings a cold chain is frozen, and a hot one -- like one
+# at the config-1 couplings, which order 4^4 -- relaxes through a
+# first-order transition far longer than a fixture run, so that the
+# reference's racing updates and the engine's colour phases would be compared
+# out of equilibrium), Ntherm 20, K 4, N 2.
 CHAINS_CONFIG1 = dict(D=4, Nt=4, Nx=4, beta=(0.0, 1.5, 0.1), K=10, N=100, Ntherm=100, seeds=list(range(3001, 3025)),
                       threads=1)
-CHAINS_CONFIG2 = dict(D=4, Nt=8, Nx=32, beta=(0.0, 1.5, 0.1), K=5, N=4, Ntherm=30, seeds=list(range(4001, 4013)),
+CHAINS_CONFIG2 = dict(D=4, Nt=8, Nx=32, beta=(0.0, 1.0, 0.1), K=4, N=2, Ntherm=20, seeds=list(range(4001, 4013)),
                       threads=os.cpu_count() or 1, wl=8)
 
 
-def make_chains_baseline():
+def make_chains_baseline(which=("chains_config1.npz", "chains_config2.npz")):
     """chains_config1.npz and chains_config2.npz: per-run GMES/RMES of the
     unmodified reference (its Makefile flags, NHIT 10, its own mys1080-v4):
     config 1 one thread per run (runs in parallel), the config-2 lattice with
@@ -341,6 +345,8 @@ def make_chains_baseline():
     from concurrent.futures import ProcessPoolExecutor
     table = os.path.join(REF_DIR, "groups", "mys1080-v4")
     for name, C in (("chains_config1.npz", CHAINS_CONFIG1), ("chains_config2.npz", CHAINS_CONFIG2)):
+        if name not in which:
+            continue
         jobs = [(table, C["D"], C["Nt"], C["Nx"], C["beta"], s, C["K"], C["N"], C["Ntherm"], C["threads"])
                 for s in C["seeds"]]
         workers = max(1, (os.cpu_count() or 1) // C["threads"])
@@ -427,11 +433,14 @@ def make_llr2d():
 def main():
     import argparse
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["iso", "staples", "sweeps", "reftables", "chains", "chains_baseline", "llr",
-                                       "llr_s2", "llr2d"])
-    only = ap.parse_args().only
-    subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True,
-                   env=dict(os.environ, REF_DIR=REF_DIR), stdout=subprocess.DEVNULL)
+    ap.add_argument("--only", choices=["iso", "staples", "sweeps", "reftables", "chains", "chains_baseline",
+                                       "chains_config1", "chains_config2", "llr", "llr_s2", "llr2d"])
+    ap.add_argument("--skip-build", action="store_true", help="use oracle/_ref as built (parallel invocations)")
+    args = ap.parse_args()
+    only = args.only
+    if not args.skip_build:
+        subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True,
+                       env=dict(os.environ, REF_DIR=REF_DIR), stdout=subprocess.DEVNULL)
     with tempfile.TemporaryDirectory() as tabdir:
         if only in (None, "iso"):
             make_iso(tabdir)
@@ -445,6 +454,8 @@ def main():
         make_chains()
     if only in (None, "chains_baseline"):
         make_chains_baseline()
+    if only in ("chains_config1", "chains_config2"):
+        make_chains_baseline((only + ".npz",))
     if only in (None, "llr"):
         make_llr()
     if only in (None, "llr_s2"):
