@@ -25,18 +25,23 @@ It builds oracle/_ref/ (oracle/build_ref.sh) and writes:
 * chains_1sigma.npz -- GMES/RMES series of the unmodified reference
   executable (its own table, NHIT 20, one thread) at the 4^4 couplings
   (0, 1.5, 0.1) for several seeds: the oracle for the 1-sigma comparison.
+* chains_config1.npz, chains_config1_eq.npz, chains_config2.npz -- per-run
+  measurement series of the unmodified reference executable (NHIT 10 build,
+  its own mys1080-v4, hot starts) at the BASELINE workloads: config 1 as
+  stated, config 1's couplings after 3,000 thermalisation sweeps, and the
+  config-2 lattice (make_chains_baseline).
 * llr_ref.npz -- the ANE table (window centre, mean a_n, sd, samples) of the
   unmodified reference llr executable (its own S(1080) table, one thread) on a
-  four-window ladder of S1 (plaquette) windows on a 4^3x2 lattice with R = 6
+  four-window ladder of S1 (plaquette) windows on a 4^3x2 lattice with R = 20
   repeats of the hot-down and cold-up passes: the statistical oracle for the
   device LLR.
 * llr_ref_s2.npz -- the same for two S2 (rectangle) windows on a 4^4 lattice
-  (axis 2; every extent >= 3 so that no 1x2 rectangle wraps), R = 4.
+  (axis 2; every extent >= 3 so that no 1x2 rectangle wraps), R = 20.
 
 * llr2d_ref.npz -- the ANE2 table (cell centres, mean a1 and a2, sds, samples)
   of the unmodified reference llr2d executable (full mode, its own S(1080)
   table, one thread) on three cells of a 4^4 lattice along the S2 ridge that
-  one-dimensional windows at beta2 = 0 hold, with R = 4 repeats of its cold
+  one-dimensional windows at beta2 = 0 hold, with R = 20 repeats of its cold
   and hot passes.
 
     python tests/golden/make_golden.py --only llr     # one fixture only
@@ -332,24 +337,33 @@ def _ref_chain(job):
 # out of equilibrium), Ntherm 20, K 4, N 2.
 CHAINS_CONFIG1 = dict(D=4, Nt=4, Nx=4, beta=(0.0, 1.5, 0.1), K=10, N=100, Ntherm=100, seeds=list(range(3001, 3025)),
                       threads=1)
+# Config 1's couplings in equilibrium: the stated protocol (Ntherm 100) ends
+# while the hot start is still relaxing (the plaquette falls from -1.6 to
+# -2.91 over its 1,100 sweeps, most of it in the first 300), so its run means
+# compare two update orders' relaxation; with Ntherm 3000 both sit on the
+# plateau (-2.915) and the runs sample the stationary distribution.
+CHAINS_CONFIG1_EQ = dict(D=4, Nt=4, Nx=4, beta=(0.0, 1.5, 0.1), K=10, N=100, Ntherm=3000,
+                         seeds=list(range(3101, 3133)), threads=1)
 CHAINS_CONFIG2 = dict(D=4, Nt=8, Nx=32, beta=(0.0, 1.0, 0.1), K=4, N=2, Ntherm=20, seeds=list(range(4001, 4013)),
                       threads=os.cpu_count() or 1, wl=8)
 
 
-def make_chains_baseline(which=("chains_config1.npz", "chains_config2.npz")):
-    """chains_config1.npz and chains_config2.npz: per-run GMES/RMES of the
-    unmodified reference (its Makefile flags, NHIT 10, its own mys1080-v4):
-    config 1 one thread per run (runs in parallel), the config-2 lattice with
-    all cores per run.  Stored per run: the measurement series of ReP, ImP,
+def make_chains_baseline(which=("chains_config1.npz", "chains_config1_eq.npz", "chains_config2.npz")):
+    """chains_config1.npz, chains_config1_eq.npz and chains_config2.npz:
+    per-run GMES/RMES of the unmodified reference (its Makefile flags, NHIT
+    10, its own mys1080-v4): config 1 (as stated and in equilibrium) one
+    thread per run (runs in parallel), the config-2 lattice with all cores per
+    run.  Stored per run: the measurement series of ReP, ImP,
     plaq, rect and the Wilson grid (config 2: its first 8 x 8)."""
     from concurrent.futures import ProcessPoolExecutor
     table = os.path.join(REF_DIR, "groups", "mys1080-v4")
-    for name, C in (("chains_config1.npz", CHAINS_CONFIG1), ("chains_config2.npz", CHAINS_CONFIG2)):
+    for name, C in (("chains_config1.npz", CHAINS_CONFIG1), ("chains_config1_eq.npz", CHAINS_CONFIG1_EQ),
+                    ("chains_config2.npz", CHAINS_CONFIG2)):
         if name not in which:
             continue
         jobs = [(table, C["D"], C["Nt"], C["Nx"], C["beta"], s, C["K"], C["N"], C["Ntherm"], C["threads"])
                 for s in C["seeds"]]
-        workers = max(1, (os.cpu_count() or 1) // C["threads"])
+        workers = max(1, int(os.environ.get("GOLDEN_WORKERS", (os.cpu_count() or 1) // C["threads"])))
         with ProcessPoolExecutor(workers) as ex:
             res = list(ex.map(_ref_chain, jobs))
         out = {}
@@ -358,7 +372,7 @@ def make_chains_baseline(which=("chains_config1.npz", "chains_config2.npz")):
             grid = g[:, 4:].reshape(len(g), C["Nx"], C["Nt"])
             if wl:
                 grid = grid[:, :wl, :wl]
-            out[f"series_{seed}"] = np.concatenate([g[:, 1:4], rm[:, 2:3], grid.reshape(len(g), -1)], 1)
+            out[f"series_{seed}"] = np.concatenate([g[:, 1:4], rm[:, 1:2], grid.reshape(len(g), -1)], 1)
             out[f"acc_{seed}"] = np.array(acc)
             print(f"{name} seed {seed}: {len(g)} measurements, <plaq> {g[:, 3].mean():.5f}, acceptance {acc:.3f}")
         out["columns"] = np.array("ReP ImP plaq rect W[k][l] (k spatial outer, l temporal inner)")
@@ -434,7 +448,8 @@ def main():
     import argparse
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", choices=["iso", "staples", "sweeps", "reftables", "chains", "chains_baseline",
-                                       "chains_config1", "chains_config2", "llr", "llr_s2", "llr2d"])
+                                       "chains_config1", "chains_config1_eq", "chains_config2", "llr", "llr_s2",
+                                       "llr2d"])
     ap.add_argument("--skip-build", action="store_true", help="use oracle/_ref as built (parallel invocations)")
     args = ap.parse_args()
     only = args.only
@@ -454,7 +469,7 @@ def main():
         make_chains()
     if only in (None, "chains_baseline"):
         make_chains_baseline()
-    if only in ("chains_config1", "chains_config2"):
+    if only in ("chains_config1", "chains_config1_eq", "chains_config2"):
         make_chains_baseline((only + ".npz",))
     if only in (None, "llr"):
         make_llr()

@@ -7,6 +7,14 @@ starts; tests/golden/make_golden.py):
 * chains_config1.npz -- config 1 as stated: 4^4, beta = (0, 1.5, 0.1), Ntherm
   100, K 10, N 100, the full 4 x 4 Wilson grid; 24 runs, one thread each (so
   each run is the reference's serial update order).
+* chains_config1_eq.npz -- the same couplings after 3,000 thermalisation
+  sweeps; 32 runs.  As stated, config 1 ends while the hot start is still
+  relaxing: the plaquette falls from -1.6 to -2.91 over the 1,100 sweeps (to
+  -2.91 only at the end), so its run means compare two update orders' approach
+  to equilibrium (the reference's serial order, the engine's colour phases:
+  both valid, not equally fast per sweep) as well as the distribution; with
+  3,000 sweeps first both sample the plateau (-2.915), the stationary
+  distribution the two must share.
 * chains_config2.npz -- the config-2 lattice, 32^3 x 8, with the Polyakov loop
   and the 8 x 8 Wilson grid, in the disordered phase (beta = (0, 1.0, 0.1);
   Ntherm 20, K 4, N 2); 12 runs with all cores (the reference's OpenMP build).
@@ -18,12 +26,19 @@ error of each side's mean is the spread of its per-run means over
 sqrt(runs), whatever the autocorrelation inside a run.  z = (engine -
 reference) / combined error, per observable.
 
-Bars.  Config 1 (20 observables): every |z| < 2, and the fraction within 1
-is printed beside the 68% expected.  Config-2 lattice (68 observables, most
-of them large Wilson loops that are zero within noise): with that many
-comparisons a few beyond 2 are expected by chance (P(all 68 < 2) ~ 4% for
-independent ones), so every |z| < 3.5 (a 3% family-wise rate), at least 85%
-within 2 and at least half within 1."""
+The observables of one run are strongly correlated (the Wilson loops of an
+ordered 4^4 lattice move together; plaquette and rectangle have correlation
+1.0 across runs), so the fraction of |z| below 1 is not a count of
+independent trials: it is printed beside the 68% expected, and the joint
+test is Hotelling's two-sample T^2 on a well-conditioned subset (ReP, ImP,
+plaquette, W[1][1], W[3][3]).
+
+Bars.  Config 1 (20 observables), as stated and in equilibrium: every
+|z| < 2 and the T^2 test's p-value above 0.01.  Config-2 lattice (68
+observables, most of them large Wilson loops that are zero within noise):
+with that many comparisons a few beyond 2 are expected by chance
+(P(all 68 < 2) ~ 4% for independent ones), so every |z| < 3.5 (a 3%
+family-wise rate), at least 85% within 2 and at least half within 1."""
 import numpy as np
 import pytest
 
@@ -58,20 +73,38 @@ def zscores(ref, ours):
     return (ours.mean(0) - ref.mean(0)) / np.where(se > 0, se, 1)
 
 
+def hotelling_p(ref, ours, cols=(0, 1, 2, 9, 19)):
+    """p-value of Hotelling's two-sample T^2 test of equal means on the
+    columns `cols` (ReP, ImP, plaquette, W[1][1], W[3][3] of config 1)."""
+    from scipy.stats import f as fdist
+    a, b = ref[:, list(cols)], ours[:, list(cols)]
+    n1, n2, p = len(a), len(b), a.shape[1]
+    S = ((n1 - 1) * np.cov(a, rowvar=False) + (n2 - 1) * np.cov(b, rowvar=False)) / (n1 + n2 - 2)
+    d = a.mean(0) - b.mean(0)
+    t2 = n1 * n2 / (n1 + n2) * d @ np.linalg.solve(S, d)
+    return float(fdist.sf((n1 + n2 - p - 1) / (p * (n1 + n2 - 2)) * t2, p, n1 + n2 - p - 1))
+
+
 def params(fix):
     import ast
     return ast.literal_eval(str(fix["params"]).split(" table=")[0])
 
 
-def test_config1_within_two_sigma_of_reference(engine, ref_table):
-    fix = golden("chains_config1.npz")
+@pytest.mark.parametrize("fixture,seeds", [("chains_config1.npz", range(5001, 5025)),
+                                           ("chains_config1_eq.npz", range(5101, 5133))],
+                         ids=["as-stated", "equilibrium"])
+def test_config1_within_two_sigma_of_reference(engine, ref_table, fixture, seeds):
+    fix = golden(fixture)
     C = params(fix)
     ref = np.array([fix[f"series_{s}"].mean(0) for s in fix["seeds"]])
-    ours = run_engine(engine, ref_table, C, range(5001, 5025), 0)
+    ours = run_engine(engine, ref_table, C, seeds, 0)
     z = zscores(ref, ours)
-    print(f"config 1: z = {np.round(z, 2).tolist()}; within 1 sigma {np.mean(np.abs(z) < 1):.2f} (68% expected)")
+    p = hotelling_p(ref, ours)
+    print(f"{fixture}: z = {np.round(z, 2).tolist()}; within 1 sigma {np.mean(np.abs(z) < 1):.2f} "
+          f"(68% expected for independent observables); Hotelling T^2 p = {p:.3f}")
     assert ours.shape[1] == ref.shape[1] == 4 + 16
     assert np.all(np.abs(z) < 2.0), z
+    assert p > 0.01, p
 
 
 def test_config2_lattice_agrees_with_reference(engine, ref_table):
