@@ -34,7 +34,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 BOUNDS = os.environ.get("DYM_BOUNDS_CHECK") == "1"
 if BOUNDS:
     OBJDIR = os.path.join(PKG, "_build_bounds")
-CU_SOURCES = ["sweep.cu", "measure.cu", "capi.cu", "probe.cu", "llr.cu", "batch.cu", "serve.cu", "noalloc.cu"]
+CU_SOURCES = ["sweep.cu", "sweep_mixed.cu", "sweep_vt.cu", "measure.cu", "capi.cu", "probe.cu", "llr.cu", "batch.cu",
+              "serve.cu", "noalloc.cu"]
 CXX_SOURCES = ["group.cpp", "schedule.cpp", "checkpoint.cpp"]
 
 

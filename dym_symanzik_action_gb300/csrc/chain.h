@@ -38,6 +38,10 @@ struct SweepArgs {
   const uint32_t* xyz;  // coordinates of sites[k], 8 bits per axis (already offset)
   const int16_t* val16;  // value-table kernel: fixed-point ReTr of every element
   int hit_unroll;        // mixed kernels: hits per group of draws computed ahead (1, 2, 5 or 10)
+  int lanes_per_link;    // value-table kernel: threads sharing a link visit (1 or 2)
+  // dym_sweep_host: the upload check's first bad index (~0 when none); a sweep
+  // launch after a refused upload does nothing.  Null for the other calls.
+  const unsigned long long* skip;
 };
 
 struct ChainDev {
@@ -88,6 +92,10 @@ constexpr uint32_t kMixedMaxP = 2048;  // 16-bit packed entries: element ids in 
 constexpr int kMixedMaxExtent = 256;   // coordinates packed 8 bits per axis
 constexpr int kMixedMaxThreads = 512;
 constexpr int kDefaultHitUnroll = 1;
+constexpr int kDefaultLanesPerLink = 1;
+// Threads per block of the two-lanes-per-link value-table kernel at most
+// (two lanes for each of 448 links; 72 registers a thread).
+constexpr int kVt2MaxThreads = 896;
 constexpr double kDefaultVtMaxAccept = 0.01;
 cudaError_t launch_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uint64_t seed, cudaStream_t s);
 cudaError_t launch_fill(uint16_t* links, size_t n, uint16_t v, cudaStream_t s);

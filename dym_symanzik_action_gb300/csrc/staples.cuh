@@ -241,4 +241,65 @@ __device__ __forceinline__ void build_u_tree(uint32_t i, const SiteGeo<D>& geo, 
 #undef DYM_S
 }
 
+// One side of the u_j = s_j * b of build_u_tree, for a lane pair sharing
+// link (i, DIR): per plane (DIR, f), f = e_d1, the staples on the +f side
+// (back false: plaquette 1 and rectangles 1-3 of build_staples) or on the -f
+// side (back true: plaquette 2 and rectangles 4-6, which are the +f staples
+// with f reflected).  With sg = +1 or -1 and F(y, s) the step from y along
+// s f (a[y,f] for s = +1, a[y-f,f]^-1 for s = -1), the four elements are
+//   plaquette    F(i+e, sg) a[i+sg f,d]^-1 F(i+sg f, -sg) b
+//   rectangle 1  F(i+e, sg) F(i+e+sg f, sg) a[i+2sg f,d]^-1 F(i+2sg f, -sg) F(i+sg f, -sg) b
+//   rectangle 2  a[i+e,d] F(i+2e, sg) a[i+e+sg f,d]^-1 a[i+sg f,d]^-1 F(i+sg f, -sg) b
+//   rectangle 3  F(i+e, sg) a[i+sg f,d]^-1 a[i+sg f-e,d]^-1 F(i-e+sg f, -sg) a[i-e,d] b
+// (for sg = -1 these are rectangles 4, 5 and 6).  Both lanes run the same
+// instructions: the side only selects site offsets and which loaded links
+// are inverted.  12 link loads and 15 table products per plane and lane.
+// up gets D-1 plaquette terms, ur 3(D-1) rectangle terms, plane by plane.
+template <int D, int DIR, class Tab, class LD>
+__device__ __forceinline__ void build_u_half(uint32_t i, const SiteGeo<D>& geo, const Tab& T, LD ld, uint32_t b,
+                                             bool back, uint32_t* up /* D-1 */, uint32_t* ur /* 3(D-1) */) {
+  int k = 0, kr = 0;
+#pragma unroll
+  for (int d1 = 0; d1 < D; ++d1) {
+    if (d1 == DIR) continue;
+    // f offsets of this side: +-1, +-2 and the F steps' site shifts.
+    const int* fo = geo.off[d1];
+    const int f1 = back ? fo[1] : fo[3];    // sg f
+    const int f2 = back ? fo[0] : fo[4];    // 2 sg f
+    const int fF = back ? fo[1] : fo[2];    // site of F(y, sg): y - f or y
+    const int fF1 = back ? fo[0] : fo[3];   // site of F(y + sg f, sg)
+    const int fB = back ? fo[1] : fo[2];    // site of F(y + sg f, -sg): y - f or y
+    const int fB2 = back ? fo[0] : fo[3];   // site of F(y + 2 sg f, -sg)
+    const int* eo = geo.off[DIR];
+    const int ip = (int)i;
+    auto maybe_inv = [&](uint32_t x, bool inv) -> uint32_t {
+      const uint32_t xi = T.iv(x);
+      return inv ? xi : x;
+    };
+    // F(., sg) is inverted on the -f side, F(., -sg) on the +f side.
+    const uint32_t F1 = maybe_inv(ld((uint32_t)(ip + eo[3] + fF), d1), back);     // F(i+e, sg)
+    const uint32_t F2 = maybe_inv(ld((uint32_t)(ip + eo[3] + fF1), d1), back);    // F(i+e+sg f, sg)
+    const uint32_t F3 = maybe_inv(ld((uint32_t)(ip + eo[4] + fF), d1), back);     // F(i+2e, sg)
+    const uint32_t G1 = maybe_inv(ld((uint32_t)(ip + fB), d1), !back);            // F(i+sg f, -sg)
+    const uint32_t G2 = maybe_inv(ld((uint32_t)(ip + fB2), d1), !back);           // F(i+2sg f, -sg)
+    const uint32_t G3 = maybe_inv(ld((uint32_t)(ip + eo[1] + fB), d1), !back);    // F(i-e+sg f, -sg)
+    const uint32_t Bd = T.iv(ld((uint32_t)(ip + f1), DIR));                        // a[i+sg f,d]^-1
+    const uint32_t B2 = T.iv(ld((uint32_t)(ip + f2), DIR));                        // a[i+2sg f,d]^-1
+    const uint32_t Be = T.iv(ld((uint32_t)(ip + eo[3] + f1), DIR));                // a[i+e+sg f,d]^-1
+    const uint32_t Bm = T.iv(ld((uint32_t)(ip + eo[1] + f1), DIR));                // a[i+sg f-e,d]^-1
+    const uint32_t Ae = ld((uint32_t)(ip + eo[3]), DIR);                           // a[i+e,d]
+    const uint32_t Am = ld((uint32_t)(ip + eo[1]), DIR);                           // a[i-e,d]
+    const uint32_t Cq = T.mul(G1, b);
+    const uint32_t q2 = T.mul(Am, b);
+    const uint32_t h = T.mul(F1, Bd);
+    const uint32_t r1a = T.mul(F1, F2), r1b = T.mul(B2, G2);
+    const uint32_t r2a = T.mul(Ae, F3), r2b = T.mul(Be, Bd);
+    const uint32_t r3b = T.mul(Bm, G3);
+    up[k++] = T.mul(h, Cq);
+    ur[kr++] = T.mul(T.mul(r1a, r1b), Cq);
+    ur[kr++] = T.mul(T.mul(r2a, r2b), Cq);
+    ur[kr++] = T.mul(T.mul(h, r3b), q2);
+  }
+}
+
 }  // namespace dym

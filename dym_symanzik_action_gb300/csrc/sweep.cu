@@ -24,7 +24,10 @@
 //    rounding noise inside a class, as the reference's shipped files do).
 //
 //  * k_sweep_vt     -- k_sweep_mixed with the shared table holding fixed-point
-//    values instead of elements (fastest while accepted moves are rare).
+//    values instead of elements (fastest while accepted moves are rare).//
+// This file holds the FP64 kernels, the lattice set-up kernels and their
+// launchers; the mixed-precision kernels are in sweep_mixed.cu and
+// sweep_vt.cu.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,6 +35,7 @@
 #include "chain.h"
 #include "dym_core.h"
 #include "staples.cuh"
+#include "sweep_launch.cuh"
 #include "visit.cuh"
 
 namespace dym {
@@ -53,6 +57,7 @@ __global__ void __launch_bounds__(256) k_sweep_direct(SweepArgs a) {
   pdl_launch_dependents();
   pdl_wait_prior();
   __syncthreads();
+  if (sweep_skipped(a)) return;
 
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned hits = 0, accs = 0;
@@ -118,107 +123,13 @@ __global__ void __launch_bounds__(256) k_sweep_sub(SweepArgs a, const uint16_t* 
   pdl_launch_dependents();
   pdl_wait_prior();
   __syncthreads();
+  if (sweep_skipped(a)) return;
 
   unsigned hits = 0, accs = 0;
   // One wave of blocks, each staging the table once and visiting several links.
   for (uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x; tid < a.n; tid += gridDim.x * blockDim.x)
     visit_sub<D, DIR>(a, a.sites[tid], a.sweep, s_retr, s_inv, s_sub, hits, accs);
   flush_counters(a.counters, hits, accs, 0);
-}
-
-// Shared memory: ReTr (FP64) | class values (int32 fixed point) | inverses |
-// packed sub-table (entries of type E, starting at mixed_psub_offset) |
-// element classes.
-template <int D, int DIR, class E, int HU>
-__global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_mixed(SweepArgs a, const E* __restrict__ psub) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  double* s_retr = reinterpret_cast<double*>(smem);
-  int32_t* s_cfix = reinterpret_cast<int32_t*>(s_retr + a.P);
-  uint16_t* s_inv = reinterpret_cast<uint16_t*>(s_cfix + kMixedMaxCls);
-  E* s_psub = reinterpret_cast<E*>(smem + mixed_psub_offset(a.P, sizeof(E)));
-  uint8_t* s_cls = reinterpret_cast<uint8_t*>(s_psub + (size_t)a.npool * a.P);
-  // The staging copies npool * P entries as halfwords.
-  stage_sub_tables(a.retr, a.inv, reinterpret_cast<const uint16_t*>(psub), a.P, a.npool * (uint32_t)(sizeof(E) / 2),
-                   s_retr, s_inv, reinterpret_cast<uint16_t*>(s_psub));
-  for (uint32_t t = threadIdx.x; t < a.P; t += blockDim.x) s_cls[t] = a.cls8[t];
-  if (threadIdx.x < kMixedMaxCls) s_cfix[threadIdx.x] = a.cfix[threadIdx.x];
-  uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t i_next = 0, xyz_next = 0;  // constant site list: fetched before the wait
-  if (tid < a.n) {
-    i_next = a.sites[tid];
-    xyz_next = a.xyz[tid];
-  }
-  pdl_launch_dependents();
-  pdl_wait_prior();
-  __syncthreads();
-
-  unsigned hits = 0, accs = 0, rechecks = 0;
-  float max_err = 0.0f;
-  for (; tid < a.n; tid += gridDim.x * blockDim.x) {
-    const uint32_t i = i_next, xyz = xyz_next;
-    const uint32_t nt = tid + gridDim.x * blockDim.x;
-    if (nt < a.n) {
-      i_next = a.sites[nt];
-      xyz_next = a.xyz[nt];
-    }
-    visit_mixed<D, DIR, E, HU>(a, i, xyz, a.sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks,
-                               max_err);
-  }
-  flush_counters(a.counters, hits, accs, rechecks);
-  flush_max_err(a.counters + 3, max_err);
-}
-
-// Value-table form of k_sweep_mixed (visit.cuh vt_prepare/vt_hits).  Shared
-// memory: value table (element-major, padded to 16 bytes) | ReTr (FP64) |
-// inverses | element values | pool.  The value table is copied with cp.async
-// and the small tables with plain loads; none of them is written by the
-// previous colour phase, so the staging runs before the programmatic wait and
-// overlaps the previous launch's tail when launched with PDL.
-template <int D, int DIR, int HU>
-__global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_vt(SweepArgs a, const int16_t* __restrict__ vsub) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const size_t vbytes = vt_table_bytes(a.P, a.npool);
-  int16_t* s_vsub = reinterpret_cast<int16_t*>(smem);
-  double* s_retr = reinterpret_cast<double*>(smem + vbytes);
-  uint16_t* s_inv = reinterpret_cast<uint16_t*>(s_retr + a.P);
-  int16_t* s_val = reinterpret_cast<int16_t*>(s_inv + a.P);
-  uint16_t* s_pool = reinterpret_cast<uint16_t*>(s_val + a.P);
-  cp_async_stage(s_vsub, vsub, vbytes);
-  for (uint32_t t = threadIdx.x; t < a.P; t += blockDim.x) {
-    s_retr[t] = a.retr[t];
-    s_inv[t] = a.inv[t];
-    s_val[t] = a.val16[t];
-  }
-  for (uint32_t t = threadIdx.x; t < a.npool; t += blockDim.x) s_pool[t] = a.pool[t];
-  // The site list and coordinates are constant: fetch this thread's first
-  // entry before the wait as well.
-  uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t i_next = 0, xyz_next = 0;
-  if (tid < a.n) {
-    i_next = a.sites[tid];
-    xyz_next = a.xyz[tid];
-  }
-  pdl_launch_dependents();
-  pdl_wait_prior();  // the previous phase's links are final from here on
-  cp_async_wait_all();
-  __syncthreads();
-  constexpr int NT = 8 * (D - 1);
-  unsigned hits = 0, accs = 0, rechecks = 0;
-  float max_err = 0.0f;
-  for (; tid < a.n; tid += gridDim.x * blockDim.x) {
-    uint32_t u[NT], b;
-    int32_t R, M;
-    const uint32_t i = i_next, xyz = xyz_next;
-    const uint32_t nt = tid + gridDim.x * blockDim.x;
-    if (nt < a.n) {
-      i_next = a.sites[nt];
-      xyz_next = a.xyz[nt];
-    }
-    vt_prepare<D, DIR>(a, i, xyz, s_inv, s_val, u, b, R, M);
-    vt_hits<D, DIR, HU>(a, i, a.sweep, s_retr, s_inv, s_vsub, s_pool, u, b, R, M, hits, accs, rechecks, max_err);
-  }
-  flush_counters(a.counters, hits, accs, rechecks);
-  flush_max_err(a.counters + 3, max_err);
 }
 
 __global__ void k_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uint64_t seed) {
@@ -298,30 +209,6 @@ __global__ void k_staples(SweepArgs a, const uint32_t* sites, uint32_t n, uint16
   for (int j = 0; j < NR; ++j) out[(size_t)tid * (NS + NR) + NS + j] = (uint16_t)re[j];
 }
 
-// Launch one colour phase with programmatic stream serialization: the next
-// phase's blocks may start, and stage their tables, as this phase's blocks
-// retire; every sweep kernel waits for the whole previous grid (pdl_wait_prior)
-// before it reads a site list entry or a link.
-template <class... K, class... A>
-cudaError_t launch_phase(void (*fn)(K...), unsigned grid, unsigned threads, size_t smem, cudaStream_t s,
-                         A... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(threads);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, fn, args...);
-}
-
-// Hit-unroll factors the mixed kernels are built for (hits whose draws are
-// computed ahead as a group, visit.cuh HitDraws): 1, 2, 5, 10.
-int hit_unroll_index(int hu) { return hu >= 10 ? 3 : hu >= 5 ? 2 : hu >= 2 ? 1 : 0; }
-
 template <int D>
 cudaError_t direct_dispatch(int dir, const SweepArgs& a, cudaStream_t s) {
   const size_t smem = (size_t)a.P * 8 + (size_t)a.P * 2 + (size_t)a.npool * 2 + 16;
@@ -368,65 +255,6 @@ cudaError_t sub_dispatch(int dir, const SweepArgs& a, const uint16_t* sub, cudaS
   return launch_phase(fn, grid, 256, smem, s, a, sub);
 }
 
-template <int D, class E>
-cudaError_t mixed_dispatch(int dir, const SweepArgs& a, const E* psub, cudaStream_t s) {
-  const size_t smem = mixed_smem_bytes(a.P, a.npool, sizeof(E));
-  void (*fn)(SweepArgs, const E*) = nullptr;
-  switch (hit_unroll_index(a.hit_unroll) * 4 + dir) {
-#define DYM_MIXED_CASE(q, hu, d) \
-    case 4 * q + d: if (D > d) fn = k_sweep_mixed<D, (D > d ? d : 0), E, hu>; break;
-#define DYM_MIXED_HU(q, hu) DYM_MIXED_CASE(q, hu, 0) DYM_MIXED_CASE(q, hu, 1) DYM_MIXED_CASE(q, hu, 2) \
-    DYM_MIXED_CASE(q, hu, 3)
-    DYM_MIXED_HU(0, 1) DYM_MIXED_HU(1, 2) DYM_MIXED_HU(2, 5) DYM_MIXED_HU(3, 10)
-#undef DYM_MIXED_HU
-#undef DYM_MIXED_CASE
-  }
-  if (!fn) return cudaErrorInvalidValue;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-  }
-  if (a.n == 0) return cudaSuccess;
-  // One block per SM (the shared tables allow no more), as many warps per
-  // block as the phase fills evenly across the SMs, 128..512 threads.
-  int dev = 0, sms = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e != cudaSuccess) return e;
-  const uint32_t per = (a.n + (uint32_t)sms - 1) / (uint32_t)sms;
-  const unsigned threads = std::min<unsigned>(kMixedMaxThreads, std::max<unsigned>(128, (per + 31) / 32 * 32));
-  // One wave: a phase larger than the SMs' blocks is walked by each block in
-  // turn (the kernel's grid-stride loop), so each SM stages its tables once.
-  const unsigned grid = std::min<unsigned>((a.n + threads - 1) / threads, (unsigned)sms);
-  return launch_phase(fn, grid, threads, smem, s, a, psub);
-}
-
-template <int D>
-cudaError_t vt_dispatch(int dir, const SweepArgs& a, const int16_t* vsub, cudaStream_t s) {
-  const size_t smem = vt_smem_bytes(a.P, a.npool);
-  void (*fn)(SweepArgs, const int16_t*) = nullptr;
-  switch (hit_unroll_index(a.hit_unroll) * 4 + dir) {
-#define DYM_VT_CASE(q, hu, d) \
-    case 4 * q + d: if (D > d) fn = k_sweep_vt<D, (D > d ? d : 0), hu>; break;
-#define DYM_VT_HU(q, hu) DYM_VT_CASE(q, hu, 0) DYM_VT_CASE(q, hu, 1) DYM_VT_CASE(q, hu, 2) DYM_VT_CASE(q, hu, 3)
-    DYM_VT_HU(0, 1) DYM_VT_HU(1, 2) DYM_VT_HU(2, 5) DYM_VT_HU(3, 10)
-#undef DYM_VT_HU
-#undef DYM_VT_CASE
-  }
-  if (!fn) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  if (a.n == 0) return cudaSuccess;
-  int dev = 0, sms = 0;
-  e = cudaGetDevice(&dev);
-  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e != cudaSuccess) return e;
-  const uint32_t per = (a.n + (uint32_t)sms - 1) / (uint32_t)sms;
-  const unsigned threads = std::min<unsigned>(kMixedMaxThreads, std::max<unsigned>(128, (per + 31) / 32 * 32));
-  const unsigned grid = std::min<unsigned>((a.n + threads - 1) / threads, (unsigned)sms);  // one wave, as above
-  return launch_phase(fn, grid, threads, smem, s, a, vsub);
-}
-
 template <int D>
 cudaError_t staples_dispatch(int dir, const SweepArgs& a, const uint32_t* sites, uint32_t n, uint16_t* out,
                              cudaStream_t s) {
@@ -455,21 +283,6 @@ size_t mixed_smem_bytes(uint32_t P, uint32_t npool, size_t entry) {
 
 size_t vt_smem_bytes(uint32_t P, uint32_t npool) {
   return vt_table_bytes(P, npool) + (size_t)P * 8 + (size_t)P * 2 + (size_t)P * 2 + (size_t)npool * 2 + 16;
-}
-
-cudaError_t launch_sweep_vt(int D, int dir, const SweepArgs& a, const int16_t* vsub, cudaStream_t s) {
-  if (D == 4) return vt_dispatch<4>(dir, a, vsub, s);
-  return cudaErrorInvalidValue;
-}
-
-cudaError_t launch_sweep_mixed(int D, int dir, const SweepArgs& a, const uint16_t* psub, cudaStream_t s) {
-  if (D == 4) return mixed_dispatch<4, uint16_t>(dir, a, psub, s);  // four dimensions only, as launch_sweep_sub
-  return cudaErrorInvalidValue;
-}
-
-cudaError_t launch_sweep_mixed_wide(int D, int dir, const SweepArgs& a, const uint32_t* psub, cudaStream_t s) {
-  if (D == 4) return mixed_dispatch<4, uint32_t>(dir, a, psub, s);
-  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_sweep_direct(int D, int dir, const SweepArgs& a, cudaStream_t s) {

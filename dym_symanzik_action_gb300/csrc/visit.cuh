@@ -28,9 +28,12 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // copies of the sub-table start on 16 bytes its whole 16-byte chunks go by
 // cp.async, so the block's copy costs about one L2 round trip instead of one
 // per eight words a thread moves; the caller's __syncthreads() publishes it.
+// wait false leaves those chunks in flight: the caller then publishes ReTr
+// and the inverses with one __syncthreads() and the sub-table with
+// cp_async_wait_all() and another.
 __device__ __forceinline__ void stage_sub_tables(const double* retr, const uint16_t* inv, const uint16_t* sub,
                                                  uint32_t P, uint32_t npool, double* s_retr, uint16_t* s_inv,
-                                                 uint16_t* s_sub) {
+                                                 uint16_t* s_sub, bool wait = true) {
   const uint32_t nsub = npool * P;
   const bool async = ((reinterpret_cast<uintptr_t>(sub) | (uintptr_t)__cvta_generic_to_shared(s_sub)) & 15u) == 0;
   if (async) {
@@ -43,7 +46,7 @@ __device__ __forceinline__ void stage_sub_tables(const double* retr, const uint1
     s_inv[t] = inv[t];
   }
   if (async) {
-    cp_async_wait_all();
+    if (wait) cp_async_wait_all();
   } else if ((P & 1u) == 0) {
     const uint32_t* src = reinterpret_cast<const uint32_t*>(sub);
     uint32_t* dst = reinterpret_cast<uint32_t*>(s_sub);
@@ -63,6 +66,11 @@ __device__ __forceinline__ void pdl_launch_dependents() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 __device__ __forceinline__ void pdl_wait_prior() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Whether this sweep launch is to do nothing because the upload before it in
+// the same dym_sweep_host call was refused (SweepArgs::skip).  Read after the
+// programmatic wait, so the upload check has completed.
+__device__ __forceinline__ bool sweep_skipped(const SweepArgs& a) { return a.skip && *a.skip != ~0ull; }
 
 // The reference's FP64 actions of the current link value b and of a proposal
 // bnew (dym-mod-metro.cpp:166-181): beta0 + beta1 r1 + beta2 m1 with r1, m1 the
@@ -421,6 +429,176 @@ __device__ __forceinline__ void vt_hits(const SweepArgs& a, uint32_t i, uint32_t
     }
   }
   if (b != b0) a.links[(size_t)DIR * a.V + i] = (uint16_t)b;
+}
+
+// Two lanes per link (vt2): the value-table visit with a link's work split
+// over an adjacent lane pair.  Lane `back` (odd lane) holds the u_j of the -f
+// side of every plane (build_u_half), lane !back those of the +f side: 3(D-1)
+// terms each.  A hit's sums are the pair's two partial sums (two shuffles);
+// the pair draws two hits' random numbers at once, one hit per lane, and
+// exchanges them; both lanes then take the same decision from the same
+// integers, so the decisions, re-evaluations and counts are the one-lane
+// visit's (vt_hits) exactly.  `pm` is the pair's shuffle mask.
+__device__ __forceinline__ unsigned pair_mask() { return 3u << (threadIdx.x & 30u); }
+
+template <int D, int DIR>
+__device__ __forceinline__ void vt2_prepare(const SweepArgs& a, uint32_t i, uint32_t xyz, bool back, unsigned pm,
+                                            const uint16_t* s_inv, const int16_t* s_val, uint32_t* up, uint32_t* ur,
+                                            uint32_t& b, int32_t& R, int32_t& M) {
+  constexpr int NP = D - 1, NQ = 3 * (D - 1);
+  SiteGeo<D> geo;
+  site_geo_packed<D>(xyz, a.Nt, a.Nx, geo);
+  GlobalTab T{a.mult, s_inv, a.P};
+  const uint16_t* L = a.links;
+  const uint32_t V = a.V;
+  auto ld = [L, V](uint32_t s, int d) -> uint32_t { return __ldg(L + (size_t)d * V + s); };
+  b = a.links[(size_t)DIR * V + i];
+  build_u_half<D, DIR>(i, geo, T, ld, b, back, up, ur);
+  int32_t r = 0, m = 0;
+#pragma unroll
+  for (int j = 0; j < NP; ++j) r += s_val[up[j]];
+#pragma unroll
+  for (int j = 0; j < NQ; ++j) m += s_val[ur[j]];
+  R = r + __shfl_xor_sync(pm, r, 1);
+  M = m + __shfl_xor_sync(pm, m, 1);
+}
+
+// exact_actions for a lane pair (four dimensions): the FP64 sums of
+// ReTr[bnew s_j] (and of ReTr[b s_j] when need_old) over the pair's 24 terms,
+// added in build_u_tree's order (plaquettes plane by plane, +f side then -f
+// side; rectangles plane by plane, 1-3 then 4-6), so that both lanes get the
+// reference's bits.  Each lane evaluates its own terms and receives its
+// partner's by shuffles, one term pair at a time.  Not inlined: a hit comes
+// here about once in 10^5, and the call keeps this path's registers out of
+// the hit loop's allocation; the terms are passed by value (an array would
+// have to live in local memory).
+struct ActPair {
+  double oldact, newact;
+};
+
+static __device__ __noinline__ ActPair vt2_exact4(const uint16_t* __restrict__ mult, uint32_t P,
+                                                  const uint16_t* s_inv, const double* s_retr, double beta0,
+                                                  double beta1, double beta2, bool back, unsigned pm, uint32_t p0,
+                                                  uint32_t p1, uint32_t p2, uint32_t q0, uint32_t q1, uint32_t q2,
+                                                  uint32_t q3, uint32_t q4, uint32_t q5, uint32_t q6, uint32_t q7,
+                                                  uint32_t q8, uint32_t b, uint32_t bnew, bool need_old,
+                                                  double oldact) {
+  const uint32_t bi = s_inv[b];
+  double r1 = 0, m1 = 0, r1n = 0, m1n = 0;
+  // own term of u and the partner's, as (+f side, -f side)
+  auto pair_terms = [&](uint32_t u, double& fo, double& bo, double& fn, double& bn) {
+    const uint32_t sj = __ldg(mult + u * P + bi);
+    const double vn = s_retr[__ldg(mult + bnew * P + sj)];
+    const double vo = need_old ? s_retr[__ldg(mult + b * P + sj)] : 0.0;
+    const double pn = __shfl_xor_sync(pm, vn, 1), po = __shfl_xor_sync(pm, vo, 1);
+    fn = back ? pn : vn;
+    bn = back ? vn : pn;
+    fo = back ? po : vo;
+    bo = back ? vo : po;
+  };
+  const uint32_t up[3] = {p0, p1, p2};
+  const uint32_t ur[9] = {q0, q1, q2, q3, q4, q5, q6, q7, q8};
+#pragma unroll
+  for (int p = 0; p < 3; ++p) {
+    double fo, bo, fn, bn;
+    pair_terms(up[p], fo, bo, fn, bn);
+    r1n = DYM_ADD(DYM_ADD(r1n, fn), bn);
+    r1 = DYM_ADD(DYM_ADD(r1, fo), bo);
+  }
+#pragma unroll
+  for (int p = 0; p < 3; ++p) {
+    double fo[3], bo[3], fn[3], bn[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) pair_terms(ur[3 * p + r], fo[r], bo[r], fn[r], bn[r]);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      m1n = DYM_ADD(m1n, fn[r]);
+      m1 = DYM_ADD(m1, fo[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      m1n = DYM_ADD(m1n, bn[r]);
+      m1 = DYM_ADD(m1, bo[r]);
+    }
+  }
+  ActPair out;
+  out.oldact = need_old ? dym_action(beta0, beta1, beta2, r1, m1) : oldact;
+  out.newact = dym_action(beta0, beta1, beta2, r1n, m1n);
+  return out;
+}
+
+template <int D, int DIR>
+__device__ __forceinline__ void vt2_hits(const SweepArgs& a, uint32_t i, uint32_t sweep, bool back, unsigned pm,
+                                         const double* s_retr, const uint16_t* s_inv, const int16_t* s_vsub,
+                                         const uint16_t* s_pool, uint32_t* up, uint32_t* ur, uint32_t b, int32_t R,
+                                         int32_t M, unsigned& hits, unsigned& accs, unsigned& rechecks,
+                                         float& max_err) {
+  constexpr int NP = D - 1, NQ = 3 * (D - 1);
+  const uint32_t b0 = b;
+  const uint16_t* __restrict__ mult = a.mult;
+  const uint32_t P = a.P, np = a.npool;
+  double oldact = 0.0;
+  bool old_ok = false;
+  for (int h0 = 0; h0 < a.nhit; h0 += 2) {
+    // This lane draws hit h0 + back; the pair swaps them.
+    const dym_u32x4 rr = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h0 + (back ? 1u : 0u), DYM_TAG_METRO);
+    const uint32_t kown = dym_pick(rr.v[0], np);
+    const float town = -__logf(__fmaf_rn((float)rr.v[1], 0x1p-32f, (float)(rr.v[2] >> 11) * 0x1p-53f));
+    const uint32_t koth = __shfl_xor_sync(pm, kown, 1);
+    const float toth = __shfl_xor_sync(pm, town, 1);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (q == 1 && h0 + 1 >= a.nhit) break;
+      const bool mine = (q == 1) == back;
+      const uint32_t k = mine ? kown : koth;
+      const float t = mine ? town : toth;
+      const int16_t* col = s_vsub + k;
+      int32_t rp = 0, mp = 0;
+#pragma unroll
+      for (int j = 0; j < NP; ++j) rp += col[up[j] * np];
+#pragma unroll
+      for (int j = 0; j < NQ; ++j) mp += col[ur[j] * np];
+      const int32_t Rn = rp + __shfl_xor_sync(pm, rp, 1), Mn = mp + __shfl_xor_sync(pm, mp, 1);
+      const float ds = __fmaf_rn(a.b2f, (float)(Mn - M), __fmul_rn(a.b1f, (float)(Rn - R))) * a.dscale;
+      const float band = a.dmargin + __fmaf_rn(t, 0x1p-20f, 0x1p-19f);
+      bool acc;
+      bool exact = false;
+      if (ds < t - band) {
+        acc = true;
+      } else if (ds > t + band) {
+        acc = false;
+      } else {  // both lanes of the pair (same ds and t)
+        const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)(h0 + q), DYM_TAG_METRO);
+        const uint32_t g = s_pool[k];
+        static_assert(D == 4, "the pair's exact re-evaluation is written for four dimensions");
+        const ActPair ap = vt2_exact4(mult, P, s_inv, s_retr, a.beta0, a.beta1, a.beta2, back, pm, up[0], up[1],
+                                      up[2], ur[0], ur[1], ur[2], ur[3], ur[4], ur[5], ur[6], ur[7], ur[8], b,
+                                      __ldg(mult + b * P + g), !old_ok, oldact);
+        oldact = ap.oldact;
+        const double newact = ap.newact;
+        old_ok = true;
+        acc = dym_accept_fast(oldact, newact, dym_u53(r.v[1], r.v[2]));
+        max_err = fmaxf(max_err, fabsf(ds - (float)DYM_SUB(newact, oldact)));
+        rechecks += back ? 0u : 1u;
+        exact = true;
+        if (acc) oldact = newact;
+      }
+      hits += back ? 0u : 1u;
+      if (acc) {
+        const uint32_t g = s_pool[k];
+        b = __ldg(mult + b * P + g);
+#pragma unroll
+        for (int j = 0; j < NP; ++j) up[j] = __ldg(mult + up[j] * P + g);
+#pragma unroll
+        for (int j = 0; j < NQ; ++j) ur[j] = __ldg(mult + ur[j] * P + g);
+        R = Rn;
+        M = Mn;
+        old_ok = exact;
+        accs += back ? 0u : 1u;
+      }
+    }
+  }
+  if (!back && b != b0) a.links[(size_t)DIR * a.V + i] = (uint16_t)b;
 }
 
 // Largest |dS_fast - dS_fp64| seen at a re-evaluation, into the low word of

@@ -12,7 +12,9 @@ bit.
   isomorphism pi, the file's own trace rows) and every sweep is compared with
   the reference's staples and hit loop run on the files themselves
   (ref_tables.npz); once as run, once with DYM_RECHECK_ALL=1, which sends
-  every hit through the FP64 re-evaluation.
+  every hit through the FP64 re-evaluation; and both again with the
+  value-table kernel on every call after the first (DYM_VT_MAX_ACCEPT=1) and
+  two lanes per link (DYM_LANES_PER_LINK=2).
 * Every shipped table staged in baseline/_ref (or $REF_DIR) -- S(1080), BI,
   BT, BO, S648 (identity at id 4), S108, the SU(4) tables siii_360x4,
   svii_120x4, sviii_120x4 and si_60x4 -- is run by the engine and by the
@@ -34,13 +36,17 @@ pytestmark = pytest.mark.gpu
 KERNEL_MIXED, KERNEL_MIXED_VALUES = 3, 4
 
 
+@pytest.mark.parametrize("lanes", [1, 2], ids=["1lane", "2lanes-vt"])
 @pytest.mark.parametrize("recheck_all", [False, True], ids=["fast", "recheck-all"])
 @pytest.mark.parametrize("name", list(ref_table_cases().keys()))
-def test_fast_kernels_on_reference_files(engine, ref_table, monkeypatch, name, recheck_all):
+def test_fast_kernels_on_reference_files(engine, ref_table, monkeypatch, name, recheck_all, lanes):
     fname, D, Nt, Nx, beta, start, seed, nhit, nsw = ref_table_cases()[name]
     gold = golden("ref_tables.npz")
     if recheck_all:
         monkeypatch.setenv("DYM_RECHECK_ALL", "1")
+    if lanes == 2:
+        monkeypatch.setenv("DYM_LANES_PER_LINK", "2")
+        monkeypatch.setenv("DYM_VT_MAX_ACCEPT", "1.0")
     g = engine.load_group(ref_table(fname))
     assert not g.classes_exact and g.class_spread > 0
     assert g.fast_path
@@ -55,6 +61,8 @@ def test_fast_kernels_on_reference_files(engine, ref_table, monkeypatch, name, r
         if recheck_all:
             assert st.rechecks == st.hits
     assert kernels <= {KERNEL_MIXED, KERNEL_MIXED_VALUES}
+    if lanes == 2 and nsw > 1:
+        assert KERNEL_MIXED_VALUES in kernels
 
 
 STAGED = ["mys1080-v4", "myBI", "myBT", "myBO", "S648", "S108", "siii_360x4", "svii_120x4", "sviii_120x4",
