@@ -13,8 +13,8 @@ table is generated (trace-isomorphic to the reference's mys1080-v4).
 Timing: W untimed sweeps, then K sweeps each timed with CUDA events on the
 chain's stream; a 256 MB buffer (> 129 MB L2) is written between sweeps so
 every step starts with the lattice and table out of L2.  `e2e` times the same
-sweep through the C ABI with the configuration copied in from and out to
-pinned host memory every step.
+sweep through the C ABI (dym_sweep_host) with the configuration copied in
+from and out to pinned host memory every step.
 
 --impl reference times the unmodified reference executable (dym-mod-metro
 built from the staged sources with its Makefile's flags and NHIT 10, all host
@@ -283,8 +283,8 @@ def bench_config(world: int) -> dict:
     w = WORKLOAD
     V = w["Nt"] * w["Nx"] ** (w["D"] - 1)
     return {"workload": WORKLOAD_NAME, "links": V * w["D"], "nhit": w["nhit"], "sweeps_per_step": 1,
-            "l2": "GPU arm: a 256 MB buffer written between steps (L2 flushed); CPU arm: the reference's own "
-                  "update timer", "parallelism": f"replicas x{world}"}
+            "l2": "GPU arm: a 256 MB buffer written between steps, also between the e2e steps (L2 flushed); CPU "
+                  "arm: the reference's own update timer", "parallelism": f"replicas x{world}"}
 
 
 def ensemble_bench(dym, device: int, sweeps: int = 5, nhit: int = 10) -> dict:
@@ -545,25 +545,28 @@ def run_ours(args):
         t_wall = time.perf_counter() - t_wall0
     clocks = clk.summary()
 
-    # e2e: configuration in from / out to pinned host memory every step, through the C ABI.
+    # e2e: the configuration in from and out to pinned host memory every step,
+    # through the C ABI's host-resident sweep (dym_sweep_host: upload and
+    # check, the sweep, read-back, one synchronisation).
     n = links_per_sweep
     host_in = torch.empty(n, dtype=torch.uint16, pin_memory=True).numpy()
     host_out = torch.empty(n, dtype=torch.uint16, pin_memory=True).numpy()
     host_in[:] = lat.links.ravel()
     stt = _lib.Stats()
     for _ in range(2):
-        check(lib().dym_links_set(lat._h, ptr(host_in, C.c_uint16)))
-        check(lib().dym_sweep(lat._h, 1, w["nhit"], C.byref(stt)))
-        check(lib().dym_links_get(lat._h, ptr(host_out, C.c_uint16)))
+        check(lib().dym_sweep_host(lat._h, ptr(host_in, C.c_uint16), ptr(host_out, C.c_uint16), 1, w["nhit"],
+                                   C.byref(stt)))
     barrier()
-    t0 = time.perf_counter()
+    e2e_s = 0.0
     for k in range(args.steps):
-        check(lib().dym_links_set(lat._h, ptr(host_in, C.c_uint16)))
-        check(lib().dym_sweep(lat._h, 1, w["nhit"], C.byref(stt)))
-        check(lib().dym_links_get(lat._h, ptr(host_out, C.c_uint16)))
+        flush.fill_(k & 0xFF)  # every step starts with L2 flushed, as the device-timed steps
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        check(lib().dym_sweep_host(lat._h, ptr(host_in, C.c_uint16), ptr(host_out, C.c_uint16), 1, w["nhit"],
+                                   C.byref(stt)))
+        e2e_s += time.perf_counter() - t0
         host_in, host_out = host_out, host_in
     barrier()
-    e2e_s = time.perf_counter() - t0
 
     times = torch.tensor([dev_ms, e2e_s], dtype=torch.float64, device=f"cuda:{local}")
     if world > 1:
@@ -632,7 +635,7 @@ def run_ours(args):
                          "hbm": {"achieved": hbm_bytes / (dev_ms * 1e-3 / args.steps) / 1e9, "peak": hbm_peak,
                                  "unit": "GB/s", "note": "compulsory link streaming, 4 B/link/sweep, of measured"}},
             "e2e": {"value": e2e_value, "unit": "link-hits/s", "h2d_bytes_per_step": n * 2,
-                    "d2h_bytes_per_step": n * 2 + 4 * 8},
+                    "d2h_bytes_per_step": n * 2 + 6 * 8, "call": "dym_sweep_host"},
             "gpu_launches": launches,
             "acceptance": acc / (hits_per_step * args.steps), "recheck_fraction": rechecks / (hits_per_step * args.steps),
             "clocks": clocks,

@@ -200,6 +200,14 @@ static int hit_unroll_setting() {
   return v >= 10 ? 10 : v >= 5 ? 5 : v >= 2 ? 2 : 1;
 }
 
+// Threads sharing a link visit in the value-table kernel (DYM_LANES_PER_LINK
+// overrides the default): 1 or 2.
+static int lanes_per_link_setting() {
+  const char* e = std::getenv("DYM_LANES_PER_LINK");
+  const int v = e ? std::atoi(e) : kDefaultLanesPerLink;
+  return v >= 2 ? 2 : 1;
+}
+
 // Largest acceptance of a chain's previous call for which its next call runs
 // the value-table kernel (DYM_VT_MAX_ACCEPT overrides the default).
 static double vt_max_accept() {
@@ -539,16 +547,18 @@ int dym_chain_set_beta(dym_chain* c, double beta0, double beta1, double beta2) {
   return DYM_OK;
 }
 
-int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
-  NvtxRange nvtx("dym_sweep");
-  if (!c) return fail(DYM_EINVAL, "dym_sweep: null chain");
-  if (nsweeps < 0 || nhit < 0 || nhit > (1 << 20)) return fail(DYM_EINVAL, "dym_sweep: bad nsweeps or nhit");
-  DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+// Enqueue nsweeps sweeps of the chain on its stream, between the events
+// ev0 and ev1, and the read-back of the counters into h_counters[0..4];
+// `skip` (see SweepArgs) may make every launch a no-op.  Advances c->sweep.
+static int sweep_enqueue(dym_chain* c, int32_t nsweeps, int32_t nhit, const unsigned long long* skip,
+                         int* kernel_out) {
   DYM_CUDA(cudaMemsetAsync(c->dev.counters, 0, 5 * sizeof(unsigned long long), c->stream), "reset counters");
   const int kernel = sweep_kernel(c);
   SweepArgs a = sweep_args(c, kernel);
   a.nhit = nhit;
   a.hit_unroll = hit_unroll_setting();
+  a.lanes_per_link = lanes_per_link_setting();
+  a.skip = skip;
   const Schedule& s = c->sched;
   DYM_CUDA(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
   for (int k = 0; k < nsweeps; ++k) {
@@ -575,7 +585,12 @@ int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
   DYM_CUDA(cudaMemcpyAsync(c->h_counters, c->dev.counters, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                            c->stream),
            "read counters");
-  DYM_CUDA(cudaStreamSynchronize(c->stream), "sweep");
+  *kernel_out = kernel;
+  return DYM_OK;
+}
+
+// After the stream has synchronised: the counters of sweep_enqueue into *out.
+static int sweep_report(dym_chain* c, int kernel, int32_t nsweeps, dym_stats* out) {
   if (c->h_counters[4])
     return fail(DYM_ECUDA, "bounds check: code " + std::to_string(c->h_counters[4] >> 32) + " value " +
                                std::to_string(c->h_counters[4] & 0xFFFFFFFFull));
@@ -590,12 +605,23 @@ int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
     std::memcpy(&me, &bits, 4);
     out->max_ds_err = me;
     out->sweep = c->sweep;
-    out->launches = (uint32_t)(nsweeps * s.phase_dir.size());
+    out->launches = (uint32_t)(nsweeps * c->sched.phase_dir.size());
     float ms = 0;
     DYM_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1), "cudaEventElapsedTime");
     out->device_ms = ms;
   }
   return DYM_OK;
+}
+
+int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
+  NvtxRange nvtx("dym_sweep");
+  if (!c) return fail(DYM_EINVAL, "dym_sweep: null chain");
+  if (nsweeps < 0 || nhit < 0 || nhit > (1 << 20)) return fail(DYM_EINVAL, "dym_sweep: bad nsweeps or nhit");
+  DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+  int kernel = 0;
+  if (int rc = sweep_enqueue(c, nsweeps, nhit, nullptr, &kernel)) return rc;
+  DYM_CUDA(cudaStreamSynchronize(c->stream), "sweep");
+  return sweep_report(c, kernel, nsweeps, out);
 }
 
 int dym_measure(dym_chain* c, const dym_meas_opts* opts, dym_obs* out, double* wloop) {
@@ -671,16 +697,15 @@ int dym_links_get(dym_chain* c, uint16_t* host_out) {
   return DYM_OK;
 }
 
-int dym_links_set(dym_chain* c, const uint16_t* host_in) {
-  if (!c || !host_in) return fail(DYM_EINVAL, "dym_links_set: null argument");
+// Enqueue the upload of a configuration from host memory into the chain's
+// stage and its check on the device: the first id >= P (or ~0) into
+// d_first_bad, the stage copied into the chain's links only if there is none,
+// so a refused configuration leaves the chain as it was.
+static int links_upload_enqueue(dym_chain* c, const uint16_t* host_in) {
   const uint32_t P = c->grp->g->P;
   const size_t n = (size_t)c->dev.V * c->p.D;
-  DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
   if (!c->d_stage) DYM_CUDA(dmalloc(&c->d_stage, n), "cudaMalloc(links stage)");
   if (!c->d_first_bad) DYM_CUDA(dmalloc(&c->d_first_bad, 1), "cudaMalloc(links check)");
-  // Upload into the stage; the device finds the first id >= P and copies the
-  // stage into the chain's links only if there is none, so a refused
-  // configuration leaves the chain as it was.
   if (const void* mh = mapped_host(host_in)) {  // page-locked: read by the checking kernel itself
     DYM_CUDA(launch_links_from_host(c->dev.links, c->d_stage, static_cast<const uint16_t*>(mh), n, P,
                                     c->d_first_bad, c->stream),
@@ -692,10 +717,40 @@ int dym_links_set(dym_chain* c, const uint16_t* host_in) {
   DYM_CUDA(cudaMemcpyAsync(c->h_counters + 5, c->d_first_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                            c->stream),
            "read links check");
+  return DYM_OK;
+}
+
+int dym_links_set(dym_chain* c, const uint16_t* host_in) {
+  if (!c || !host_in) return fail(DYM_EINVAL, "dym_links_set: null argument");
+  DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+  if (int rc = links_upload_enqueue(c, host_in)) return rc;
   DYM_CUDA(cudaStreamSynchronize(c->stream), "upload links");
   if (c->h_counters[5] != ~0ull)
     return fail(DYM_EINVAL, "dym_links_set: element id out of range at " + std::to_string(c->h_counters[5]));
   return DYM_OK;
+}
+
+int dym_sweep_host(dym_chain* c, const uint16_t* host_in, uint16_t* host_out, int32_t nsweeps, int32_t nhit,
+                   dym_stats* out) {
+  NvtxRange nvtx("dym_sweep_host");
+  if (!c) return fail(DYM_EINVAL, "dym_sweep_host: null chain");
+  if (nsweeps < 0 || nhit < 0 || nhit > (1 << 20)) return fail(DYM_EINVAL, "dym_sweep_host: bad nsweeps or nhit");
+  DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+  if (host_in)
+    if (int rc = links_upload_enqueue(c, host_in)) return rc;
+  int kernel = 0;
+  const uint32_t sweep0 = c->sweep;
+  if (int rc = sweep_enqueue(c, nsweeps, nhit, host_in ? c->d_first_bad : nullptr, &kernel)) return rc;
+  if (host_out)
+    DYM_CUDA(cudaMemcpyAsync(host_out, c->dev.links, (size_t)c->dev.V * c->p.D * 2, cudaMemcpyDeviceToHost,
+                             c->stream),
+             "download links");
+  DYM_CUDA(cudaStreamSynchronize(c->stream), "dym_sweep_host");
+  if (host_in && c->h_counters[5] != ~0ull) {
+    c->sweep = sweep0;  // the sweeps did nothing
+    return fail(DYM_EINVAL, "dym_sweep_host: element id out of range at " + std::to_string(c->h_counters[5]));
+  }
+  return sweep_report(c, kernel, nsweeps, out);
 }
 
 static dym_checkpoint_info chain_checkpoint_info(const dym_chain* c) {

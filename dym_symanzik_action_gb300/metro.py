@@ -236,6 +236,31 @@ class Lattice:
         return SweepStats(st.hits, st.accepts, st.rechecks, st.max_ds_err, st.sweep, st.launches, st.device_ms,
                           st.kernel)
 
+    def update_host(self, links_in, links_out=None, nsweeps: int = 1, nhit: int = 20) -> SweepStats:
+        """update() on a configuration held in host memory (dym_sweep_host):
+        links_in (uint16, D*V entries, or None to keep the chain's) is
+        uploaded and checked, nsweeps sweeps run, and the result is written
+        into links_out (or not read back when None), with one synchronisation.
+        Both must be C-contiguous uint16 arrays; page-locked ones (e.g. from
+        torch's pin_memory) are read and written without a staging copy."""
+        n = self.D * self.V
+        for x in (links_in, links_out):
+            if x is not None and (x.dtype != np.uint16 or x.size != n or not x.flags["C_CONTIGUOUS"]):
+                raise ValueError("links must be C-contiguous uint16 arrays of D*V entries")
+        if links_out is not None and not links_out.flags["WRITEABLE"]:
+            raise ValueError("links_out must be writeable")
+        st = _lib.Stats()
+        check(lib().dym_sweep_host(self._h, None if links_in is None else ptr(links_in, C.c_uint16),
+                                   None if links_out is None else ptr(links_out, C.c_uint16), nsweeps, nhit,
+                                   C.byref(st)))
+        self.hit += st.hits
+        self.acc += st.accepts
+        self.rechecks += st.rechecks
+        self.max_ds_err = max(self.max_ds_err, st.max_ds_err)
+        self.sweeps = st.sweep
+        return SweepStats(st.hits, st.accepts, st.rechecks, st.max_ds_err, st.sweep, st.launches, st.device_ms,
+                          st.kernel)
+
     def measure(self, wl_nx: int = 0, wl_nt: int = 0) -> Measurement:
         """Observables (dym-mod-metro.cpp:282-318); wl_nx/wl_nt 0 = full Nx x Nt
         grid as the reference, -1 = no Wilson grid."""

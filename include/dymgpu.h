@@ -234,6 +234,20 @@ int dym_measure_noalloc(dym_chain* c, const dym_meas_opts* opts, dym_obs* out, d
 int dym_links_get(dym_chain* c, uint16_t* host_out);
 int dym_links_set(dym_chain* c, const uint16_t* host_in);
 
+/* nsweeps sweeps of a configuration held in host memory, in one call: the
+ * drop-in for the reference's update() (dym-mod-metro.cpp:146-197) applied to
+ * its host-resident link array `a` (malloc at dym-mod-metro.cpp:253).
+ * host_in (may be NULL: keep the chain's configuration) is uploaded and
+ * checked as by dym_links_set, the sweeps run as by dym_sweep, and the
+ * result is copied into host_out (may be NULL; may equal host_in), with one
+ * synchronisation at the end instead of one per step.  Page-locked host
+ * buffers are read by the checking kernel directly.  A host_in with an id >=
+ * the group order returns DYM_EINVAL with the chain unchanged (the sweeps do
+ * nothing, the chain's sweep counter is not advanced) and host_out, if
+ * given, holding the chain's unchanged configuration. */
+int dym_sweep_host(dym_chain* c, const uint16_t* host_in, uint16_t* host_out, int32_t nsweeps, int32_t nhit,
+                   dym_stats* out);
+
 /* Lattice and schedule facts: V, number of colour phases per sweep, and the
  * phase layout (arrays may be NULL; sizes nphase, nphase, V*D). */
 int dym_chain_get_schedule(const dym_chain* c, uint32_t* V, int32_t* nphase,
