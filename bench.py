@@ -59,19 +59,24 @@ def gathers_per_link_hit(nhit: int) -> float:
 # build_u_tree); the hits run from shared memory.  FP64 shared-table kernel:
 # 84 staple products + 24 u_j products.  Direct kernel (fp64): those 108 plus
 # 25 per hit.  Per launch every block also stages its shared tables from L2.
-# dram__bytes_read.sum + dram__bytes_write.sum of one sweep launch of this
-# workload, from the ncu --set full captures summarised in
-# profiles/sweep_vt_s1080_32x32x32x8_ncu.md and profiles/sweep_sub_s1080_32x32x32x8_ncu.md
-# (cold cache after ncu's flush).  The mixed kernel runs this workload only on
-# a chain's first call (the cold chain accepts nothing, so later calls use the
-# value table) and has no capture of it; None leaves its roofline unreported.
-DRAM_BYTES_PER_LAUNCH = {"k_sweep_vt": 2835968, "k_sweep_mixed": None, "k_sweep_sub": 2563584}
+# dram__bytes_read.sum + dram__bytes_write.sum per sweep launch of this
+# workload in the bench's own regime: the mean over the 16 launches of one
+# timed step (after the 256 MB flush), from an ncu capture with
+# --cache-control none (profiles/sweep_vt_s1080_32x32x32x8_ncu.md: the first
+# launch of the step 3.7 MB -- the table and lattice from DRAM and write-backs
+# of the flush buffer's dirty lines -- the others 0.6-0.8 MB).  The FP64
+# kernel's figure is its capture after ncu's own per-launch flush.  The mixed
+# kernel runs this workload only on a chain's first call (the cold chain
+# accepts nothing, so later calls use the value table) and has no capture of
+# it; None leaves its roofline unreported.
+DRAM_BYTES_PER_LAUNCH = {"k_sweep_vt": 1023632, "k_sweep_mixed": None, "k_sweep_sub": 2563584}
 # smsp__inst_executed.sum (warp instructions) and lts__t_sectors_srcunit_tex.sum
 # (L2 sectors requested by the SMs) of one sweep launch of this workload, from
-# the same captures.  Both are fixed for the workload: the cold chain accepts
-# no proposal, so every launch runs the same instructions.
-INST_PER_LAUNCH = {"k_sweep_vt": 7216867, "k_sweep_mixed": None, "k_sweep_sub": None}
-L2_SECTORS_PER_LAUNCH = {"k_sweep_vt": 410158, "k_sweep_mixed": None, "k_sweep_sub": None}
+# the --set full capture in the same file.  Both are fixed for the workload:
+# the cold chain accepts no proposal, so every launch runs the same
+# instructions.
+INST_PER_LAUNCH = {"k_sweep_vt": 7680320, "k_sweep_mixed": None, "k_sweep_sub": None}
+L2_SECTORS_PER_LAUNCH = {"k_sweep_vt": 423259, "k_sweep_mixed": None, "k_sweep_sub": None}
 # Warp instructions an SM can issue per cycle (four schedulers, one each).
 ISSUE_PER_SM_CYCLE = 4
 
@@ -86,16 +91,12 @@ PRECISION_TEXT = {
 def kernel_model(kernel: int, P: int, npool: int, nhit: int, links_per_launch: int, sms: int):
     """(kernel name, table gathers per link visit, blocks, staged bytes per block) of the
     sweep kernel dym_sweep reported (DYM_KERNEL_*)."""
-    if kernel == 4:  # value table (sweep.cu vt_smem_bytes); accepted moves add 25 gathers each
-        per = -(-links_per_launch // sms)
-        threads = min(512, max(128, -(-per // 32) * 32))
-        return ("k_sweep_vt", 87, -(-links_per_launch // threads),
-                -(-(npool * P * 2) // 16) * 16 + P * 8 + P * 2 + P * 2 + npool * 2 + 16)
-    if kernel == 3:  # sweep.cu mixed_smem_bytes; 128..512 threads, one block per SM
-        per = -(-links_per_launch // sms)
-        threads = min(512, max(128, -(-per // 32) * 32))
-        return ("k_sweep_mixed", 87, -(-links_per_launch // threads),
-                P * 8 + 32 * 4 + P * 2 + npool * P * 2 + P + 16)
+    # one-wave launches of chunks of max(ceil(links / SMs), 128) links (sweep_launch.cuh phase_shape)
+    blocks = -(-links_per_launch // max(-(-links_per_launch // sms), 128))
+    if kernel == 4:  # value table (sweep_vt.cu, vt_smem_bytes); accepted moves add 25 gathers each
+        return ("k_sweep_vt", 87, blocks, -(-(npool * P * 2) // 16) * 16 + P * 8 + P * 2 + P * 2 + npool * 2 + 16)
+    if kernel == 3:  # sweep_mixed.cu, mixed_smem_bytes
+        return ("k_sweep_mixed", 87, blocks, P * 8 + 32 * 4 + P * 2 + npool * P * 2 + P + 16)
     if kernel == 2:  # sweep.cu sub_smem_bytes; one wave of 256-thread blocks
         return ("k_sweep_sub", 108, min(sms, -(-links_per_launch // 256)), P * 8 + P * 2 + npool * P * 2 + 16)
     return ("k_sweep_direct", 108 + 25 * nhit, -(-links_per_launch // 256), P * 8 + P * 2 + npool * 2 + 16)

@@ -700,7 +700,8 @@ int dym_links_get(dym_chain* c, uint16_t* host_out) {
 // Enqueue the upload of a configuration from host memory into the chain's
 // stage and its check on the device: the first id >= P (or ~0) into
 // d_first_bad, the stage copied into the chain's links only if there is none,
-// so a refused configuration leaves the chain as it was.
+// so a refused configuration leaves the chain as it was.  The caller enqueues
+// the read-back of d_first_bad (links_check_readback) where it needs it.
 static int links_upload_enqueue(dym_chain* c, const uint16_t* host_in) {
   const uint32_t P = c->grp->g->P;
   const size_t n = (size_t)c->dev.V * c->p.D;
@@ -714,6 +715,11 @@ static int links_upload_enqueue(dym_chain* c, const uint16_t* host_in) {
     DYM_CUDA(cudaMemcpyAsync(c->d_stage, host_in, n * 2, cudaMemcpyHostToDevice, c->stream), "upload links");
     DYM_CUDA(launch_links_commit(c->dev.links, c->d_stage, n, P, c->d_first_bad, c->stream), "check links");
   }
+  return DYM_OK;
+}
+
+// Enqueue the copy of the upload check's result into h_counters[5].
+static int links_check_readback(dym_chain* c) {
   DYM_CUDA(cudaMemcpyAsync(c->h_counters + 5, c->d_first_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                            c->stream),
            "read links check");
@@ -724,6 +730,7 @@ int dym_links_set(dym_chain* c, const uint16_t* host_in) {
   if (!c || !host_in) return fail(DYM_EINVAL, "dym_links_set: null argument");
   DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
   if (int rc = links_upload_enqueue(c, host_in)) return rc;
+  if (int rc = links_check_readback(c)) return rc;
   DYM_CUDA(cudaStreamSynchronize(c->stream), "upload links");
   if (c->h_counters[5] != ~0ull)
     return fail(DYM_EINVAL, "dym_links_set: element id out of range at " + std::to_string(c->h_counters[5]));
@@ -745,6 +752,8 @@ int dym_sweep_host(dym_chain* c, const uint16_t* host_in, uint16_t* host_out, in
     DYM_CUDA(cudaMemcpyAsync(host_out, c->dev.links, (size_t)c->dev.V * c->p.D * 2, cudaMemcpyDeviceToHost,
                              c->stream),
              "download links");
+  if (host_in)  // read back after the sweeps, off their path
+    if (int rc = links_check_readback(c)) return rc;
   DYM_CUDA(cudaStreamSynchronize(c->stream), "dym_sweep_host");
   if (host_in && c->h_counters[5] != ~0ull) {
     c->sweep = sweep0;  // the sweeps did nothing

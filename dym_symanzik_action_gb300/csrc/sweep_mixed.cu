@@ -25,11 +25,9 @@ __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_mixed(SweepArgs a
   uint16_t* s_inv = reinterpret_cast<uint16_t*>(s_cfix + kMixedMaxCls);
   E* s_psub = reinterpret_cast<E*>(smem + mixed_psub_offset(a.P, sizeof(E)));
   uint8_t* s_cls = reinterpret_cast<uint8_t*>(s_psub + (size_t)a.npool * a.P);
-  // The staging copies npool * P entries as halfwords; the staple phase of a
-  // block's first links needs only the small tables, so the block waits for
-  // the sub-table after it, before the first hit.
+  // The staging copies npool * P entries as halfwords.
   stage_sub_tables(a.retr, a.inv, reinterpret_cast<const uint16_t*>(psub), a.P, a.npool * (uint32_t)(sizeof(E) / 2),
-                   s_retr, s_inv, reinterpret_cast<uint16_t*>(s_psub), false);
+                   s_retr, s_inv, reinterpret_cast<uint16_t*>(s_psub));
   for (uint32_t t = threadIdx.x; t < a.P; t += blockDim.x) s_cls[t] = a.cls8[t];
   if (threadIdx.x < kMixedMaxCls) s_cfix[threadIdx.x] = a.cfix[threadIdx.x];
   uint32_t lo, hi;
@@ -42,34 +40,20 @@ __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_mixed(SweepArgs a
   }
   pdl_launch_dependents();
   pdl_wait_prior();
-  __syncthreads();  // the small tables
-  if (sweep_skipped(a)) {
-    cp_async_wait_all();  // no block leaves with copies in flight
-    return;
-  }
+  cp_async_wait_all();
+  __syncthreads();
+  if (sweep_skipped(a)) return;
 
-  constexpr int NT = 8 * (D - 1);
   unsigned hits = 0, accs = 0, rechecks = 0;
   float max_err = 0.0f;
-  for (bool first = true;; first = false, t += blockDim.x) {
-    const bool have = t < hi;
-    uint32_t u[NT];
-    uint32_t b, R, M;
+  for (; t < hi; t += blockDim.x) {
     const uint32_t i = i_next, xyz = xyz_next;
-    if (have) {
-      if (t + blockDim.x < hi) {
-        i_next = a.sites[t + blockDim.x];
-        xyz_next = a.xyz[t + blockDim.x];
-      }
-      mixed_prepare<D, DIR>(a, i, xyz, s_inv, s_cls, s_cfix, u, b, R, M);
+    if (t + blockDim.x < hi) {
+      i_next = a.sites[t + blockDim.x];
+      xyz_next = a.xyz[t + blockDim.x];
     }
-    if (first) {  // every thread of the block, with or without a link
-      cp_async_wait_all();
-      __syncthreads();  // the sub-table
-    }
-    if (!have) break;
-    mixed_hits<D, DIR, E, HU>(a, i, a.sweep, s_retr, s_inv, s_psub, s_cfix, u, b, R, M, hits, accs, rechecks,
-                              max_err);
+    visit_mixed<D, DIR, E, HU>(a, i, xyz, a.sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks,
+                               max_err);
   }
   flush_counters(a.counters, hits, accs, rechecks);
   flush_max_err(a.counters + 3, max_err);

@@ -28,12 +28,9 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // copies of the sub-table start on 16 bytes its whole 16-byte chunks go by
 // cp.async, so the block's copy costs about one L2 round trip instead of one
 // per eight words a thread moves; the caller's __syncthreads() publishes it.
-// wait false leaves those chunks in flight: the caller then publishes ReTr
-// and the inverses with one __syncthreads() and the sub-table with
-// cp_async_wait_all() and another.
 __device__ __forceinline__ void stage_sub_tables(const double* retr, const uint16_t* inv, const uint16_t* sub,
                                                  uint32_t P, uint32_t npool, double* s_retr, uint16_t* s_inv,
-                                                 uint16_t* s_sub, bool wait = true) {
+                                                 uint16_t* s_sub) {
   const uint32_t nsub = npool * P;
   const bool async = ((reinterpret_cast<uintptr_t>(sub) | (uintptr_t)__cvta_generic_to_shared(s_sub)) & 15u) == 0;
   if (async) {
@@ -46,7 +43,7 @@ __device__ __forceinline__ void stage_sub_tables(const double* retr, const uint1
     s_inv[t] = inv[t];
   }
   if (async) {
-    if (wait) cp_async_wait_all();
+    cp_async_wait_all();
   } else if ((P & 1u) == 0) {
     const uint32_t* src = reinterpret_cast<const uint32_t*>(sub);
     uint32_t* dst = reinterpret_cast<uint32_t*>(s_sub);
