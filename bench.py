@@ -332,7 +332,7 @@ def ensemble_bench(dym, device: int, sweeps: int = 5, nhit: int = 10) -> dict:
            "single_chain_device_link_hits_per_s": hits_single / (single_dev_ms * 1e-3),
            "speedup_batched_vs_single": (hits_batch / batch_wall) / (hits_single / single_wall),
            "tuning": {"tile": tuning.tile, "threads": tuning.threads, "grid_per_sm": tuning.grid_per_sm,
-                      "cuda_graph": tuning.use_graph}}
+                      "cuda_graph": tuning.use_graph, "hit_unroll": tuning.hit_unroll}}
     b.close()
     for lat in chains:
         lat.close()

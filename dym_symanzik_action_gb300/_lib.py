@@ -84,7 +84,8 @@ class Llr2dResult(C.Structure):
 
 
 class BatchTuning(C.Structure):
-    _fields_ = [("tile", C.c_int32), ("threads", C.c_int32), ("grid_per_sm", C.c_int32), ("use_graph", C.c_int32)]
+    _fields_ = [("tile", C.c_int32), ("threads", C.c_int32), ("grid_per_sm", C.c_int32), ("use_graph", C.c_int32),
+                ("hit_unroll", C.c_int32)]
 
 
 SERVE_MAX_NRM = 64

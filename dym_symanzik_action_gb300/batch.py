@@ -21,6 +21,7 @@ class Tuning:
     threads: int = 256
     grid_per_sm: int = 1
     use_graph: bool = True
+    hit_unroll: int = 1
 
 
 class Batch:
@@ -44,11 +45,12 @@ class Batch:
     def tuning(self) -> Tuning:
         t = _lib.BatchTuning()
         check(lib().dym_batch_get_tuning(self._h, C.byref(t)))
-        return Tuning(t.tile, t.threads, t.grid_per_sm, bool(t.use_graph))
+        return Tuning(t.tile, t.threads, t.grid_per_sm, bool(t.use_graph), t.hit_unroll or 1)
 
     @tuning.setter
     def tuning(self, t: Tuning) -> None:
-        bt = _lib.BatchTuning(tile=t.tile, threads=t.threads, grid_per_sm=t.grid_per_sm, use_graph=int(t.use_graph))
+        bt = _lib.BatchTuning(tile=t.tile, threads=t.threads, grid_per_sm=t.grid_per_sm, use_graph=int(t.use_graph),
+                              hit_unroll=t.hit_unroll)
         check(lib().dym_batch_set_tuning(self._h, C.byref(bt)))
 
     def update(self, nsweeps: int = 1, nhit: int = 20) -> SweepStats:
@@ -66,7 +68,7 @@ class Batch:
     def autotune(self, nhit: int = 10, nsweeps_per_trial: int = 2) -> Tuning:
         t = _lib.BatchTuning()
         check(lib().dym_batch_autotune(self._h, nhit, nsweeps_per_trial, C.byref(t)))
-        return Tuning(t.tile, t.threads, t.grid_per_sm, bool(t.use_graph))
+        return Tuning(t.tile, t.threads, t.grid_per_sm, bool(t.use_graph), t.hit_unroll or 1)
 
     def close(self) -> None:
         if getattr(self, "_h", None):

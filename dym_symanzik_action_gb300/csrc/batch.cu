@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(256) k_batch_sub(const BatchTile* __restrict__
 // The same work list with the mixed-precision visit (visit_mixed): every group
 // of the batch stages ReTr, inverses, packed sub-table, element classes and
 // fixed-point class values.
-template <int D>
+template <int D, int HU>
 __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_batch_mixed(const BatchTile* __restrict__ tiles, uint32_t ntiles,
                                                      const BatchChainDev* __restrict__ chains, const __grid_constant__ BatchGroups groups,
                                                      const uint32_t* __restrict__ sweeps, int nhit) {
@@ -123,10 +123,10 @@ __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_batch_mixed(const Batch
       const uint32_t i = c.sites[tl.begin + k];
       const uint32_t xyz = c.xyz[tl.begin + k];
       switch (tl.dir) {
-        case 0: visit_mixed<D, 0>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
-        case 1: visit_mixed<D, 1>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
-        case 2: visit_mixed<D, 2>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
-        case 3: visit_mixed<D, 3>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
+        case 0: visit_mixed<D, 0, uint16_t, HU>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
+        case 1: visit_mixed<D, 1, uint16_t, HU>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
+        case 2: visit_mixed<D, 2, uint16_t, HU>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
+        case 3: visit_mixed<D, 3, uint16_t, HU>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
       }
     }
     flush_counters(c.ctr, hits, accs, rechecks);
@@ -144,21 +144,38 @@ void* batch_kernel() {
   return (void*)k_batch_sub<D>;
 }
 
-}  // namespace
+// The mixed kernel for a hit-unroll factor (1, 2, 5, 10: HitDraws groups).
+using BatchMixedFn = void (*)(const BatchTile*, uint32_t, const BatchChainDev*, const BatchGroups, const uint32_t*,
+                              int);
 
-void* batch_kernel_for(int D, bool mixed) {
-  if (D != 4) return nullptr;
-  return mixed ? (void*)k_batch_mixed<4> : batch_kernel<4>();
+template <int D>
+BatchMixedFn batch_mixed_for(int hu) {
+  switch (hu >= 10 ? 10 : hu >= 5 ? 5 : hu >= 2 ? 2 : 1) {
+    case 2: return k_batch_mixed<D, 2>;
+    case 5: return k_batch_mixed<D, 5>;
+    case 10: return k_batch_mixed<D, 10>;
+    default: return k_batch_mixed<D, 1>;
+  }
 }
 
-cudaError_t launch_batch_slot(int D, bool mixed, const BatchTile* tiles, uint32_t ntiles, const BatchChainDev* chains,
-                              const BatchGroups& groups, const uint32_t* sweeps, int nhit, unsigned grid,
-                              unsigned threads, size_t smem, cudaStream_t s) {
+}  // namespace
+
+void* batch_kernel_for(int D, bool mixed, int hit_unroll) {
+  if (D != 4) return nullptr;
+  return mixed ? (void*)batch_mixed_for<4>(hit_unroll) : batch_kernel<4>();
+}
+
+
+
+cudaError_t launch_batch_slot(int D, bool mixed, int hit_unroll, const BatchTile* tiles, uint32_t ntiles,
+                              const BatchChainDev* chains, const BatchGroups& groups, const uint32_t* sweeps, int nhit,
+                              unsigned grid, unsigned threads, size_t smem, cudaStream_t s) {
   if (ntiles == 0) return cudaSuccess;
   if (D != 4) return cudaErrorInvalidValue;  // four dimensions only (see launch_sweep_sub)
-  if (mixed)
-    k_batch_mixed<4><<<grid, threads, smem, s>>>(tiles, ntiles, chains, groups, sweeps, nhit);
-  else
+  if (mixed) {
+    const BatchMixedFn fn = batch_mixed_for<4>(hit_unroll);
+    fn<<<grid, threads, smem, s>>>(tiles, ntiles, chains, groups, sweeps, nhit);
+  } else
     k_batch_sub<4><<<grid, threads, smem, s>>>(tiles, ntiles, chains, groups, sweeps, nhit);
   return cudaGetLastError();
 }

@@ -78,10 +78,10 @@ cudaError_t launch_llr_slot(int D, const LlrTile* tiles, uint32_t ntiles, const 
                             const LlrChainDev* chains, const BatchGroups& groups, int nhit, unsigned grid,
                             size_t smem, cudaStream_t s);
 
-void* batch_kernel_for(int D, bool mixed);
-cudaError_t launch_batch_slot(int D, bool mixed, const BatchTile* tiles, uint32_t ntiles, const BatchChainDev* chains,
-                              const BatchGroups& groups, const uint32_t* sweeps, int nhit, unsigned grid,
-                              unsigned threads, size_t smem, cudaStream_t s);
+void* batch_kernel_for(int D, bool mixed, int hit_unroll);
+cudaError_t launch_batch_slot(int D, bool mixed, int hit_unroll, const BatchTile* tiles, uint32_t ntiles,
+                              const BatchChainDev* chains, const BatchGroups& groups, const uint32_t* sweeps, int nhit,
+                              unsigned grid, unsigned threads, size_t smem, cudaStream_t s);
 cudaError_t launch_batch_advance(uint32_t* sweeps, uint32_t n, cudaStream_t s);
 
 }  // namespace dym

@@ -883,7 +883,7 @@ struct dym_batch {
   std::vector<uint32_t> slot_off, slot_cnt;
   size_t smem = 0;
   uint64_t nlinks = 0;
-  dym_batch_tuning tune{256, 256, 1, 1};
+  dym_batch_tuning tune{256, 256, 1, 1, 1};
   bool dirty = true;
   cudaStream_t stream = nullptr;
   cudaGraph_t graph = nullptr;
@@ -1035,25 +1035,25 @@ static int batch_build(dym_batch* b) {
   DYM_CUDA(dmalloc(&b->d_tiles, std::max<size_t>(tiles.size(), 1)), "cudaMalloc(batch tiles)");
   DYM_CUDA(copy_sync(b->d_tiles, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice, b->stream),
            "upload tiles");
-  void* fn = batch_kernel_for(b->D, b->mixed);
-  if (!fn) return fail(DYM_ENOTSUP, "batch: unsupported D");
-  DYM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem), "smem attribute");
+  if (!batch_kernel_for(b->D, b->mixed, b->tune.hit_unroll)) return fail(DYM_ENOTSUP, "batch: unsupported D");
   b->dirty = false;
   return DYM_OK;
 }
 
 static int batch_grid(dym_batch* b, unsigned* grid) {
   int per_sm = 0;
-  DYM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel_for(b->D, b->mixed), b->tune.threads, b->smem),
-           "occupancy");
+  void* fn = batch_kernel_for(b->D, b->mixed, b->tune.hit_unroll);  // this tuning's instantiation
+  if (!fn) return fail(DYM_ENOTSUP, "batch: unsupported D");
+  DYM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem), "smem attribute");
+  DYM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, b->tune.threads, b->smem), "occupancy");
   *grid = (unsigned)std::max(1, b->sms * std::max(1, std::min(per_sm, b->tune.grid_per_sm)));
   return DYM_OK;
 }
 
 static int batch_enqueue_sweep(dym_batch* b, int nhit, unsigned grid) {
   for (size_t k = 0; k < b->slot_cnt.size(); ++k) {
-    cudaError_t e = launch_batch_slot(b->D, b->mixed, b->d_tiles + b->slot_off[k], b->slot_cnt[k], b->d_chains, b->bg,
-                                      b->d_sweeps, nhit, std::min<unsigned>(grid, b->slot_cnt[k]),
+    cudaError_t e = launch_batch_slot(b->D, b->mixed, b->tune.hit_unroll, b->d_tiles + b->slot_off[k], b->slot_cnt[k],
+                                      b->d_chains, b->bg, b->d_sweeps, nhit, std::min<unsigned>(grid, b->slot_cnt[k]),
                                       (unsigned)b->tune.threads, b->smem, b->stream);
     if (e != cudaSuccess) return cuda_fail(e, "batch slot launch");
   }
@@ -1116,13 +1116,16 @@ int dym_batch_size(const dym_batch* b, int32_t* nchains, uint64_t* nlinks, int32
 int dym_batch_set_tuning(dym_batch* b, const dym_batch_tuning* t) {
   if (!b || !t) return fail(DYM_EINVAL, "dym_batch_set_tuning: null argument");
   if (t->tile < 32 || t->tile % 32 || (t->threads != 128 && t->threads != 256 && t->threads != 512) ||
-      t->grid_per_sm < 1)
-    return fail(DYM_EINVAL, "tuning: tile a multiple of 32, threads 128, 256 or 512, grid_per_sm >= 1");
+      t->grid_per_sm < 1 || (t->hit_unroll != 0 && t->hit_unroll != 1 && t->hit_unroll != 2 && t->hit_unroll != 5 &&
+                             t->hit_unroll != 10))
+    return fail(DYM_EINVAL,
+                "tuning: tile a multiple of 32, threads 128, 256 or 512, grid_per_sm >= 1, hit_unroll 1, 2, 5 or 10");
   if (t->threads == 512 && !b->mixed && !b->chains.empty() &&
       !std::all_of(b->chains.begin(), b->chains.end(), batch_mixed_chain))
     return fail(DYM_EINVAL, "tuning: 512 threads need the mixed-precision batch kernel");
   if (t->tile != b->tune.tile) b->dirty = true;
   b->tune = *t;
+  if (b->tune.hit_unroll == 0) b->tune.hit_unroll = 1;
   if (b->exec) {
     cudaGraphExecDestroy(b->exec);
     b->exec = nullptr;
@@ -1251,19 +1254,20 @@ int dym_batch_autotune(dym_batch* b, int32_t nhit, int32_t nsweeps_per_trial, dy
       std::all_of(b->chains.begin(), b->chains.end(), batch_mixed_chain);
   for (int threads : {128, 256, 512})
     for (int tile : {128, 256, 512, 1024})
-      for (int gps : {1, 2}) {
-        if (rc) break;
-        if (threads == 512 && !all_mixed) continue;
-        dym_batch_tuning t{tile, threads, gps, 1};
-        rc = dym_batch_set_tuning(b, &t);
-        dym_stats st;
-        if (!rc) rc = dym_batch_sweep(b, 1, nhit, &st);  // warm-up, graph capture
-        if (!rc) rc = dym_batch_sweep(b, nsweeps_per_trial, nhit, &st);
-        if (!rc && st.device_ms < win_ms) {
-          win_ms = st.device_ms;
-          win = t;
+      for (int gps : {1, 2})
+        for (int hu : {1, 2}) {
+          if (rc) break;
+          if ((threads == 512 || hu > 1) && !all_mixed) continue;  // the FP64 batch kernel has neither
+          dym_batch_tuning t{tile, threads, gps, 1, hu};
+          rc = dym_batch_set_tuning(b, &t);
+          dym_stats st;
+          if (!rc) rc = dym_batch_sweep(b, 1, nhit, &st);  // warm-up, graph capture
+          if (!rc) rc = dym_batch_sweep(b, nsweeps_per_trial, nhit, &st);
+          if (!rc && st.device_ms < win_ms) {
+            win_ms = st.device_ms;
+            win = t;
+          }
         }
-      }
   for (size_t i = 0; i < b->chains.size(); ++i) {
     dym_chain* c = b->chains[i];
     copy_sync(c->dev.links, saved[i], (size_t)c->dev.V * c->p.D * 2, cudaMemcpyDeviceToDevice, b->stream);

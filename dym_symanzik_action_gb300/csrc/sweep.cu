@@ -150,6 +150,7 @@ __global__ void k_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uint
 // *first (set to ~0 beforehand), then the stage copied into the links only if
 // there is none.
 __global__ void k_ids_first_bad(const uint16_t* __restrict__ ids, size_t n, uint32_t P, unsigned long long* first) {
+  pdl_launch_dependents();  // the commit may be scheduled; it waits for this grid
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
     if (ids[k] >= P) atomicMin(first, (unsigned long long)k);
 }
@@ -162,6 +163,7 @@ __global__ void k_ids_first_bad(const uint16_t* __restrict__ ids, size_t n, uint
 // go one by one.
 __global__ void k_ids_from_host(uint16_t* __restrict__ stage, const uint16_t* __restrict__ host, size_t n, size_t nv,
                                 uint32_t P, unsigned long long* first) {
+  pdl_launch_dependents();  // the commit may be scheduled; it waits for this grid
   const size_t t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x, dt = (size_t)gridDim.x * blockDim.x;
   for (size_t q = t0; q < nv; q += dt) {
     const uint4 w = reinterpret_cast<const uint4*>(host)[q];
@@ -180,8 +182,11 @@ __global__ void k_ids_from_host(uint16_t* __restrict__ stage, const uint16_t* __
   }
 }
 
+// Launched with programmatic serialization behind the check: waits for it
+// (its result in *first) before reading anything.
 __global__ void k_ids_commit(uint16_t* __restrict__ links, const uint16_t* __restrict__ stage, size_t n,
                              const unsigned long long* first) {
+  pdl_wait_prior();
   if (*first != ~0ull) return;
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
     links[k] = stage[k];
@@ -326,8 +331,10 @@ cudaError_t launch_links_commit(uint16_t* links, const uint16_t* stage, size_t n
   if (e != cudaSuccess || n == 0) return e;
   const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 8);
   k_ids_first_bad<<<grid, 256, 0, s>>>(stage, n, P, first);
-  k_ids_commit<<<grid, 256, 0, s>>>(links, stage, n, first);
-  return cudaGetLastError();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return launch_phase(k_ids_commit, grid, 256, 0, s, links, (const uint16_t*)stage, n,
+                      (const unsigned long long*)first);
 }
 
 cudaError_t launch_links_from_host(uint16_t* links, uint16_t* stage, const uint16_t* host_mapped, size_t n,
@@ -337,8 +344,10 @@ cudaError_t launch_links_from_host(uint16_t* links, uint16_t* stage, const uint1
   const size_t nv = (reinterpret_cast<uintptr_t>(host_mapped) & 15u) ? 0 : n / 8;
   const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 8);
   k_ids_from_host<<<grid, 256, 0, s>>>(stage, host_mapped, n, nv, P, first);
-  k_ids_commit<<<grid, 256, 0, s>>>(links, stage, n, first);
-  return cudaGetLastError();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return launch_phase(k_ids_commit, grid, 256, 0, s, links, (const uint16_t*)stage, n,
+                      (const unsigned long long*)first);
 }
 
 cudaError_t launch_fill(uint16_t* links, size_t n, uint16_t v, cudaStream_t s) {

@@ -286,6 +286,8 @@ typedef struct {
   int32_t threads;      /* threads per block (128, 256; 512 when every chain is DYM_PREC_MIXED) */
   int32_t grid_per_sm;  /* blocks launched per SM per slot (>= 1) */
   int32_t use_graph;    /* 1: replay each sweep as a captured CUDA graph */
+  int32_t hit_unroll;   /* mixed-precision batches: hits whose random draws are computed ahead as a group
+                           (1, 2, 5 or 10; 0 means 1); configurations do not depend on it */
 } dym_batch_tuning;
 
 int dym_batch_create(int32_t device, dym_batch** out);
@@ -298,7 +300,9 @@ int dym_batch_sweep(dym_batch* b, int32_t nsweeps, int32_t nhit, dym_stats* tota
 /* Counters of chain `idx` (order of dym_batch_add) for the last dym_batch_sweep. */
 int dym_batch_chain_counters(const dym_batch* b, int32_t idx, uint64_t* hits, uint64_t* accepts);
 /* Time candidate tunings on the batch's own chains (their configurations,
- * sweep counters and counters are restored afterwards) and keep the fastest. */
+ * sweep counters and counters are restored afterwards) and keep the fastest:
+ * tile 128..1024, threads 128/256/512, 1 or 2 blocks per SM, hit_unroll 1 or
+ * 2 (the last two choices for mixed-precision batches only). */
 int dym_batch_autotune(dym_batch* b, int32_t nhit, int32_t nsweeps_per_trial, dym_batch_tuning* best);
 int dym_batch_free(dym_batch* b);
 

@@ -21,8 +21,9 @@ def make_chains(engine, seed0=700, precision="mixed"):
             for k, (g, Nx, Nt, beta) in enumerate(SHAPES)], groups
 
 
-@pytest.mark.parametrize("tuning", [Tuning(256, 256, 1, True), Tuning(128, 128, 2, False), Tuning(1024, 256, 1, True)],
-                         ids=["graph-256", "nograph-128", "graph-tile1024"])
+@pytest.mark.parametrize("tuning", [Tuning(256, 256, 1, True), Tuning(128, 128, 2, False), Tuning(1024, 256, 1, True),
+                                    Tuning(512, 256, 1, True, 2), Tuning(256, 128, 2, False, 5)],
+                         ids=["graph-256", "nograph-128", "graph-tile1024", "graph-hitunroll2", "nograph-hitunroll5"])
 @pytest.mark.parametrize("precision", ["mixed", "shared"])
 def test_batch_matches_single_chains(engine, tuning, precision):
     alone, _ = make_chains(engine, precision="fp64")
@@ -54,7 +55,7 @@ def test_batch_autotune_restores_state(engine):
         b.add(lat)
     before = [lat.links.copy() for lat in chains]
     best = b.autotune(nhit=10, nsweeps_per_trial=1)
-    assert best.tile in (128, 256, 512, 1024) and best.threads in (128, 256, 512)
+    assert best.tile in (128, 256, 512, 1024) and best.threads in (128, 256, 512) and best.hit_unroll in (1, 2)
     for x, lat in zip(before, chains):
         assert (x == lat.links).all()
     ref, _ = make_chains(engine, seed0=900)
