@@ -140,6 +140,7 @@ PROTOTYPES = {
     "dym_links_get": (C.c_int, [_P, _u16p]),
     "dym_links_set": (C.c_int, [_P, _u16p]),
     "dym_sweep_host": (C.c_int, [_P, _u16p, _u16p, C.c_int32, C.c_int32, C.POINTER(Stats)]),
+    "dym_sweep_refarray": (C.c_int, [_P, _i32p, C.c_int32, C.c_int32, C.POINTER(Stats)]),
     "dym_chain_get_schedule": (C.c_int, [_P, _u32p, _i32p, _i32p, _u32p, _u32p]),
     "dym_chain_staples": (C.c_int, [_P, C.c_int32, _u32p, C.c_int32, _u16p]),
     "dym_schedule_check": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _i32p, _u64p]),

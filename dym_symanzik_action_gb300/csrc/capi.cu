@@ -322,6 +322,7 @@ static void chain_release(dym_chain* c) {
   cudaFree(c->d_llr_blk);
   cudaFree(c->d_llr_bref);
   cudaFree(c->d_stage);
+  cudaFree(c->d_ref32);
   cudaFree(c->d_first_bad);
   if (c->h_counters) cudaFreeHost(c->h_counters);
   if (c->h_hist) cudaFreeHost(c->h_hist);
@@ -759,6 +760,42 @@ int dym_sweep_host(dym_chain* c, const uint16_t* host_in, uint16_t* host_out, in
     c->sweep = sweep0;  // the sweeps did nothing
     return fail(DYM_EINVAL, "dym_sweep_host: element id out of range at " + std::to_string(c->h_counters[5]));
   }
+  return sweep_report(c, kernel, nsweeps, out);
+}
+
+int dym_sweep_refarray(dym_chain* c, int32_t* a, int32_t nsweeps, int32_t nhit, dym_stats* out) {
+  NvtxRange nvtx("dym_sweep_refarray");
+  if (!c || !a) return fail(DYM_EINVAL, "dym_sweep_refarray: null argument");
+  if (nsweeps < 0 || nhit < 0 || nhit > (1 << 20)) return fail(DYM_EINVAL, "dym_sweep_refarray: bad nsweeps or nhit");
+  DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+  const uint32_t P = c->grp->g->P, V = c->dev.V;
+  const int D = c->p.D;
+  const size_t n = (size_t)V * D;
+  if (!c->d_stage) DYM_CUDA(dmalloc(&c->d_stage, n), "cudaMalloc(links stage)");
+  if (!c->d_first_bad) DYM_CUDA(dmalloc(&c->d_first_bad, 1), "cudaMalloc(links check)");
+  // Page-locked arrays are read and written by the kernels through their
+  // device mapping; any other goes through a device copy of the array.
+  int32_t* mapped = static_cast<int32_t*>(mapped_host(a));
+  if (!mapped && !c->d_ref32) DYM_CUDA(dmalloc(&c->d_ref32, n), "cudaMalloc(reference-layout array)");
+  if (!mapped)
+    DYM_CUDA(cudaMemcpyAsync(c->d_ref32, a, n * 4, cudaMemcpyHostToDevice, c->stream), "upload reference array");
+  DYM_CUDA(launch_links_from_ref(c->dev.links, c->d_stage, mapped ? mapped : c->d_ref32, V, D, P, c->d_first_bad,
+                                 c->stream),
+           "check reference array");
+  int kernel = 0;
+  const uint32_t sweep0 = c->sweep;
+  if (int rc = sweep_enqueue(c, nsweeps, nhit, c->d_first_bad, &kernel)) return rc;
+  DYM_CUDA(launch_links_to_ref(mapped ? mapped : c->d_ref32, c->dev.links, V, D, c->d_first_bad, c->stream),
+           "write reference array");
+  if (int rc = links_check_readback(c)) return rc;
+  DYM_CUDA(cudaStreamSynchronize(c->stream), "dym_sweep_refarray");
+  if (c->h_counters[5] != ~0ull) {
+    c->sweep = sweep0;  // the sweeps did nothing, `a` was not written
+    return fail(DYM_EINVAL, "dym_sweep_refarray: element id out of range at a[" + std::to_string(c->h_counters[5]) +
+                                "]");
+  }
+  if (!mapped)
+    DYM_CUDA(copy_sync(a, c->d_ref32, n * 4, cudaMemcpyDeviceToHost, c->stream), "download reference array");
   return sweep_report(c, kernel, nsweeps, out);
 }
 

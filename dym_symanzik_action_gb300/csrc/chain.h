@@ -107,6 +107,17 @@ cudaError_t launch_links_commit(uint16_t* links, const uint16_t* stage, size_t n
 // mapping (no copy-engine transfer).
 cudaError_t launch_links_from_host(uint16_t* links, uint16_t* stage, const uint16_t* host_mapped, size_t n,
                                    uint32_t P, unsigned long long* first, cudaStream_t s);
+// The reference's link array a[i*D + d] (int32 ids, site-major; device
+// memory or the device mapping of page-locked host memory): its ids checked
+// against P (negative ones too) and narrowed into the stage, direction-major
+// (stage[d*V + i]), then committed into the links as launch_links_commit.
+cudaError_t launch_links_from_ref(uint16_t* links, uint16_t* stage, const int32_t* ref, uint32_t V, int D, uint32_t P,
+                                  unsigned long long* first, cudaStream_t s);
+// The links written back into the reference's layout, ref[i*D + d] =
+// links[d*V + i]; nothing is written when *skip holds a refused upload's
+// index (skip may be null).
+cudaError_t launch_links_to_ref(int32_t* ref, const uint16_t* links, uint32_t V, int D,
+                                const unsigned long long* skip, cudaStream_t s);
 cudaError_t launch_staples(int D, int dir, const SweepArgs& a, const uint32_t* sites, uint32_t n, uint16_t* out,
                            cudaStream_t s);
 // Shared memory of k_sweep_mixed: ReTr (FP64) | class values | inverses | packed
@@ -221,6 +232,7 @@ struct dym_chain {
   dym::LlrBlockRec* d_llr_blk = nullptr;  // per block of it (as many)
   uint8_t* d_llr_bref = nullptr;          // per block: refused by the last scan
   uint16_t* d_stage = nullptr;  // dym_links_set: upload buffer, copied into the links once checked
+  int32_t* d_ref32 = nullptr;   // dym_sweep_refarray: the reference-layout array in device memory (pageable callers)
   unsigned long long* d_first_bad = nullptr;  // dym_links_set: smallest out-of-range index, or ~0
   bool l2_window = false;  // dym_chain_set_l2_window: the stream pins the Cayley table in L2
 };

@@ -192,6 +192,34 @@ __global__ void k_ids_commit(uint16_t* __restrict__ links, const uint16_t* __res
     links[k] = stage[k];
 }
 
+// dym_sweep_refarray's upload: the reference's a[i*D + d] (int32) read in
+// order, checked (ids outside [0, P), the smallest index into *first) and
+// written to the stage direction-major.
+__global__ void k_ids_from_ref(uint16_t* __restrict__ stage, const int32_t* __restrict__ ref, uint32_t V, int D,
+                               uint32_t P, unsigned long long* first) {
+  pdl_launch_dependents();  // the commit may be scheduled; it waits for this grid
+  const size_t n = (size_t)V * D;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const int32_t v = ref[k];
+    const uint32_t i = (uint32_t)(k / (uint32_t)D), d = (uint32_t)(k % (uint32_t)D);
+    if (v < 0 || (uint32_t)v >= P) atomicMin(first, (unsigned long long)k);
+    stage[(size_t)d * V + i] = (uint16_t)v;
+  }
+}
+
+// dym_sweep_refarray's read-back: ref[i*D + d] = links[d*V + i], skipped
+// entirely after a refused upload.
+__global__ void k_links_to_ref(int32_t* __restrict__ ref, const uint16_t* __restrict__ links, uint32_t V, int D,
+                               const unsigned long long* skip) {
+  pdl_wait_prior();
+  if (skip && *skip != ~0ull) return;
+  const size_t n = (size_t)V * D;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t i = (uint32_t)(k / (uint32_t)D), d = (uint32_t)(k % (uint32_t)D);
+    ref[k] = links[(size_t)d * V + i];
+  }
+}
+
 __global__ void k_fill(uint16_t* p, size_t n, uint16_t v) {
   for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) p[l] = v;
 }
@@ -348,6 +376,27 @@ cudaError_t launch_links_from_host(uint16_t* links, uint16_t* stage, const uint1
   if (e != cudaSuccess) return e;
   return launch_phase(k_ids_commit, grid, 256, 0, s, links, (const uint16_t*)stage, n,
                       (const unsigned long long*)first);
+}
+
+cudaError_t launch_links_from_ref(uint16_t* links, uint16_t* stage, const int32_t* ref, uint32_t V, int D, uint32_t P,
+                                  unsigned long long* first, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(first, 0xFF, sizeof(unsigned long long), s);
+  const size_t n = (size_t)V * D;
+  if (e != cudaSuccess || n == 0) return e;
+  const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 8);
+  k_ids_from_ref<<<grid, 256, 0, s>>>(stage, ref, V, D, P, first);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return launch_phase(k_ids_commit, grid, 256, 0, s, links, (const uint16_t*)stage, n,
+                      (const unsigned long long*)first);
+}
+
+cudaError_t launch_links_to_ref(int32_t* ref, const uint16_t* links, uint32_t V, int D,
+                                const unsigned long long* skip, cudaStream_t s) {
+  const size_t n = (size_t)V * D;
+  if (n == 0) return cudaSuccess;
+  const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 8);
+  return launch_phase(k_links_to_ref, grid, 256, 0, s, ref, links, V, D, skip);
 }
 
 cudaError_t launch_fill(uint16_t* links, size_t n, uint16_t v, cudaStream_t s) {

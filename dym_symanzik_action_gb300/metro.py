@@ -261,6 +261,23 @@ class Lattice:
         return SweepStats(st.hits, st.accepts, st.rechecks, st.max_ds_err, st.sweep, st.launches, st.device_ms,
                           st.kernel)
 
+    def update_refarray(self, a: np.ndarray, nsweeps: int = 1, nhit: int = 20) -> SweepStats:
+        """update() applied in place to a link array in the reference's layout
+        (dym_sweep_refarray): `a` is int32 with a[i*D + d] the id of link
+        (site i, direction d), C-contiguous and writeable."""
+        if a.dtype != np.int32 or a.size != self.D * self.V or not a.flags["C_CONTIGUOUS"] or \
+                not a.flags["WRITEABLE"]:
+            raise ValueError("a must be a writeable C-contiguous int32 array of V*D entries")
+        st = _lib.Stats()
+        check(lib().dym_sweep_refarray(self._h, ptr(a, C.c_int32), nsweeps, nhit, C.byref(st)))
+        self.hit += st.hits
+        self.acc += st.accepts
+        self.rechecks += st.rechecks
+        self.max_ds_err = max(self.max_ds_err, st.max_ds_err)
+        self.sweeps = st.sweep
+        return SweepStats(st.hits, st.accepts, st.rechecks, st.max_ds_err, st.sweep, st.launches, st.device_ms,
+                          st.kernel)
+
     def measure(self, wl_nx: int = 0, wl_nt: int = 0) -> Measurement:
         """Observables (dym-mod-metro.cpp:282-318); wl_nx/wl_nt 0 = full Nx x Nt
         grid as the reference, -1 = no Wilson grid."""

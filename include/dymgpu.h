@@ -248,6 +248,20 @@ int dym_links_set(dym_chain* c, const uint16_t* host_in);
 int dym_sweep_host(dym_chain* c, const uint16_t* host_in, uint16_t* host_out, int32_t nsweeps, int32_t nhit,
                    dym_stats* out);
 
+/* nsweeps sweeps applied in place to an array in the reference's own layout:
+ * a[i*D + d] holds the element id (int32, group_t of group.h:6) of link
+ * (site i, direction d), site i = getidx(pos) (lattice.c), the array that
+ * update() (dym-mod-metro.cpp:146-197) reads and writes, malloc'd at
+ * dym-mod-metro.cpp:253.  So the reference's `for (k < K) update();` becomes
+ * one call on its own array.  The array is uploaded and checked (every id in
+ * [0, P)), the sweeps run, and the result is written back into it.  A
+ * page-locked array (cudaHostAlloc / cudaHostRegister) is read and written by
+ * the kernels through its device mapping; any other is copied through a
+ * device array of V*D int32 (allocated on first use, kept with the chain).
+ * An id outside [0, P) returns DYM_EINVAL with the chain, its sweep counter
+ * and `a` unchanged. */
+int dym_sweep_refarray(dym_chain* c, int32_t* a, int32_t nsweeps, int32_t nhit, dym_stats* out);
+
 /* Lattice and schedule facts: V, number of colour phases per sweep, and the
  * phase layout (arrays may be NULL; sizes nphase, nphase, V*D). */
 int dym_chain_get_schedule(const dym_chain* c, uint32_t* V, int32_t* nphase,
