@@ -193,10 +193,12 @@ static int build_vt_tables(dym_chain* c, const std::vector<uint16_t>& pool) {
 }
 
 // Hits per group whose draws the mixed kernels compute ahead (1, 2, 5 or
-// 10; DYM_HIT_UNROLL overrides the default).
-static int hit_unroll_setting() {
+// 10; for the value-table kernel 2 means speculative pairs, visit.cuh
+// vt_hits).  The default is per kernel, the measured faster one:
+// value-table 2, element-table 1; DYM_HIT_UNROLL overrides both.
+static int hit_unroll_setting(int kernel) {
   const char* e = std::getenv("DYM_HIT_UNROLL");
-  const int v = e ? std::atoi(e) : kDefaultHitUnroll;
+  const int v = e ? std::atoi(e) : kernel == DYM_KERNEL_MIXED_VALUES ? kDefaultHitUnrollValues : kDefaultHitUnroll;
   return v >= 10 ? 10 : v >= 5 ? 5 : v >= 2 ? 2 : 1;
 }
 
@@ -557,7 +559,7 @@ static int sweep_enqueue(dym_chain* c, int32_t nsweeps, int32_t nhit, const unsi
   const int kernel = sweep_kernel(c);
   SweepArgs a = sweep_args(c, kernel);
   a.nhit = nhit;
-  a.hit_unroll = hit_unroll_setting();
+  a.hit_unroll = hit_unroll_setting(kernel);
   a.lanes_per_link = lanes_per_link_setting();
   a.skip = skip;
   const Schedule& s = c->sched;

@@ -91,7 +91,8 @@ constexpr int kMixedMaxCls = 32;    // classes addressable by the 5 high bits of
 constexpr uint32_t kMixedMaxP = 2048;  // 16-bit packed entries: element ids in the 11 low bits
 constexpr int kMixedMaxExtent = 256;   // coordinates packed 8 bits per axis
 constexpr int kMixedMaxThreads = 512;
-constexpr int kDefaultHitUnroll = 1;
+constexpr int kDefaultHitUnroll = 1;        // element-table kernel (k_sweep_mixed)
+constexpr int kDefaultHitUnrollValues = 2;  // value-table kernel (k_sweep_vt): speculative pairs
 constexpr int kDefaultLanesPerLink = 1;
 // Threads per block of the two-lanes-per-link value-table kernel at most
 // (two lanes for each of 448 links; 72 registers a thread).

@@ -357,6 +357,13 @@ __device__ __forceinline__ void vt_prepare(const SweepArgs& a, uint32_t i, uint3
   for (int j = NS; j < NT; ++j) M += s_val[u[j]];
 }
 
+// The hits of a value-table visit.  HU = 1: one hit at a time.  HU = 2: the
+// hits are taken in pairs whose sums are both formed from the current state
+// before the first is decided (48 independent shared loads instead of two
+// dependent rounds of 24); when the first is accepted the second's sums are
+// formed again from the new state, so the decisions are HU = 1's exactly.
+// HU = 5 or 10: the draws of a group are computed ahead (HitDraws), the hits
+// then taken one at a time.
 template <int D, int DIR, int HU = 1>
 __device__ __forceinline__ void vt_hits(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
                                         const uint16_t* s_inv, const int16_t* s_vsub, const uint16_t* s_pool,
@@ -368,60 +375,73 @@ __device__ __forceinline__ void vt_hits(const SweepArgs& a, uint32_t i, uint32_t
   const uint32_t P = a.P, np = a.npool;
   double oldact = 0.0;
   bool old_ok = false;
-  for (int h0 = 0; h0 < a.nhit; h0 += HU) {
-    HitDraws<HU> dr;
-    dr.fill(a, sweep, i, DIR, h0);
+  // The fixed-point sums of proposal k from the current u.
+  auto sums = [&](uint32_t k, int32_t& Rn, int32_t& Mn) {
+    const int16_t* col = s_vsub + k;
+    Rn = 0;
+    Mn = 0;
 #pragma unroll
-    for (int q = 0; q < HU; ++q) {
-      if (HU > 1 && h0 + q >= a.nhit) break;
-      const uint32_t k = dr.k[q];
-      const int16_t* col = s_vsub + k;
-      int32_t Rn = 0, Mn = 0;
+    for (int j = 0; j < NS; ++j) Rn += col[u[j] * np];
 #pragma unroll
-      for (int j = 0; j < NS; ++j) Rn += col[u[j] * np];
+    for (int j = NS; j < NT; ++j) Mn += col[u[j] * np];
+  };
+  // Decide hit h (proposal k, threshold t, sums Rn, Mn) and apply it;
+  // returns whether it was accepted.
+  auto hit = [&](int h, uint32_t k, float t, int32_t Rn, int32_t Mn) -> bool {
+    const float ds = __fmaf_rn(a.b2f, (float)(Mn - M), __fmul_rn(a.b1f, (float)(Rn - R))) * a.dscale;
+    const float band = a.dmargin + __fmaf_rn(t, 0x1p-20f, 0x1p-19f);
+    bool acc;
+    bool exact = false;
+    if (ds < t - band) {
+      acc = true;
+    } else if (ds > t + band) {
+      acc = false;
+    } else {
+      const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_METRO);
+      const uint32_t g = s_pool[k];
+      double newact;
+      exact_actions<D>(a, s_inv, s_retr, u, b, __ldg(mult + b * P + g), !old_ok, oldact, newact);
+      old_ok = true;
+      acc = dym_accept_fast(oldact, newact, dym_u53(r.v[1], r.v[2]));
+      max_err = fmaxf(max_err, fabsf(ds - (float)DYM_SUB(newact, oldact)));
+      ++rechecks;
+      exact = true;
+      if (acc) oldact = newact;
+    }
+    ++hits;
+    if (acc) {
+      const uint32_t g = s_pool[k];
+      b = __ldg(mult + b * P + g);
 #pragma unroll
-      for (int j = NS; j < NT; ++j) Mn += col[u[j] * np];
-      const float ds = __fmaf_rn(a.b2f, (float)(Mn - M), __fmul_rn(a.b1f, (float)(Rn - R))) * a.dscale;
-      const float t = dr.t[q];
-      const float band = a.dmargin + __fmaf_rn(t, 0x1p-20f, 0x1p-19f);
-      bool acc;
-      bool exact = false;
-      uint32_t e[NT];
-      bool have_e = false;
-      if (ds < t - band) {
-        acc = true;
-      } else if (ds > t + band) {
-        acc = false;
-      } else {
-        const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)(h0 + q), DYM_TAG_METRO);
-        const uint32_t g = s_pool[k];
+      for (int j = 0; j < NT; ++j) u[j] = __ldg(mult + u[j] * P + g);
+      R = Rn;
+      M = Mn;
+      old_ok = exact;
+      ++accs;
+    }
+    return acc;
+  };
+  if constexpr (HU == 2) {
+    for (int h0 = 0; h0 < a.nhit; h0 += 2) {
+      HitDraws<2> dr;
+      dr.fill(a, sweep, i, DIR, h0);
+      const bool two = h0 + 1 < a.nhit;
+      int32_t R0, M0, R1 = 0, M1 = 0;
+      sums(dr.k[0], R0, M0);
+      if (two) sums(dr.k[1], R1, M1);
+      if (hit(h0, dr.k[0], dr.t[0], R0, M0) && two) sums(dr.k[1], R1, M1);  // the state moved
+      if (two) hit(h0 + 1, dr.k[1], dr.t[1], R1, M1);
+    }
+  } else {
+    for (int h0 = 0; h0 < a.nhit; h0 += HU) {
+      HitDraws<HU> dr;
+      dr.fill(a, sweep, i, DIR, h0);
 #pragma unroll
-        for (int j = 0; j < NT; ++j) e[j] = __ldg(mult + u[j] * P + g);
-        have_e = true;
-        double newact;
-        exact_actions<D>(a, s_inv, s_retr, u, b, __ldg(mult + b * P + g), !old_ok, oldact, newact);
-        old_ok = true;
-        acc = dym_accept_fast(oldact, newact, dym_u53(r.v[1], r.v[2]));
-        max_err = fmaxf(max_err, fabsf(ds - (float)DYM_SUB(newact, oldact)));
-        ++rechecks;
-        exact = true;
-        if (acc) oldact = newact;
-      }
-      ++hits;
-      if (acc) {
-        const uint32_t g = s_pool[k];
-        b = __ldg(mult + b * P + g);
-        if (have_e) {
-#pragma unroll
-          for (int j = 0; j < NT; ++j) u[j] = e[j];
-        } else {
-#pragma unroll
-          for (int j = 0; j < NT; ++j) u[j] = __ldg(mult + u[j] * P + g);
-        }
-        R = Rn;
-        M = Mn;
-        old_ok = exact;
-        ++accs;
+      for (int q = 0; q < HU; ++q) {
+        if (HU > 1 && h0 + q >= a.nhit) break;
+        int32_t Rn, Mn;
+        sums(dr.k[q], Rn, Mn);
+        hit(h0 + q, dr.k[q], dr.t[q], Rn, Mn);
       }
     }
   }

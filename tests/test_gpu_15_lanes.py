@@ -1,4 +1,5 @@
-"""Two lanes per link in the value-table kernel (DYM_LANES_PER_LINK=2).
+"""Two lanes per link in the value-table kernel (DYM_LANES_PER_LINK=2), and
+its hit-unroll variants (DYM_HIT_UNROLL).
 
 The pair splits a link's staples by side (+f / -f of every plane), sums its
 partial fixed-point sums with shuffles and takes each decision from the same
@@ -68,3 +69,20 @@ def test_two_lanes_moving_chain_matches_oracle(engine, monkeypatch):
         h, a = ol.sweep(sched, beta, seed, s, 1, nhit)
         assert (got[s][1], got[s][2]) == (h, a), s
         assert (got[s][0].ravel() == ol.links).all(), f"sweep {s}"
+
+
+@pytest.mark.parametrize("name", ["cold_32x8_b3", "hot_8x8_b2", "hot_16x8_b1"])
+def test_hit_unroll_variants_equal(engine, monkeypatch, name):
+    """The value-table kernel's hits one at a time (DYM_HIT_UNROLL=1), in
+    speculative pairs (2, the default: both sums from the current state, the
+    second re-formed after an accept) and in groups of draws computed ahead
+    (5, 10) take the same decisions."""
+    shape, beta, seed, start, sweeps, nhit = CASES[name]
+    runs = {}
+    for hu in ("1", "2", "5", "10"):
+        monkeypatch.setenv("DYM_HIT_UNROLL", hu)
+        runs[hu] = run(engine, monkeypatch, 1, shape, beta, seed, start, sweeps, nhit)
+    for hu in ("2", "5", "10"):
+        for s, (a, b) in enumerate(zip(runs["1"], runs[hu])):
+            assert a[1:5] == b[1:5], (hu, s)
+            assert np.array_equal(a[0], b[0]), (hu, s)
