@@ -368,10 +368,10 @@ def serving_bench(dym, device: int, n_requests: int, nhit: int = 20, step_sweeps
 
 
 def sharded_bench(local: int, rank: int, world: int, n_requests: int, sweeps: int = 5, nhit: int = 10) -> dict:
-    """The forms that shard (configs 3 and 5): every rank runs its share of the
-    256-chain ensemble as one Batch and its share of the request stream
-    through one Server (shard.run_sharded; partition by work, no data-path
-    collective), results gathered to rank 0.  Value = all ranks' link-hits /
+    """The forms that shard: every rank runs its share of the 256-chain
+    ensemble as one Batch and its share of the LLR request stream through one
+    Server (shard.run_sharded; partition by work, no data-path collective),
+    results gathered to rank 0.  Value = all ranks' link-hits /
     the slowest rank's wall time (total work fixed: strong scaling)."""
     import numpy as np
     import torch.distributed as dist
@@ -396,7 +396,7 @@ def sharded_bench(local: int, rank: int, world: int, n_requests: int, sweeps: in
     if rank == 0:
         wall = max(x["wall_s"] for x in ts)
         hits = sum(x.get("hits", 0) for x in ts)
-        out["ensemble"] = {"workload": "256 chains (config 3), 5 sweeps, 10 hits/link, sharded by work",
+        out["ensemble"] = {"workload": "the 256-chain ensemble, 5 sweeps, 10 hits/link, sharded by work",
                            "ranks": world, "chains_per_rank": [x["chains"] for x in ts],
                            "links_per_rank": [x["links"] for x in ts], "chains_gathered": len(merged),
                            "link_hits_per_s": hits / wall, "slowest_rank_wall_s": wall, "scaling": "strong"}
@@ -409,7 +409,7 @@ def sharded_bench(local: int, rank: int, world: int, n_requests: int, sweeps: in
         if rank == 0:
             wall = max(x["wall_s"] for x in ts)
             L = np.array([v[3] for v in merged.values()])
-            out["serving"] = {"workload": f"first {len(reqs)} requests of the config-5 stream, sharded by work",
+            out["serving"] = {"workload": f"first {len(reqs)} requests of the LLR request stream, sharded by work",
                               "ranks": world, "requests_per_rank": [x["requests"] for x in ts],
                               "link_hits_per_s": sum(x["link_hits"] for x in ts) / wall,
                               "latency_p50_s": float(np.percentile(L, 50)),
@@ -658,7 +658,7 @@ def run_ours(args):
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline()
     if world > 1:
-        # every rank takes part: each runs its share of configs 3 and 5
+        # every rank takes part: each runs its share of the ensemble and the stream
         sh = sharded_bench(local, rank, world, min(args.serve_requests, 400))
         if rank == 0:
             line["sharded"] = sh

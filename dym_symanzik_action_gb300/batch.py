@@ -1,4 +1,4 @@
-"""Batched ensemble of independent chains (config-3 style workloads).
+"""Batched ensemble of independent chains (many lattices of uneven size).
 
 The reference runs one process per chain (evermore.sh, jobs2run); here the
 chains stay separate Lattice objects, and a Batch updates all of them with one

@@ -25,11 +25,11 @@ It builds oracle/_ref/ (oracle/build_ref.sh) and writes:
 * chains_1sigma.npz -- GMES/RMES series of the unmodified reference
   executable (its own table, NHIT 20, one thread) at the 4^4 couplings
   (0, 1.5, 0.1) for several seeds: the oracle for the 1-sigma comparison.
-* chains_config1.npz, chains_config1_eq.npz, chains_config2.npz -- per-run
-  measurement series of the unmodified reference executable (NHIT 10 build,
-  its own mys1080-v4, hot starts) at the BASELINE workloads: config 1 as
-  stated, config 1's couplings after 3,000 thermalisation sweeps, and the
-  config-2 lattice (make_chains_baseline).
+* chains_4x4x4x4_hot.npz, chains_4x4x4x4_hot_eq.npz, chains_32x32x32x8_hot.npz
+  -- per-run measurement series of the unmodified reference executable (NHIT
+  10 build, its own mys1080-v4, hot starts) at the benchmark workloads: the
+  4^4 lattice at beta = (0, 1.5, 0.1) with Ntherm 100, the same after 3,000
+  thermalisation sweeps, and the 32^3 x 8 lattice (make_chains_workloads).
 * llr_ref.npz -- the ANE table (window centre, mean a_n, sd, samples) of the
   unmodified reference llr executable (its own S(1080) table, one thread) on a
   four-window ladder of S1 (plaquette) windows on a 4^3x2 lattice with R = 20
@@ -325,40 +325,40 @@ def _ref_chain(job):
     return seed, g, rm, acc[-1]
 
 
-# The BASELINE workloads as statistical fixtures: config 1 as stated (4^4 hot,
+# The benchmark workloads as statistical fixtures: the 4^4 run as stated (hot,
 # beta = (0, 1.5, 0.1), NHIT 10, Ntherm 100, K 10, N 100, the reference's
-# nearest-element pool), and the config-2 lattice (32^3 x 8) with Polyakov
+# nearest-element pool), and the 32^3 x 8 lattice of the single-chain benchmark with Polyakov
 # loop and the 8 x 8 Wilson grid, from a hot start in the disordered phase,
 # beta = (0, 1.0, 0.1), where the plaquette settles within a few sweeps (at
-# config 2's own couplings a cold chain is frozen, and a hot one -- like one
-# at the config-1 couplings, which order 4^4 -- relaxes through a
+# the benchmark's own couplings (0, 3.0, -0.15) a cold chain is frozen, and a hot one -- like one
+# at the 4^4 run's couplings, which order 4^4 -- relaxes through a
 # first-order transition far longer than a fixture run, so that the
 # reference's racing updates and the engine's colour phases would be compared
 # out of equilibrium), Ntherm 20, K 4, N 2.
-CHAINS_CONFIG1 = dict(D=4, Nt=4, Nx=4, beta=(0.0, 1.5, 0.1), K=10, N=100, Ntherm=100, seeds=list(range(3001, 3025)),
+CHAINS_4444 = dict(D=4, Nt=4, Nx=4, beta=(0.0, 1.5, 0.1), K=10, N=100, Ntherm=100, seeds=list(range(3001, 3025)),
                       threads=1)
-# Config 1's couplings in equilibrium: the stated protocol (Ntherm 100) ends
+# The 4^4 couplings in equilibrium: the stated protocol (Ntherm 100) ends
 # while the hot start is still relaxing (the plaquette falls from -1.6 to
 # -2.91 over its 1,100 sweeps, most of it in the first 300), so its run means
 # compare two update orders' relaxation; with Ntherm 3000 both sit on the
 # plateau (-2.915) and the runs sample the stationary distribution.
-CHAINS_CONFIG1_EQ = dict(D=4, Nt=4, Nx=4, beta=(0.0, 1.5, 0.1), K=10, N=100, Ntherm=3000,
+CHAINS_4444_EQ = dict(D=4, Nt=4, Nx=4, beta=(0.0, 1.5, 0.1), K=10, N=100, Ntherm=3000,
                          seeds=list(range(3101, 3133)), threads=1)
-CHAINS_CONFIG2 = dict(D=4, Nt=8, Nx=32, beta=(0.0, 1.0, 0.1), K=4, N=2, Ntherm=20, seeds=list(range(4001, 4013)),
+CHAINS_32C8 = dict(D=4, Nt=8, Nx=32, beta=(0.0, 1.0, 0.1), K=4, N=2, Ntherm=20, seeds=list(range(4001, 4013)),
                       threads=os.cpu_count() or 1, wl=8)
 
 
-def make_chains_baseline(which=("chains_config1.npz", "chains_config1_eq.npz", "chains_config2.npz")):
-    """chains_config1.npz, chains_config1_eq.npz and chains_config2.npz:
-    per-run GMES/RMES of the unmodified reference (its Makefile flags, NHIT
-    10, its own mys1080-v4): config 1 (as stated and in equilibrium) one
-    thread per run (runs in parallel), the config-2 lattice with all cores per
-    run.  Stored per run: the measurement series of ReP, ImP,
-    plaq, rect and the Wilson grid (config 2: its first 8 x 8)."""
+def make_chains_workloads(which=("chains_4x4x4x4_hot.npz", "chains_4x4x4x4_hot_eq.npz", "chains_32x32x32x8_hot.npz")):
+    """chains_4x4x4x4_hot.npz, chains_4x4x4x4_hot_eq.npz and
+    chains_32x32x32x8_hot.npz: per-run GMES/RMES of the unmodified reference
+    (its Makefile flags, NHIT 10, its own mys1080-v4): the 4^4 runs (as stated
+    and in equilibrium) one thread per run (runs in parallel), the 32^3 x 8
+    lattice with all cores per run.  Stored per run: the measurement series of ReP, ImP,
+    plaq, rect and the Wilson grid (32^3 x 8: its first 8 x 8)."""
     from concurrent.futures import ProcessPoolExecutor
     table = os.path.join(REF_DIR, "groups", "mys1080-v4")
-    for name, C in (("chains_config1.npz", CHAINS_CONFIG1), ("chains_config1_eq.npz", CHAINS_CONFIG1_EQ),
-                    ("chains_config2.npz", CHAINS_CONFIG2)):
+    for name, C in (("chains_4x4x4x4_hot.npz", CHAINS_4444), ("chains_4x4x4x4_hot_eq.npz", CHAINS_4444_EQ),
+                    ("chains_32x32x32x8_hot.npz", CHAINS_32C8)):
         if name not in which:
             continue
         jobs = [(table, C["D"], C["Nt"], C["Nx"], C["beta"], s, C["K"], C["N"], C["Ntherm"], C["threads"])
@@ -447,8 +447,8 @@ def make_llr2d():
 def main():
     import argparse
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["iso", "staples", "sweeps", "reftables", "chains", "chains_baseline",
-                                       "chains_config1", "chains_config1_eq", "chains_config2", "llr", "llr_s2",
+    ap.add_argument("--only", choices=["iso", "staples", "sweeps", "reftables", "chains", "chains_workloads",
+                                       "chains_4444", "chains_4444_eq", "chains_32c8", "llr", "llr_s2",
                                        "llr2d"])
     ap.add_argument("--skip-build", action="store_true", help="use oracle/_ref as built (parallel invocations)")
     args = ap.parse_args()
@@ -467,10 +467,11 @@ def main():
         make_reftables()
     if only in (None, "chains"):
         make_chains()
-    if only in (None, "chains_baseline"):
-        make_chains_baseline()
-    if only in ("chains_config1", "chains_config1_eq", "chains_config2"):
-        make_chains_baseline((only + ".npz",))
+    if only in (None, "chains_workloads"):
+        make_chains_workloads()
+    if only in ("chains_4444", "chains_4444_eq", "chains_32c8"):
+        make_chains_workloads(({"chains_4444": "chains_4x4x4x4_hot", "chains_4444_eq": "chains_4x4x4x4_hot_eq",
+                                "chains_32c8": "chains_32x32x32x8_hot"}[only] + ".npz",))
     if only in (None, "llr"):
         make_llr()
     if only in (None, "llr_s2"):

@@ -1,21 +1,21 @@
-"""Statistical parity with the unmodified reference at the BASELINE workloads.
+"""Statistical parity with the unmodified reference at the benchmark workloads.
 
 The fixtures hold measurement series of the reference's own executable (its
 Makefile flags, NHIT 10, its own mys1080-v4, nearest-element pool, hot
 starts; tests/golden/make_golden.py):
 
-* chains_config1.npz -- config 1 as stated: 4^4, beta = (0, 1.5, 0.1), Ntherm
+* chains_4x4x4x4_hot.npz -- the 4^4 run as stated: beta = (0, 1.5, 0.1), Ntherm
   100, K 10, N 100, the full 4 x 4 Wilson grid; 24 runs, one thread each (so
   each run is the reference's serial update order).
-* chains_config1_eq.npz -- the same couplings after 3,000 thermalisation
-  sweeps; 32 runs.  As stated, config 1 ends while the hot start is still
+* chains_4x4x4x4_hot_eq.npz -- the same couplings after 3,000 thermalisation
+  sweeps; 32 runs.  As stated, the 4^4 run ends while the hot start is still
   relaxing: the plaquette falls from -1.6 to -2.91 over the 1,100 sweeps (to
   -2.91 only at the end), so its run means compare two update orders' approach
   to equilibrium (the reference's serial order, the engine's colour phases:
   both valid, not equally fast per sweep) as well as the distribution; with
   3,000 sweeps first both sample the plateau (-2.915), the stationary
   distribution the two must share.
-* chains_config2.npz -- the config-2 lattice, 32^3 x 8, with the Polyakov loop
+* chains_32x32x32x8_hot.npz -- the single-chain benchmark's lattice, 32^3 x 8, with the Polyakov loop
   and the 8 x 8 Wilson grid, in the disordered phase (beta = (0, 1.0, 0.1);
   Ntherm 20, K 4, N 2); 12 runs with all cores (the reference's OpenMP build).
 
@@ -33,8 +33,8 @@ independent trials: it is printed beside the 68% expected, and the joint
 test is Hotelling's two-sample T^2 on a well-conditioned subset (ReP, ImP,
 plaquette, W[1][1], W[3][3]).
 
-Bars.  Config 1 (20 observables), as stated and in equilibrium: every
-|z| < 2 and the T^2 test's p-value above 0.01.  Config-2 lattice (68
+Bars.  The 4^4 runs (20 observables), as stated and in equilibrium: every
+|z| < 2 and the T^2 test's p-value above 0.01.  The 32^3 x 8 lattice (68
 observables, most of them large Wilson loops that are zero within noise):
 with that many comparisons a few beyond 2 are expected by chance
 (P(all 68 < 2) ~ 4% for independent ones), so every |z| < 3.5 (a 3%
@@ -75,7 +75,7 @@ def zscores(ref, ours):
 
 def hotelling_p(ref, ours, cols=(0, 1, 2, 9, 19)):
     """p-value of Hotelling's two-sample T^2 test of equal means on the
-    columns `cols` (ReP, ImP, plaquette, W[1][1], W[3][3] of config 1)."""
+    columns `cols` (ReP, ImP, plaquette, W[1][1], W[3][3] of the 4^4 runs)."""
     from scipy.stats import f as fdist
     a, b = ref[:, list(cols)], ours[:, list(cols)]
     n1, n2, p = len(a), len(b), a.shape[1]
@@ -90,10 +90,10 @@ def params(fix):
     return ast.literal_eval(str(fix["params"]).split(" table=")[0])
 
 
-@pytest.mark.parametrize("fixture,seeds", [("chains_config1.npz", range(5001, 5025)),
-                                           ("chains_config1_eq.npz", range(5101, 5133))],
+@pytest.mark.parametrize("fixture,seeds", [("chains_4x4x4x4_hot.npz", range(5001, 5025)),
+                                           ("chains_4x4x4x4_hot_eq.npz", range(5101, 5133))],
                          ids=["as-stated", "equilibrium"])
-def test_config1_within_two_sigma_of_reference(engine, ref_table, fixture, seeds):
+def test_4x4x4x4_within_two_sigma_of_reference(engine, ref_table, fixture, seeds):
     fix = golden(fixture)
     C = params(fix)
     ref = np.array([fix[f"series_{s}"].mean(0) for s in fix["seeds"]])
@@ -107,8 +107,8 @@ def test_config1_within_two_sigma_of_reference(engine, ref_table, fixture, seeds
     assert p > 0.01, p
 
 
-def test_config2_lattice_agrees_with_reference(engine, ref_table):
-    fix = golden("chains_config2.npz")
+def test_32x32x32x8_lattice_agrees_with_reference(engine, ref_table):
+    fix = golden("chains_32x32x32x8_hot.npz")
     C = params(fix)
     ref = np.array([fix[f"series_{s}"].mean(0) for s in fix["seeds"]])
     ours = run_engine(engine, ref_table, C, range(6001, 6013), C["wl"])
