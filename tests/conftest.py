@@ -111,3 +111,16 @@ def staged_reference():
     oracle/stage_ref.sh) or $REF_DIR, if present; else None."""
     from oracle.oracle import ref_dir
     return ref_dir()
+
+
+def hotelling_p(ref, ours, cols):
+    """p-value of Hotelling's two-sample T^2 test of equal means of the per-run
+    observables ref, ours ([runs, observables]) on the columns `cols` (a
+    subset whose pooled covariance is well conditioned)."""
+    from scipy.stats import f as fdist
+    a, b = ref[:, list(cols)], ours[:, list(cols)]
+    n1, n2, p = len(a), len(b), a.shape[1]
+    S = ((n1 - 1) * np.cov(a, rowvar=False) + (n2 - 1) * np.cov(b, rowvar=False)) / (n1 + n2 - 2)
+    d = a.mean(0) - b.mean(0)
+    t2 = n1 * n2 / (n1 + n2) * d @ np.linalg.solve(S, d)
+    return float(fdist.sf((n1 + n2 - p - 1) / (p * (n1 + n2 - 2)) * t2, p, n1 + n2 - p - 1))

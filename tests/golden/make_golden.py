@@ -24,7 +24,8 @@ It builds oracle/_ref/ (oracle/build_ref.sh) and writes:
   the reference's get_staples and get_rect_loops.
 * chains_1sigma.npz -- GMES/RMES series of the unmodified reference
   executable (its own table, NHIT 20, one thread) at the 4^4 couplings
-  (0, 1.5, 0.1) for several seeds: the oracle for the 1-sigma comparison.
+  (0, 1.5, 0.1) for 24 seeds: the statistical oracle at the reference's
+  compiled NHIT.
 * chains_4x4x4x4_hot.npz, chains_4x4x4x4_hot_eq.npz, chains_32x32x32x8_hot.npz
   -- per-run measurement series of the unmodified reference executable (NHIT
   10 build, its own mys1080-v4, hot starts) at the benchmark workloads: the
@@ -292,18 +293,24 @@ def parse_log(text):
     return np.array(gmes), np.array(rmes), np.array(acc)
 
 
-def make_chains():
+def _ref_chain20(seed):
+    """One run of the unmodified reference executable (NHIT 20, its compiled
+    default), 4^4 at (0, 1.5, 0.1), K 10, N 100, Ntherm 100, hot, one thread."""
     exe = os.path.join(ROOT, "oracle", "_ref", "dym-mod-metro")
     table = os.path.join(REF_DIR, "groups", "mys1080-v4")
-    seeds = [101, 202, 303, 404, 505, 606]
-    out = {}
-    env = dict(os.environ, OMP_NUM_THREADS="1")
     with tempfile.TemporaryDirectory() as td:  # the -pg build writes gmon.out into its cwd
-        for s in seeds:
-            r = subprocess.run([exe, table, "4", "4", "4", "0", "1.5", "0.1", str(s), "10", "100", "100"],
-                               cwd=td, env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
-                               check=True)
-            g, rm, acc = parse_log(r.stdout)
+        r = subprocess.run([exe, table, "4", "4", "4", "0", "1.5", "0.1", str(seed), "10", "100", "100"], cwd=td,
+                           env=dict(os.environ, OMP_NUM_THREADS="1"), stdout=subprocess.PIPE,
+                           stderr=subprocess.STDOUT, text=True, check=True)
+    return seed, parse_log(r.stdout)
+
+
+def make_chains():
+    from concurrent.futures import ProcessPoolExecutor
+    seeds = list(range(101, 125))
+    out = {}
+    with ProcessPoolExecutor(max(1, int(os.environ.get("GOLDEN_WORKERS", os.cpu_count() or 1)))) as ex:
+        for s, (g, rm, acc) in ex.map(_ref_chain20, seeds):
             out[f"gmes_{s}"] = g
             out[f"rmes_{s}"] = rm
             out[f"acc_{s}"] = acc

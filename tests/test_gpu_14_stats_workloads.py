@@ -42,7 +42,7 @@ family-wise rate), at least 85% within 2 and at least half within 1."""
 import numpy as np
 import pytest
 
-from conftest import golden
+from conftest import golden, hotelling_p
 
 pytestmark = pytest.mark.gpu
 
@@ -73,18 +73,6 @@ def zscores(ref, ours):
     return (ours.mean(0) - ref.mean(0)) / np.where(se > 0, se, 1)
 
 
-def hotelling_p(ref, ours, cols=(0, 1, 2, 9, 19)):
-    """p-value of Hotelling's two-sample T^2 test of equal means on the
-    columns `cols` (ReP, ImP, plaquette, W[1][1], W[3][3] of the 4^4 runs)."""
-    from scipy.stats import f as fdist
-    a, b = ref[:, list(cols)], ours[:, list(cols)]
-    n1, n2, p = len(a), len(b), a.shape[1]
-    S = ((n1 - 1) * np.cov(a, rowvar=False) + (n2 - 1) * np.cov(b, rowvar=False)) / (n1 + n2 - 2)
-    d = a.mean(0) - b.mean(0)
-    t2 = n1 * n2 / (n1 + n2) * d @ np.linalg.solve(S, d)
-    return float(fdist.sf((n1 + n2 - p - 1) / (p * (n1 + n2 - 2)) * t2, p, n1 + n2 - p - 1))
-
-
 def params(fix):
     import ast
     return ast.literal_eval(str(fix["params"]).split(" table=")[0])
@@ -99,7 +87,7 @@ def test_4x4x4x4_within_two_sigma_of_reference(engine, ref_table, fixture, seeds
     ref = np.array([fix[f"series_{s}"].mean(0) for s in fix["seeds"]])
     ours = run_engine(engine, ref_table, C, seeds, 0)
     z = zscores(ref, ours)
-    p = hotelling_p(ref, ours)
+    p = hotelling_p(ref, ours, (0, 1, 2, 9, 19))  # ReP, ImP, plaquette, W[1][1], W[3][3]
     print(f"{fixture}: z = {np.round(z, 2).tolist()}; within 1 sigma {np.mean(np.abs(z) < 1):.2f} "
           f"(68% expected for independent observables); Hotelling T^2 p = {p:.3f}")
     assert ours.shape[1] == ref.shape[1] == 4 + 16
