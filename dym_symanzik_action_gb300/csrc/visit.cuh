@@ -79,17 +79,21 @@ __device__ __forceinline__ bool sweep_skipped(const SweepArgs& a) { return a.ski
 // the conjugate u_j g used by the fast path would not do.  Three table
 // gathers per term; only hits within the error bound of their threshold come
 // here.  need_old false leaves oldact as it is.
+// The value-table kernel passes its terms as shared-memory row offsets
+// u_j * rb (rb = row bytes); `magic` = ceil(2^32 / rb) recovers u_j exactly
+// (__umulhi, since u_j rb < 2^32).  magic 0: the terms are the elements.
 template <int D>
 __device__ __forceinline__ void exact_actions(const SweepArgs& a, const uint16_t* s_inv, const double* s_retr,
                                               const uint32_t* u, uint32_t b, uint32_t bnew, bool need_old,
-                                              double& oldact, double& newact) {
+                                              double& oldact, double& newact, uint32_t magic = 0) {
   constexpr int NS = 2 * (D - 1), NT = 8 * (D - 1);
   const uint16_t* __restrict__ mult = a.mult;
   const uint32_t P = a.P, bi = s_inv[b];
   double r1 = 0, m1 = 0, r1n = 0, m1n = 0;
 #pragma unroll
   for (int j = 0; j < NT; ++j) {
-    const uint32_t sj = __ldg(mult + u[j] * P + bi);
+    const uint32_t uj = magic ? __umulhi(u[j], magic) : u[j];
+    const uint32_t sj = __ldg(mult + uj * P + bi);
     const double vn = s_retr[__ldg(mult + bnew * P + sj)];
     if (j < NS) r1n = DYM_ADD(r1n, vn);
     else m1n = DYM_ADD(m1n, vn);
@@ -372,18 +376,25 @@ __device__ __forceinline__ void vt_hits(const SweepArgs& a, uint32_t i, uint32_t
   constexpr int NS = 2 * (D - 1), NR = 6 * (D - 1), NT = NS + NR;
   const uint32_t b0 = b;
   const uint16_t* __restrict__ mult = a.mult;
-  const uint32_t P = a.P, np = a.npool;
+  const uint32_t P = a.P;
+  // The terms are kept as byte offsets of their rows in the element-major
+  // table, u_j * rb: a hit's 24 loads then need one integer add each (ALU
+  // pipe) instead of a multiply-add (FMA pipe, which the Philox rounds and
+  // the FP32 decision also use).  `magic` recovers u_j for the rare paths.
+  const uint32_t rb = 2u * a.npool, magic = 0xFFFFFFFFu / rb + 1u;
+#pragma unroll
+  for (int j = 0; j < NT; ++j) u[j] *= rb;
   double oldact = 0.0;
   bool old_ok = false;
-  // The fixed-point sums of proposal k from the current u.
+  // The fixed-point sums of proposal k from the current terms.
   auto sums = [&](uint32_t k, int32_t& Rn, int32_t& Mn) {
-    const int16_t* col = s_vsub + k;
+    const char* col = reinterpret_cast<const char*>(s_vsub) + 2u * k;
     Rn = 0;
     Mn = 0;
 #pragma unroll
-    for (int j = 0; j < NS; ++j) Rn += col[u[j] * np];
+    for (int j = 0; j < NS; ++j) Rn += *reinterpret_cast<const int16_t*>(col + u[j]);
 #pragma unroll
-    for (int j = NS; j < NT; ++j) Mn += col[u[j] * np];
+    for (int j = NS; j < NT; ++j) Mn += *reinterpret_cast<const int16_t*>(col + u[j]);
   };
   // Decide hit h (proposal k, threshold t, sums Rn, Mn) and apply it;
   // returns whether it was accepted.
@@ -400,7 +411,7 @@ __device__ __forceinline__ void vt_hits(const SweepArgs& a, uint32_t i, uint32_t
       const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_METRO);
       const uint32_t g = s_pool[k];
       double newact;
-      exact_actions<D>(a, s_inv, s_retr, u, b, __ldg(mult + b * P + g), !old_ok, oldact, newact);
+      exact_actions<D>(a, s_inv, s_retr, u, b, __ldg(mult + b * P + g), !old_ok, oldact, newact, magic);
       old_ok = true;
       acc = dym_accept_fast(oldact, newact, dym_u53(r.v[1], r.v[2]));
       max_err = fmaxf(max_err, fabsf(ds - (float)DYM_SUB(newact, oldact)));
@@ -413,7 +424,7 @@ __device__ __forceinline__ void vt_hits(const SweepArgs& a, uint32_t i, uint32_t
       const uint32_t g = s_pool[k];
       b = __ldg(mult + b * P + g);
 #pragma unroll
-      for (int j = 0; j < NT; ++j) u[j] = __ldg(mult + u[j] * P + g);
+      for (int j = 0; j < NT; ++j) u[j] = (uint32_t)__ldg(mult + __umulhi(u[j], magic) * P + g) * rb;
       R = Rn;
       M = Mn;
       old_ok = exact;
