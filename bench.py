@@ -69,14 +69,14 @@ def gathers_per_link_hit(nhit: int) -> float:
 # kernel runs this workload only on a chain's first call (the cold chain
 # accepts nothing, so later calls use the value table) and has no capture of
 # it; None leaves its roofline unreported.
-DRAM_BYTES_PER_LAUNCH = {"k_sweep_vt": 892992, "k_sweep_mixed": None, "k_sweep_sub": 2563584}
+DRAM_BYTES_PER_LAUNCH = {"k_sweep_vt": 907104, "k_sweep_mixed": None, "k_sweep_sub": 2563584}
 # smsp__inst_executed.sum (warp instructions) and lts__t_sectors_srcunit_tex.sum
 # (L2 sectors requested by the SMs) of one sweep launch of this workload, from
-# the --set full capture in the same file.  Both are fixed for the workload:
+# the capture of the current kernel in the same file.  Both are fixed for the workload:
 # the cold chain accepts no proposal, so every launch runs the same
 # instructions.
-INST_PER_LAUNCH = {"k_sweep_vt": 7191788, "k_sweep_mixed": None, "k_sweep_sub": None}
-L2_SECTORS_PER_LAUNCH = {"k_sweep_vt": 426015, "k_sweep_mixed": None, "k_sweep_sub": None}
+INST_PER_LAUNCH = {"k_sweep_vt": 6987888, "k_sweep_mixed": None, "k_sweep_sub": None}
+L2_SECTORS_PER_LAUNCH = {"k_sweep_vt": 423123, "k_sweep_mixed": None, "k_sweep_sub": None}
 # Warp instructions an SM can issue per cycle (four schedulers, one each).
 ISSUE_PER_SM_CYCLE = 4
 
