@@ -15,6 +15,11 @@
 #                       reference Makefile flags
 #   _ref/llr2d          the unmodified two-dimensional LLR executable
 #                       (llr2d.cpp), reference Makefile flags
+#   _ref/dym-mod-metro-gpu      the reference's dym-mod-metro with its two sweep
+#                       loops turned into calls of oracle/ref_gpu_driver.cpp
+#                       (dym_sweep_refarray on its own link array), streamed
+#                       through sed into the compiler, linked with libdymgpu;
+#                       built only when the engine's library has been built
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 REF_DIR=${REF_DIR:-$HERE/../baseline/_ref}
@@ -50,4 +55,22 @@ $CXX -O3 -g -pg -fopenmp -std=c++11 -w -I"$REF_DIR" "$REF_DIR/llr.cpp" \
   "$OUT/lattice.o" "$OUT/group.o" "$OUT/timer.o" -lm -o "$OUT/llr"
 $CXX -O3 -g -pg -fopenmp -std=c++11 -w -I"$REF_DIR" "$REF_DIR/llr2d.cpp" \
   "$OUT/lattice.o" "$OUT/group.o" "$OUT/timer.o" -lm -o "$OUT/llr2d"
+# the reference's driver on the engine (needs lib/libdymgpu.so)
+ENGINE_LIB="$CORE/../lib"
+if [ -f "$ENGINE_LIB/libdymgpu.so" ]; then
+  SRC="$REF_DIR/dym-mod-metro.cpp"
+  THERM='for (unsigned k = 0; k < NTHERM; k++) update();'
+  BLOCK='for (unsigned k = 0; k < K; k++) update();'
+  if [ "$(grep -cF "$THERM" "$SRC")" != 1 ] || [ "$(grep -cF "$BLOCK" "$SRC")" != 1 ]; then
+    echo "dym-mod-metro.cpp: sweep loops not found as expected; dym-mod-metro-gpu not built" >&2
+    exit 3
+  fi
+  $CXX -O3 -std=c++17 -w -I"$REF_DIR" -I"$HERE/../include" -c "$HERE/ref_gpu_driver.cpp" -o "$OUT/ref_gpu_driver.o"
+  sed -e '1i void dym_ref_sweeps(const char*, int, unsigned, int);' \
+      -e 's/for (unsigned k = 0; k < NTHERM; k++) update();/dym_ref_sweeps(groupfilename, iseed, NTHERM, NHIT);/' \
+      -e 's/for (unsigned k = 0; k < K; k++) update();/dym_ref_sweeps(groupfilename, iseed, K, NHIT);/' "$SRC" | \
+    $CXX -O3 -fopenmp -std=c++11 -w -I"$REF_DIR" -x c++ - -x none "$OUT/ref_gpu_driver.o" \
+      "$OUT/lattice.o" "$OUT/group.o" "$OUT/timer.o" -lm -L"$ENGINE_LIB" -ldymgpu -Wl,-rpath,"$ENGINE_LIB" \
+      -o "$OUT/dym-mod-metro-gpu"
+fi
 echo "built $OUT"
