@@ -325,7 +325,6 @@ static void chain_release(dym_chain* c) {
   cudaFree(c->d_llr_bref);
   cudaFree(c->d_stage);
   cudaFree(c->d_ref32);
-  cudaFree(c->d_first_bad);
   if (c->h_counters) cudaFreeHost(c->h_counters);
   if (c->h_hist) cudaFreeHost(c->h_hist);
   if (c->ev0) cudaEventDestroy(c->ev0);
@@ -470,8 +469,8 @@ int dym_chain_create(const dym_group* gh, const dym_chain_params* p, dym_chain**
   d.npool = (uint32_t)pool.size();
   DYM_CUDA(dmalloc(&d.pool, pool.size()), "cudaMalloc(pool)");
   DYM_CUDA(copy_sync(d.pool, pool.data(), pool.size() * 2, cudaMemcpyHostToDevice, c->stream), "upload pool");
-  DYM_CUDA(dmalloc(&d.counters, 5), "cudaMalloc(counters)");
-  // Pinned words: [0..4] dym_sweep's counters, [5] dym_links_set's check.
+  DYM_CUDA(dmalloc(&d.counters, 6), "cudaMalloc(counters)");
+  // Pinned copy of the six words (ChainDev::counters).
   DYM_CUDA(cudaHostAlloc((void**)&c->h_counters, 6 * sizeof(unsigned long long), cudaHostAllocDefault),
            "cudaHostAlloc");
   if (p->precision != DYM_PREC_FP64 && shared_structure_ok(g, p->D)) {
@@ -550,12 +549,27 @@ int dym_chain_set_beta(dym_chain* c, double beta0, double beta1, double beta2) {
   return DYM_OK;
 }
 
+// Clear the chain's six counter words (sweep counters and upload check) on
+// its stream; every call that sweeps or uploads starts with it.
+static int counters_reset(dym_chain* c) {
+  DYM_CUDA(cudaMemsetAsync(c->dev.counters, 0, 6 * sizeof(unsigned long long), c->stream), "reset counters");
+  return DYM_OK;
+}
+
+// Whether the upload check read back into h_counters refused the upload, and
+// the smallest bad index if so.
+static bool upload_refused(const dym_chain* c, unsigned long long* index) {
+  *index = ~c->h_counters[5];
+  return c->h_counters[5] != 0;
+}
+
 // Enqueue nsweeps sweeps of the chain on its stream, between the events
-// ev0 and ev1, and the read-back of the counters into h_counters[0..4];
-// `skip` (see SweepArgs) may make every launch a no-op.  Advances c->sweep.
+// ev0 and ev1, and the read-back of the six counter words into h_counters
+// (after counters_reset); `skip` (see SweepArgs) may make every launch a
+// no-op, and the final sweep writes every link into `out` / `out_ref` when
+// given (SweepArgs).  Advances c->sweep.
 static int sweep_enqueue(dym_chain* c, int32_t nsweeps, int32_t nhit, const unsigned long long* skip,
-                         int* kernel_out) {
-  DYM_CUDA(cudaMemsetAsync(c->dev.counters, 0, 5 * sizeof(unsigned long long), c->stream), "reset counters");
+                         int* kernel_out, uint16_t* out = nullptr, int32_t* out_ref = nullptr) {
   const int kernel = sweep_kernel(c);
   SweepArgs a = sweep_args(c, kernel);
   a.nhit = nhit;
@@ -566,6 +580,10 @@ static int sweep_enqueue(dym_chain* c, int32_t nsweeps, int32_t nhit, const unsi
   DYM_CUDA(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
   for (int k = 0; k < nsweeps; ++k) {
     a.sweep = c->sweep;
+    if (k == nsweeps - 1) {
+      a.out = out;
+      a.out_ref = out_ref;
+    }
     for (size_t p = 0; p < s.phase_dir.size(); ++p) {
       a.sites = c->dev.sites + s.phase_off[p];
       a.xyz = c->dev.xyz ? c->dev.xyz + s.phase_off[p] : nullptr;
@@ -585,7 +603,7 @@ static int sweep_enqueue(dym_chain* c, int32_t nsweeps, int32_t nhit, const unsi
     ++c->sweep;
   }
   DYM_CUDA(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");
-  DYM_CUDA(cudaMemcpyAsync(c->h_counters, c->dev.counters, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+  DYM_CUDA(cudaMemcpyAsync(c->h_counters, c->dev.counters, 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                            c->stream),
            "read counters");
   *kernel_out = kernel;
@@ -622,6 +640,7 @@ int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
   if (nsweeps < 0 || nhit < 0 || nhit > (1 << 20)) return fail(DYM_EINVAL, "dym_sweep: bad nsweeps or nhit");
   DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
   int kernel = 0;
+  if (int rc = counters_reset(c)) return rc;
   if (int rc = sweep_enqueue(c, nsweeps, nhit, nullptr, &kernel)) return rc;
   DYM_CUDA(cudaStreamSynchronize(c->stream), "sweep");
   return sweep_report(c, kernel, nsweeps, out);
@@ -701,42 +720,38 @@ int dym_links_get(dym_chain* c, uint16_t* host_out) {
 }
 
 // Enqueue the upload of a configuration from host memory into the chain's
-// stage and its check on the device: the first id >= P (or ~0) into
-// d_first_bad, the stage copied into the chain's links only if there is none,
-// so a refused configuration leaves the chain as it was.  The caller enqueues
-// the read-back of d_first_bad (links_check_readback) where it needs it.
+// stage and its check on the device (after counters_reset): the complement
+// of the first id >= P into counter word 5, the stage copied into the chain's
+// links only if there is none, so a refused configuration leaves the chain as
+// it was.
 static int links_upload_enqueue(dym_chain* c, const uint16_t* host_in) {
   const uint32_t P = c->grp->g->P;
   const size_t n = (size_t)c->dev.V * c->p.D;
   if (!c->d_stage) DYM_CUDA(dmalloc(&c->d_stage, n), "cudaMalloc(links stage)");
-  if (!c->d_first_bad) DYM_CUDA(dmalloc(&c->d_first_bad, 1), "cudaMalloc(links check)");
+  unsigned long long* check = c->dev.counters + 5;
   if (const void* mh = mapped_host(host_in)) {  // page-locked: read by the checking kernel itself
-    DYM_CUDA(launch_links_from_host(c->dev.links, c->d_stage, static_cast<const uint16_t*>(mh), n, P,
-                                    c->d_first_bad, c->stream),
+    DYM_CUDA(launch_links_from_host(c->dev.links, c->d_stage, static_cast<const uint16_t*>(mh), n, P, check,
+                                    c->stream),
              "check links");
   } else {
     DYM_CUDA(cudaMemcpyAsync(c->d_stage, host_in, n * 2, cudaMemcpyHostToDevice, c->stream), "upload links");
-    DYM_CUDA(launch_links_commit(c->dev.links, c->d_stage, n, P, c->d_first_bad, c->stream), "check links");
+    DYM_CUDA(launch_links_commit(c->dev.links, c->d_stage, n, P, check, c->stream), "check links");
   }
-  return DYM_OK;
-}
-
-// Enqueue the copy of the upload check's result into h_counters[5].
-static int links_check_readback(dym_chain* c) {
-  DYM_CUDA(cudaMemcpyAsync(c->h_counters + 5, c->d_first_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                           c->stream),
-           "read links check");
   return DYM_OK;
 }
 
 int dym_links_set(dym_chain* c, const uint16_t* host_in) {
   if (!c || !host_in) return fail(DYM_EINVAL, "dym_links_set: null argument");
   DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+  if (int rc = counters_reset(c)) return rc;
   if (int rc = links_upload_enqueue(c, host_in)) return rc;
-  if (int rc = links_check_readback(c)) return rc;
+  DYM_CUDA(cudaMemcpyAsync(c->h_counters + 5, c->dev.counters + 5, sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, c->stream),
+           "read links check");
   DYM_CUDA(cudaStreamSynchronize(c->stream), "upload links");
-  if (c->h_counters[5] != ~0ull)
-    return fail(DYM_EINVAL, "dym_links_set: element id out of range at " + std::to_string(c->h_counters[5]));
+  unsigned long long bad;
+  if (upload_refused(c, &bad))
+    return fail(DYM_EINVAL, "dym_links_set: element id out of range at " + std::to_string(bad));
   return DYM_OK;
 }
 
@@ -746,21 +761,26 @@ int dym_sweep_host(dym_chain* c, const uint16_t* host_in, uint16_t* host_out, in
   if (!c) return fail(DYM_EINVAL, "dym_sweep_host: null chain");
   if (nsweeps < 0 || nhit < 0 || nhit > (1 << 20)) return fail(DYM_EINVAL, "dym_sweep_host: bad nsweeps or nhit");
   DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
+  if (int rc = counters_reset(c)) return rc;
   if (host_in)
     if (int rc = links_upload_enqueue(c, host_in)) return rc;
+  // A page-locked host_out is written by the final sweep itself; any other
+  // (or no sweep) by a copy after the sweeps.
+  uint16_t* out_mapped = host_out && nsweeps > 0 ? static_cast<uint16_t*>(mapped_host(host_out)) : nullptr;
   int kernel = 0;
   const uint32_t sweep0 = c->sweep;
-  if (int rc = sweep_enqueue(c, nsweeps, nhit, host_in ? c->d_first_bad : nullptr, &kernel)) return rc;
-  if (host_out)
-    DYM_CUDA(cudaMemcpyAsync(host_out, c->dev.links, (size_t)c->dev.V * c->p.D * 2, cudaMemcpyDeviceToHost,
-                             c->stream),
-             "download links");
-  if (host_in)  // read back after the sweeps, off their path
-    if (int rc = links_check_readback(c)) return rc;
+  if (int rc = sweep_enqueue(c, nsweeps, nhit, host_in ? c->dev.counters + 5 : nullptr, &kernel, out_mapped))
+    return rc;
+  const size_t bytes = (size_t)c->dev.V * c->p.D * 2;
+  if (host_out && !out_mapped)
+    DYM_CUDA(cudaMemcpyAsync(host_out, c->dev.links, bytes, cudaMemcpyDeviceToHost, c->stream), "download links");
   DYM_CUDA(cudaStreamSynchronize(c->stream), "dym_sweep_host");
-  if (host_in && c->h_counters[5] != ~0ull) {
+  unsigned long long bad;
+  if (host_in && upload_refused(c, &bad)) {
     c->sweep = sweep0;  // the sweeps did nothing
-    return fail(DYM_EINVAL, "dym_sweep_host: element id out of range at " + std::to_string(c->h_counters[5]));
+    if (out_mapped)     // nor wrote host_out: it receives the unchanged configuration
+      DYM_CUDA(copy_sync(host_out, c->dev.links, bytes, cudaMemcpyDeviceToHost, c->stream), "download links");
+    return fail(DYM_EINVAL, "dym_sweep_host: element id out of range at " + std::to_string(bad));
   }
   return sweep_report(c, kernel, nsweeps, out);
 }
@@ -774,29 +794,32 @@ int dym_sweep_refarray(dym_chain* c, int32_t* a, int32_t nsweeps, int32_t nhit, 
   const int D = c->p.D;
   const size_t n = (size_t)V * D;
   if (!c->d_stage) DYM_CUDA(dmalloc(&c->d_stage, n), "cudaMalloc(links stage)");
-  if (!c->d_first_bad) DYM_CUDA(dmalloc(&c->d_first_bad, 1), "cudaMalloc(links check)");
-  // Page-locked arrays are read and written by the kernels through their
-  // device mapping; any other goes through a device copy of the array.
+  // Page-locked arrays are read by the checking kernel and written back by a
+  // coalesced pass through their device mapping; any other goes through a
+  // device copy of the array, which the final sweep writes.
   int32_t* mapped = static_cast<int32_t*>(mapped_host(a));
   if (!mapped && !c->d_ref32) DYM_CUDA(dmalloc(&c->d_ref32, n), "cudaMalloc(reference-layout array)");
+  int32_t* dev_a = mapped ? mapped : c->d_ref32;
+  if (int rc = counters_reset(c)) return rc;
   if (!mapped)
     DYM_CUDA(cudaMemcpyAsync(c->d_ref32, a, n * 4, cudaMemcpyHostToDevice, c->stream), "upload reference array");
-  DYM_CUDA(launch_links_from_ref(c->dev.links, c->d_stage, mapped ? mapped : c->d_ref32, V, D, P, c->d_first_bad,
-                                 c->stream),
+  DYM_CUDA(launch_links_from_ref(c->dev.links, c->d_stage, dev_a, V, D, P, c->dev.counters + 5, c->stream),
            "check reference array");
   int kernel = 0;
   const uint32_t sweep0 = c->sweep;
-  if (int rc = sweep_enqueue(c, nsweeps, nhit, c->d_first_bad, &kernel)) return rc;
-  DYM_CUDA(launch_links_to_ref(mapped ? mapped : c->d_ref32, c->dev.links, V, D, c->d_first_bad, c->stream),
-           "write reference array");
-  if (int rc = links_check_readback(c)) return rc;
+  // The array is written after the last sweep (not at all when nsweeps is 0:
+  // it then already holds the configuration).
+  if (int rc = sweep_enqueue(c, nsweeps, nhit, c->dev.counters + 5, &kernel, nullptr, mapped ? nullptr : dev_a))
+    return rc;
+  if (mapped && nsweeps > 0)
+    DYM_CUDA(launch_links_to_ref(mapped, c->dev.links, V, D, c->dev.counters + 5, c->stream), "write reference array");
   DYM_CUDA(cudaStreamSynchronize(c->stream), "dym_sweep_refarray");
-  if (c->h_counters[5] != ~0ull) {
+  unsigned long long bad;
+  if (upload_refused(c, &bad)) {
     c->sweep = sweep0;  // the sweeps did nothing, `a` was not written
-    return fail(DYM_EINVAL, "dym_sweep_refarray: element id out of range at a[" + std::to_string(c->h_counters[5]) +
-                                "]");
+    return fail(DYM_EINVAL, "dym_sweep_refarray: element id out of range at a[" + std::to_string(bad) + "]");
   }
-  if (!mapped)
+  if (!mapped && nsweeps > 0)
     DYM_CUDA(copy_sync(a, c->d_ref32, n * 4, cudaMemcpyDeviceToHost, c->stream), "download reference array");
   return sweep_report(c, kernel, nsweeps, out);
 }

@@ -39,9 +39,21 @@ struct SweepArgs {
   const int16_t* val16;  // value-table kernel: fixed-point ReTr of every element
   int hit_unroll;        // mixed kernels: hits per group of draws computed ahead (1, 2, 5 or 10)
   int lanes_per_link;    // value-table kernel: threads sharing a link visit (1 or 2)
-  // dym_sweep_host: the upload check's first bad index (~0 when none); a sweep
-  // launch after a refused upload does nothing.  Null for the other calls.
+  // dym_sweep_host, dym_sweep_refarray: the upload check's word (0 when every
+  // id was valid, else the complement of the first bad index); a sweep launch
+  // after a refused upload does nothing.  Null for the other calls.
   const unsigned long long* skip;
+  // The final sweep of a host-resident call also writes the value of every
+  // link it visits into the caller's buffer: `out` direction-major
+  // (out[dir*V + site], dym_sweep_host's page-locked host_out through its
+  // device mapping), `out_ref` the reference's layout (out_ref[site*D + dir],
+  // int32: dym_sweep_refarray's device copy of a pageable array; a
+  // page-locked one is written by a coalesced pass instead, since these
+  // scattered 4-byte writes are slow over the host link).  Every link is
+  // visited once a sweep, so no copy of the configuration follows the sweeps.
+  // Null otherwise.
+  uint16_t* out;
+  int32_t* out_ref;
 };
 
 struct ChainDev {
@@ -51,6 +63,10 @@ struct ChainDev {
   uint32_t* sites = nullptr;
   uint16_t* pool = nullptr;    // proposal pool actually used
   uint32_t npool = 0;
+  // [0..4] the sweep counters (SweepArgs::counters), [5] the upload check of
+  // dym_links_set / dym_sweep_host / dym_sweep_refarray: 0 when every id was
+  // valid, else the complement of the smallest bad index (atomicMax), so one
+  // memset clears all six words and one copy reads them back.
   unsigned long long* counters = nullptr;
   uint16_t* sub = nullptr;     // sub[k*P + u] = u * pool[k] (shared sub-table kernel)
   bool sub_ok = false;
@@ -100,8 +116,10 @@ constexpr int kVt2MaxThreads = 896;
 constexpr double kDefaultVtMaxAccept = 0.01;
 cudaError_t launch_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uint64_t seed, cudaStream_t s);
 cudaError_t launch_fill(uint16_t* links, size_t n, uint16_t v, cudaStream_t s);
-// Check n uploaded ids against P on the device (*first = smallest bad index,
-// or ~0) and copy the stage into the links only if all are in range.
+// Check n uploaded ids against P on the device and copy the stage into the
+// links only if all are in range.  *first is the check word: 0 beforehand
+// (the caller clears it), afterwards the complement of the smallest bad index
+// if there is one.
 cudaError_t launch_links_commit(uint16_t* links, const uint16_t* stage, size_t n, uint32_t P,
                                 unsigned long long* first, cudaStream_t s);
 // The same reading the ids from page-locked host memory through its device
@@ -115,8 +133,8 @@ cudaError_t launch_links_from_host(uint16_t* links, uint16_t* stage, const uint1
 cudaError_t launch_links_from_ref(uint16_t* links, uint16_t* stage, const int32_t* ref, uint32_t V, int D, uint32_t P,
                                   unsigned long long* first, cudaStream_t s);
 // The links written back into the reference's layout, ref[i*D + d] =
-// links[d*V + i]; nothing is written when *skip holds a refused upload's
-// index (skip may be null).
+// links[d*V + i] (coalesced writes, for page-locked host arrays); nothing is
+// written when the upload check word *skip is set.
 cudaError_t launch_links_to_ref(int32_t* ref, const uint16_t* links, uint32_t V, int D,
                                 const unsigned long long* skip, cudaStream_t s);
 cudaError_t launch_staples(int D, int dir, const SweepArgs& a, const uint32_t* sites, uint32_t n, uint16_t* out,
@@ -234,6 +252,5 @@ struct dym_chain {
   uint8_t* d_llr_bref = nullptr;          // per block: refused by the last scan
   uint16_t* d_stage = nullptr;  // dym_links_set: upload buffer, copied into the links once checked
   int32_t* d_ref32 = nullptr;   // dym_sweep_refarray: the reference-layout array in device memory (pageable callers)
-  unsigned long long* d_first_bad = nullptr;  // dym_links_set: smallest out-of-range index, or ~0
   bool l2_window = false;  // dym_chain_set_l2_window: the stream pins the Cayley table in L2
 };

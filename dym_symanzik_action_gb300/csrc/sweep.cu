@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(256) k_sweep_direct(SweepArgs a) {
         ++accs;
       }
     }
-    if (b != b0) *own = (uint16_t)b;
+    finish_link<D>(a, DIR, i, b, b0);
   }
   flush_counters(a.counters, hits, accs, 0);
 }
@@ -146,13 +146,17 @@ __global__ void k_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uint
   }
 }
 
-// dym_links_set on the device: the smallest index whose id is >= P into
-// *first (set to ~0 beforehand), then the stage copied into the links only if
-// there is none.
+// dym_links_set on the device: the complement of the smallest index whose id
+// is >= P into *first (0 beforehand; the smallest index has the largest
+// complement), then the stage copied into the links only if there is none.
+__device__ __forceinline__ void note_bad(unsigned long long* first, size_t k) {
+  atomicMax(first, ~(unsigned long long)k);
+}
+
 __global__ void k_ids_first_bad(const uint16_t* __restrict__ ids, size_t n, uint32_t P, unsigned long long* first) {
   pdl_launch_dependents();  // the commit may be scheduled; it waits for this grid
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-    if (ids[k] >= P) atomicMin(first, (unsigned long long)k);
+    if (ids[k] >= P) note_bad(first, k);
 }
 
 // The same check reading the ids straight from page-locked host memory (the
@@ -172,13 +176,13 @@ __global__ void k_ids_from_host(uint16_t* __restrict__ stage, const uint16_t* __
 #pragma unroll
     for (int h = 0; h < 8; ++h) {
       const uint32_t v = (x[h >> 1] >> (16 * (h & 1))) & 0xFFFFu;
-      if (v >= P) atomicMin(first, (unsigned long long)(8 * q + h));
+      if (v >= P) note_bad(first, 8 * q + h);
     }
   }
   for (size_t k = 8 * nv + t0; k < n; k += dt) {
     const uint16_t v = host[k];
     stage[k] = v;
-    if (v >= P) atomicMin(first, (unsigned long long)k);
+    if (v >= P) note_bad(first, k);
   }
 }
 
@@ -187,7 +191,8 @@ __global__ void k_ids_from_host(uint16_t* __restrict__ stage, const uint16_t* __
 __global__ void k_ids_commit(uint16_t* __restrict__ links, const uint16_t* __restrict__ stage, size_t n,
                              const unsigned long long* first) {
   pdl_wait_prior();
-  if (*first != ~0ull) return;
+  pdl_launch_dependents();  // the first sweep may stage its tables
+  if (*first != 0) return;
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
     links[k] = stage[k];
 }
@@ -202,17 +207,18 @@ __global__ void k_ids_from_ref(uint16_t* __restrict__ stage, const int32_t* __re
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
     const int32_t v = ref[k];
     const uint32_t i = (uint32_t)(k / (uint32_t)D), d = (uint32_t)(k % (uint32_t)D);
-    if (v < 0 || (uint32_t)v >= P) atomicMin(first, (unsigned long long)k);
+    if (v < 0 || (uint32_t)v >= P) note_bad(first, k);
     stage[(size_t)d * V + i] = (uint16_t)v;
   }
 }
 
-// dym_sweep_refarray's read-back: ref[i*D + d] = links[d*V + i], skipped
-// entirely after a refused upload.
+// dym_sweep_refarray's read-back into a page-locked array: ref[i*D + d] =
+// links[d*V + i] in the array's order, so that the writes through the
+// device mapping are coalesced; skipped entirely after a refused upload.
 __global__ void k_links_to_ref(int32_t* __restrict__ ref, const uint16_t* __restrict__ links, uint32_t V, int D,
                                const unsigned long long* skip) {
   pdl_wait_prior();
-  if (skip && *skip != ~0ull) return;
+  if (*skip != 0) return;
   const size_t n = (size_t)V * D;
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
     const uint32_t i = (uint32_t)(k / (uint32_t)D), d = (uint32_t)(k % (uint32_t)D);
@@ -355,11 +361,10 @@ cudaError_t launch_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uin
 
 cudaError_t launch_links_commit(uint16_t* links, const uint16_t* stage, size_t n, uint32_t P,
                                 unsigned long long* first, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(first, 0xFF, sizeof(unsigned long long), s);
-  if (e != cudaSuccess || n == 0) return e;
+  if (n == 0) return cudaSuccess;
   const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 8);
   k_ids_first_bad<<<grid, 256, 0, s>>>(stage, n, P, first);
-  e = cudaGetLastError();
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   return launch_phase(k_ids_commit, grid, 256, 0, s, links, (const uint16_t*)stage, n,
                       (const unsigned long long*)first);
@@ -367,12 +372,11 @@ cudaError_t launch_links_commit(uint16_t* links, const uint16_t* stage, size_t n
 
 cudaError_t launch_links_from_host(uint16_t* links, uint16_t* stage, const uint16_t* host_mapped, size_t n,
                                    uint32_t P, unsigned long long* first, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(first, 0xFF, sizeof(unsigned long long), s);
-  if (e != cudaSuccess || n == 0) return e;
+  if (n == 0) return cudaSuccess;
   const size_t nv = (reinterpret_cast<uintptr_t>(host_mapped) & 15u) ? 0 : n / 8;
   const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 8);
   k_ids_from_host<<<grid, 256, 0, s>>>(stage, host_mapped, n, nv, P, first);
-  e = cudaGetLastError();
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   return launch_phase(k_ids_commit, grid, 256, 0, s, links, (const uint16_t*)stage, n,
                       (const unsigned long long*)first);
@@ -380,12 +384,11 @@ cudaError_t launch_links_from_host(uint16_t* links, uint16_t* stage, const uint1
 
 cudaError_t launch_links_from_ref(uint16_t* links, uint16_t* stage, const int32_t* ref, uint32_t V, int D, uint32_t P,
                                   unsigned long long* first, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(first, 0xFF, sizeof(unsigned long long), s);
   const size_t n = (size_t)V * D;
-  if (e != cudaSuccess || n == 0) return e;
+  if (n == 0) return cudaSuccess;
   const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 8);
   k_ids_from_ref<<<grid, 256, 0, s>>>(stage, ref, V, D, P, first);
-  e = cudaGetLastError();
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   return launch_phase(k_ids_commit, grid, 256, 0, s, links, (const uint16_t*)stage, n,
                       (const unsigned long long*)first);

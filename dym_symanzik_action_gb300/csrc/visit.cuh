@@ -67,7 +67,17 @@ __device__ __forceinline__ void pdl_wait_prior() { asm volatile("griddepcontrol.
 // Whether this sweep launch is to do nothing because the upload before it in
 // the same dym_sweep_host call was refused (SweepArgs::skip).  Read after the
 // programmatic wait, so the upload check has completed.
-__device__ __forceinline__ bool sweep_skipped(const SweepArgs& a) { return a.skip && *a.skip != ~0ull; }
+__device__ __forceinline__ bool sweep_skipped(const SweepArgs& a) { return a.skip && *a.skip != 0; }
+
+// The end of a link visit: the link's new value into the lattice when it
+// changed, and -- in the final sweep of a host-resident call -- into the
+// caller's buffer whether or not it changed (SweepArgs::out, out_ref).
+template <int D>
+__device__ __forceinline__ void finish_link(const SweepArgs& a, int dir, uint32_t i, uint32_t b, uint32_t b0) {
+  if (b != b0) a.links[(size_t)dir * a.V + i] = (uint16_t)b;
+  if (a.out) a.out[(size_t)dir * a.V + i] = (uint16_t)b;
+  if (a.out_ref) a.out_ref[(size_t)i * D + dir] = (int32_t)b;
+}
 
 // The reference's FP64 actions of the current link value b and of a proposal
 // bnew (dym-mod-metro.cpp:166-181): beta0 + beta1 r1 + beta2 m1 with r1, m1 the
@@ -160,7 +170,7 @@ __device__ __forceinline__ void visit_sub(const SweepArgs& a, uint32_t i, uint32
       ++accs;
     }
   }
-  if (b != b0) *own = (uint16_t)b;
+  finish_link<D>(a, DIR, i, b, b0);
 }
 
 // Mixed-precision visit of link (i, DIR): the decisions of visit_sub, taken
@@ -304,7 +314,7 @@ __device__ __forceinline__ void mixed_hits(const SweepArgs& a, uint32_t i, uint3
       }
     }
   }
-  if (b != b0) a.links[(size_t)DIR * a.V + i] = (uint16_t)b;
+  finish_link<D>(a, DIR, i, b, b0);
 }
 
 __device__ __forceinline__ void flush_counters(unsigned long long* ctr, unsigned hits, unsigned accs,
@@ -456,7 +466,7 @@ __device__ __forceinline__ void vt_hits(const SweepArgs& a, uint32_t i, uint32_t
       }
     }
   }
-  if (b != b0) a.links[(size_t)DIR * a.V + i] = (uint16_t)b;
+  finish_link<D>(a, DIR, i, b, b0);
 }
 
 // Two lanes per link (vt2): the value-table visit with a link's work split
@@ -626,7 +636,7 @@ __device__ __forceinline__ void vt2_hits(const SweepArgs& a, uint32_t i, uint32_
       }
     }
   }
-  if (!back && b != b0) a.links[(size_t)DIR * a.V + i] = (uint16_t)b;
+  if (!back) finish_link<D>(a, DIR, i, b, b0);
 }
 
 // Largest |dS_fast - dS_fp64| seen at a re-evaluation, into the low word of

@@ -239,9 +239,12 @@ int dym_links_set(dym_chain* c, const uint16_t* host_in);
  * its host-resident link array `a` (malloc at dym-mod-metro.cpp:253).
  * host_in (may be NULL: keep the chain's configuration) is uploaded and
  * checked as by dym_links_set, the sweeps run as by dym_sweep, and the
- * result is copied into host_out (may be NULL; may equal host_in), with one
+ * result is written into host_out (may be NULL; may equal host_in), with one
  * synchronisation at the end instead of one per step.  Page-locked host
- * buffers are read by the checking kernel directly.  A host_in with an id >=
+ * buffers are read by the checking kernel directly, and a page-locked
+ * host_out is written by the final sweep itself (every link as it is
+ * visited), so no copy of the configuration follows the sweeps; other
+ * buffers go through copies.  A host_in with an id >=
  * the group order returns DYM_EINVAL with the chain unchanged (the sweeps do
  * nothing, the chain's sweep counter is not advanced) and host_out, if
  * given, holding the chain's unchanged configuration. */

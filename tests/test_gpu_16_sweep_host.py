@@ -140,3 +140,65 @@ def test_refarray_refused_leaves_array_and_chain(engine, bad):
     sa, sb = a.update(1, 10), b.update(1, 10)
     assert (sa.sweep, sa.hits, sa.accepts) == (sb.sweep, sb.hits, sb.accepts) and sb.sweep == 1
     assert np.array_equal(a.links, b.links)
+
+
+@pytest.mark.parametrize("kernel", ["values", "values-2-lanes", "elements", "fp64-shared", "fp64-direct",
+                                    "fp64-direct-3d"])
+def test_final_sweep_writes_pinned_output(engine, monkeypatch, kernel):
+    """A page-locked host_out (and a page-locked reference array) is written by
+    the final sweep itself, every link once: the result equals dym_sweep +
+    dym_links_get for each sweep kernel, with host_out aliasing host_in too."""
+    torch = pytest.importorskip("torch")
+    monkeypatch.setenv("DYM_VT_MAX_ACCEPT", "2.0" if kernel.startswith("values") else "-1")
+    monkeypatch.setenv("DYM_LANES_PER_LINK", "2" if kernel == "values-2-lanes" else "1")
+    D, precision, want_kernel = 4, "mixed", {"values": 4, "values-2-lanes": 4, "elements": 3}.get(kernel)
+    if kernel == "fp64-shared":
+        precision, want_kernel = "shared", 2
+    if kernel.startswith("fp64-direct"):
+        precision, want_kernel = "fp64", 1
+        D = 3 if kernel.endswith("3d") else 4
+    g = engine.load_group(tables.ensure_table("S1080"))
+    mk = lambda: engine.Lattice(g, D, 4, 8, 0.0, 2.0, -0.1, 77, start="hot", precision=precision)  # noqa: E731
+    ref, ours, arr = mk(), mk(), mk()
+    n = ref.D * ref.V
+    buf = pinned(n)
+    ref_arr = torch.empty(n, dtype=torch.int32, pin_memory=True).numpy()
+    cfg = ref.links.ravel().copy()
+    for step in range(3):
+        sr = ref.update(2, 10)
+        buf[:] = cfg
+        so = ours.update_host(buf, buf, 2, 10)
+        ref_arr[:] = to_ref(cfg, D)
+        sa = arr.update_refarray(ref_arr, 2, 10)
+        want = ref.links.ravel()
+        assert so.kernel == sa.kernel == sr.kernel == want_kernel, (step, so.kernel, sr.kernel)
+        assert (so.hits, so.accepts) == (sa.hits, sa.accepts) == (sr.hits, sr.accepts), step
+        assert np.array_equal(buf, want), step
+        assert np.array_equal(ref_arr, to_ref(want, D)), step
+        cfg = want.copy()
+
+
+def test_refused_upload_pinned_buffers(engine):
+    """With page-locked buffers a refused upload still leaves host_out holding
+    the chain's unchanged configuration and the reference array untouched."""
+    torch = pytest.importorskip("torch")
+    b = chain(engine, "mixed", seed=41)
+    b.update(1, 10)
+    before = b.links.ravel().copy()
+    n = before.size
+    hin, hout = pinned(n), pinned(n)
+    hin[:] = before
+    hin[999] = 1080
+    hout[:] = 0
+    st = _lib.Stats()
+    rc = lib().dym_sweep_host(b._h, ptr(hin, C.c_uint16), ptr(hout, C.c_uint16), 2, 10, C.byref(st))
+    assert _lib.ERRORS.get(rc) == "DYM_EINVAL" and b"at 999" in lib().dym_last_error()
+    assert np.array_equal(hout, before) and np.array_equal(b.links.ravel(), before)
+    ref = torch.empty(n, dtype=torch.int32, pin_memory=True).numpy()
+    ref[:] = to_ref(before, b.D)
+    ref[5] = -3
+    keep = ref.copy()
+    rc = lib().dym_sweep_refarray(b._h, ptr(ref, C.c_int32), 2, 10, C.byref(st))
+    assert _lib.ERRORS.get(rc) == "DYM_EINVAL" and b"a[5]" in lib().dym_last_error()
+    assert np.array_equal(ref, keep) and np.array_equal(b.links.ravel(), before)
+    assert b.update(1, 10).sweep == 2
