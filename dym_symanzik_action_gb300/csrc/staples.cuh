@@ -59,6 +59,27 @@ __device__ __forceinline__ void site_geo_packed(uint32_t xyz, int Nt, int Nx, Si
   site_geo_xyz<D>(x, Nt, Nx, g);
 }
 
+// The same offsets with one compare and one select each: for an axis of
+// extent N and stride s, a move of -2..+2 wraps at most once (N >= 2; N = 1
+// maps every move to 0), so each offset is one of two per-axis constants.
+// Equal to site_geo_packed for every extent.
+template <int D>
+__device__ __forceinline__ void site_geo_fast(uint32_t xyz, int Nt, int Nx, SiteGeo<D>& g) {
+  int stride = 1;
+#pragma unroll
+  for (int b = 0; b < D; ++b) {
+    const int N = (b == 0) ? Nt : Nx;
+    const int x = (int)((xyz >> (8 * b)) & 0xFFu);
+    const int s = stride;
+    g.off[b][0] = (x < 2) ? (N >= 2 ? (N - 2) * s : 0) : -2 * s;
+    g.off[b][1] = (x == 0) ? (N - 1) * s : -s;
+    g.off[b][2] = 0;
+    g.off[b][3] = (x == N - 1) ? (1 - N) * s : s;
+    g.off[b][4] = (x >= N - 2) ? (N >= 2 ? (2 - N) * s : 0) : 2 * s;
+    stride *= N;
+  }
+}
+
 // Table access policies.  `Tab` provides mul(g, h), inv(g) for uint32 ids.
 // Opt-in self-checking build (-DDYM_BOUNDS_CHECK): every table and lattice
 // index is checked; the first bad one is recorded in *status as
