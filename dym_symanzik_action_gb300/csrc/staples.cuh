@@ -206,7 +206,8 @@ __device__ __forceinline__ void build_staples(uint32_t i, const SiteGeo<D>& geo,
 // a[i+e,f] a[i+f,d]^-1 (plaquette 1, rectangle 3) and
 // a[i+e-f,f]^-1 a[i-f,d]^-1 (plaquette 2, rectangle 6) are formed once, and
 // the rest is grouped pairwise: 29 table products per plane instead of 36,
-// at most three dependent on one another instead of five.
+// at most three dependent on one another instead of five, and 11 inverse
+// lookups.
 template <int D, int DIR, class Tab, class LD>
 __device__ __forceinline__ void build_u_tree(uint32_t i, const SiteGeo<D>& geo, const Tab& T, LD ld, uint32_t b,
                                              uint32_t* up /* 2(D-1) */, uint32_t* ur /* 6(D-1) */) {
@@ -237,17 +238,19 @@ __device__ __forceinline__ void build_u_tree(uint32_t i, const SiteGeo<D>& geo, 
     const uint32_t l_emf_d = ld(DYM_S(1, -1), DIR);  // a[i+e-f, d]
     const uint32_t l_mfme_d = ld(DYM_S(-1, -1), DIR);  // a[i-f-e, d]
     const uint32_t l_mfme_f = ld(DYM_S(-1, -1), d1);   // a[i-e-f, f]
-    // First level: every product of two links (or link and b).
+    // First level: every product of two links (or link and b).  A product of
+    // two inverses is taken as the inverse of the reversed product, x^-1 y^-1
+    // = (y x)^-1: one inverse lookup instead of two, the same element.
     const uint32_t q0 = T.mul(T.iv(a_0_d1), b);
     const uint32_t q1 = T.mul(a_mf_f, b);
     const uint32_t q2 = T.mul(a_me_d, b);
     const uint32_t h0 = T.mul(a_e_f1, T.iv(a_f_d));
-    const uint32_t h1 = T.mul(T.iv(a_emf_f), T.iv(a_mf_d));
-    const uint32_t p1a = T.mul(a_e_f1, l_ef_f), p1b = T.mul(T.iv(l_2f_d), T.iv(l_f_f));
-    const uint32_t p2a = T.mul(a_e_d, l_2e_f), p2b = T.mul(T.iv(l_ef_d), T.iv(a_f_d));
-    const uint32_t p3b = T.mul(T.iv(l_fme_d), T.iv(a_me_f));
-    const uint32_t p4a = T.mul(T.iv(a_emf_f), T.iv(l_e2f_f)), p4b = T.mul(T.iv(l_m2f_d), l_m2f_f);
-    const uint32_t p5a = T.mul(a_e_d, T.iv(l_2emf_f)), p5b = T.mul(T.iv(l_emf_d), T.iv(a_mf_d));
+    const uint32_t h1 = T.iv(T.mul(a_mf_d, a_emf_f));
+    const uint32_t p1a = T.mul(a_e_f1, l_ef_f), p1b = T.iv(T.mul(l_f_f, l_2f_d));
+    const uint32_t p2a = T.mul(a_e_d, l_2e_f), p2b = T.iv(T.mul(a_f_d, l_ef_d));
+    const uint32_t p3b = T.iv(T.mul(a_me_f, l_fme_d));
+    const uint32_t p4a = T.iv(T.mul(l_e2f_f, a_emf_f)), p4b = T.mul(T.iv(l_m2f_d), l_m2f_f);
+    const uint32_t p5a = T.mul(a_e_d, T.iv(l_2emf_f)), p5b = T.iv(T.mul(a_mf_d, l_emf_d));
     const uint32_t p6b = T.mul(T.iv(l_mfme_d), l_mfme_f);
     // Plaquettes (dym-mod-metro.cpp:68-76) and rectangles 1-6 (:88-140), times b.
     up[k++] = T.mul(h0, q0);
