@@ -245,6 +245,7 @@ static SweepArgs sweep_args(dym_chain* c, int kernel = DYM_KERNEL_MIXED) {
   a.beta1 = c->p.beta1;
   a.beta2 = c->p.beta2;
   a.seed = c->p.seed;
+  dym_philox_round_keys(c->p.seed, a.rk);
   a.counters = c->dev.counters;
   if (c->dev.mixed_ok) {
     a.cls8 = c->dev.cls8;

@@ -54,6 +54,9 @@ struct SweepArgs {
   // Null otherwise.
   uint16_t* out;
   int32_t* out_ref;
+  // Philox round keys of `seed` (dym_philox_round_keys): the single-chain
+  // kernels' hit draws read them as kernel parameters (dym_metro_hit).
+  uint32_t rk[20];
 };
 
 struct ChainDev {

@@ -77,6 +77,73 @@ DYM_HD dym_u32x4 dym_hit_random(uint64_t seed, uint32_t sweep, uint32_t site,
   return dym_philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
 }
 
+// The same block for the hits of one link, with the work that does not
+// depend on the hit index done once.  Round keys rk[2r], rk[2r+1] = k0 + r W0,
+// k1 + r W1 (dym_philox_round_keys; in a kernel's parameters they are
+// constant-bank operands).  In the counter (site, sweep, dir<<20 | hit, tag)
+// only word 2 changes with the hit: round 0's product of word 0 and the words
+// it feeds, and round 1's product of word 2 (made of those), are the link's.
+typedef struct {
+  uint32_t s0;    // sweep ^ rk[0]: round 0's word-1 operand
+  uint32_t c1;    // round 1: hi(M1 (hi(M0 site) ^ tag ^ rk[1])) ^ rk[2]
+  uint32_t e1;    // round 1: lo(M1 (hi(M0 site) ^ tag ^ rk[1])), its output word 1
+  uint32_t b1;    // round 1: lo(M0 site) ^ rk[3]
+  uint32_t dir20; // dir << 20
+} dym_metro_link;
+
+DYM_HD void dym_philox_round_keys(uint64_t seed, uint32_t rk[20]) {
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  for (int r = 0; r < 10; ++r) {
+    rk[2 * r] = k0;
+    rk[2 * r + 1] = k1;
+    k0 += DYM_PHILOX_W0;
+    k1 += DYM_PHILOX_W1;
+  }
+}
+
+DYM_HD dym_metro_link dym_metro_link_init(const uint32_t* rk, uint32_t sweep, uint32_t site, uint32_t dir,
+                                          uint32_t tag) {
+  const uint64_t p0 = (uint64_t)DYM_PHILOX_M0 * site;
+  const uint32_t a = (uint32_t)(p0 >> 32) ^ tag ^ rk[1];  // round 0 output word 2
+  const uint64_t p1 = (uint64_t)DYM_PHILOX_M1 * a;
+  dym_metro_link L;
+  L.s0 = sweep ^ rk[0];
+  L.c1 = (uint32_t)(p1 >> 32) ^ rk[2];
+  L.e1 = (uint32_t)p1;
+  L.b1 = (uint32_t)p0 ^ rk[3];
+  L.dir20 = dir << 20;
+  return L;
+}
+
+// Equal to dym_hit_random(seed, sweep, site, dir, hit, tag) for the link of
+// dym_metro_link_init(rk of seed, sweep, site, dir, tag).
+DYM_HD dym_u32x4 dym_metro_hit(const uint32_t* rk, dym_metro_link L, uint32_t hit) {
+  // round 0: only word 2's product depends on the hit
+  const uint64_t q1 = (uint64_t)DYM_PHILOX_M1 * (L.dir20 | (hit & 0xFFFFFu));
+  const uint32_t o0 = (uint32_t)(q1 >> 32) ^ L.s0, o1 = (uint32_t)q1;
+  // round 1: word 0's product depends on the hit, word 2's is the link's
+  const uint64_t q0 = (uint64_t)DYM_PHILOX_M0 * o0;
+  dym_u32x4 c;
+  c.v[0] = L.c1 ^ o1;
+  c.v[1] = L.e1;
+  c.v[2] = (uint32_t)(q0 >> 32) ^ L.b1;
+  c.v[3] = (uint32_t)q0;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int r = 2; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)DYM_PHILOX_M0 * c.v[0];
+    const uint64_t p1 = (uint64_t)DYM_PHILOX_M1 * c.v[2];
+    dym_u32x4 o;
+    o.v[0] = (uint32_t)(p1 >> 32) ^ c.v[1] ^ rk[2 * r];
+    o.v[1] = (uint32_t)p1;
+    o.v[2] = (uint32_t)(p0 >> 32) ^ c.v[3] ^ rk[2 * r + 1];
+    o.v[3] = (uint32_t)p0;
+    c = o;
+  }
+  return c;
+}
+
 // u1 = r0 * 2^-32 in [0,1); the proposal index floor(n * u1) equals
 // (r0 * n) >> 32 exactly for n < 2^21 (both products are exact in double).
 DYM_HD uint32_t dym_pick(uint32_t r0, uint32_t n) {

@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_sweep_mixed(SweepArgs a
       i_next = a.sites[t + blockDim.x];
       xyz_next = a.xyz[t + blockDim.x];
     }
-    visit_mixed<D, DIR, E, HU>(a, i, xyz, a.sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks,
+    visit_mixed<D, DIR, E, HU, true>(a, i, xyz, a.sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks,
                                max_err);
   }
   flush_counters(a.counters, hits, accs, rechecks);

@@ -230,13 +230,20 @@ template <int HU>
 struct HitDraws {
   uint32_t k[HU];
   float t[HU];
+  __device__ __forceinline__ void set(int q, const dym_u32x4& r, uint32_t npool) {
+    k[q] = dym_pick(r.v[0], npool);
+    t[q] = -__logf(__fmaf_rn((float)r.v[1], 0x1p-32f, (float)(r.v[2] >> 11) * 0x1p-53f));
+  }
   __device__ __forceinline__ void fill(const SweepArgs& a, uint32_t sweep, uint32_t i, uint32_t dir, int h0) {
 #pragma unroll
-    for (int q = 0; q < HU; ++q) {
-      const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, dir, (uint32_t)(h0 + q), DYM_TAG_METRO);
-      k[q] = dym_pick(r.v[0], a.npool);
-      t[q] = -__logf(__fmaf_rn((float)r.v[1], 0x1p-32f, (float)(r.v[2] >> 11) * 0x1p-53f));
-    }
+    for (int q = 0; q < HU; ++q) set(q, dym_hit_random(a.seed, sweep, i, dir, (uint32_t)(h0 + q), DYM_TAG_METRO), a.npool);
+  }
+  // The same draws from the link's precomputed Philox state and the kernel
+  // parameters' round keys (dym_metro_hit: the same bits, fewer
+  // instructions); for kernels whose SweepArgs is their parameter.
+  __device__ __forceinline__ void fill(const SweepArgs& a, const dym_metro_link& L, int h0) {
+#pragma unroll
+    for (int q = 0; q < HU; ++q) set(q, dym_metro_hit(a.rk, L, (uint32_t)(h0 + q)), a.npool);
   }
 };
 
@@ -251,7 +258,9 @@ struct Packed {
 // Second half: the nhit hits of link (i, DIR) from the shared tables, starting
 // from mixed_prepare's state, in groups of HU hits whose draws are computed
 // ahead (HitDraws); the link is written when it changed.
-template <int D, int DIR, class E = uint16_t, int HU = 1>
+// kSplit: the draws from the link's precomputed Philox state (HitDraws, for
+// kernels whose SweepArgs is their parameter).
+template <int D, int DIR, class E = uint16_t, int HU = 1, bool kSplit = false>
 __device__ __forceinline__ void mixed_hits(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
                                            const uint16_t* s_inv, const E* s_psub, const int32_t* s_cfix,
                                            uint32_t* u, uint32_t b,
@@ -262,9 +271,12 @@ __device__ __forceinline__ void mixed_hits(const SweepArgs& a, uint32_t i, uint3
   const uint32_t b0 = b;
   double oldact = 0.0;
   bool old_ok = false;
+  dym_metro_link L{};
+  if (kSplit) L = dym_metro_link_init(a.rk, sweep, i, DIR, DYM_TAG_METRO);
   for (int h0 = 0; h0 < a.nhit; h0 += HU) {
     HitDraws<HU> dr;
-    dr.fill(a, sweep, i, DIR, h0);
+    if (kSplit) dr.fill(a, L, h0);
+    else dr.fill(a, sweep, i, DIR, h0);
 #pragma unroll
     for (int q = 0; q < HU; ++q) {
       if (HU > 1 && h0 + q >= a.nhit) break;
@@ -330,7 +342,7 @@ __device__ __forceinline__ void flush_counters(unsigned long long* ctr, unsigned
 }
 
 
-template <int D, int DIR, class E = uint16_t, int HU = 1>
+template <int D, int DIR, class E = uint16_t, int HU = 1, bool kSplit = false>
 __device__ __forceinline__ void visit_mixed(const SweepArgs& a, uint32_t i, uint32_t xyz, uint32_t sweep,
                                             const double* s_retr, const uint16_t* s_inv, const E* s_psub,
                                             const uint8_t* s_cls, const int32_t* s_cfix, unsigned& hits,
@@ -339,7 +351,8 @@ __device__ __forceinline__ void visit_mixed(const SweepArgs& a, uint32_t i, uint
   uint32_t u[NT];
   uint32_t b, R, M;
   mixed_prepare<D, DIR>(a, i, xyz, s_inv, s_cls, s_cfix, u, b, R, M);
-  mixed_hits<D, DIR, E, HU>(a, i, sweep, s_retr, s_inv, s_psub, s_cfix, u, b, R, M, hits, accs, rechecks, max_err);
+  mixed_hits<D, DIR, E, HU, kSplit>(a, i, sweep, s_retr, s_inv, s_psub, s_cfix, u, b, R, M, hits, accs, rechecks,
+                                    max_err);
 }
 
 // Value-table form of the mixed visit.  The shared table holds, for pool
@@ -445,10 +458,11 @@ __device__ __forceinline__ void vt_hits(const SweepArgs& a, uint32_t i, uint32_t
     }
     return acc;
   };
+  const dym_metro_link L = dym_metro_link_init(a.rk, sweep, i, DIR, DYM_TAG_METRO);
   if constexpr (HU == 2) {
     for (int h0 = 0; h0 < a.nhit; h0 += 2) {
       HitDraws<2> dr;
-      dr.fill(a, sweep, i, DIR, h0);
+      dr.fill(a, L, h0);
       const bool two = h0 + 1 < a.nhit;
       int32_t R0, M0, R1 = 0, M1 = 0;
       sums(dr.k[0], R0, M0);
@@ -459,7 +473,7 @@ __device__ __forceinline__ void vt_hits(const SweepArgs& a, uint32_t i, uint32_t
   } else {
     for (int h0 = 0; h0 < a.nhit; h0 += HU) {
       HitDraws<HU> dr;
-      dr.fill(a, sweep, i, DIR, h0);
+      dr.fill(a, L, h0);
 #pragma unroll
       for (int q = 0; q < HU; ++q) {
         if (HU > 1 && h0 + q >= a.nhit) break;
