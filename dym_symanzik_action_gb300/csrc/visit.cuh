@@ -123,7 +123,9 @@ __device__ __forceinline__ void exact_actions(const SweepArgs& a, const uint16_t
 // table whose ReTr is one double per conjugacy class ReTr[u_j g_k] equals the
 // reference's ReTr[mult[bnew][s_j]] bit for bit, summed in the same order
 // (dym-mod-metro.cpp:166-192).
-template <int D, int DIR>
+// kSplit: the draws from the link's precomputed Philox state (dym_metro_hit;
+// for kernels whose SweepArgs is their parameter).
+template <int D, int DIR, bool kSplit = false>
 __device__ __forceinline__ void visit_sub(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
                                           const uint16_t* s_inv, const uint16_t* s_sub, unsigned& hits,
                                           unsigned& accs) {
@@ -145,8 +147,11 @@ __device__ __forceinline__ void visit_sub(const SweepArgs& a, uint32_t i, uint32
 #pragma unroll
   for (int j = NS; j < NT; ++j) m1 = DYM_ADD(m1, s_retr[u[j]]);
   double oldact = dym_action(a.beta0, a.beta1, a.beta2, r1, m1);  // changes only on accept
+  dym_metro_link Lk{};
+  if (kSplit) Lk = dym_metro_link_init(a.rk, sweep, i, DIR, DYM_TAG_METRO);
   for (int h = 0; h < a.nhit; ++h) {
-    const dym_u32x4 r = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_METRO);
+    const dym_u32x4 r = kSplit ? dym_metro_hit(a.rk, Lk, (uint32_t)h)
+                               : dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h, DYM_TAG_METRO);
     const uint16_t* row = s_sub + dym_pick(r.v[0], a.npool) * a.P;
     uint32_t e[NT];
     double r1n = 0, m1n = 0;
@@ -594,9 +599,10 @@ __device__ __forceinline__ void vt2_hits(const SweepArgs& a, uint32_t i, uint32_
   const uint32_t P = a.P, np = a.npool;
   double oldact = 0.0;
   bool old_ok = false;
+  const dym_metro_link L = dym_metro_link_init(a.rk, sweep, i, DIR, DYM_TAG_METRO);
   for (int h0 = 0; h0 < a.nhit; h0 += 2) {
     // This lane draws hit h0 + back; the pair swaps them.
-    const dym_u32x4 rr = dym_hit_random(a.seed, sweep, i, DIR, (uint32_t)h0 + (back ? 1u : 0u), DYM_TAG_METRO);
+    const dym_u32x4 rr = dym_metro_hit(a.rk, L, (uint32_t)h0 + (back ? 1u : 0u));
     const uint32_t kown = dym_pick(rr.v[0], np);
     const float town = -__logf(__fmaf_rn((float)rr.v[1], 0x1p-32f, (float)(rr.v[2] >> 11) * 0x1p-53f));
     const uint32_t koth = __shfl_xor_sync(pm, kown, 1);
