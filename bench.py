@@ -63,21 +63,21 @@ def gathers_per_link_hit(nhit: int) -> float:
 # workload in the bench's own regime: the mean over the 16 launches of one
 # timed step (after the 256 MB flush), from an ncu capture with
 # --cache-control none (profiles/sweep_vt_s1080_32x32x32x8_ncu.md: the first
-# launch of the step 3.6 MB -- the table and lattice from DRAM and write-backs
+# launch of the step 3.7 MB -- the table and lattice from DRAM and write-backs
 # of the flush buffer's dirty lines -- the others 0.6-0.8 MB).  The FP64
 # kernel's figure is its capture after ncu's own per-launch flush.  The mixed
 # kernel runs this workload only on a chain's first call (the cold chain
 # accepts nothing, so later calls use the value table) and has no capture of
 # it; None leaves its roofline unreported.
-DRAM_BYTES_PER_LAUNCH = {"k_sweep_vt": 882416, "k_sweep_mixed": None, "k_sweep_sub": 2563584}
+DRAM_BYTES_PER_LAUNCH = {"k_sweep_vt": 899424, "k_sweep_mixed": None, "k_sweep_sub": 2563584}
 # smsp__inst_executed.sum (warp instructions) and lts__t_sectors_srcunit_tex.sum
 # (L2 sectors requested by the SMs) of one sweep launch of this workload: the
 # mean over the 16 launches of a timed step in the same capture (the four
 # directions differ by 3% in instructions).  Both are fixed for the workload:
 # the cold chain accepts no proposal, so every sweep runs the same
 # instructions.
-INST_PER_LAUNCH = {"k_sweep_vt": 6720264, "k_sweep_mixed": None, "k_sweep_sub": None}
-L2_SECTORS_PER_LAUNCH = {"k_sweep_vt": 491648, "k_sweep_mixed": None, "k_sweep_sub": None}
+INST_PER_LAUNCH = {"k_sweep_vt": 6107522, "k_sweep_mixed": None, "k_sweep_sub": None}
+L2_SECTORS_PER_LAUNCH = {"k_sweep_vt": 492695, "k_sweep_mixed": None, "k_sweep_sub": None}
 # Warp instructions an SM can issue per cycle (four schedulers, one each).
 ISSUE_PER_SM_CYCLE = 4
 
