@@ -472,8 +472,9 @@ int dym_chain_create(const dym_group* gh, const dym_chain_params* p, dym_chain**
   DYM_CUDA(copy_sync(d.pool, pool.data(), pool.size() * 2, cudaMemcpyHostToDevice, c->stream), "upload pool");
   DYM_CUDA(dmalloc(&d.counters, 6), "cudaMalloc(counters)");
   // Pinned copy of the six words (ChainDev::counters).
-  DYM_CUDA(cudaHostAlloc((void**)&c->h_counters, 6 * sizeof(unsigned long long), cudaHostAllocDefault),
+  DYM_CUDA(cudaHostAlloc((void**)&c->h_counters, 6 * sizeof(unsigned long long), cudaHostAllocMapped),
            "cudaHostAlloc");
+  DYM_CUDA(cudaHostGetDevicePointer((void**)&c->h_counters_dev, c->h_counters, 0), "cudaHostGetDevicePointer");
   if (p->precision != DYM_PREC_FP64 && shared_structure_ok(g, p->D)) {
     if (sub_eligible(g, d.npool, p->device, p->D)) {
       rc = build_sub_table(c.get(), pool);
@@ -553,7 +554,18 @@ int dym_chain_set_beta(dym_chain* c, double beta0, double beta1, double beta2) {
 // Clear the chain's six counter words (sweep counters and upload check) on
 // its stream; every call that sweeps or uploads starts with it.
 static int counters_reset(dym_chain* c) {
-  DYM_CUDA(cudaMemsetAsync(c->dev.counters, 0, 6 * sizeof(unsigned long long), c->stream), "reset counters");
+  if (c->counters_dirty)
+    DYM_CUDA(cudaMemsetAsync(c->dev.counters, 0, 6 * sizeof(unsigned long long), c->stream), "reset counters");
+  c->counters_dirty = true;  // until counters_readback is enqueued
+  return DYM_OK;
+}
+
+// The end of a call's device work: the six counter words into h_counters and
+// cleared on the device (k_counters_out, behind everything the call
+// enqueued, since the upload check word may still be read before it).
+static int counters_readback(dym_chain* c) {
+  DYM_CUDA(launch_counters_out(c->dev.counters, c->h_counters_dev, 6, c->stream), "read counters");
+  c->counters_dirty = false;
   return DYM_OK;
 }
 
@@ -565,8 +577,8 @@ static bool upload_refused(const dym_chain* c, unsigned long long* index) {
 }
 
 // Enqueue nsweeps sweeps of the chain on its stream, between the events
-// ev0 and ev1, and the read-back of the six counter words into h_counters
-// (after counters_reset); `skip` (see SweepArgs) may make every launch a
+// ev0 and ev1 (after counters_reset; the caller ends with
+// counters_readback); `skip` (see SweepArgs) may make every launch a
 // no-op, and the final sweep writes every link into `out` / `out_ref` when
 // given (SweepArgs).  Advances c->sweep.
 static int sweep_enqueue(dym_chain* c, int32_t nsweeps, int32_t nhit, const unsigned long long* skip,
@@ -604,9 +616,6 @@ static int sweep_enqueue(dym_chain* c, int32_t nsweeps, int32_t nhit, const unsi
     ++c->sweep;
   }
   DYM_CUDA(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");
-  DYM_CUDA(cudaMemcpyAsync(c->h_counters, c->dev.counters, 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                           c->stream),
-           "read counters");
   *kernel_out = kernel;
   return DYM_OK;
 }
@@ -643,6 +652,7 @@ int dym_sweep(dym_chain* c, int32_t nsweeps, int32_t nhit, dym_stats* out) {
   int kernel = 0;
   if (int rc = counters_reset(c)) return rc;
   if (int rc = sweep_enqueue(c, nsweeps, nhit, nullptr, &kernel)) return rc;
+  if (int rc = counters_readback(c)) return rc;
   DYM_CUDA(cudaStreamSynchronize(c->stream), "sweep");
   return sweep_report(c, kernel, nsweeps, out);
 }
@@ -746,9 +756,7 @@ int dym_links_set(dym_chain* c, const uint16_t* host_in) {
   DYM_CUDA(cudaSetDevice(c->p.device), "cudaSetDevice");
   if (int rc = counters_reset(c)) return rc;
   if (int rc = links_upload_enqueue(c, host_in)) return rc;
-  DYM_CUDA(cudaMemcpyAsync(c->h_counters + 5, c->dev.counters + 5, sizeof(unsigned long long),
-                           cudaMemcpyDeviceToHost, c->stream),
-           "read links check");
+  if (int rc = counters_readback(c)) return rc;
   DYM_CUDA(cudaStreamSynchronize(c->stream), "upload links");
   unsigned long long bad;
   if (upload_refused(c, &bad))
@@ -775,6 +783,7 @@ int dym_sweep_host(dym_chain* c, const uint16_t* host_in, uint16_t* host_out, in
   const size_t bytes = (size_t)c->dev.V * c->p.D * 2;
   if (host_out && !out_mapped)
     DYM_CUDA(cudaMemcpyAsync(host_out, c->dev.links, bytes, cudaMemcpyDeviceToHost, c->stream), "download links");
+  if (int rc = counters_readback(c)) return rc;
   DYM_CUDA(cudaStreamSynchronize(c->stream), "dym_sweep_host");
   unsigned long long bad;
   if (host_in && upload_refused(c, &bad)) {
@@ -814,6 +823,7 @@ int dym_sweep_refarray(dym_chain* c, int32_t* a, int32_t nsweeps, int32_t nhit, 
     return rc;
   if (mapped && nsweeps > 0)
     DYM_CUDA(launch_links_to_ref(mapped, c->dev.links, V, D, c->dev.counters + 5, c->stream), "write reference array");
+  if (int rc = counters_readback(c)) return rc;  // after the write-back, which reads the check word
   DYM_CUDA(cudaStreamSynchronize(c->stream), "dym_sweep_refarray");
   unsigned long long bad;
   if (upload_refused(c, &bad)) {

@@ -117,6 +117,10 @@ constexpr int kDefaultLanesPerLink = 1;
 // (two lanes for each of 448 links; 72 registers a thread).
 constexpr int kVt2MaxThreads = 896;
 constexpr double kDefaultVtMaxAccept = 0.01;
+// Copy n counter words into page-locked host memory (its device mapping) and
+// clear them for the next call, behind the previous kernel (programmatic
+// serialization): one kernel instead of a copy-engine read-back and a memset.
+cudaError_t launch_counters_out(unsigned long long* dev, unsigned long long* host_mapped, int n, cudaStream_t s);
 cudaError_t launch_hot_start(uint16_t* links, uint32_t V, int D, uint32_t P, uint64_t seed, cudaStream_t s);
 cudaError_t launch_fill(uint16_t* links, size_t n, uint16_t v, cudaStream_t s);
 // Check n uploaded ids against P on the device and copy the stage into the
@@ -241,6 +245,11 @@ struct dym_chain {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // device timing of sweeps
   uint32_t sweep = 0;
   unsigned long long* h_counters = nullptr;  // pinned
+  unsigned long long* h_counters_dev = nullptr;  // its device mapping (k_counters_out writes it)
+  // Whether the device counter words may be non-zero on entry to a call: a
+  // call ends by reading them out and clearing them in one kernel; one that
+  // returned before that leaves this set, and the next call clears them first.
+  bool counters_dirty = true;
   // Measurement buffers (allocated on first use, sized for the largest grid).
   unsigned long long* d_hist = nullptr;
   size_t hist_elems = 0;

@@ -227,6 +227,16 @@ __global__ void k_links_to_ref(int32_t* __restrict__ ref, const uint16_t* __rest
   }
 }
 
+__global__ void k_counters_out(unsigned long long* dev, unsigned long long* host, int n) {
+  pdl_wait_prior();
+  const int t = threadIdx.x;
+  if (t < n) {
+    host[t] = dev[t];
+    dev[t] = 0;
+  }
+  __threadfence_system();
+}
+
 __global__ void k_fill(uint16_t* p, size_t n, uint16_t v) {
   for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) p[l] = v;
 }
@@ -401,6 +411,10 @@ cudaError_t launch_links_to_ref(int32_t* ref, const uint16_t* links, uint32_t V,
   if (n == 0) return cudaSuccess;
   const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 8);
   return launch_phase(k_links_to_ref, grid, 256, 0, s, ref, links, V, D, skip);
+}
+
+cudaError_t launch_counters_out(unsigned long long* dev, unsigned long long* host_mapped, int n, cudaStream_t s) {
+  return launch_phase(k_counters_out, 1, 32, 0, s, dev, host_mapped, n);
 }
 
 cudaError_t launch_fill(uint16_t* links, size_t n, uint16_t v, cudaStream_t s) {
