@@ -111,6 +111,7 @@ __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_batch_mixed(const Batch
     a.b2f = c.b2f;
     a.dscale = G.dscale;
     a.dmargin = c.dmargin;
+    dym_philox_round_keys(c.seed, a.rk);  // block-uniform: the tile's chain
     const uint32_t sweep = sweeps[tl.chain];
     const double* s_retr = reinterpret_cast<const double*>(smem + G.off_retr);
     const uint16_t* s_inv = reinterpret_cast<const uint16_t*>(smem + G.off_inv);
@@ -123,10 +124,10 @@ __global__ void __launch_bounds__(kMixedMaxThreads, 1) k_batch_mixed(const Batch
       const uint32_t i = c.sites[tl.begin + k];
       const uint32_t xyz = c.xyz[tl.begin + k];
       switch (tl.dir) {
-        case 0: visit_mixed<D, 0, uint16_t, HU>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
-        case 1: visit_mixed<D, 1, uint16_t, HU>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
-        case 2: visit_mixed<D, 2, uint16_t, HU>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
-        case 3: visit_mixed<D, 3, uint16_t, HU>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
+        case 0: visit_mixed<D, 0, uint16_t, HU, true>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
+        case 1: visit_mixed<D, 1, uint16_t, HU, true>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
+        case 2: visit_mixed<D, 2, uint16_t, HU, true>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
+        case 3: visit_mixed<D, 3, uint16_t, HU, true>(a, i, xyz, sweep, s_retr, s_inv, s_psub, s_cls, s_cfix, hits, accs, rechecks, max_err); break;
       }
     }
     flush_counters(c.ctr, hits, accs, rechecks);
