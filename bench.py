@@ -290,7 +290,7 @@ def bench_config(world: int) -> dict:
 
 
 def ensemble_bench(dym, device: int, sweeps: int = 5, nhit: int = 10) -> dict:
-    """Config 3: 256 chains of uneven size, 200 on S(1080) and 56 on BI, hot
+    """Batched ensemble: 256 chains of uneven size, 200 on S(1080) and 56 on BI, hot
     starts, (beta1, beta2) on a 16x16 grid.  The single-chain GPU path runs
     each chain's sweep with its own dym_sweep call, one chain after another;
     the batched path updates all chains with one kernel per colour-phase slot
@@ -342,7 +342,7 @@ def ensemble_bench(dym, device: int, sweeps: int = 5, nhit: int = 10) -> dict:
 
 def serving_bench(dym, device: int, n_requests: int, nhit: int = 20, step_sweeps: int = 5,
                   max_chains: int = 512, max_links: int = 0) -> dict:
-    """Config 5: LLR windows arriving as a Poisson stream (200/s) on S(1080)
+    """Served LLR stream: windows arriving as a Poisson stream (200/s) on S(1080)
     lattices Nx in {6,8,12,16}, Nt in {2,4}, beta2 in {0,-0.1}; each request one
     window of 0.5% of the plaquette-energy range, 20 Robbins-Monro iterations of
     50 sweeps.  Requests are submitted when their arrival time has passed (wall
