@@ -123,8 +123,8 @@ __device__ __forceinline__ void exact_actions(const SweepArgs& a, const uint16_t
 // table whose ReTr is one double per conjugacy class ReTr[u_j g_k] equals the
 // reference's ReTr[mult[bnew][s_j]] bit for bit, summed in the same order
 // (dym-mod-metro.cpp:166-192).
-// kSplit: the draws from the link's precomputed Philox state (dym_metro_hit;
-// for kernels whose SweepArgs is their parameter).
+// kSplit: the draws from the link's precomputed Philox state (dym_metro_hit,
+// with the round keys in SweepArgs::rk filled in).
 template <int D, int DIR, bool kSplit = false>
 __device__ __forceinline__ void visit_sub(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
                                           const uint16_t* s_inv, const uint16_t* s_sub, unsigned& hits,
@@ -243,9 +243,11 @@ struct HitDraws {
 #pragma unroll
     for (int q = 0; q < HU; ++q) set(q, dym_hit_random(a.seed, sweep, i, dir, (uint32_t)(h0 + q), DYM_TAG_METRO), a.npool);
   }
-  // The same draws from the link's precomputed Philox state and the kernel
-  // parameters' round keys (dym_metro_hit: the same bits, fewer
-  // instructions); for kernels whose SweepArgs is their parameter.
+  // The same draws from the link's precomputed Philox state and the round
+  // keys (dym_metro_hit: the same bits, fewer
+  // instructions); SweepArgs::rk must hold the seed's round keys (kernel
+  // parameters in the single-chain kernels, block-uniform values in the batch
+  // kernel).
   __device__ __forceinline__ void fill(const SweepArgs& a, const dym_metro_link& L, int h0) {
 #pragma unroll
     for (int q = 0; q < HU; ++q) set(q, dym_metro_hit(a.rk, L, (uint32_t)(h0 + q)), a.npool);
@@ -263,8 +265,8 @@ struct Packed {
 // Second half: the nhit hits of link (i, DIR) from the shared tables, starting
 // from mixed_prepare's state, in groups of HU hits whose draws are computed
 // ahead (HitDraws); the link is written when it changed.
-// kSplit: the draws from the link's precomputed Philox state (HitDraws, for
-// kernels whose SweepArgs is their parameter).
+// kSplit: the draws from the link's precomputed Philox state (HitDraws; the
+// round keys in SweepArgs::rk filled in).
 template <int D, int DIR, class E = uint16_t, int HU = 1, bool kSplit = false>
 __device__ __forceinline__ void mixed_hits(const SweepArgs& a, uint32_t i, uint32_t sweep, const double* s_retr,
                                            const uint16_t* s_inv, const E* s_psub, const int32_t* s_cfix,
