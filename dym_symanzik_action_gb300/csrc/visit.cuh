@@ -244,10 +244,9 @@ struct HitDraws {
     for (int q = 0; q < HU; ++q) set(q, dym_hit_random(a.seed, sweep, i, dir, (uint32_t)(h0 + q), DYM_TAG_METRO), a.npool);
   }
   // The same draws from the link's precomputed Philox state and the round
-  // keys (dym_metro_hit: the same bits, fewer
-  // instructions); SweepArgs::rk must hold the seed's round keys (kernel
-  // parameters in the single-chain kernels, block-uniform values in the batch
-  // kernel).
+  // keys (dym_metro_hit: the same bits, fewer instructions); SweepArgs::rk
+  // must hold the seed's round keys (kernel parameters in the single-chain
+  // kernels, block-uniform values in the batch kernel).
   __device__ __forceinline__ void fill(const SweepArgs& a, const dym_metro_link& L, int h0) {
 #pragma unroll
     for (int q = 0; q < HU; ++q) set(q, dym_metro_hit(a.rk, L, (uint32_t)(h0 + q)), a.npool);
